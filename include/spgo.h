@@ -1,0 +1,196 @@
+/*
+ * spgo.h - C ABI of the GB300-native stereo pose-graph / bundle-adjustment
+ * Levenberg-Marquardt solver (drop-in for S-PGO's CUDA solver).
+ *
+ * Plain C: pointers, sizes and an int status on every call; no C++ or torch
+ * types.  All device memory is caller-owned (for example torch tensors): the
+ * library sizes it, the caller allocates it, the library only reads and
+ * writes it.  Every call that touches the GPU takes an explicit cudaStream_t
+ * (passed as void*) and only enqueues work on it unless stated otherwise.
+ *
+ * Reference interface each entry point replaces (paths inside S-PGO):
+ *   spgo_plan_create          Solver::Solver + loadCalibration + writeObservations
+ *                             (include/Solver.hpp:20-57, src/Optimization/Solver.cpp:29-56):
+ *                             one bulk, landmark-major upload instead of one
+ *                             index_put_ per scalar
+ *   spgo_solver_create        LMvariables::allocateMemory (src/Optimization/LMutils.cu:5-130),
+ *                             done once instead of on every step()
+ *   spgo_gn_step              Solver::step / updateState (Solver.cpp:5-27,
+ *                             src/Optimization/Solver_cuda.cu:557-795)
+ *   spgo_lm_reset/iterate/status   new: Nielsen-damped LM with FP64 gain ratio
+ *                             (no counterpart in the reference)
+ *   spgo_export_system        LMvariables::*_to_txt debug dumps (LMutils.cu:188-536)
+ *                             and Optimizer.getHessians (PythonUtils/Optimizer.py:376-383)
+ * Pose and inverse-depth read/write (Solver.cpp:59-128) are plain copies of the
+ * caller-owned state buffers and need no entry point.
+ */
+#ifndef SPGO_H
+#define SPGO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define SPGO_OK                   0
+#define SPGO_ERR_INVALID_ARG     -1
+#define SPGO_ERR_UNSUPPORTED     -2   /* e.g. a landmark window wider than SPGO_MAX_WINDOW */
+#define SPGO_ERR_BUFFER_SMALL    -3
+#define SPGO_ERR_CUDA            -4
+#define SPGO_ERR_NOT_SPD         -5   /* reduced camera system not positive definite */
+
+#define SPGO_MAX_WINDOW          96   /* max pose blocks one landmark's Jacobian spans */
+
+/* precision of the linearisation, Schur complement and factorisation */
+#define SPGO_PREC_MIXED           0   /* FP32 J/H/Schur, FP32 Cholesky + FP64 refinement, FP64 cost */
+#define SPGO_PREC_FP64            1   /* plain FP64 everywhere */
+
+/* robust loss */
+#define SPGO_LOSS_L2              0
+#define SPGO_LOSS_CAUCHY          1
+#define SPGO_LOSS_HUBER           2
+
+/* per-problem LM status */
+#define SPGO_STATUS_RUNNING       0
+#define SPGO_STATUS_CONVERGED     1   /* relative cost decrease below tol on an accepted step */
+#define SPGO_STATUS_MAX_ITERS     2
+#define SPGO_STATUS_STALLED       3   /* lambda exceeded lambda_max */
+
+/* ---- host-side problem description (one problem, host memory) ---------
+ * Landmark-major CSR: landmark l has its host (anchor) frame host[l], the
+ * left pixel it was observed at in the host, and observations
+ * [obs_ptr[l], obs_ptr[l+1]) with strictly ascending frames.  Frame 0 is
+ * fixed; frames run 0..n_poses.  The host frame's own observation is part of
+ * the list (it carries the stereo depth constraint).  Mirrors the arguments of
+ * Solver::loadCalibration and Solver::writeObservations (Solver.cpp:29-56). */
+typedef struct spgo_host_problem {
+    int32_t        n_poses;      /* N incremental poses, N + 1 frames        */
+    int32_t        n_landmarks;  /* L                                         */
+    int64_t        n_obs;        /* O stereo observations                     */
+    const float   *intrinsics;   /* [8] fx_l, fy_l, cx_l, cy_l, fx_r, fy_r, cx_r, cy_r */
+    const double  *T_r_to_l;     /* [16] row-major pose of the right camera in the left frame */
+    const int32_t *host;         /* [L]                                       */
+    const float   *anchor_uv;    /* [L*2]                                     */
+    const int64_t *obs_ptr;      /* [L+1]                                     */
+    const int32_t *obs_frame;    /* [O]                                       */
+    const float   *obs_uv;       /* [O*4] uL, vL, uR, vR                      */
+} spgo_host_problem;
+
+/* sizes a plan needs (bytes unless noted) */
+typedef struct spgo_plan_sizes {
+    int32_t n_problems;
+    int32_t total_poses;         /* length of the pose state in 12-double records */
+    int32_t total_landmarks;     /* length of the inverse-depth state            */
+    int64_t total_obs;
+    int32_t n_chunks;
+    int32_t n_schur_items;
+    int32_t max_params;          /* max 6N over problems */
+    int32_t reserved;
+    size_t  static_bytes;        /* device buffer for the uploaded problem data   */
+    size_t  workspace_bytes;     /* device buffer for per-iteration scratch       */
+    int64_t slab_elems;          /* elements of the landmark-chunk slabs (W blocks) */
+    int64_t pair_records;        /* (lo, hi) pose-pair accumulators               */
+} spgo_plan_sizes;
+
+/* solver parameters */
+typedef struct spgo_params {
+    int32_t loss;                /* SPGO_LOSS_*                                  */
+    int32_t near_boost;          /* 1: x4 weight when |target-anchor| < 2 (Solver_cuda.cu:226-228) */
+    float   loss_scale;          /* Cauchy c (reference c^2 = 9) or Huber delta  */
+    float   eps;                 /* inverse-depth diagonal guard (LMutils.h:50: 1e-4) */
+    float   alpha_min;           /* inverse-depth clamp (LMutils.h:54-55)        */
+    float   alpha_max;
+    double  lambda0;             /* Nielsen initial damping (Marquardt scaling)  */
+    double  lambda_max;
+    double  tol;                 /* relative cost decrease that counts as converged */
+    int32_t max_iters;           /* per-problem LM iteration cap                 */
+    int32_t refine_steps;        /* FP64 iterative-refinement steps (mixed precision) */
+} spgo_params;
+
+typedef struct spgo_problem_status {
+    double  cost0;               /* cost at the first linearisation */
+    double  cost;                /* current (accepted) cost          */
+    double  lambda;
+    int32_t iterations;          /* LM solves (accepted + rejected)  */
+    int32_t accepted;
+    int32_t status;              /* SPGO_STATUS_*                    */
+    int32_t factor_failures;
+} spgo_problem_status;
+
+typedef struct spgo_plan   spgo_plan;
+typedef struct spgo_solver spgo_solver;
+
+int         spgo_version(void);
+const char *spgo_last_error(void);
+void        spgo_default_params(spgo_params *p);
+
+/* Host-side planning: validates the problems, orders landmarks by Jacobian
+ * window, groups them into 32-landmark chunks and builds the Schur tile work
+ * list.  Allocates host memory only. */
+int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems,
+                     int32_t precision, spgo_plan **out);
+int spgo_plan_sizes_get(const spgo_plan *plan, spgo_plan_sizes *out);
+int spgo_plan_destroy(spgo_plan *plan);
+/* Landmark permutation: internal slot -> (problem-local) landmark order is
+ * handled inside; this returns the global landmark offset of each problem
+ * ([n_problems]) and the pose offset ([n_problems]) into the state buffers. */
+int spgo_plan_offsets(const spgo_plan *plan, int32_t *lm_off, int32_t *pose_off);
+
+/* Binds caller-owned device memory and uploads the plan (asynchronous H2D on
+ * `stream`; the plan must outlive the copy, i.e. synchronise before
+ * destroying it).  State buffers: poses [total_poses*12] (3x4 row-major
+ * incremental T_curr_to_next, FP64) and alpha [total_landmarks] (FP64), both
+ * in the caller's problem/landmark order. */
+int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_bytes,
+                       void *d_workspace, size_t workspace_bytes,
+                       double *d_poses, double *d_alpha, void *stream, spgo_solver **out);
+int spgo_solver_destroy(spgo_solver *s);
+int spgo_set_params(spgo_solver *s, const spgo_params *p);
+
+/* The reference's step(iterations): undamped Gauss-Newton with C + eps, pose
+ * step scaled by step_size, unscaled clamped inverse-depth update
+ * (Solver_cuda.cu:594-782).  Enqueue only. */
+int spgo_gn_step(spgo_solver *s, int32_t iterations, float step_size, void *stream);
+
+/* Nielsen LM.  reset: lambda = lambda0, nu = 2, counters cleared, first
+ * linearisation pending.  iterate: enqueue n_iters LM iterations for every
+ * problem still running (no host synchronisation; capturable in a CUDA
+ * graph).  status: synchronises `stream` and copies per-problem status to
+ * host memory out[n_problems]. */
+int spgo_lm_reset(spgo_solver *s, void *stream);
+int spgo_lm_iterate(spgo_solver *s, int32_t n_iters, void *stream);
+int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream);
+/* Convenience: reset, iterate until every problem stops or max_iters, with a
+ * status check every `check_every` iterations.  Returns the iteration count
+ * in *iters_done (max over problems). */
+int spgo_lm_solve(spgo_solver *s, int32_t check_every, int32_t *iters_done, void *stream);
+
+/* Linearise at the current state and export one problem's dense system into
+ * caller-owned DEVICE buffers (any pointer may be NULL):
+ * A [P*P] and g [P] (FP64, incremental parameterisation), B [P*L] (FP64,
+ * row-major, the problem's landmark order), C [L], g_a [L] (FP64), cost [1].
+ * For parity checks on small problems. */
+int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, double *B,
+                       double *C, double *g_a, double *cost, void *stream);
+
+/* Count of kernel launches enqueued by this solver since creation. */
+int64_t spgo_launch_count(const spgo_solver *s);
+
+/* Optional per-kernel timing with CUDA events on the launching stream.
+ * enable: create `capacity` event pairs (0 disables); each profiled launch
+ * uses one pair until they run out.  read: synchronise `stream`, return the
+ * summed milliseconds and launch counts per kind, and recycle the events.
+ * Kinds (n_kinds >= 10): 0 pose chain, 1 linearisation, 2 cost pass,
+ * 3 pair reduction, 4 Schur complement, 5 assembly, 6 factor + solve,
+ * 7 inverse-depth back-substitution, 8 pose update, 9 LM bookkeeping. */
+#define SPGO_PROFILE_KINDS 10
+int spgo_profile_enable(spgo_solver *s, int32_t capacity);
+int spgo_profile_read(spgo_solver *s, double *ms, int64_t *count, int32_t n_kinds, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPGO_H */

@@ -1,0 +1,688 @@
+// C ABI: planner (host), solver binding and the LM / Gauss-Newton orchestration.
+//
+// The reference allocates every workspace with cudaMalloc and frees it on each
+// step() (src/Optimization/LMutils.cu:5-185, Solver_cuda.cu:576-580, :793-794),
+// creates a cuBLAS handle per iteration (Solver_cuda.cu:627-628) and
+// synchronises about ten times per iteration.  Here the caller owns two device
+// buffers (static problem data and scratch) sized once by the plan; an LM
+// iteration is a fixed, host-synchronisation-free sequence of kernels whose
+// per-problem work is gated on device-side status, so any number of iterations
+// can be enqueued (or captured in a CUDA graph) and the host only reads status.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "spgo_internal.h"
+
+namespace spgo {
+int64_t g_launches = 0;
+}
+
+using namespace spgo;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                     \
+  do {                                                                                     \
+    int _e = (int)(expr);                                                                  \
+    if (_e != 0) return fail(SPGO_ERR_CUDA, std::string(#expr) + ": " +                    \
+                                                cudaGetErrorString((cudaError_t)_e));      \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------------
+struct Seg {
+  size_t off;
+  size_t bytes;
+  const void *src;
+};
+
+struct spgo_plan {
+  int32_t precision = SPGO_PREC_MIXED;
+  int32_t B = 0, F = 0, NP = 0, L = 0;
+  int64_t O = 0;
+  int32_t max_P = 0, max_D = 1, max_nb = 1, total_params = 0;
+  int64_t total_S = 0, total_pairs = 0, total_slab = 0;
+  std::vector<int32_t> p_npose, p_frame_off, p_pose_off, p_lm_off, p_lm_cnt, p_pair_D, p_param_off, p_chunk_off,
+      p_chunk_cnt, fr_prob, pose_prob;
+  std::vector<int64_t> p_S_off, p_pair_off;
+  std::vector<float> p_intr;
+  std::vector<double> p_Trl;
+  std::vector<int32_t> lm_prob, lm_host, lm_lo, lm_hi, lm_user, lm_chunk, lm_slot;
+  std::vector<float> lm_uv;
+  std::vector<int64_t> lm_obs;
+  std::vector<int32_t> obs_frame;
+  std::vector<float> obs_uv;
+  std::vector<int32_t> ch_prob, ch_f0, ch_nb, ch_lm0, ch_cnt;
+  std::vector<int64_t> ch_slab;
+  std::vector<int32_t> wk_prob, wk_ti, wk_tj, wk_cbeg, wk_cend, wk_chunks;
+  std::vector<Seg> segs;
+  size_t static_bytes = 0, ws_bytes = 0;
+  // workspace segment offsets
+  size_t w_frRf, w_frRd, w_frc, w_pcand, w_acand, w_pacc, w_p64, w_A, w_g, w_SL, w_gL, w_S, w_gS, w_fac, w_delta, w_C,
+      w_ga, w_slab, w_lm, w_cost, w_pred;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+template <typename V>
+static void add_seg(spgo_plan *p, const V &v) {
+  Seg s;
+  s.off = p->static_bytes;
+  s.bytes = v.size() * sizeof(typename V::value_type);
+  s.src = v.data();
+  p->segs.push_back(s);
+  p->static_bytes = align256(p->static_bytes + s.bytes);
+}
+
+static void build_layout(spgo_plan *p) {
+  // static segments, in PlanView order (see make_views)
+  p->segs.clear();
+  p->static_bytes = 0;
+  add_seg(p, p->p_npose); add_seg(p, p->p_frame_off); add_seg(p, p->p_pose_off); add_seg(p, p->p_lm_off);
+  add_seg(p, p->p_lm_cnt); add_seg(p, p->p_pair_D); add_seg(p, p->p_param_off); add_seg(p, p->p_chunk_off);
+  add_seg(p, p->p_chunk_cnt); add_seg(p, p->p_S_off); add_seg(p, p->p_pair_off); add_seg(p, p->p_intr);
+  add_seg(p, p->p_Trl); add_seg(p, p->lm_prob); add_seg(p, p->lm_host); add_seg(p, p->lm_lo); add_seg(p, p->lm_hi);
+  add_seg(p, p->lm_user); add_seg(p, p->lm_chunk); add_seg(p, p->lm_slot); add_seg(p, p->lm_uv);
+  add_seg(p, p->lm_obs); add_seg(p, p->obs_frame); add_seg(p, p->obs_uv); add_seg(p, p->ch_prob);
+  add_seg(p, p->ch_f0); add_seg(p, p->ch_nb); add_seg(p, p->ch_lm0); add_seg(p, p->ch_cnt); add_seg(p, p->ch_slab);
+  add_seg(p, p->wk_prob); add_seg(p, p->wk_ti); add_seg(p, p->wk_tj); add_seg(p, p->wk_cbeg);
+  add_seg(p, p->wk_cend); add_seg(p, p->wk_chunks); add_seg(p, p->fr_prob); add_seg(p, p->pose_prob);
+  // workspace
+  const size_t ts = p->precision == SPGO_PREC_FP64 ? 8 : 4;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t r = o;
+    o = align256(o + bytes);
+    return r;
+  };
+  p->w_frRf = take((size_t)p->F * 18 * 4);
+  p->w_frRd = take((size_t)p->F * 18 * 8);
+  p->w_frc = take((size_t)p->F * 6 * 8);
+  p->w_pcand = take((size_t)p->NP * 12 * 8);
+  p->w_acand = take((size_t)p->L * 8);
+  p->w_pacc = take((size_t)p->total_pairs * 27 * ts);
+  p->w_p64 = take((size_t)p->total_pairs * 27 * 8);
+  p->w_A = take((size_t)p->total_S * 8);
+  p->w_g = take((size_t)p->total_params * 8);
+  p->w_SL = take((size_t)p->total_S * ts);
+  p->w_gL = take((size_t)p->total_params * ts);
+  p->w_S = take((size_t)p->total_S * 8);
+  p->w_gS = take((size_t)p->total_params * 8);
+  // global factor storage only when a problem is too large for the shared-memory path
+  const size_t P = (size_t)p->max_P;
+  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts) + 16;
+  p->w_fac = take(packed <= 200 * 1024 ? 0 : (size_t)p->total_S * ts);
+  p->w_delta = take((size_t)p->total_params * 8);
+  p->w_C = take((size_t)p->L * ts);
+  p->w_ga = take((size_t)p->L * ts);
+  p->w_slab = take((size_t)p->total_slab * ts);
+  p->w_lm = take((size_t)p->B * sizeof(LMState));
+  p->w_cost = take((size_t)p->B * 8);
+  p->w_pred = take((size_t)p->B * 8);
+  p->ws_bytes = o;
+}
+
+static int plan_build(const spgo_host_problem *probs, int nprob, int precision, spgo_plan *p) {
+  if (nprob <= 0 || !probs) return fail(SPGO_ERR_INVALID_ARG, "no problems");
+  if (precision != SPGO_PREC_MIXED && precision != SPGO_PREC_FP64)
+    return fail(SPGO_ERR_INVALID_ARG, "unknown precision");
+  p->precision = precision;
+  p->B = nprob;
+  int32_t frame_off = 0, pose_off = 0, lm_off = 0, param_off = 0;
+  int64_t S_off = 0, pair_off = 0, slab_off = 0, obs_total = 0;
+  for (int b = 0; b < nprob; ++b) {
+    const spgo_host_problem &q = probs[b];
+    const int N = q.n_poses, L = q.n_landmarks;
+    if (N < 1) return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": n_poses < 1");
+    if (L < 0 || q.n_obs < 0) return fail(SPGO_ERR_INVALID_ARG, "negative size");
+    if (!q.intrinsics || !q.T_r_to_l || (L > 0 && (!q.host || !q.anchor_uv || !q.obs_ptr)) ||
+        (q.n_obs > 0 && (!q.obs_frame || !q.obs_uv)))
+      return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": null array");
+    if (L > 0 && (q.obs_ptr[0] != 0 || q.obs_ptr[L] != q.n_obs))
+      return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": obs_ptr is not a CSR over n_obs");
+    // per-landmark window [lo, hi) of pose blocks
+    std::vector<int32_t> lo(L), hi(L);
+    int32_t maxw = 1;
+    for (int l = 0; l < L; ++l) {
+      const int a = q.host[l];
+      if (a < 0 || a > N) return fail(SPGO_ERR_INVALID_ARG, "landmark " + std::to_string(l) + ": host out of range");
+      if (q.obs_ptr[l + 1] < q.obs_ptr[l]) return fail(SPGO_ERR_INVALID_ARG, "obs_ptr decreasing");
+      int32_t mn = a, mx = a, prev = -1;
+      for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) {
+        const int n = q.obs_frame[o];
+        if (n < 0 || n > N) return fail(SPGO_ERR_INVALID_ARG, "observation frame out of range");
+        if (n <= prev) return fail(SPGO_ERR_INVALID_ARG, "frames must ascend strictly inside a landmark");
+        prev = n;
+        mn = std::min(mn, n);
+        mx = std::max(mx, n);
+      }
+      lo[l] = mn;
+      hi[l] = mx;
+      if (mx - mn > SPGO_MAX_WINDOW)
+        return fail(SPGO_ERR_UNSUPPORTED, "landmark " + std::to_string(l) + " spans more than SPGO_MAX_WINDOW poses");
+      maxw = std::max(maxw, mx - mn);
+    }
+    // order landmarks by window, group into chunks of <= 32 with a common slab window
+    std::vector<int32_t> order(L);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return lo[x] != lo[y] ? lo[x] < lo[y] : hi[x] < hi[y];
+    });
+    const int32_t ch_begin = (int32_t)p->ch_prob.size();
+    int32_t cur = -1;
+    for (int k = 0; k < L; ++k) {
+      const int l = order[k];
+      bool fresh = cur < 0 || p->ch_cnt[cur] == SPGO_CHUNK;
+      if (!fresh) {
+        const int f0 = p->ch_f0[cur];
+        const int nb_new = std::max(p->ch_f0[cur] + p->ch_nb[cur], hi[l]) - f0;
+        if (nb_new > SPGO_MAX_WINDOW) fresh = true;
+      }
+      if (fresh) {
+        if (cur >= 0) slab_off += (int64_t)6 * p->ch_nb[cur] * SPGO_CHUNK;
+        cur = (int32_t)p->ch_prob.size();
+        p->ch_prob.push_back(b);
+        p->ch_f0.push_back(std::min(lo[l], N - 1));
+        p->ch_nb.push_back(1);
+        p->ch_lm0.push_back(lm_off + k);
+        p->ch_cnt.push_back(0);
+        p->ch_slab.push_back(slab_off);
+      }
+      const int f0 = p->ch_f0[cur];
+      p->ch_nb[cur] = std::max(p->ch_nb[cur], hi[l] - f0);
+      p->ch_cnt[cur] += 1;
+      // internal landmark lm_off + k
+      p->lm_prob.push_back(b);
+      p->lm_host.push_back(q.host[l]);
+      p->lm_lo.push_back(lo[l]);
+      p->lm_hi.push_back(hi[l]);
+      p->lm_user.push_back(lm_off + l);
+      p->lm_chunk.push_back(cur);
+      p->lm_slot.push_back(p->ch_cnt[cur] - 1);
+      p->lm_uv.push_back(q.anchor_uv[2 * l]);
+      p->lm_uv.push_back(q.anchor_uv[2 * l + 1]);
+      p->lm_obs.push_back(obs_total);
+      for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) {
+        p->obs_frame.push_back(q.obs_frame[o]);
+        for (int c = 0; c < 4; ++c) p->obs_uv.push_back(q.obs_uv[4 * o + c]);
+      }
+      obs_total += q.obs_ptr[l + 1] - q.obs_ptr[l];
+    }
+    if (cur >= 0) slab_off += (int64_t)6 * p->ch_nb[cur] * SPGO_CHUNK;
+    const int32_t ch_end = (int32_t)p->ch_prob.size();
+    for (int c = ch_begin; c < ch_end; ++c) {
+      if (p->ch_f0[c] < 0 || p->ch_f0[c] + p->ch_nb[c] > N)
+        return fail(SPGO_ERR_INVALID_ARG, "internal: chunk window outside the problem");
+      p->max_nb = std::max(p->max_nb, p->ch_nb[c]);
+    }
+    // Schur work list: every (ti >= tj) tile pair a chunk's window touches
+    const int ntile = (N + SPGO_TILE_BLOCKS - 1) / SPGO_TILE_BLOCKS;
+    std::vector<std::vector<int32_t>> lists((size_t)ntile * ntile);
+    for (int c = ch_begin; c < ch_end; ++c) {
+      const int t0 = p->ch_f0[c] / SPGO_TILE_BLOCKS;
+      const int t1 = std::min(ntile - 1, (p->ch_f0[c] + p->ch_nb[c] - 1) / SPGO_TILE_BLOCKS);
+      for (int ti = t0; ti <= t1; ++ti)
+        for (int tj = t0; tj <= ti; ++tj) lists[(size_t)ti * ntile + tj].push_back(c);
+    }
+    for (int ti = 0; ti < ntile; ++ti)
+      for (int tj = 0; tj <= ti; ++tj) {
+        const auto &lst = lists[(size_t)ti * ntile + tj];
+        for (size_t s = 0; s < lst.size(); s += SPGO_KSPLIT) {
+          p->wk_prob.push_back(b);
+          p->wk_ti.push_back(ti);
+          p->wk_tj.push_back(tj);
+          p->wk_cbeg.push_back((int32_t)p->wk_chunks.size());
+          for (size_t k = s; k < std::min(lst.size(), s + SPGO_KSPLIT); ++k) p->wk_chunks.push_back(lst[k]);
+          p->wk_cend.push_back((int32_t)p->wk_chunks.size());
+        }
+      }
+    // per-problem records
+    const int P = 6 * N;
+    p->p_npose.push_back(N);
+    p->p_frame_off.push_back(frame_off);
+    p->p_pose_off.push_back(pose_off);
+    p->p_lm_off.push_back(lm_off);
+    p->p_lm_cnt.push_back(L);
+    p->p_pair_D.push_back(maxw);
+    p->p_param_off.push_back(param_off);
+    p->p_chunk_off.push_back(ch_begin);
+    p->p_chunk_cnt.push_back(ch_end - ch_begin);
+    p->p_S_off.push_back(S_off);
+    p->p_pair_off.push_back(pair_off);
+    for (int k = 0; k < 8; ++k) p->p_intr.push_back(q.intrinsics[k]);
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 4; ++c) p->p_Trl.push_back(q.T_r_to_l[4 * r + c]);
+    for (int k = 0; k <= N; ++k) p->fr_prob.push_back(b);
+    for (int k = 0; k < N; ++k) p->pose_prob.push_back(b);
+    p->max_P = std::max(p->max_P, P);
+    p->max_D = std::max(p->max_D, maxw);
+    frame_off += N + 1;
+    pose_off += N;
+    lm_off += L;
+    param_off += P;
+    S_off += (int64_t)P * P;
+    pair_off += (int64_t)N * maxw;
+  }
+  p->lm_obs.push_back(obs_total);
+  p->F = frame_off;
+  p->NP = pose_off;
+  p->L = lm_off;
+  p->O = obs_total;
+  p->total_params = param_off;
+  p->total_S = S_off;
+  p->total_pairs = pair_off;
+  p->total_slab = slab_off;
+  build_layout(p);
+  return SPGO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// solver
+// ---------------------------------------------------------------------------
+struct spgo_solver {
+  const spgo_plan *plan;
+  PlanView pv;
+  WorkView wv;
+  Params prm;
+  double *poses, *alpha;
+  unsigned char *d_static, *d_ws;
+  int64_t launches0;
+  // optional per-kernel timing: event pairs recorded around each launch
+  bool prof = false;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> ev_kind;
+  size_t ev_used = 0;
+};
+
+// profiled kernel kinds (spgo_profile_read order)
+enum { K_CHAIN, K_LINEARIZE, K_COST, K_SYSTEM, K_SCHUR, K_ASSEMBLE, K_FACTOR, K_BACKSUB, K_UPDATE,
+       K_BOOKKEEP, K_NKINDS };
+
+struct ProfScope {
+  spgo_solver *s;
+  cudaStream_t st;
+  int kind;
+  size_t slot;
+  ProfScope(spgo_solver *s_, cudaStream_t st_, int kind_) : s(s_), st(st_), kind(kind_), slot((size_t)-1) {
+    if (s->prof && s->ev_used + 2 <= s->ev.size()) {
+      slot = s->ev_used;
+      s->ev_used += 2;
+      s->ev_kind[slot / 2] = kind;
+      cudaEventRecord(s->ev[slot], st);
+    }
+  }
+  ~ProfScope() {
+    if (slot != (size_t)-1) cudaEventRecord(s->ev[slot + 1], st);
+  }
+};
+#define PROF(kind) ProfScope _prof_scope(s, st, kind)
+
+template <typename T>
+static const T *seg_ptr(const spgo_plan *p, unsigned char *base, int idx) {
+  return reinterpret_cast<const T *>(base + p->segs[idx].off);
+}
+
+static void make_views(spgo_solver *s) {
+  const spgo_plan *p = s->plan;
+  unsigned char *st = s->d_static;
+  PlanView &v = s->pv;
+  std::memset(&v, 0, sizeof(v));
+  v.B = p->B; v.F = p->F; v.NP = p->NP; v.L = p->L; v.O = p->O;
+  v.n_chunks = (int32_t)p->ch_prob.size();
+  v.n_items = (int32_t)p->wk_prob.size();
+  v.max_P = p->max_P; v.max_D = p->max_D; v.max_nb = p->max_nb;
+  v.n_work_chunks = (int32_t)p->wk_chunks.size();
+  v.total_S = p->total_S; v.total_pairs = p->total_pairs; v.total_params = p->total_params;
+  int i = 0;
+  v.p_npose = seg_ptr<int32_t>(p, st, i++); v.p_frame_off = seg_ptr<int32_t>(p, st, i++);
+  v.p_pose_off = seg_ptr<int32_t>(p, st, i++); v.p_lm_off = seg_ptr<int32_t>(p, st, i++);
+  v.p_lm_cnt = seg_ptr<int32_t>(p, st, i++); v.p_pair_D = seg_ptr<int32_t>(p, st, i++);
+  v.p_param_off = seg_ptr<int32_t>(p, st, i++); v.p_chunk_off = seg_ptr<int32_t>(p, st, i++);
+  v.p_chunk_cnt = seg_ptr<int32_t>(p, st, i++); v.p_S_off = seg_ptr<int64_t>(p, st, i++);
+  v.p_pair_off = seg_ptr<int64_t>(p, st, i++); v.p_intr = seg_ptr<float>(p, st, i++);
+  v.p_Trl = seg_ptr<double>(p, st, i++); v.lm_prob = seg_ptr<int32_t>(p, st, i++);
+  v.lm_host = seg_ptr<int32_t>(p, st, i++); v.lm_lo = seg_ptr<int32_t>(p, st, i++);
+  v.lm_hi = seg_ptr<int32_t>(p, st, i++); v.lm_user = seg_ptr<int32_t>(p, st, i++);
+  v.lm_chunk = seg_ptr<int32_t>(p, st, i++); v.lm_slot = seg_ptr<int32_t>(p, st, i++);
+  v.lm_uv = seg_ptr<float>(p, st, i++); v.lm_obs = seg_ptr<int64_t>(p, st, i++);
+  v.obs_frame = seg_ptr<int32_t>(p, st, i++); v.obs_uv = seg_ptr<float>(p, st, i++);
+  v.ch_prob = seg_ptr<int32_t>(p, st, i++); v.ch_f0 = seg_ptr<int32_t>(p, st, i++);
+  v.ch_nb = seg_ptr<int32_t>(p, st, i++); v.ch_lm0 = seg_ptr<int32_t>(p, st, i++);
+  v.ch_cnt = seg_ptr<int32_t>(p, st, i++); v.ch_slab = seg_ptr<int64_t>(p, st, i++);
+  v.wk_prob = seg_ptr<int32_t>(p, st, i++); v.wk_ti = seg_ptr<int32_t>(p, st, i++);
+  v.wk_tj = seg_ptr<int32_t>(p, st, i++); v.wk_cbeg = seg_ptr<int32_t>(p, st, i++);
+  v.wk_cend = seg_ptr<int32_t>(p, st, i++); v.wk_chunks = seg_ptr<int32_t>(p, st, i++);
+  v.fr_prob = seg_ptr<int32_t>(p, st, i++); v.pose_prob = seg_ptr<int32_t>(p, st, i++);
+  unsigned char *w = s->d_ws;
+  WorkView &x = s->wv;
+  x.fr_Rf = reinterpret_cast<float *>(w + p->w_frRf);
+  x.fr_Rd = reinterpret_cast<double *>(w + p->w_frRd);
+  x.fr_c = reinterpret_cast<double *>(w + p->w_frc);
+  x.poses_cand = reinterpret_cast<double *>(w + p->w_pcand);
+  x.alpha_cand = reinterpret_cast<double *>(w + p->w_acand);
+  x.pair_acc = w + p->w_pacc;
+  x.pair64 = reinterpret_cast<double *>(w + p->w_p64);
+  x.A = reinterpret_cast<double *>(w + p->w_A);
+  x.g = reinterpret_cast<double *>(w + p->w_g);
+  x.SL = w + p->w_SL;
+  x.gL = w + p->w_gL;
+  x.S = reinterpret_cast<double *>(w + p->w_S);
+  x.gS = reinterpret_cast<double *>(w + p->w_gS);
+  x.fac = w + p->w_fac;
+  x.delta = reinterpret_cast<double *>(w + p->w_delta);
+  x.C = w + p->w_C;
+  x.ga = w + p->w_ga;
+  x.slab = w + p->w_slab;
+  x.lm = reinterpret_cast<LMState *>(w + p->w_lm);
+  x.cost_acc = reinterpret_cast<double *>(w + p->w_cost);
+  x.pred_acc = reinterpret_cast<double *>(w + p->w_pred);
+}
+
+// one linearisation + reduced system (+ damping from the device-side lambda)
+template <typename T>
+static int enqueue_linearize(spgo_solver *s, cudaStream_t st) {
+  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_RELIN, st)); }
+  { PROF(K_LINEARIZE); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 0, GATE_RELIN, st)); }
+  { PROF(K_SYSTEM); CUDA_TRY(launch_system<T>(s->pv, s->wv, GATE_RELIN, st)); }
+  { PROF(K_BOOKKEEP); CUDA_TRY(launch_post_linearize(s->pv, s->wv, st)); }
+  return SPGO_OK;
+}
+
+template <typename T>
+static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
+  const int mixed = s->plan->precision == SPGO_PREC_MIXED;
+  { PROF(K_SCHUR); CUDA_TRY(launch_schur<T>(s->pv, s->wv, s->prm, st)); }
+  { PROF(K_ASSEMBLE); CUDA_TRY(launch_assemble<T>(s->pv, s->wv, st)); }
+  { PROF(K_FACTOR); CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st)); }
+  return SPGO_OK;
+}
+
+template <typename T>
+static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
+  int rc;
+  if ((rc = enqueue_linearize<T>(s, st)) != SPGO_OK) return rc;
+  if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
+  { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st)); }
+  { PROF(K_UPDATE); CUDA_TRY(launch_update_poses(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
+  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, st)); }
+  { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st)); }
+  { PROF(K_BOOKKEEP); CUDA_TRY(launch_decide(s->pv, s->wv, s->prm, st)); }
+  { PROF(K_BOOKKEEP); CUDA_TRY(launch_commit(s->pv, s->wv, s->poses, s->alpha, st)); }
+  return SPGO_OK;
+}
+
+template <typename T>
+static int enqueue_gn(spgo_solver *s, int iters, float step_size, cudaStream_t st) {
+  for (int it = 0; it < iters; ++it) {
+    { PROF(K_BOOKKEEP); CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, 0.0, st)); }
+    int rc;
+    if ((rc = enqueue_linearize<T>(s, st)) != SPGO_OK) return rc;
+    if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
+    { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->alpha, 1, st)); }
+    { PROF(K_UPDATE); CUDA_TRY(launch_update_poses(s->pv, s->wv, s->poses, s->poses, (double)step_size, 1, st)); }
+  }
+  return SPGO_OK;
+}
+
+extern "C" {
+
+int spgo_version(void) { return 1; }
+
+const char *spgo_last_error(void) { return g_err.c_str(); }
+
+void spgo_default_params(spgo_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->loss = SPGO_LOSS_L2;
+  p->near_boost = 0;
+  p->loss_scale = 3.0f;
+  p->eps = 1e-4f;
+  p->alpha_min = 1.0f / 30.0f;
+  p->alpha_max = 1.0f / 0.2f;
+  p->lambda0 = 1e-4;
+  p->lambda_max = 1e16;
+  p->tol = 1e-6;
+  p->max_iters = 30;
+  p->refine_steps = 1;
+}
+
+int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
+  if (!out) return fail(SPGO_ERR_INVALID_ARG, "out is null");
+  *out = nullptr;
+  spgo_plan *p = new (std::nothrow) spgo_plan();
+  if (!p) return fail(SPGO_ERR_INVALID_ARG, "host allocation failed");
+  int rc;
+  try {
+    rc = plan_build(problems, n_problems, precision, p);
+  } catch (const std::exception &e) {
+    rc = fail(SPGO_ERR_INVALID_ARG, e.what());
+  }
+  if (rc != SPGO_OK) {
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return SPGO_OK;
+}
+
+int spgo_plan_sizes_get(const spgo_plan *p, spgo_plan_sizes *o) {
+  if (!p || !o) return fail(SPGO_ERR_INVALID_ARG, "null argument");
+  std::memset(o, 0, sizeof(*o));
+  o->n_problems = p->B;
+  o->total_poses = p->NP;
+  o->total_landmarks = p->L;
+  o->total_obs = p->O;
+  o->n_chunks = (int32_t)p->ch_prob.size();
+  o->n_schur_items = (int32_t)p->wk_prob.size();
+  o->max_params = p->max_P;
+  o->static_bytes = p->static_bytes;
+  o->workspace_bytes = p->ws_bytes;
+  o->slab_elems = p->total_slab;
+  o->pair_records = p->total_pairs;
+  return SPGO_OK;
+}
+
+int spgo_plan_offsets(const spgo_plan *p, int32_t *lm_off, int32_t *pose_off) {
+  if (!p) return fail(SPGO_ERR_INVALID_ARG, "null plan");
+  for (int b = 0; b < p->B; ++b) {
+    if (lm_off) lm_off[b] = p->p_lm_off[b];
+    if (pose_off) pose_off[b] = p->p_pose_off[b];
+  }
+  return SPGO_OK;
+}
+
+int spgo_plan_destroy(spgo_plan *p) {
+  delete p;
+  return SPGO_OK;
+}
+
+int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_bytes, void *d_workspace,
+                       size_t workspace_bytes, double *d_poses, double *d_alpha, void *stream, spgo_solver **out) {
+  if (!out || !plan || !d_poses || !d_alpha) return fail(SPGO_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  if (static_bytes < plan->static_bytes || workspace_bytes < plan->ws_bytes)
+    return fail(SPGO_ERR_BUFFER_SMALL, "device buffers smaller than spgo_plan_sizes_get reports");
+  if ((plan->static_bytes && !d_static) || (plan->ws_bytes && !d_workspace))
+    return fail(SPGO_ERR_INVALID_ARG, "null device buffer");
+  if (((uintptr_t)d_static & 255) || ((uintptr_t)d_workspace & 255))
+    return fail(SPGO_ERR_INVALID_ARG, "device buffers must be 256-byte aligned");
+  spgo_solver *s = new (std::nothrow) spgo_solver();
+  if (!s) return fail(SPGO_ERR_INVALID_ARG, "host allocation failed");
+  s->plan = plan;
+  s->d_static = (unsigned char *)d_static;
+  s->d_ws = (unsigned char *)d_workspace;
+  s->poses = d_poses;
+  s->alpha = d_alpha;
+  spgo_params dp;
+  spgo_default_params(&dp);
+  std::memcpy(&s->prm, &dp, sizeof(Params));
+  cudaStream_t st = (cudaStream_t)stream;
+  for (const Seg &g : plan->segs)
+    if (g.bytes) {
+      cudaError_t e = cudaMemcpyAsync(s->d_static + g.off, g.src, g.bytes, cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) {
+        delete s;
+        return fail(SPGO_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
+      }
+    }
+  cudaError_t e = cudaMemsetAsync(s->d_ws, 0, plan->ws_bytes, st);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(SPGO_ERR_CUDA, std::string("workspace clear: ") + cudaGetErrorString(e));
+  }
+  make_views(s);
+  s->launches0 = g_launches;
+  *out = s;
+  return SPGO_OK;
+}
+
+int spgo_solver_destroy(spgo_solver *s) {
+  if (s)
+    for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+  delete s;
+  return SPGO_OK;
+}
+
+int spgo_profile_enable(spgo_solver *s, int32_t capacity) {
+  if (!s || capacity < 0) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+  s->ev.assign((size_t)capacity * 2, nullptr);
+  s->ev_kind.assign((size_t)capacity, 0);
+  for (auto &e : s->ev) CUDA_TRY(cudaEventCreate(&e));
+  s->ev_used = 0;
+  s->prof = capacity > 0;
+  return SPGO_OK;
+}
+
+int spgo_profile_read(spgo_solver *s, double *ms, int64_t *count, int32_t n_kinds, void *stream) {
+  if (!s || !ms || !count || n_kinds < K_NKINDS) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  for (int k = 0; k < n_kinds; ++k) {
+    ms[k] = 0.0;
+    count[k] = 0;
+  }
+  for (size_t i = 0; i + 1 < s->ev_used; i += 2) {
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, s->ev[i], s->ev[i + 1]));
+    ms[s->ev_kind[i / 2]] += t;
+    count[s->ev_kind[i / 2]] += 1;
+  }
+  s->ev_used = 0;
+  return SPGO_OK;
+}
+
+int spgo_set_params(spgo_solver *s, const spgo_params *p) {
+  if (!s || !p) return fail(SPGO_ERR_INVALID_ARG, "null argument");
+  if (p->loss < 0 || p->loss > 2) return fail(SPGO_ERR_INVALID_ARG, "unknown loss");
+  if (!(p->loss_scale > 0) || !(p->eps >= 0) || !(p->alpha_min < p->alpha_max) || p->max_iters < 0 ||
+      p->refine_steps < 0 || !(p->lambda0 >= 0))
+    return fail(SPGO_ERR_INVALID_ARG, "parameter out of range");
+  static_assert(sizeof(Params) == sizeof(spgo_params), "params layout");
+  std::memcpy(&s->prm, p, sizeof(Params));
+  return SPGO_OK;
+}
+
+int spgo_gn_step(spgo_solver *s, int32_t iterations, float step_size, void *stream) {
+  if (!s || iterations < 0) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  return s->plan->precision == SPGO_PREC_FP64 ? enqueue_gn<double>(s, iterations, step_size, st)
+                                              : enqueue_gn<float>(s, iterations, step_size, st);
+}
+
+int spgo_lm_reset(spgo_solver *s, void *stream) {
+  if (!s) return fail(SPGO_ERR_INVALID_ARG, "null solver");
+  CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, stream));
+  return SPGO_OK;
+}
+
+int spgo_lm_iterate(spgo_solver *s, int32_t n_iters, void *stream) {
+  if (!s || n_iters < 0) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int it = 0; it < n_iters; ++it) {
+    int rc = s->plan->precision == SPGO_PREC_FP64 ? enqueue_lm_iteration<double>(s, st)
+                                                  : enqueue_lm_iteration<float>(s, st);
+    if (rc != SPGO_OK) return rc;
+  }
+  return SPGO_OK;
+}
+
+int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream) {
+  if (!s || !out) return fail(SPGO_ERR_INVALID_ARG, "null argument");
+  std::vector<LMState> h(s->plan->B);
+  CUDA_TRY(cudaMemcpyAsync(h.data(), s->wv.lm, h.size() * sizeof(LMState), cudaMemcpyDeviceToHost,
+                           (cudaStream_t)stream));
+  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  for (int b = 0; b < s->plan->B; ++b) {
+    out[b].cost0 = h[b].cost0;
+    out[b].cost = h[b].cost;
+    out[b].lambda = h[b].lam;
+    out[b].iterations = h[b].iters;
+    out[b].accepted = h[b].accepted;
+    out[b].status = h[b].status;
+    out[b].factor_failures = h[b].factor_failures;
+  }
+  return SPGO_OK;
+}
+
+int spgo_lm_solve(spgo_solver *s, int32_t check_every, int32_t *iters_done, void *stream) {
+  if (!s) return fail(SPGO_ERR_INVALID_ARG, "null solver");
+  if (check_every < 1) check_every = 1;
+  int rc = spgo_lm_reset(s, stream);
+  if (rc != SPGO_OK) return rc;
+  std::vector<spgo_problem_status> stv(s->plan->B);
+  int done = 0;
+  while (done < s->prm.max_iters) {
+    const int n = std::min(check_every, s->prm.max_iters - done);
+    if ((rc = spgo_lm_iterate(s, n, stream)) != SPGO_OK) return rc;
+    done += n;
+    if ((rc = spgo_lm_status(s, stv.data(), stream)) != SPGO_OK) return rc;
+    bool running = false;
+    for (const auto &x : stv) running |= (x.status == SPGO_STATUS_RUNNING);
+    if (!running) break;
+  }
+  if (iters_done) {
+    int mx = 0;
+    for (const auto &x : stv) mx = std::max(mx, (int)x.iterations);
+    *iters_done = mx;
+  }
+  return SPGO_OK;
+}
+
+int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, double *B, double *C, double *g_a,
+                       double *cost, void *stream) {
+  if (!s || problem < 0 || problem >= s->plan->B) return fail(SPGO_ERR_INVALID_ARG, "bad problem index");
+  cudaStream_t st = (cudaStream_t)stream;
+  const spgo_plan *p = s->plan;
+  // linearise every problem at its current state (lambda untouched: reset sets lambda0)
+  CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, st));
+  int rc = p->precision == SPGO_PREC_FP64 ? enqueue_linearize<double>(s, st) : enqueue_linearize<float>(s, st);
+  if (rc != SPGO_OK) return rc;
+  const int N = p->p_npose[problem], P = 6 * N, L = p->p_lm_cnt[problem];
+  if (A) CUDA_TRY(cudaMemcpyAsync(A, s->wv.A + p->p_S_off[problem], (size_t)P * P * 8, cudaMemcpyDeviceToDevice, st));
+  if (g) CUDA_TRY(cudaMemcpyAsync(g, s->wv.g + p->p_param_off[problem], (size_t)P * 8, cudaMemcpyDeviceToDevice, st));
+  if (B) CUDA_TRY(cudaMemsetAsync(B, 0, (size_t)P * L * 8, st));
+  rc = p->precision == SPGO_PREC_FP64
+           ? launch_export_B_n<double>(s->pv, s->wv, problem, p->p_chunk_cnt[problem], B, C, g_a, st)
+           : launch_export_B_n<float>(s->pv, s->wv, problem, p->p_chunk_cnt[problem], B, C, g_a, st);
+  CUDA_TRY(rc);
+  if (cost)
+    CUDA_TRY(cudaMemcpyAsync(cost, &s->wv.lm[problem].cost, sizeof(double), cudaMemcpyDeviceToDevice, st));
+  return SPGO_OK;
+}
+
+int64_t spgo_launch_count(const spgo_solver *s) { return s ? g_launches - s->launches0 : 0; }
+
+}  // extern "C"

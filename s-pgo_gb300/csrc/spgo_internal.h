@@ -1,0 +1,126 @@
+// Internal definitions shared by the planner (host C++) and the CUDA kernels.
+//
+// Data layout in HBM (all offsets are element offsets into per-kind arrays):
+//   frames      f = frame_off[b] + k, k = 0..N_b           (N_b + 1 frames per problem)
+//   poses       p = pose_off[b] + k,  k = 0..N_b - 1       (12 doubles: 3x4 row-major)
+//   params      param_off[b] + 6k + {psi0..2, rho0..2}     (P_b = 6 N_b)
+//   dense PxP   S_off[b] + r * P_b + c                     (A, S_L, S, factor)
+//   landmarks   internal order = problem-major, sorted by Jacobian window;
+//               lm_user[li] maps to the caller's (problem-major) order
+//   obs         grouped by internal landmark, frames ascending
+//   pairs       pair_off[b] + lo * D_b + (d - 1), d = hi - lo in [1, D_b]: the
+//               (lo, hi) accumulators of the incremental-chain Hessian
+//   chunks      <= 32 landmarks of one problem with windows inside
+//               [f0, f0 + nb); slab = (6 nb) x 32 row-major (landmark-contiguous)
+#pragma once
+#include <stdint.h>
+#include <stddef.h>
+#include "spgo.h"
+
+#define SPGO_CHUNK 32          // landmarks per chunk (slab columns)
+#define SPGO_TILE_BLOCKS 8     // pose blocks per Schur output tile (48 rows)
+#define SPGO_KSPLIT 16         // chunks per Schur work item
+
+namespace spgo {
+
+// which problems a kernel works on: all, those needing a relinearisation, those still running
+enum Gate { GATE_ALL = 0, GATE_RELIN = 1, GATE_RUNNING = 2 };
+
+struct PlanView {                 // device pointers into the static buffer
+  int32_t B, F, NP, L;
+  int64_t O;
+  int32_t n_chunks, n_items, max_P, max_D, max_nb, n_work_chunks;
+  int64_t total_S, total_pairs;
+  int32_t total_params;
+  // per problem
+  const int32_t *p_npose, *p_frame_off, *p_pose_off, *p_lm_off, *p_lm_cnt, *p_pair_D,
+      *p_param_off, *p_chunk_off, *p_chunk_cnt;
+  const int64_t *p_S_off, *p_pair_off;
+  const float *p_intr;    // [B][8]
+  const double *p_Trl;    // [B][12]
+  // per landmark (internal order)
+  const int32_t *lm_prob, *lm_host, *lm_lo, *lm_hi, *lm_user, *lm_chunk, *lm_slot;
+  const float *lm_uv;     // [L][2]
+  const int64_t *lm_obs;  // [L+1]
+  // per observation
+  const int32_t *obs_frame;
+  const float *obs_uv;    // [O][4]
+  // chunks
+  const int32_t *ch_prob, *ch_f0, *ch_nb, *ch_lm0, *ch_cnt;
+  const int64_t *ch_slab;
+  // Schur work items
+  const int32_t *wk_prob, *wk_ti, *wk_tj, *wk_cbeg, *wk_cend, *wk_chunks;
+  // frame -> problem
+  const int32_t *fr_prob;
+  const int32_t *pose_prob;
+};
+
+struct LMState {
+  double lam, nu, cost, cost_cand, pred, cost0, cost_lin;
+  int32_t iters, accepted, status, relin, fail, flag, factor_failures, pad;
+};
+
+// per-iteration scratch (precision-dependent arrays typed at the kernel)
+struct WorkView {
+  // frame tables: [F][2 cams] rotation (cam->world) and centre
+  float *fr_Rf;     // [F][2][9]
+  double *fr_Rd;    // [F][2][9]
+  double *fr_c;     // [F][2][3]
+  double *poses_cand;   // [NP][12]
+  double *alpha_cand;   // [L] (caller order)
+  void *pair_acc;       // [total_pairs][27] T
+  double *pair64;       // [total_pairs][27]
+  double *A;            // [total_S]
+  double *g;            // [total_params]
+  void *SL;             // [total_S] T
+  void *gL;             // [total_params] T
+  double *S;            // [total_S]
+  double *gS;           // [total_params]
+  void *fac;            // [total_S] T   (global-memory factor for large problems)
+  double *delta;        // [total_params]
+  void *C;              // [L] T
+  void *ga;             // [L] T
+  void *slab;           // [sum slab] T
+  LMState *lm;          // [B]
+  double *cost_acc;     // [B]
+  double *pred_acc;     // [B]
+};
+
+struct Params {
+  int32_t loss, near_boost;
+  float loss_scale, eps, alpha_min, alpha_max;
+  double lambda0, lambda_max, tol;
+  int32_t max_iters, refine_steps;
+};
+
+// launch wrappers (defined in the .cu files); all return cudaError_t as int
+int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, void *stream);
+template <typename T>
+int launch_linearize(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
+                     int cost_only, int gate, void *stream);
+template <typename T>
+int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream);
+template <typename T>
+int launch_schur(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
+template <typename T>
+int launch_assemble(const PlanView &pv, const WorkView &wv, void *stream);
+template <typename T>
+int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed,
+                        void *stream);
+template <typename T>
+int launch_backsub(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
+                   double *alpha_out, int direct, void *stream);
+int launch_update_poses(const PlanView &pv, const WorkView &wv, const double *poses, double *poses_out,
+                        double scale, int direct, void *stream);
+int launch_decide(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
+int launch_commit(const PlanView &pv, const WorkView &wv, double *poses, double *alpha, void *stream);
+int launch_post_linearize(const PlanView &pv, const WorkView &wv, void *stream);
+int launch_reset(const PlanView &pv, const WorkView &wv, const Params &prm, double lam, void *stream);
+template <typename T>
+int launch_export_B_n(const PlanView &pv, const WorkView &wv, int problem, int n_chunks, double *B,
+                      double *C, double *ga, void *stream);
+
+// count of kernel launches made by this library in this process
+extern int64_t g_launches;
+
+}  // namespace spgo

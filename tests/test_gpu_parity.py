@@ -1,0 +1,258 @@
+"""CUDA path against the FP64 oracle (and the reference's own golden vectors),
+through the C ABI.  Tolerances: FP64 path 1e-9 relative; mixed path (FP32
+Jacobians / Hessian blocks) 1e-4 relative on H and g blocks (relative to the
+largest entry), 1e-6 relative on the FP64 cost; converged LM state: cost 1e-6
+relative, poses 1e-5 rad / 1e-5 m."""
+import os
+import types
+
+import numpy as np
+import pytest
+
+import spgo_gb300.native as nat
+import spgo_gb300.scenes as scenes
+from spgo_gb300 import se3
+from spgo_gb300.problem import Problem
+from spgo_gb300.solver import BatchSolver, CudaSolver
+from oracle import solver as S
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+LOSSES = {
+    "l2": (S.Loss(), dict(loss="l2", near_boost=False)),
+    "cauchy_ref_gpu": (S.REFERENCE_GPU_LOSS, dict(loss="cauchy", loss_scale=3.0, near_boost=True)),
+    "huber": (S.Loss(S.LOSS_HUBER, 2.0), dict(loss="huber", loss_scale=2.0, near_boost=False)),
+}
+TOL = {"fp64": 1e-9, "mixed": 1e-4}
+
+
+def relmax(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def check_system(sys_, lin, prec):
+    t = TOL[prec]
+    assert relmax(sys_["A"], lin.A) < t
+    assert relmax(sys_["g"], lin.g_T) < t
+    assert relmax(sys_["B"], lin.B) < t
+    assert relmax(sys_["C"], lin.C) < t
+    assert relmax(sys_["g_a"], lin.g_a) < t
+    assert abs(sys_["cost"] - lin.cost) / lin.cost < (1e-12 if prec == "fp64" else 1e-6)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("loss", list(LOSSES))
+def test_linear_system_matches_oracle(built_lib, cuda_device, prec, loss):
+    ol, kw = LOSSES[loss]
+    p = scenes.circle_scene(21, 7, 90)     # targets before and after the anchor
+    bs = BatchSolver([p], precision=prec)
+    bs.set_params(**kw)
+    check_system(bs.export_system(0), S.linearize(f32_obs(p), ol), prec)
+
+
+@pytest.mark.parametrize("name", ["ref_small", "ref_medium"])
+def test_linear_system_matches_reference_golden(built_lib, cuda_device, name):
+    """GPU H_TT, g_TT, H_aa, g_aa, BB against getHessians of the reference."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    p = Problem(n_poses=int(z["n_poses"]), intrinsics=z["intrinsics"], T_rl=z["T_rl"], host=z["host"],
+                anchor_uv=z["anchor_uv"], obs_ptr=z["obs_ptr"], obs_frame=z["obs_frame"], obs_uv=z["obs_uv"],
+                poses=z["poses"], alpha=z["alpha"])
+    bs = BatchSolver([p], precision="fp64")
+    bs.set_params(loss="cauchy", loss_scale=3.0, near_boost=False)
+    s = bs.export_system(0)
+    # Pixels cross the C ABI as float32, as in the reference binding (Solver.pyx:34-38);
+    # that rounding alone moves these FP64 blocks by up to 4e-6 relative, so the
+    # reference's values are matched at 1e-5 and the oracle on the rounded inputs at 1e-9.
+    for key, ref in (("A", "ref_H_TT"), ("g", "ref_g_TT"), ("C", "ref_H_aa_diag"), ("g_a", "ref_g_aa"),
+                     ("B", "ref_BB")):
+        assert relmax(s[key], z[ref]) < 1e-5, key
+    check_system(s, S.linearize(f32_obs(p), S.REFERENCE_CPU_LOSS), "fp64")
+
+
+def f32_obs(p):
+    """The problem with observations rounded to float32, as the device sees them."""
+    q = p.copy()
+    q.obs_uv = p.obs_uv.astype(np.float32).astype(np.float64)
+    q.anchor_uv = p.anchor_uv.astype(np.float32).astype(np.float64)
+    q.intrinsics = p.intrinsics.astype(np.float32).astype(np.float64)
+    return q
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 2e-4)])
+def test_gn_step_matches_oracle(built_lib, cuda_device, prec, tol):
+    """The reference step(): undamped GN, C + 1e-4, pose step size 0.5."""
+    p = f32_obs(scenes.circle_scene(31, 6, 80))
+    ref = p.copy()
+    S.reference_gn_step(ref, iterations=3, step_size=0.5)
+    bs = BatchSolver([p], precision=prec)
+    bs.set_params(loss="cauchy", loss_scale=3.0, near_boost=True, eps=1e-4)
+    bs.gn_step(3, 0.5)
+    P = bs.get_poses(0)
+    assert np.abs(P - ref.poses).max() < tol
+    assert relmax(bs.get_alpha(0), ref.alpha) < tol
+
+
+def pose_errors(P, Q):
+    e = np.array([se3.pose_error(P[k], Q[k]) for k in range(len(P))])
+    return e[:, 0].max(), e[:, 1].max()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_lm_solve_matches_oracle_config0(built_lib, cuda_device, prec):
+    """Config 0 (10 LM iterations, lambda0 = 1e-4) reaches the oracle's cost; run on to a
+    1e-10 stopping rule, the states agree to 1e-5 rad / 1e-5 m (a 1e-6 rule alone leaves
+    about 1e-5 m of slack along flat directions)."""
+    p = f32_obs(scenes.config0())
+    ref = p.copy()
+    res = S.lm_solve(ref, S.Loss(), max_iters=10, tol=1e-6, lam0=1e-4)
+    bs = BatchSolver([p], precision=prec)
+    bs.set_params(loss="l2", max_iters=10, tol=1e-6, lambda0=1e-4)
+    st = bs.solve()[0]
+    assert st["status"] in (nat.STATUS_CONVERGED, nat.STATUS_MAX_ITERS)
+    assert abs(st["cost"] - res.cost) / res.cost < 1e-6
+    # FP32 residuals at the ~40 px initial errors carry ~2e-6 relative rounding
+    assert abs(st["cost0"] - res.cost0) / res.cost0 < (1e-9 if prec == "fp64" else 1e-5)
+    if prec == "fp64":
+        assert st["iterations"] == res.iterations and st["accepted"] == res.accepted
+    ref2 = ref.copy()
+    S.lm_solve(ref2, S.Loss(), max_iters=30, tol=1e-10)
+    bs.set_params(max_iters=30, tol=1e-10)
+    bs.solve()
+    er, et = pose_errors(bs.get_poses(0), ref2.poses)
+    assert er < 1e-5 and et < 1e-5
+    assert relmax(bs.get_alpha(0), ref2.alpha) < 1e-5
+
+
+def test_batched_equals_individual(built_lib, cuda_device):
+    """Uneven problems in one batch reach each problem's own oracle optimum."""
+    probs = [f32_obs(scenes.circle_scene(s, n, l)) for s, n, l in
+             [(200, 8, 500), (204, 11, 324), (205, 18, 455), (209, 21, 279), (210, 28, 410), (214, 31, 234)]]
+    bs = BatchSolver(probs, precision="mixed")
+    bs.set_params(loss="l2", max_iters=30, tol=1e-6)
+    sts = bs.solve()
+    refs = []
+    for b, p in enumerate(probs):
+        ref = p.copy()
+        res = S.lm_solve(ref, S.Loss(), max_iters=30, tol=1e-6)
+        refs.append(ref)
+        assert sts[b]["status"] == nat.STATUS_CONVERGED
+        assert abs(sts[b]["cost"] - res.cost) / res.cost < 1e-6
+    bs.set_params(max_iters=40, tol=1e-10)
+    bs.solve()
+    for b, ref in enumerate(refs):
+        S.lm_solve(ref, S.Loss(), max_iters=40, tol=1e-10)
+        er, et = pose_errors(bs.get_poses(b), ref.poses)
+        assert er < 1e-5 and et < 1e-5
+
+
+def test_huber_outliers_converge(built_lib, cuda_device):
+    p = f32_obs(scenes.corridor_scene(7, 40, 1500, window=20, outlier_frac=0.05))
+    ref = p.copy()
+    res = S.lm_solve(ref, S.Loss(S.LOSS_HUBER, 2.0), max_iters=30, tol=1e-6)
+    bs = BatchSolver([p], precision="mixed")
+    bs.set_params(loss="huber", loss_scale=2.0, max_iters=30, tol=1e-6)
+    st = bs.solve()[0]
+    assert abs(st["cost"] - res.cost) / res.cost < 1e-6
+    S.lm_solve(ref, S.Loss(S.LOSS_HUBER, 2.0), max_iters=40, tol=1e-10)
+    bs.set_params(max_iters=40, tol=1e-10)
+    bs.solve()
+    er, et = pose_errors(bs.get_poses(0), ref.poses)
+    assert er < 1e-5 and et < 1e-5
+
+
+def test_cudasolver_dropin_flow(built_lib, cuda_device):
+    """CUDAmanager.py-style use: calibration, writeObservations, identity poses, step(k)."""
+    truth = scenes.circle_scene(41, 5, 60)
+    N, M = truth.n_poses, 12
+    s = CudaSolver(N, M)
+    s.loadCalibration(truth.intrinsics.astype(np.float32), truth.T_rl.reshape(16).astype(np.float32))
+    for l in range(truth.n_landmarks):
+        a = int(truth.host[l])
+        for o in range(truth.obs_ptr[l], truth.obs_ptr[l + 1]):
+            uv = truth.obs_uv[o].astype(np.float32)
+            lo_ = uv[:2] if truth.obs_frame[o] != a else truth.anchor_uv[l].astype(np.float32)
+            s.writeObservations(a, int(truth.obs_frame[o]), l, np.r_[lo_, 1.0].astype(np.float32),
+                                np.r_[uv[2:], 1.0].astype(np.float32))
+    for k in range(N):
+        s.writeIncrementalPose(k, truth.poses[k].reshape(16).astype(np.float32))
+    alpha = np.ones(N * M, np.float32)
+    alpha[:truth.n_landmarks] = truth.alpha
+    s.loadInverseDepths(alpha)
+    s.setStepSize(0.5)
+    s.step(2)
+    ref = f32_obs(truth)
+    ref.poses = truth.poses.astype(np.float32).astype(np.float64)
+    ref.alpha = truth.alpha.astype(np.float32).astype(np.float64)
+    S.reference_gn_step(ref, iterations=2, step_size=0.5)
+    for k in range(N):
+        assert np.abs(s.getIncrementalPose(k) - ref.poses[k]).max() < 2e-4
+    got = s.getInverseDepths()
+    assert np.abs(got[:truth.n_landmarks] - ref.alpha).max() / np.abs(ref.alpha).max() < 2e-4
+    assert np.all(got[truth.n_landmarks:] == 1.0)
+
+
+def test_edge_cases(built_lib, cuda_device):
+    """A landmark seen only in its host, a single-pose problem and a landmark-free problem."""
+    p = scenes.circle_scene(51, 5, 40)
+    # landmark 0: keep only the host observation
+    l0 = slice(p.obs_ptr[0], p.obs_ptr[1])
+    keep = np.ones(p.n_obs, bool)
+    idx = np.arange(p.obs_ptr[0], p.obs_ptr[1])
+    keep[idx[p.obs_frame[idx] != p.host[0]]] = False
+    p.obs_frame = p.obs_frame[keep]
+    p.obs_uv = p.obs_uv[keep]
+    cnt = np.diff(p.obs_ptr)
+    cnt[0] = 1
+    p.obs_ptr = np.r_[0, np.cumsum(cnt)]
+    single = scenes.circle_scene(52, 1, 30)
+    empty = Problem(n_poses=2, intrinsics=p.intrinsics, T_rl=p.T_rl, host=np.zeros(0, np.int32),
+                    anchor_uv=np.zeros((0, 2)), obs_ptr=np.zeros(1, np.int64), obs_frame=np.zeros(0, np.int32),
+                    obs_uv=np.zeros((0, 4)), poses=np.tile(np.eye(4), (2, 1, 1)), alpha=np.zeros(0))
+    for prec in ("fp64", "mixed"):
+        for q in (p, single):
+            lin = S.linearize(f32_obs(q), S.Loss())
+            bs = BatchSolver([q], precision=prec)
+            check_system(bs.export_system(0), lin, prec)
+        bs = BatchSolver([p, empty, single], precision=prec)
+        bs.set_params(max_iters=5)
+        st = bs.solve()
+        assert np.isfinite(bs.get_poses(0)).all() and np.isfinite(bs.get_alpha(2)).all()
+        assert st[1]["cost"] == 0.0
+
+
+def test_unconstrained_pose_is_rejected_not_nan(built_lib, cuda_device):
+    """A pose no observation constrains makes S singular: every step is rejected,
+    lambda grows until the problem is reported stalled; the state stays finite."""
+    p = scenes.circle_scene(61, 4, 60)
+    # drop every observation whose range covers pose 3 (frames 3-4 vs others)
+    lm = np.repeat(np.arange(p.n_landmarks), np.diff(p.obs_ptr))
+    a = p.host[lm]
+    lo, hi = np.minimum(a, p.obs_frame), np.maximum(a, p.obs_frame)
+    keep = ~((lo <= 3) & (3 < hi))
+    p.obs_frame, p.obs_uv = p.obs_frame[keep], p.obs_uv[keep]
+    cnt = np.bincount(lm[keep], minlength=p.n_landmarks)
+    p.obs_ptr = np.r_[0, np.cumsum(cnt)]
+    bs = BatchSolver([p], precision="mixed")
+    bs.set_params(max_iters=40, lambda_max=1e6)
+    st = bs.solve()[0]
+    assert st["factor_failures"] > 0
+    assert st["status"] in (nat.STATUS_STALLED, nat.STATUS_MAX_ITERS, nat.STATUS_CONVERGED)
+    assert np.isfinite(bs.get_poses(0)).all()
+
+
+def test_config1_full_size(built_lib, cuda_device):
+    """config 1 at full size (N = 100, 20k landmarks, ~400k observations):
+    size-independent properties (monotone cost, FP64 cost re-evaluated by the
+    oracle at the returned state, pose error against ground truth)."""
+    p = scenes.config1()
+    bs = BatchSolver([p], precision="mixed")
+    bs.set_params(loss="l2", max_iters=20, tol=1e-6)
+    st = bs.solve()[0]
+    assert st["status"] in (nat.STATUS_CONVERGED, nat.STATUS_MAX_ITERS)
+    assert st["cost"] < 1e-2 * st["cost0"]
+    q = f32_obs(p)
+    q.poses, q.alpha = bs.get_poses(0), bs.get_alpha(0)
+    assert abs(S.cost(q, S.Loss()) - st["cost"]) / st["cost"] < 1e-6
+    er, et = pose_errors(q.poses, p.gt_poses)
+    assert er < 5e-3 and et < 5e-2

@@ -1,0 +1,109 @@
+"""The C-ABI library without a GPU: it builds, loads, exports every symbol the
+header declares, and its host-side planner validates input like the
+reference's asserts (src/Optimization/Solver.cpp:41-44)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import spgo_gb300.native as nat
+import spgo_gb300.scenes as scenes
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "spgo.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(spgo_[a-z_]+)\s*\(", src)))
+
+
+def test_exports_every_declared_symbol(built_lib):
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(built_lib, n), n
+    assert set(names) == set(nat.EXPORTED)
+    assert built_lib.spgo_version() == 1
+
+
+def host_problem(p, keep):
+    arrs = dict(intr=np.ascontiguousarray(p.intrinsics, np.float32),
+                trl=np.ascontiguousarray(p.T_rl, np.float64).reshape(16),
+                host=np.ascontiguousarray(p.host, np.int32),
+                auv=np.ascontiguousarray(p.anchor_uv, np.float32).reshape(-1),
+                ptr=np.ascontiguousarray(p.obs_ptr, np.int64),
+                fr=np.ascontiguousarray(p.obs_frame, np.int32),
+                uv=np.ascontiguousarray(p.obs_uv, np.float32).reshape(-1))
+    keep.append(arrs)
+    h = nat.HostProblem()
+    h.n_poses, h.n_landmarks, h.n_obs = int(p.n_poses), p.n_landmarks, p.n_obs
+    h.intrinsics = arrs["intr"].ctypes.data_as(C.POINTER(C.c_float))
+    h.T_r_to_l = arrs["trl"].ctypes.data_as(C.POINTER(C.c_double))
+    h.host = arrs["host"].ctypes.data_as(C.POINTER(C.c_int32))
+    h.anchor_uv = arrs["auv"].ctypes.data_as(C.POINTER(C.c_float))
+    h.obs_ptr = arrs["ptr"].ctypes.data_as(C.POINTER(C.c_int64))
+    h.obs_frame = arrs["fr"].ctypes.data_as(C.POINTER(C.c_int32))
+    h.obs_uv = arrs["uv"].ctypes.data_as(C.POINTER(C.c_float))
+    return h
+
+
+def plan(problems, prec=nat.PREC_MIXED):
+    keep = []
+    arr = (nat.HostProblem * len(problems))(*[host_problem(p, keep) for p in problems])
+    out = C.c_void_p()
+    rc = nat.lib().spgo_plan_create(arr, len(problems), prec, C.byref(out))
+    return rc, out
+
+
+def test_plan_sizes(built_lib):
+    ps = [scenes.circle_scene(s, 8 + s, 100 + 37 * s) for s in range(5)]
+    rc, pl = plan(ps)
+    assert rc == 0
+    sz = nat.PlanSizes()
+    assert built_lib.spgo_plan_sizes_get(pl, C.byref(sz)) == 0
+    assert sz.n_problems == 5
+    assert sz.total_poses == sum(p.n_poses for p in ps)
+    assert sz.total_landmarks == sum(p.n_landmarks for p in ps)
+    assert sz.total_obs == sum(p.n_obs for p in ps)
+    assert sz.n_chunks >= sum((p.n_landmarks + 31) // 32 for p in ps)
+    assert sz.max_params == 6 * 12
+    assert sz.static_bytes > 0 and sz.workspace_bytes > 0
+    lm_off = (C.c_int32 * 5)()
+    pose_off = (C.c_int32 * 5)()
+    assert built_lib.spgo_plan_offsets(pl, lm_off, pose_off) == 0
+    assert list(lm_off) == list(np.cumsum([0] + [p.n_landmarks for p in ps])[:-1])
+    built_lib.spgo_plan_destroy(pl)
+
+
+def test_plan_rejects_bad_input(built_lib):
+    base = scenes.circle_scene(3, 6, 50)
+    bad = base.copy()
+    bad.host = base.host.copy()
+    bad.host[0] = 99
+    assert plan([bad])[0] == -1
+    bad = base.copy()
+    bad.obs_frame = base.obs_frame.copy()
+    bad.obs_frame[1], bad.obs_frame[0] = base.obs_frame[0], base.obs_frame[1]  # not ascending
+    assert plan([bad])[0] == -1
+    bad = base.copy()
+    bad.obs_ptr = base.obs_ptr.copy()
+    bad.obs_ptr[-1] += 1
+    assert plan([bad])[0] == -1
+    msg = built_lib.spgo_last_error().decode()
+    assert "obs_ptr" in msg
+    rc, _ = plan([base], prec=7)
+    assert rc == -1
+
+
+def test_plan_rejects_too_wide_window(built_lib):
+    p = scenes.corridor_scene(1, 120, 400)
+    p.obs_frame = p.obs_frame.copy()
+    # stretch landmark 0 over more than SPGO_MAX_WINDOW poses
+    s, e = p.obs_ptr[0], p.obs_ptr[1]
+    p.host = p.host.copy()
+    p.host[0] = 0
+    p.obs_frame[s:e] = np.linspace(0, 120, e - s).astype(np.int32)
+    if e - s >= 2:
+        assert plan([p])[0] == -2
