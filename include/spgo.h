@@ -190,6 +190,47 @@ int64_t spgo_launch_count(const spgo_solver *s);
 int spgo_profile_enable(spgo_solver *s, int32_t capacity);
 int spgo_profile_read(spgo_solver *s, double *ms, int64_t *count, int32_t n_kinds, void *stream);
 
+/* ---- allocation-free cost evaluation ------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: code running inside a CUDA graph capture it does not own, plugins
+ * whose host framework owns the device memory pool and forbids cudaMalloc,
+ * and real-time threads where an allocation (and the synchronisation it can
+ * imply) is not allowed.  It evaluates the same robust cost as the cost pass
+ * of the solver (0.5 * sum of the weighted robust loss over both cameras of
+ * every observation, FP64) for ONE problem whose arrays the caller already
+ * holds in device memory, at the state d_poses [n_poses*12] (3x4 row-major
+ * incremental poses) and d_alpha [n_landmarks], and writes it to d_cost[0].
+ * Only params->loss, loss_scale and near_boost are read.
+ *
+ * It calls no cudaMalloc/cudaFree or allocating library routine: its scratch
+ * is a file-scope device array of about 0.9 MB that every GPU loading this
+ * library keeps until the process exits, so problems are limited to
+ * n_poses + 1 <= SPGO_NOALLOC_MAX_FRAMES and n_landmarks <=
+ * SPGO_NOALLOC_MAX_LANDMARKS (larger ones return SPGO_ERR_UNSUPPORTED).
+ * The first call on a device looks up that array's device address (no
+ * allocation); make that first call before any stream capture.  All calls
+ * share the array: calls whose kernels overlap on the GPU race, so order them
+ * (one stream, or events).  Enqueue only; d_cost is valid once `stream`
+ * reaches the end of the call. */
+#define SPGO_NOALLOC_MAX_FRAMES     2048
+#define SPGO_NOALLOC_MAX_LANDMARKS  (1 << 21)
+
+typedef struct spgo_device_problem {   /* same fields as spgo_host_problem, DEVICE pointers */
+    int32_t        n_poses;
+    int32_t        n_landmarks;
+    int64_t        n_obs;
+    const float   *intrinsics;   /* [8]   */
+    const double  *T_r_to_l;     /* [16]  */
+    const int32_t *host;         /* [L]   */
+    const float   *anchor_uv;    /* [L*2] */
+    const int64_t *obs_ptr;      /* [L+1] */
+    const int32_t *obs_frame;    /* [O]   */
+    const float   *obs_uv;       /* [O*4] */
+} spgo_device_problem;
+
+int spgo_cost_noalloc(const spgo_device_problem *prob, const double *d_poses, const double *d_alpha,
+                      const spgo_params *params, double *d_cost, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

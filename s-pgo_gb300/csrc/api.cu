@@ -20,13 +20,14 @@
 
 #include "spgo_internal.h"
 
+static thread_local std::string g_err;
+
 namespace spgo {
 int64_t g_launches = 0;
-}
+void set_last_error(const char *msg) { g_err = msg; }
+}  // namespace spgo
 
 using namespace spgo;
-
-static thread_local std::string g_err;
 
 static int fail(int code, const std::string &msg) {
   g_err = msg;

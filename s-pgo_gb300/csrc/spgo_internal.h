@@ -122,5 +122,7 @@ int launch_export_B_n(const PlanView &pv, const WorkView &wv, int problem, int n
 
 // count of kernel launches made by this library in this process
 extern int64_t g_launches;
+// sets the message spgo_last_error returns (thread-local)
+void set_last_error(const char *msg);
 
 }  // namespace spgo

@@ -24,6 +24,7 @@ EXPORTED = [
     "spgo_plan_destroy", "spgo_plan_offsets", "spgo_solver_create", "spgo_solver_destroy", "spgo_set_params",
     "spgo_gn_step", "spgo_lm_reset", "spgo_lm_iterate", "spgo_lm_status", "spgo_lm_solve",
     "spgo_export_system", "spgo_launch_count", "spgo_profile_enable", "spgo_profile_read",
+    "spgo_cost_noalloc",
 ]
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
                  "update", "bookkeeping"]
@@ -54,6 +55,12 @@ class Params(C.Structure):
 class ProblemStatus(C.Structure):
     _fields_ = [("cost0", C.c_double), ("cost", C.c_double), ("lambda_", C.c_double), ("iterations", C.c_int32),
                 ("accepted", C.c_int32), ("status", C.c_int32), ("factor_failures", C.c_int32)]
+
+
+class DeviceProblem(C.Structure):
+    """spgo_device_problem: HostProblem's fields, device pointers."""
+    _fields_ = [(n, t if not n.startswith(("intr", "T_r", "host", "anchor", "obs_p", "obs_f", "obs_u")) else C.c_void_p)
+                for n, t in HostProblem._fields_]
 
 
 class SpgoError(RuntimeError):
@@ -91,6 +98,8 @@ def lib() -> C.CDLL:
     L.spgo_export_system.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
     L.spgo_profile_enable.argtypes = [vp, i32]
     L.spgo_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), i32, vp]
+    L.spgo_cost_noalloc.argtypes = [C.POINTER(DeviceProblem), vp, vp, C.POINTER(Params), vp, vp]
+    L.spgo_cost_noalloc.restype = C.c_int
     L.spgo_launch_count.argtypes = [vp]
     L.spgo_launch_count.restype = i64
     for name in ("spgo_plan_create", "spgo_plan_sizes_get", "spgo_plan_destroy", "spgo_plan_offsets",
