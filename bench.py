@@ -135,16 +135,22 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # algorithmic bytes per launch (roofline numerators)
 # ---------------------------------------------------------------------------
-def algorithmic_bytes(kind: str, sizes, slab_floats: int, ts: int) -> float:
+def roofline_numerator(kind: str, sizes, slab_floats: int, ts: int, probs):
+    """(bound, unit, algorithmic amount per launch) for a profiled kernel kind.
+
+    linearisation / cost: HBM bytes (observations 20 B, landmark record 40 B, C/g_a,
+    slab written); Schur: tensor-shaped FLOPs of the (chunk, 48x48 tile) products;
+    factor_solve: dense Cholesky + two solves + one FP64 residual per problem."""
     O, L = sizes.total_obs, sizes.total_landmarks
-    if kind in ("linearize",):
-        # obs (frame + 4 pixels) + landmark record + C/g_a + the chunk slabs written
-        return 20.0 * O + 40.0 * L + 2.0 * ts * L + ts * slab_floats
+    if kind == "linearize":
+        return "hbm", "GB/s", 20.0 * O + 40.0 * L + 2.0 * ts * L + ts * slab_floats
     if kind == "cost":
-        return 20.0 * O + 40.0 * L
+        return "hbm", "GB/s", 20.0 * O + 40.0 * L
     if kind == "schur":
-        return float(ts * slab_floats)
-    return 0.0
+        return "tensor", "TFLOP/s", 2.0 * 48 * 48 * 32 * sizes.schur_chunk_tiles
+    if kind == "factor_solve":
+        return "tensor", "TFLOP/s", float(sum((6 * p.n_poses) ** 3 / 3.0 + 6 * (6 * p.n_poses) ** 2 for p in probs))
+    return None, None, 0.0
 
 
 def run_reference(args):
@@ -206,16 +212,18 @@ def run_ours(args):
     probs = scenes.config3(seed=_batch_seed(rank))
     n_obs = sum(p.n_obs for p in probs)
     n_lm = sum(p.n_landmarks for p in probs)
+    # a non-default stream: the solver replays its LM iterations as CUDA graphs on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
 
     def make(precision):
-        s = sv.BatchSolver(probs, precision=precision, device=dev)
-        s.set_params(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4)
+        s = sv.BatchSolver(probs, precision=precision, device=dev, stream=stream)
+        s.set_params(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4, use_tc=args.tc)
         return s
 
     bs = make("mixed")
     p0, a0 = bs.poses.clone(), bs.alpha.clone()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
 
     def one_step():
         bs.poses.copy_(p0)
@@ -225,8 +233,6 @@ def run_ours(args):
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize(dev)
-    bs.profile(200000)
-    bs.profile_read()
     launches0 = bs.launch_count()
     clocks = ClockSampler(local)
     clocks.start()
@@ -250,6 +256,13 @@ def run_ours(args):
         torch.distributed.barrier()
     clk = clocks.stop()
     launches = bs.launch_count() - launches0
+    # per-kernel CUDA-event timing (graphs off while the events are recorded): one more
+    # step of the same work, after the timed region
+    bs.profile(200000)
+    bs.profile_read()
+    flush.fill_(7)
+    torch.cuda.synchronize(dev)
+    one_step()
     prof = bs.profile_read()
     bs.profile(0)
     total_ms = float(sum(ms))
@@ -272,21 +285,27 @@ def run_ours(args):
     tot = sum(v[0] for v in prof.values()) or 1.0
     kernels = {k: {"ms": round(v[0], 4), "launches": v[1], "share": round(v[0] / tot, 4)} for k, v in prof.items()}
     dom = max(prof, key=lambda k: prof[k][0])
-    slab_floats = int(bs.slab_floats()) if hasattr(bs, "slab_floats") else 0
-    ts = 4
+    slab_floats = int(bs.slab_floats())
     avg_ms = prof[dom][0] / max(1, prof[dom][1])
-    ab = algorithmic_bytes(dom, bs.sizes, slab_floats, ts)
-    roof = {"kernel": dom, "bound": "hbm", "achieved": (ab / (avg_ms / 1e3) / 1e9) if ab else None,
-            "peak": hbm_peak, "unit": "GB/s", "frac": (ab / (avg_ms / 1e3) / 1e9 / hbm_peak) if ab else None,
+    bound, unit, amount = roofline_numerator(dom, bs.sizes, slab_floats, 4, probs)
+    if bound == "hbm":
+        achieved, peak = amount / (avg_ms / 1e3) / 1e9, hbm_peak
+    elif bound == "tensor":
+        achieved, peak = amount / (avg_ms / 1e3) / 1e12, float(peaks.get("bf16_tflops", 1900.0))
+    else:
+        achieved, peak = None, None
+    roof = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": (achieved / peak) if achieved else None,
             "traffic": None, "avg_launch_ms": avg_ms, "peak_source": peak_src,
-            "note": "algorithmic bytes per launch / CUDA-event launch duration"}
+            "note": "algorithmic bytes per launch / CUDA-event launch duration (profiled step after the "
+                    "timed region, CUDA graphs off)"}
 
     # plain FP64 GPU solver, one problem at a time (untimed for the headline)
     plain = None
     if not args.no_plain:
         plain_costs, t_plain = [], 0.0
         for p in probs:
-            s1 = sv.BatchSolver([p], precision="fp64", device=dev)
+            s1 = sv.BatchSolver([p], precision="fp64", device=dev, stream=stream)
             s1.set_params(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4)
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
@@ -324,7 +343,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
             "data": "synthetic (seeded config-3 generator)",
             "config": {"workload": WORKLOAD, "problems_per_gpu": N_PROBLEMS, "landmarks": n_lm, "obs": n_obs,
-                       "precision": "mixed", "l2": "256 MB flush written between timed steps",
+                       "precision": "mixed", "schur": "tcgen05 TF32" if args.tc else "SIMT FP32",
+                       "l2": "256 MB flush written between timed steps",
                        "parallelism": f"replicas x{world} (independent batches)",
                        "iterations_max": int(max(iters)), "iterations_mean": float(np.mean(iters))},
             "roofline": roof, "kernels": kernels, "gpu_launches": int(launches), "clocks": clk,
@@ -347,6 +367,7 @@ def main():
     ap.add_argument("--check-every", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--tc", type=int, default=0, help="1: tensor-core Schur complement in the mixed path")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -88,7 +88,7 @@ typedef struct spgo_plan_sizes {
     int32_t n_chunks;
     int32_t n_schur_items;
     int32_t max_params;          /* max 6N over problems */
-    int32_t reserved;
+    int32_t schur_chunk_tiles;   /* (chunk, 48x48 output tile) products per Schur pass */
     size_t  static_bytes;        /* device buffer for the uploaded problem data   */
     size_t  workspace_bytes;     /* device buffer for per-iteration scratch       */
     int64_t slab_elems;          /* elements of the landmark-chunk slabs (W blocks) */
@@ -108,6 +108,10 @@ typedef struct spgo_params {
     double  tol;                 /* relative cost decrease that counts as converged */
     int32_t max_iters;           /* per-problem LM iteration cap                 */
     int32_t refine_steps;        /* FP64 iterative-refinement steps (mixed precision) */
+    int32_t use_graph;           /* 1: spgo_lm_iterate replays a captured CUDA graph
+                                    (not on the legacy default stream, not while profiling) */
+    int32_t use_tc;              /* 1: mixed path forms the landmark Schur complement on the
+                                    tensor cores (tcgen05, TF32 in / FP32 accumulate) */
 } spgo_params;
 
 typedef struct spgo_problem_status {
@@ -175,6 +179,12 @@ int spgo_lm_solve(spgo_solver *s, int32_t check_every, int32_t *iters_done, void
  * For parity checks on small problems. */
 int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, double *B,
                        double *C, double *g_a, double *cost, void *stream);
+
+/* Linearise every problem at its current state and export one problem's damped
+ * reduced camera system S = A + lambda diag(A) - B D^-1 B^T, D = C (1 + lambda) + eps,
+ * and g_S = g - B D^-1 g_a, as FP64 into caller-owned DEVICE buffers S [P*P],
+ * gS [P].  For parity checks of the Schur complement. */
+int spgo_export_reduced(spgo_solver *s, int32_t problem, double lambda, double *S, double *gS, void *stream);
 
 /* Count of kernel launches enqueued by this solver since creation. */
 int64_t spgo_launch_count(const spgo_solver *s);

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -66,14 +67,17 @@ struct spgo_plan {
   std::vector<int64_t> lm_obs;
   std::vector<int32_t> obs_frame;
   std::vector<float> obs_uv;
+  std::vector<uint8_t> obs_slot;
   std::vector<int32_t> ch_prob, ch_f0, ch_nb, ch_lm0, ch_cnt;
   std::vector<int64_t> ch_slab;
   std::vector<int32_t> wk_prob, wk_ti, wk_tj, wk_cbeg, wk_cend, wk_chunks;
+  // tensor-core Schur work: (problem, 128-row tile, column range <= 256, chunks)
+  std::vector<int32_t> tc_prob, tc_row0, tc_col0, tc_ncols, tc_cbeg, tc_cend, tc_chunks;
   std::vector<Seg> segs;
   size_t static_bytes = 0, ws_bytes = 0;
   // workspace segment offsets
-  size_t w_frRf, w_frRd, w_frc, w_pcand, w_acand, w_pacc, w_p64, w_A, w_g, w_SL, w_gL, w_S, w_gS, w_fac, w_delta, w_C,
-      w_ga, w_slab, w_lm, w_cost, w_pred;
+  size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
+      w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -101,6 +105,9 @@ static void build_layout(spgo_plan *p) {
   add_seg(p, p->ch_f0); add_seg(p, p->ch_nb); add_seg(p, p->ch_lm0); add_seg(p, p->ch_cnt); add_seg(p, p->ch_slab);
   add_seg(p, p->wk_prob); add_seg(p, p->wk_ti); add_seg(p, p->wk_tj); add_seg(p, p->wk_cbeg);
   add_seg(p, p->wk_cend); add_seg(p, p->wk_chunks); add_seg(p, p->fr_prob); add_seg(p, p->pose_prob);
+  add_seg(p, p->obs_slot);
+  add_seg(p, p->tc_prob); add_seg(p, p->tc_row0); add_seg(p, p->tc_col0); add_seg(p, p->tc_ncols);
+  add_seg(p, p->tc_cbeg); add_seg(p, p->tc_cend); add_seg(p, p->tc_chunks);
   // workspace
   const size_t ts = p->precision == SPGO_PREC_FP64 ? 8 : 4;
   size_t o = 0;
@@ -110,21 +117,22 @@ static void build_layout(spgo_plan *p) {
     return r;
   };
   p->w_frRf = take((size_t)p->F * 18 * 4);
+  p->w_frRl = take((size_t)p->F * 18 * 4);
   p->w_frRd = take((size_t)p->F * 18 * 8);
   p->w_frc = take((size_t)p->F * 6 * 8);
+  p->w_frch = take((size_t)p->F * 6 * 4);
+  p->w_frcl = take((size_t)p->F * 6 * 4);
   p->w_pcand = take((size_t)p->NP * 12 * 8);
   p->w_acand = take((size_t)p->L * 8);
   p->w_pacc = take((size_t)p->total_pairs * 27 * ts);
-  p->w_p64 = take((size_t)p->total_pairs * 27 * 8);
-  p->w_A = take((size_t)p->total_S * 8);
-  p->w_g = take((size_t)p->total_params * 8);
+  p->w_pF = take((size_t)p->total_pairs * 27 * ts);
+  p->w_A = take((size_t)p->total_S * ts);
+  p->w_g = take((size_t)p->total_params * ts);
   p->w_SL = take((size_t)p->total_S * ts);
   p->w_gL = take((size_t)p->total_params * ts);
-  p->w_S = take((size_t)p->total_S * 8);
-  p->w_gS = take((size_t)p->total_params * 8);
   // global factor storage only when a problem is too large for the shared-memory path
   const size_t P = (size_t)p->max_P;
-  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts) + 16;
+  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8) + 16;
   p->w_fac = take(packed <= 200 * 1024 ? 0 : (size_t)p->total_S * ts);
   p->w_delta = take((size_t)p->total_params * 8);
   p->w_C = take((size_t)p->L * ts);
@@ -176,24 +184,41 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
         return fail(SPGO_ERR_UNSUPPORTED, "landmark " + std::to_string(l) + " spans more than SPGO_MAX_WINDOW poses");
       maxw = std::max(maxw, mx - mn);
     }
-    // order landmarks by window, group into chunks of <= 32 with a common slab window
+    // order landmarks by host frame, then window; a chunk holds <= 32 landmarks of ONE
+    // host, so all its pose-pair contributions (host, target) are indexed by the target
     std::vector<int32_t> order(L);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      if (q.host[x] != q.host[y]) return q.host[x] < q.host[y];
       return lo[x] != lo[y] ? lo[x] < lo[y] : hi[x] < hi[y];
     });
     const int32_t ch_begin = (int32_t)p->ch_prob.size();
     int32_t cur = -1;
+    // observations of the open chunk: (frame, slot, source index), emitted sorted by frame
+    std::vector<std::array<int64_t, 3>> pend;
+    auto close_chunk = [&]() {
+      if (cur < 0) return;
+      slab_off += (int64_t)6 * p->ch_nb[cur] * SPGO_CHUNK;
+      std::stable_sort(pend.begin(), pend.end(),
+                       [](const std::array<int64_t, 3> &x, const std::array<int64_t, 3> &y) { return x[0] < y[0]; });
+      for (const auto &e : pend) {
+        p->obs_frame.push_back((int32_t)e[0]);
+        p->obs_slot.push_back((uint8_t)e[1]);
+        for (int c = 0; c < 4; ++c) p->obs_uv.push_back(q.obs_uv[4 * e[2] + c]);
+      }
+      obs_total += (int64_t)pend.size();
+      pend.clear();
+    };
     for (int k = 0; k < L; ++k) {
       const int l = order[k];
-      bool fresh = cur < 0 || p->ch_cnt[cur] == SPGO_CHUNK;
+      bool fresh = cur < 0 || p->ch_cnt[cur] == SPGO_CHUNK || p->lm_host.back() != q.host[l];
       if (!fresh) {
         const int f0 = p->ch_f0[cur];
         const int nb_new = std::max(p->ch_f0[cur] + p->ch_nb[cur], hi[l]) - f0;
         if (nb_new > SPGO_MAX_WINDOW) fresh = true;
       }
       if (fresh) {
-        if (cur >= 0) slab_off += (int64_t)6 * p->ch_nb[cur] * SPGO_CHUNK;
+        close_chunk();
         cur = (int32_t)p->ch_prob.size();
         p->ch_prob.push_back(b);
         p->ch_f0.push_back(std::min(lo[l], N - 1));
@@ -205,7 +230,7 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
       const int f0 = p->ch_f0[cur];
       p->ch_nb[cur] = std::max(p->ch_nb[cur], hi[l] - f0);
       p->ch_cnt[cur] += 1;
-      // internal landmark lm_off + k
+      // internal landmark lm_off + k; lm_obs holds the start of its CHUNK's observations
       p->lm_prob.push_back(b);
       p->lm_host.push_back(q.host[l]);
       p->lm_lo.push_back(lo[l]);
@@ -216,13 +241,10 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
       p->lm_uv.push_back(q.anchor_uv[2 * l]);
       p->lm_uv.push_back(q.anchor_uv[2 * l + 1]);
       p->lm_obs.push_back(obs_total);
-      for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) {
-        p->obs_frame.push_back(q.obs_frame[o]);
-        for (int c = 0; c < 4; ++c) p->obs_uv.push_back(q.obs_uv[4 * o + c]);
-      }
-      obs_total += q.obs_ptr[l + 1] - q.obs_ptr[l];
+      for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o)
+        pend.push_back({(int64_t)q.obs_frame[o], (int64_t)(p->ch_cnt[cur] - 1), o});
     }
-    if (cur >= 0) slab_off += (int64_t)6 * p->ch_nb[cur] * SPGO_CHUNK;
+    close_chunk();
     const int32_t ch_end = (int32_t)p->ch_prob.size();
     for (int c = ch_begin; c < ch_end; ++c) {
       if (p->ch_f0[c] < 0 || p->ch_f0[c] + p->ch_nb[c] > N)
@@ -250,6 +272,31 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
           p->wk_cend.push_back((int32_t)p->wk_chunks.size());
         }
       }
+    // tensor-core Schur work list: 128-row tiles, lower-triangle columns in ranges of <= 256
+    {
+      const int P = 6 * N;
+      const int kTcSplit = 64;
+      for (int row0 = 0; row0 < P; row0 += 128) {
+        const int colmax = std::min(P, row0 + 128);
+        for (int col0 = 0; col0 < colmax; col0 += 256) {
+          const int ncols = ((std::min(256, colmax - col0) + 15) / 16) * 16;
+          std::vector<int32_t> lst;
+          for (int c = ch_begin; c < ch_end; ++c) {
+            const int s0 = 6 * p->ch_f0[c], s1 = 6 * (p->ch_f0[c] + p->ch_nb[c]);
+            if (s1 > row0 && s0 < row0 + 128 && s1 > col0 && s0 < col0 + ncols) lst.push_back(c);
+          }
+          for (size_t st = 0; st < lst.size(); st += kTcSplit) {
+            p->tc_prob.push_back(b);
+            p->tc_row0.push_back(row0);
+            p->tc_col0.push_back(col0);
+            p->tc_ncols.push_back(ncols);
+            p->tc_cbeg.push_back((int32_t)p->tc_chunks.size());
+            for (size_t k = st; k < std::min(lst.size(), st + kTcSplit); ++k) p->tc_chunks.push_back(lst[k]);
+            p->tc_cend.push_back((int32_t)p->tc_chunks.size());
+          }
+        }
+      }
+    }
     // per-problem records
     const int P = 6 * N;
     p->p_npose.push_back(N);
@@ -306,7 +353,19 @@ struct spgo_solver {
   std::vector<cudaEvent_t> ev;
   std::vector<int> ev_kind;
   size_t ev_used = 0;
+  // captured LM iterations: one graph per iteration count, rebuilt when parameters change
+  struct Graph {
+    int n_iters;
+    cudaGraphExec_t exec;
+    int64_t kernels;  // kernel nodes, for the launch count
+  };
+  std::vector<Graph> graphs;
 };
+
+static void drop_graphs(spgo_solver *s) {
+  for (auto &g : s->graphs) cudaGraphExecDestroy(g.exec);
+  s->graphs.clear();
+}
 
 // profiled kernel kinds (spgo_profile_read order)
 enum { K_CHAIN, K_LINEARIZE, K_COST, K_SYSTEM, K_SCHUR, K_ASSEMBLE, K_FACTOR, K_BACKSUB, K_UPDATE,
@@ -367,21 +426,28 @@ static void make_views(spgo_solver *s) {
   v.wk_tj = seg_ptr<int32_t>(p, st, i++); v.wk_cbeg = seg_ptr<int32_t>(p, st, i++);
   v.wk_cend = seg_ptr<int32_t>(p, st, i++); v.wk_chunks = seg_ptr<int32_t>(p, st, i++);
   v.fr_prob = seg_ptr<int32_t>(p, st, i++); v.pose_prob = seg_ptr<int32_t>(p, st, i++);
+  v.obs_slot = seg_ptr<uint8_t>(p, st, i++);
+  v.tc_prob = seg_ptr<int32_t>(p, st, i++); v.tc_row0 = seg_ptr<int32_t>(p, st, i++);
+  v.tc_col0 = seg_ptr<int32_t>(p, st, i++); v.tc_ncols = seg_ptr<int32_t>(p, st, i++);
+  v.tc_cbeg = seg_ptr<int32_t>(p, st, i++); v.tc_cend = seg_ptr<int32_t>(p, st, i++);
+  v.tc_chunks = seg_ptr<int32_t>(p, st, i++);
+  v.n_tc_items = (int32_t)p->tc_prob.size();
   unsigned char *w = s->d_ws;
   WorkView &x = s->wv;
   x.fr_Rf = reinterpret_cast<float *>(w + p->w_frRf);
+  x.fr_Rl = reinterpret_cast<float *>(w + p->w_frRl);
   x.fr_Rd = reinterpret_cast<double *>(w + p->w_frRd);
   x.fr_c = reinterpret_cast<double *>(w + p->w_frc);
+  x.fr_ch = reinterpret_cast<float *>(w + p->w_frch);
+  x.fr_cl = reinterpret_cast<float *>(w + p->w_frcl);
   x.poses_cand = reinterpret_cast<double *>(w + p->w_pcand);
   x.alpha_cand = reinterpret_cast<double *>(w + p->w_acand);
   x.pair_acc = w + p->w_pacc;
-  x.pair64 = reinterpret_cast<double *>(w + p->w_p64);
-  x.A = reinterpret_cast<double *>(w + p->w_A);
-  x.g = reinterpret_cast<double *>(w + p->w_g);
+  x.pairF = w + p->w_pF;
+  x.A = w + p->w_A;
+  x.g = w + p->w_g;
   x.SL = w + p->w_SL;
   x.gL = w + p->w_gL;
-  x.S = reinterpret_cast<double *>(w + p->w_S);
-  x.gS = reinterpret_cast<double *>(w + p->w_gS);
   x.fac = w + p->w_fac;
   x.delta = reinterpret_cast<double *>(w + p->w_delta);
   x.C = w + p->w_C;
@@ -405,8 +471,13 @@ static int enqueue_linearize(spgo_solver *s, cudaStream_t st) {
 template <typename T>
 static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
   const int mixed = s->plan->precision == SPGO_PREC_MIXED;
-  { PROF(K_SCHUR); CUDA_TRY(launch_schur<T>(s->pv, s->wv, s->prm, st)); }
-  { PROF(K_ASSEMBLE); CUDA_TRY(launch_assemble<T>(s->pv, s->wv, st)); }
+  if (mixed && s->prm.use_tc) {
+    PROF(K_SCHUR);
+    CUDA_TRY(launch_schur_tc(s->pv, s->wv, s->prm, st));
+  } else {
+    PROF(K_SCHUR);
+    CUDA_TRY(launch_schur<T>(s->pv, s->wv, s->prm, st));
+  }
   { PROF(K_FACTOR); CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st)); }
   return SPGO_OK;
 }
@@ -417,7 +488,7 @@ static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
   if ((rc = enqueue_linearize<T>(s, st)) != SPGO_OK) return rc;
   if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
   { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st)); }
-  { PROF(K_UPDATE); CUDA_TRY(launch_update_poses(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
+  { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
   { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, st)); }
   { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st)); }
   { PROF(K_BOOKKEEP); CUDA_TRY(launch_decide(s->pv, s->wv, s->prm, st)); }
@@ -433,7 +504,7 @@ static int enqueue_gn(spgo_solver *s, int iters, float step_size, cudaStream_t s
     if ((rc = enqueue_linearize<T>(s, st)) != SPGO_OK) return rc;
     if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
     { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->alpha, 1, st)); }
-    { PROF(K_UPDATE); CUDA_TRY(launch_update_poses(s->pv, s->wv, s->poses, s->poses, (double)step_size, 1, st)); }
+    { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->poses, (double)step_size, 1, st)); }
   }
   return SPGO_OK;
 }
@@ -458,6 +529,8 @@ void spgo_default_params(spgo_params *p) {
   p->tol = 1e-6;
   p->max_iters = 30;
   p->refine_steps = 1;
+  p->use_graph = 1;
+  p->use_tc = 0;
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
@@ -489,6 +562,7 @@ int spgo_plan_sizes_get(const spgo_plan *p, spgo_plan_sizes *o) {
   o->n_chunks = (int32_t)p->ch_prob.size();
   o->n_schur_items = (int32_t)p->wk_prob.size();
   o->max_params = p->max_P;
+  o->schur_chunk_tiles = (int32_t)p->wk_chunks.size();
   o->static_bytes = p->static_bytes;
   o->workspace_bytes = p->ws_bytes;
   o->slab_elems = p->total_slab;
@@ -551,8 +625,10 @@ int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_byte
 }
 
 int spgo_solver_destroy(spgo_solver *s) {
-  if (s)
+  if (s) {
     for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+    drop_graphs(s);
+  }
   delete s;
   return SPGO_OK;
 }
@@ -593,6 +669,7 @@ int spgo_set_params(spgo_solver *s, const spgo_params *p) {
     return fail(SPGO_ERR_INVALID_ARG, "parameter out of range");
   static_assert(sizeof(Params) == sizeof(spgo_params), "params layout");
   std::memcpy(&s->prm, p, sizeof(Params));
+  drop_graphs(s);  // captured launches carry the old parameters
   return SPGO_OK;
 }
 
@@ -609,14 +686,50 @@ int spgo_lm_reset(spgo_solver *s, void *stream) {
   return SPGO_OK;
 }
 
-int spgo_lm_iterate(spgo_solver *s, int32_t n_iters, void *stream) {
-  if (!s || n_iters < 0) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
-  cudaStream_t st = (cudaStream_t)stream;
+static int enqueue_iterations(spgo_solver *s, int32_t n_iters, cudaStream_t st) {
   for (int it = 0; it < n_iters; ++it) {
     int rc = s->plan->precision == SPGO_PREC_FP64 ? enqueue_lm_iteration<double>(s, st)
                                                   : enqueue_lm_iteration<float>(s, st);
     if (rc != SPGO_OK) return rc;
   }
+  return SPGO_OK;
+}
+
+int spgo_lm_iterate(spgo_solver *s, int32_t n_iters, void *stream) {
+  if (!s || n_iters < 0) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool graphable = s->prm.use_graph && !s->prof && st != nullptr && st != cudaStreamLegacy &&
+                         st != cudaStreamPerThread;
+  if (!graphable || n_iters == 0) return enqueue_iterations(s, n_iters, st);
+  for (auto &g : s->graphs)
+    if (g.n_iters == n_iters) {
+      CUDA_TRY(cudaGraphLaunch(g.exec, st));
+      g_launches += g.kernels;
+      return SPGO_OK;
+    }
+  // capture n_iters iterations once; device-side gating keeps replays exact
+  cudaStreamCaptureStatus cs;
+  CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return enqueue_iterations(s, n_iters, st);  // caller is capturing
+  CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int64_t l0 = g_launches;
+  int rc = enqueue_iterations(s, n_iters, st);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(st, &graph);
+  if (rc != SPGO_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(SPGO_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(SPGO_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  const int64_t kernels = g_launches - l0;
+  g_launches = l0;  // the capture itself ran nothing; replays are counted
+  s->graphs.push_back(spgo_solver::Graph{n_iters, exec, kernels});
+  CUDA_TRY(cudaGraphLaunch(exec, st));
+  g_launches += kernels;
   return SPGO_OK;
 }
 
@@ -672,15 +785,38 @@ int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, do
   int rc = p->precision == SPGO_PREC_FP64 ? enqueue_linearize<double>(s, st) : enqueue_linearize<float>(s, st);
   if (rc != SPGO_OK) return rc;
   const int N = p->p_npose[problem], P = 6 * N, L = p->p_lm_cnt[problem];
-  if (A) CUDA_TRY(cudaMemcpyAsync(A, s->wv.A + p->p_S_off[problem], (size_t)P * P * 8, cudaMemcpyDeviceToDevice, st));
-  if (g) CUDA_TRY(cudaMemcpyAsync(g, s->wv.g + p->p_param_off[problem], (size_t)P * 8, cudaMemcpyDeviceToDevice, st));
+  const bool f64 = p->precision == SPGO_PREC_FP64;
+  const size_t ts = f64 ? 8 : 4;
+  if (A)
+    CUDA_TRY(launch_to_double(static_cast<unsigned char *>(s->wv.A) + p->p_S_off[problem] * ts, f64, A,
+                              (int64_t)P * P, st));
+  if (g)
+    CUDA_TRY(launch_to_double(static_cast<unsigned char *>(s->wv.g) + (size_t)p->p_param_off[problem] * ts, f64, g,
+                              P, st));
   if (B) CUDA_TRY(cudaMemsetAsync(B, 0, (size_t)P * L * 8, st));
-  rc = p->precision == SPGO_PREC_FP64
-           ? launch_export_B_n<double>(s->pv, s->wv, problem, p->p_chunk_cnt[problem], B, C, g_a, st)
+  rc = f64 ? launch_export_B_n<double>(s->pv, s->wv, problem, p->p_chunk_cnt[problem], B, C, g_a, st)
            : launch_export_B_n<float>(s->pv, s->wv, problem, p->p_chunk_cnt[problem], B, C, g_a, st);
   CUDA_TRY(rc);
   if (cost)
     CUDA_TRY(cudaMemcpyAsync(cost, &s->wv.lm[problem].cost, sizeof(double), cudaMemcpyDeviceToDevice, st));
+  return SPGO_OK;
+}
+
+int spgo_export_reduced(spgo_solver *s, int32_t problem, double lambda, double *S, double *gS, void *stream) {
+  if (!s || problem < 0 || problem >= s->plan->B || !S || !gS) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const spgo_plan *p = s->plan;
+  const bool f64 = p->precision == SPGO_PREC_FP64;
+  CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, lambda, st));
+  int rc = f64 ? enqueue_linearize<double>(s, st) : enqueue_linearize<float>(s, st);
+  if (rc != SPGO_OK) return rc;
+  if (!f64 && s->prm.use_tc) {
+    CUDA_TRY(launch_schur_tc(s->pv, s->wv, s->prm, st));
+  } else {
+    CUDA_TRY(f64 ? launch_schur<double>(s->pv, s->wv, s->prm, st) : launch_schur<float>(s->pv, s->wv, s->prm, st));
+  }
+  CUDA_TRY(f64 ? launch_export_S<double>(s->pv, s->wv, problem, S, gS, st)
+               : launch_export_S<float>(s->pv, s->wv, problem, S, gS, st));
   return SPGO_OK;
 }
 

@@ -21,58 +21,99 @@
 // Pair accumulators use the left centre of frame lo as origin and the slab
 // uses the landmark's anchor centre, so no large world coordinates enter FP32.
 #include "kernels.cuh"
+#include "frames.cuh"
+#include "dfloat.cuh"
+
+#include <type_traits>
 
 namespace spgo {
 
-template <typename T> __device__ __forceinline__ const T *frame_R(const WorkView &wv, int f, int cam);
-template <> __device__ __forceinline__ const float *frame_R<float>(const WorkView &wv, int f, int cam) {
-  return wv.fr_Rf + (size_t)f * 18 + cam * 9;
-}
-template <> __device__ __forceinline__ const double *frame_R<double>(const WorkView &wv, int f, int cam) {
-  return wv.fr_Rd + (size_t)f * 18 + cam * 9;
+// ---- global poses: G[0] = I, G[k+1] = G[k] inv(T_k); right camera G T_r_to_l ----
+// One warp per problem: an inclusive shuffle scan of the 3x4 products (FP64),
+// 32 frames per pass with the running prefix carried between passes
+// (the reference walks the chain with one thread, Solver_cuda.cu:472-491).
+__device__ __forceinline__ void write_frame(const WorkView &wv, size_t f, const double *G, const double *Trl) {
+  double Gr[12];
+  compose34(G, Trl, Gr);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      wv.fr_Rd[f * 18 + 3 * i + j] = G[4 * i + j];
+      wv.fr_Rd[f * 18 + 9 + 3 * i + j] = Gr[4 * i + j];
+      const float gl = (float)G[4 * i + j], gr = (float)Gr[4 * i + j];
+      wv.fr_Rf[f * 18 + 3 * i + j] = gl;
+      wv.fr_Rf[f * 18 + 9 + 3 * i + j] = gr;
+      wv.fr_Rl[f * 18 + 3 * i + j] = (float)(G[4 * i + j] - (double)gl);
+      wv.fr_Rl[f * 18 + 9 + 3 * i + j] = (float)(Gr[4 * i + j] - (double)gr);
+    }
+    const double cl = G[4 * i + 3], cr = Gr[4 * i + 3];
+    wv.fr_c[f * 6 + i] = cl;
+    wv.fr_c[f * 6 + 3 + i] = cr;
+    const float hl = (float)cl, hr = (float)cr;
+    wv.fr_ch[f * 6 + i] = hl;
+    wv.fr_ch[f * 6 + 3 + i] = hr;
+    wv.fr_cl[f * 6 + i] = (float)(cl - (double)hl);
+    wv.fr_cl[f * 6 + 3 + i] = (float)(cr - (double)hr);
+  }
 }
 
-// ---- global poses: G[0] = I, G[k+1] = G[k] inv(T_k); right camera G T_r_to_l ----
-// One thread per problem, FP64 (Solver_cuda.cu:472-491).
 __global__ void k_chain(PlanView pv, WorkView wv, const double *__restrict__ poses, int gate) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (b >= pv.B) return;
   if (!problem_active(wv.lm, b, gate)) return;
   const int N = pv.p_npose[b], fo = pv.p_frame_off[b], po = pv.p_pose_off[b];
   const double *Trl = pv.p_Trl + 12 * b;
-  double G[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
-  for (int k = 0; k <= N; ++k) {
-    if (k > 0) {
-      double Ti[12], Gn[12];
-      invert34(poses + 12 * (size_t)(po + k - 1), Ti);
-      compose34(G, Ti, Gn);
+  double carry[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  if (lane == 0) write_frame(wv, (size_t)fo, carry, Trl);
+  for (int s = 0; s < N; s += 32) {
+    const int k = s + lane;
+    double M[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    if (k < N) invert34(poses + 12 * (size_t)(po + k), M);
+    // inclusive scan: M_k <- M_0 M_1 ... M_k (earlier factors on the left)
 #pragma unroll
-      for (int q = 0; q < 12; ++q) G[q] = Gn[q];
-    }
-    double Gr[12];
-    compose34(G, Trl, Gr);
-    const size_t f = (size_t)(fo + k);
+    for (int d = 1; d < 32; d <<= 1) {
+      double P[12];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
+      for (int q = 0; q < 12; ++q) P[q] = __shfl_up_sync(0xffffffffu, M[q], d);
+      if (lane >= d) {
+        double C[12];
+        compose34(P, M, C);
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        wv.fr_Rd[f * 18 + 3 * i + j] = G[4 * i + j];
-        wv.fr_Rd[f * 18 + 9 + 3 * i + j] = Gr[4 * i + j];
-        wv.fr_Rf[f * 18 + 3 * i + j] = (float)G[4 * i + j];
-        wv.fr_Rf[f * 18 + 9 + 3 * i + j] = (float)Gr[4 * i + j];
+        for (int q = 0; q < 12; ++q) M[q] = C[q];
       }
-      wv.fr_c[f * 6 + i] = G[4 * i + 3];
-      wv.fr_c[f * 6 + 3 + i] = Gr[4 * i + 3];
     }
+    double G[12];
+    compose34(carry, M, G);
+    if (k < N) write_frame(wv, (size_t)(fo + k + 1), G, Trl);
+#pragma unroll
+    for (int q = 0; q < 12; ++q) carry[q] = __shfl_sync(0xffffffffu, G[q], 31);
   }
 }
 
 // upper-triangle index of a symmetric 6x6 (row i <= col j)
 __device__ __forceinline__ constexpr int tri6(int i, int j) { return i * 6 - (i * (i - 1)) / 2 + (j - i); }
 
+template <typename T>
+struct LinSmem {
+  T X[SPGO_CHUNK][3];      // anchor point, world axes, relative to the anchor centre
+  float Xl[SPGO_CHUNK][3]; // FP32 path: low words of X as a double-float
+  T dX[SPGO_CHUNK][3];     // dX / d alpha
+  T C[SPGO_CHUNK], ga[SPGO_CHUNK];
+  int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
+  double cost[8];
+  T pair[SPGO_MAX_WINDOW + 1][27];  // (host, target) pair terms of the chunk, by target - f0
+};
+
 // ---- fused linearisation / cost -----------------------------------------------
-// Grid: one CTA (8 warps) per chunk of <= 32 landmarks; one warp per landmark,
-// lanes over its observations.  COST = true evaluates the cost only.
+// One CTA per chunk of <= 32 landmarks.  Phase A: per-landmark anchor point.
+// Phase B: one thread per observation (both cameras): residual, robust weight,
+// inverse-depth Jacobian (C, g_a by shared atomics), pair accumulators (global
+// reductions), and the observation's s K^T j_alpha written into the slab row of
+// its frame.  Phase C: per landmark, the suffix (frames after the anchor) and
+// prefix (frames before it) sums that turn those rows into b_l(i), then
+// B_l(i) = Ad_i^T b_l(i).  COST = true runs phase B's residual part only.
 template <typename T, bool COST>
 __global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Params prm,
                                                    const double *__restrict__ alpha_state, int gate) {
@@ -80,193 +121,284 @@ __global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Par
   const int c = blockIdx.x;
   const int b = pv.ch_prob[c];
   if (!problem_active(wv.lm, b, gate)) return;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x;
   const int f0 = pv.ch_f0[c], nb = pv.ch_nb[c], lm0 = pv.ch_lm0[c], cnt = pv.ch_cnt[c];
   const int fo = pv.p_frame_off[b];
-  const int D = pv.p_pair_D[b];
-  const int64_t pair_base = pv.p_pair_off[b];
   const float *intr = pv.p_intr + 8 * b;
   const T fxs[2] = {(T)intr[0], (T)intr[4]}, fys[2] = {(T)intr[1], (T)intr[5]};
   const T cxs[2] = {(T)intr[2], (T)intr[6]}, cys[2] = {(T)intr[3], (T)intr[7]};
-  const T lscale = (T)prm.loss_scale;
-
+  LinSmem<T> &sm = *reinterpret_cast<LinSmem<T> *>(smem_raw);
+  T *slab_s = reinterpret_cast<T *>(smem_raw + ((sizeof(LinSmem<T>) + 15) & ~(size_t)15));  // [6 nb][32]
   const int rows = 6 * nb;
-  T *slab_s = reinterpret_cast<T *>(smem_raw);                 // [rows][32]
-  T *q_s = slab_s + (COST ? 0 : rows * SPGO_CHUNK);            // [8][32][6]
-  int *qr_s = reinterpret_cast<int *>(q_s + (COST ? 0 : 8 * 32 * 6));  // [8][32][2]
-  if (!COST) {
-    for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_s[i] = T(0);
-    __syncthreads();
-  }
-  T *pair_acc = reinterpret_cast<T *>(wv.pair_acc);
 
-  double cost_lane = 0.0;
-  for (int s = warp; s < cnt; s += 8) {
-    const int li = lm0 + s;
+  // phase A
+  if (tid < cnt) {
+    const int li = lm0 + tid;
     const int a = pv.lm_host[li];
-    const int lo_l = pv.lm_lo[li], hi_l = pv.lm_hi[li];
     const T alpha = (T)alpha_state[pv.lm_user[li]];
     const T ua = (T)pv.lm_uv[2 * li], va = (T)pv.lm_uv[2 * li + 1];
-    const int fa = fo + a;
-    const T *Ra = frame_R<T>(wv, fa, 0);
-    const double *ca = wv.fr_c + (size_t)fa * 6;
-    // anchor ray t_a = K_l^-1 p_a / alpha, rotated to world axes (origin: anchor centre)
+    const T *Ra = FramesT<T>::R(wv, fo + a, 0);
     const Vec3<T> ta = v3<T>((ua - cxs[0]) / fxs[0] / alpha, (va - cys[0]) / fys[0] / alpha, T(1) / alpha);
-    const Vec3<T> X = mul(Ra, ta);
-    const Vec3<T> dXda = v3<T>(-X.x / alpha, -X.y / alpha, -X.z / alpha);
-    T accC = T(0), accG = T(0);
-    const int64_t ob = pv.lm_obs[li], oe = pv.lm_obs[li + 1];
-    for (int64_t base = ob; base < oe; base += 32) {
-      const int64_t o = base + lane;
-      T q[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-      int qlo = 0, qhi = 0;
-      if (o < oe) {
-        const int n = pv.obs_frame[o];
-        const float4 z = reinterpret_cast<const float4 *>(pv.obs_uv)[o];
-        const int fn = fo + n;
-        const bool has_pose = (n != a);
-        const int lo = min(a, n), hi = max(a, n);
-        const T sgn = n > a ? T(1) : T(-1);
-        Vec3<T> Xp = X;  // point relative to the pair origin (left centre of frame lo)
-        if (!COST && has_pose && lo != a) {
-          const double *cl = wv.fr_c + (size_t)(fo + lo) * 6;
-          Xp = v3<T>(X.x + (T)(ca[0] - cl[0]), X.y + (T)(ca[1] - cl[1]), X.z + (T)(ca[2] - cl[2]));
+    Vec3<T> X = mul(Ra, ta);
+    if constexpr (std::is_same<T, float>::value) {
+      // the same point as a double-float, for the residuals
+      const df al = df_from_double(alpha_state[pv.lm_user[li]]);
+      const df t3[3] = {df_sub(pv.lm_uv[2 * li], intr[2]) / df_make(intr[0]) / al,
+                        df_sub(pv.lm_uv[2 * li + 1], intr[3]) / df_make(intr[1]) / al, df_make(1.f) / al};
+      const float *Rh = wv.fr_Rf + (size_t)(fo + a) * 18, *Rl = wv.fr_Rl + (size_t)(fo + a) * 18;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const df v = df{Rh[3 * k], Rl[3 * k]} * t3[0] + df{Rh[3 * k + 1], Rl[3 * k + 1]} * t3[1] +
+                     df{Rh[3 * k + 2], Rl[3 * k + 2]} * t3[2];
+        sm.Xl[tid][k] = v.l;
+        if (k == 0) X.x = v.h;
+        if (k == 1) X.y = v.h;
+        if (k == 2) X.z = v.h;
+      }
+    }
+    sm.X[tid][0] = X.x; sm.X[tid][1] = X.y; sm.X[tid][2] = X.z;
+    sm.dX[tid][0] = -X.x / alpha; sm.dX[tid][1] = -X.y / alpha; sm.dX[tid][2] = -X.z / alpha;
+    sm.C[tid] = T(0);
+    sm.ga[tid] = T(0);
+    sm.a[tid] = a;
+    sm.lo[tid] = pv.lm_lo[li];
+    sm.hi[tid] = pv.lm_hi[li];
+  }
+  if (!COST) {
+    for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_s[i] = T(0);
+    for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) (&sm.pair[0][0])[i] = T(0);
+  }
+  __syncthreads();
+
+  // phase B: observations are sorted by target frame inside the chunk and every
+  // landmark of the chunk has the same host, so a warp's pair terms (host, target)
+  // form contiguous runs: reduce each run with shuffles, add it to the chunk's
+  // shared pair slot, and flush the slots to the global accumulators once.
+  const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
+  const int D = pv.p_pair_D[b];
+  const int lane = tid & 31;
+  const T lscale = (T)prm.loss_scale;
+  T cost_t = T(0);  // a thread sums a handful of terms; the FP64 reduction starts at the warp
+  for (int64_t base = ob + (tid & ~31); base < oe; base += blockDim.x) {
+    const int64_t o = base + lane;
+    T M[21], m[6];
+    int key = -1;
+    if (!COST) {
+#pragma unroll
+      for (int k = 0; k < 21; ++k) M[k] = T(0);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) m[k] = T(0);
+    }
+    if (o < oe) {
+      const int slot = pv.obs_slot[o];
+      const int n = pv.obs_frame[o];
+      const float4 z = reinterpret_cast<const float4 *>(pv.obs_uv)[o];
+      const int a = sm.a[slot];
+      const Vec3<T> X = v3<T>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
+      const int fa = fo + a, fn = fo + n;
+      const bool has_pose = (n != a);
+      const int lo = min(a, n);
+      const T sgn = n > a ? T(1) : T(-1);
+      const T boost = (prm.near_boost && abs(n - a) < 2) ? T(16) : T(1);
+      T q[6], accC = T(0), accG = T(0);
+      Vec3<T> Xp = X, dXda = X;
+      if (!COST) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) q[k] = T(0);
+        dXda = v3<T>(sm.dX[slot][0], sm.dX[slot][1], sm.dX[slot][2]);
+        if (has_pose && lo != a) {  // point relative to the pair origin: left centre of frame lo
+          const Vec3<T> d = FramesT<T>::rel(wv, fa, 0, fo + lo, 0);
+          Xp = v3<T>(X.x + d.x, X.y + d.y, X.z + d.z);
         }
-        T M[21], m[6];
-        if (!COST) {
+      }
 #pragma unroll
-          for (int k = 0; k < 21; ++k) M[k] = T(0);
+      for (int cam = 0; cam < 2; ++cam) {
+        const T *Rn = FramesT<T>::R(wv, fn, cam);
+        const T fx = fxs[cam], fy = fys[cam];
+        Vec3<T> t;
+        T r0, r1;
+        if constexpr (std::is_same<T, float>::value) {
+          // residual in double-float: X + (c_a - c_n), rotated, projected
+          const float *ah = wv.fr_ch + (size_t)fa * 6, *al = wv.fr_cl + (size_t)fa * 6;
+          const float *nh = wv.fr_ch + (size_t)fn * 6 + cam * 3, *nl = wv.fr_cl + (size_t)fn * 6 + cam * 3;
+          const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
+          df Xc[3];
 #pragma unroll
-          for (int k = 0; k < 6; ++k) m[k] = T(0);
+          for (int k = 0; k < 3; ++k)
+            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + (df_sub(ah[k], nh[k]) + df_make(al[k] - nl[k]));
+          df tt[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            tt[k] = df{Rn[k], Rl[k]} * Xc[0] + df{Rn[3 + k], Rl[3 + k]} * Xc[1] + df{Rn[6 + k], Rl[6 + k]} * Xc[2];
+          const df pu = (tt[0] / tt[2]) * fx + df_make(cxs[cam]);
+          const df pv_ = (tt[1] / tt[2]) * fy + df_make(cys[cam]);
+          r0 = df_to_float(df_make(cam ? z.z : z.x) - pu);
+          r1 = df_to_float(df_make(cam ? z.w : z.y) - pv_);
+          t = v3<T>(tt[0].h, tt[1].h, tt[2].h);
+        } else {
+          const Vec3<T> d = FramesT<T>::rel(wv, fa, 0, fn, cam);
+          t = mulT(Rn, v3<T>(X.x + d.x, X.y + d.y, X.z + d.z));
+          const T izr = T(1) / t.z;
+          r0 = (T)(cam ? z.z : z.x) - (fx * t.x * izr + cxs[cam]);
+          r1 = (T)(cam ? z.w : z.y) - (fy * t.y * izr + cys[cam]);
         }
-        const T boost = (prm.near_boost && abs(n - a) < 2) ? T(16) : T(1);
+        const T iz = T(1) / t.z;
+        T rho;
+        const T w2 = boost * robust<T>(prm.loss, lscale, r0 * r0 + r1 * r1, rho);
+        cost_t += T(0.5) * boost * rho;
+        if (COST) continue;
+        // dpi/dt (2x3) then u = dpi/dt R_n^T (rows u0, u1)
+        const T j00 = fx * iz, j02 = -fx * t.x * iz * iz, j11 = fy * iz, j12 = -fy * t.y * iz * iz;
+        const Vec3<T> u0 = v3<T>(j00 * Rn[0] + j02 * Rn[2], j00 * Rn[3] + j02 * Rn[5], j00 * Rn[6] + j02 * Rn[8]);
+        const Vec3<T> u1 = v3<T>(j11 * Rn[1] + j12 * Rn[2], j11 * Rn[4] + j12 * Rn[5], j11 * Rn[7] + j12 * Rn[8]);
+        const T ja0 = dot(u0, dXda), ja1 = dot(u1, dXda);
+        accC += w2 * (ja0 * ja0 + ja1 * ja1);
+        accG += w2 * (ja0 * r0 + ja1 * r1);
+        if (has_pose) {
+          const Vec3<T> k0 = cross(Xp, u0), k1 = cross(Xp, u1);
+          const T K0[6] = {k0.x, k0.y, k0.z, u0.x, u0.y, u0.z};
+          const T K1[6] = {k1.x, k1.y, k1.z, u1.x, u1.y, u1.z};
 #pragma unroll
-        for (int cam = 0; cam < 2; ++cam) {
-          const T *Rn = frame_R<T>(wv, fn, cam);
-          const double *cn = wv.fr_c + (size_t)fn * 6 + cam * 3;
-          const Vec3<T> Xc = v3<T>(X.x + (T)(ca[0] - cn[0]), X.y + (T)(ca[1] - cn[1]), X.z + (T)(ca[2] - cn[2]));
-          const Vec3<T> t = mulT(Rn, Xc);
-          const T iz = T(1) / t.z;
-          const T fx = fxs[cam], fy = fys[cam];
-          const T r0 = (T)(cam ? z.z : z.x) - (fx * t.x * iz + cxs[cam]);
-          const T r1 = (T)(cam ? z.w : z.y) - (fy * t.y * iz + cys[cam]);
-          T rho;
-          const T w2 = boost * robust<T>(prm.loss, lscale, r0 * r0 + r1 * r1, rho);
-          cost_lane += 0.5 * (double)(boost * rho);
-          if (COST) continue;
-          // dpi/dt (2x3) then u = dpi/dt R_n^T (rows u0, u1)
-          const T j00 = fx * iz, j02 = -fx * t.x * iz * iz, j11 = fy * iz, j12 = -fy * t.y * iz * iz;
-          const Vec3<T> u0 = v3<T>(j00 * Rn[0] + j02 * Rn[2], j00 * Rn[3] + j02 * Rn[5], j00 * Rn[6] + j02 * Rn[8]);
-          const Vec3<T> u1 = v3<T>(j11 * Rn[1] + j12 * Rn[2], j11 * Rn[4] + j12 * Rn[5], j11 * Rn[7] + j12 * Rn[8]);
-          const T ja0 = dot(u0, dXda), ja1 = dot(u1, dXda);
-          accC += w2 * (ja0 * ja0 + ja1 * ja1);
-          accG += w2 * (ja0 * r0 + ja1 * r1);
-          if (has_pose) {
-            const Vec3<T> k0 = cross(Xp, u0), k1 = cross(Xp, u1);
-            const T K0[6] = {k0.x, k0.y, k0.z, u0.x, u0.y, u0.z};
-            const T K1[6] = {k1.x, k1.y, k1.z, u1.x, u1.y, u1.z};
+          for (int i = 0; i < 6; ++i) {
 #pragma unroll
-            for (int i = 0; i < 6; ++i) {
-#pragma unroll
-              for (int j = i; j < 6; ++j) M[tri6(i, j)] += w2 * (K0[i] * K0[j] + K1[i] * K1[j]);
-              m[i] += sgn * w2 * (K0[i] * r0 + K1[i] * r1);
-            }
-            const Vec3<T> h0 = cross(X, u0), h1 = cross(X, u1);
-            const T sj0 = sgn * w2 * ja0, sj1 = sgn * w2 * ja1;
-            q[0] += h0.x * sj0 + h1.x * sj1;
-            q[1] += h0.y * sj0 + h1.y * sj1;
-            q[2] += h0.z * sj0 + h1.z * sj1;
-            q[3] += u0.x * sj0 + u1.x * sj1;
-            q[4] += u0.y * sj0 + u1.y * sj1;
-            q[5] += u0.z * sj0 + u1.z * sj1;
+            for (int j = i; j < 6; ++j) M[tri6(i, j)] += w2 * (K0[i] * K0[j] + K1[i] * K1[j]);
+            m[i] += sgn * w2 * (K0[i] * r0 + K1[i] * r1);
           }
-        }
-        if (!COST && has_pose) {
-          T *dst = pair_acc + (size_t)(pair_base + (int64_t)lo * D + (hi - lo - 1)) * 27;
-#pragma unroll
-          for (int k = 0; k < 21; ++k) red_add(dst + k, M[k]);
-#pragma unroll
-          for (int k = 0; k < 6; ++k) red_add(dst + 21 + k, m[k]);
-          qlo = lo;
-          qhi = hi;
+          const Vec3<T> h0 = cross(X, u0), h1 = cross(X, u1);
+          const T sj0 = sgn * w2 * ja0, sj1 = sgn * w2 * ja1;
+          q[0] += h0.x * sj0 + h1.x * sj1;
+          q[1] += h0.y * sj0 + h1.y * sj1;
+          q[2] += h0.z * sj0 + h1.z * sj1;
+          q[3] += u0.x * sj0 + u1.x * sj1;
+          q[4] += u0.y * sj0 + u1.y * sj1;
+          q[5] += u0.z * sj0 + u1.z * sj1;
         }
       }
       if (!COST) {
-        // b_l(i) += sum of q over this batch's observations whose range covers i
-        T *qw = q_s + (size_t)(warp * 32 + lane) * 6;
+        atomicAdd(&sm.C[slot], accC);
+        atomicAdd(&sm.ga[slot], accG);
+        if (has_pose) {
+          key = n;
+          // frames after the anchor cover blocks [a, n): row n - 1 feeds a suffix sum;
+          // frames before it cover [n, a): row n feeds a prefix sum.  Rows are distinct.
+          const int row = (n > a ? n - 1 : n) - f0;
+          T *dstq = slab_s + (size_t)(6 * row) * SPGO_CHUNK + slot;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) qw[k] = q[k];
-        qr_s[(warp * 32 + lane) * 2] = qlo;
-        qr_s[(warp * 32 + lane) * 2 + 1] = qhi;
-        __syncwarp();
-        const int nq = (int)min((int64_t)32, oe - base);
-        for (int bi = lane; bi < hi_l - lo_l; bi += 32) {
-          const int i = lo_l + bi;
-          T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-          for (int j = 0; j < nq; ++j) {
-            const int jlo = qr_s[(warp * 32 + j) * 2], jhi = qr_s[(warp * 32 + j) * 2 + 1];
-            if (jlo <= i && i < jhi) {
-              const T *qj = q_s + (size_t)(warp * 32 + j) * 6;
-#pragma unroll
-              for (int k = 0; k < 6; ++k) acc[k] += qj[k];
-            }
-          }
-          T *dst = slab_s + (size_t)(6 * (i - f0)) * SPGO_CHUNK + s;
-#pragma unroll
-          for (int k = 0; k < 6; ++k) dst[k * SPGO_CHUNK] += acc[k];
+          for (int k = 0; k < 6; ++k) dstq[k * SPGO_CHUNK] = q[k];
         }
-        __syncwarp();
       }
     }
     if (!COST) {
-      accC = warp_sum(accC);
-      accG = warp_sum(accG);
-      if (lane == 0) {
-        reinterpret_cast<T *>(wv.C)[li] = accC;
-        reinterpret_cast<T *>(wv.ga)[li] = accG;
+      // segmented sum over runs of equal target frame (runs are contiguous)
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int kd = __shfl_down_sync(0xffffffffu, key, d);
+        const bool take = (lane + d < 32) && (kd == key);
+#pragma unroll
+        for (int k = 0; k < 21; ++k) {
+          const T v = __shfl_down_sync(0xffffffffu, M[k], d);
+          if (take) M[k] += v;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          const T v = __shfl_down_sync(0xffffffffu, m[k], d);
+          if (take) m[k] += v;
+        }
       }
-      // B_l(i) = Ad_i^T b_l(i) about the anchor centre:
-      //   [R_i^T (b_w - (c_i - c_a) x b_v) ; R_i^T b_v]
-      for (int bi = lane; bi < hi_l - lo_l; bi += 32) {
-        const int i = lo_l + bi;
-        const int fi = fo + i;
-        const T *Ri = frame_R<T>(wv, fi, 0);
-        const double *ci = wv.fr_c + (size_t)fi * 6;
-        const Vec3<T> d = v3<T>((T)(ci[0] - ca[0]), (T)(ci[1] - ca[1]), (T)(ci[2] - ca[2]));
-        T *dst = slab_s + (size_t)(6 * (i - f0)) * SPGO_CHUNK + s;
-        const Vec3<T> bw = v3<T>(dst[0], dst[SPGO_CHUNK], dst[2 * SPGO_CHUNK]);
-        const Vec3<T> bv = v3<T>(dst[3 * SPGO_CHUNK], dst[4 * SPGO_CHUNK], dst[5 * SPGO_CHUNK]);
-        const Vec3<T> dxb = cross(d, bv);
-        const Vec3<T> Bw = mulT(Ri, v3<T>(bw.x - dxb.x, bw.y - dxb.y, bw.z - dxb.z));
-        const Vec3<T> Bv = mulT(Ri, bv);
-        dst[0] = Bw.x;
-        dst[SPGO_CHUNK] = Bw.y;
-        dst[2 * SPGO_CHUNK] = Bw.z;
-        dst[3 * SPGO_CHUNK] = Bv.x;
-        dst[4 * SPGO_CHUNK] = Bv.y;
-        dst[5 * SPGO_CHUNK] = Bv.z;
+      const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+      if (key >= 0 && (lane == 0 || kprev != key)) {
+        T *dst = sm.pair[key - f0];
+#pragma unroll
+        for (int k = 0; k < 21; ++k) atomicAdd(dst + k, M[k]);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) atomicAdd(dst + 21 + k, m[k]);
       }
     }
   }
-  const double cw = warp_sum(cost_lane);
-  if (lane == 0 && cw != 0.0) atomicAdd(wv.cost_acc + b, cw);
-  if (!COST) {
-    __syncthreads();
-    T *gslab = reinterpret_cast<T *>(wv.slab) + pv.ch_slab[c];
-    for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) gslab[i] = slab_s[i];
+  // cost: warp sums, then one FP64 atomic per CTA
+  const double cost = warp_sum((double)cost_t);
+  if ((tid & 31) == 0) sm.cost[tid >> 5] = cost;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm.cost[w];
+    if (t != 0.0) atomicAdd(wv.cost_acc + b, t);
+  }
+  if (COST) return;
+
+  // pair slots -> global accumulators: (lo, hi) = (min, max)(host, target)
+  {
+    const int a = sm.a[0];
+    T *pair_acc = reinterpret_cast<T *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
+    for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) {
+      const int sl = i / 27, comp = i % 27;
+      const int n = f0 + sl;
+      const T v = sm.pair[sl][comp];
+      if (n == a || v == T(0)) continue;
+      const int lo = min(a, n), hi = max(a, n);
+      red_add(pair_acc + ((size_t)lo * D + (hi - lo - 1)) * 27 + comp, v);
+    }
+  }
+
+  // phase C.1: per (landmark, component) suffix / prefix sums along the window
+  for (int idx = tid; idx < cnt * 6; idx += blockDim.x) {
+    const int slot = idx % cnt, k = idx / cnt;  // consecutive threads: consecutive slots (banks)
+    const int a = sm.a[slot], lo_l = sm.lo[slot], hi_l = sm.hi[slot];
+    T acc = T(0);
+    for (int i = hi_l - 1; i >= a; --i) {
+      T *p = slab_s + (size_t)(6 * (i - f0) + k) * SPGO_CHUNK + slot;
+      acc += *p;
+      *p = acc;
+    }
+    acc = T(0);
+    for (int i = lo_l; i < a; ++i) {
+      T *p = slab_s + (size_t)(6 * (i - f0) + k) * SPGO_CHUNK + slot;
+      acc += *p;
+      *p = acc;
+    }
+  }
+  __syncthreads();
+  // phase C.2: B_l(i) = Ad_i^T b_l(i) about the anchor centre:
+  //   [R_i^T (b_w - (c_i - c_a) x b_v) ; R_i^T b_v]
+  for (int idx = tid; idx < cnt * nb; idx += blockDim.x) {
+    const int slot = idx % cnt, i = f0 + idx / cnt;
+    if (i < sm.lo[slot] || i >= sm.hi[slot]) continue;
+    const int fi = fo + i;
+    const T *Ri = FramesT<T>::R(wv, fi, 0);
+    const Vec3<T> d = FramesT<T>::rel(wv, fi, 0, fo + sm.a[slot], 0);
+    T *dst = slab_s + (size_t)(6 * (i - f0)) * SPGO_CHUNK + slot;
+    const Vec3<T> bw = v3<T>(dst[0], dst[SPGO_CHUNK], dst[2 * SPGO_CHUNK]);
+    const Vec3<T> bv = v3<T>(dst[3 * SPGO_CHUNK], dst[4 * SPGO_CHUNK], dst[5 * SPGO_CHUNK]);
+    const Vec3<T> dxb = cross(d, bv);
+    const Vec3<T> Bw = mulT(Ri, v3<T>(bw.x - dxb.x, bw.y - dxb.y, bw.z - dxb.z));
+    const Vec3<T> Bv = mulT(Ri, bv);
+    dst[0] = Bw.x;
+    dst[SPGO_CHUNK] = Bw.y;
+    dst[2 * SPGO_CHUNK] = Bw.z;
+    dst[3 * SPGO_CHUNK] = Bv.x;
+    dst[4 * SPGO_CHUNK] = Bv.y;
+    dst[5 * SPGO_CHUNK] = Bv.z;
+  }
+  __syncthreads();
+  // phase D: slab, C and g_a to global
+  T *gslab = reinterpret_cast<T *>(wv.slab) + pv.ch_slab[c];
+  for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) gslab[i] = slab_s[i];
+  if (tid < cnt) {
+    reinterpret_cast<T *>(wv.C)[lm0 + tid] = sm.C[tid];
+    reinterpret_cast<T *>(wv.ga)[lm0 + tid] = sm.ga[tid];
   }
 }
 
 int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, void *stream) {
-  k_chain<<<grid_for(pv.B, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, poses, gate);
+  k_chain<<<grid_for(pv.B, 4), 128, 0, (cudaStream_t)stream>>>(pv, wv, poses, gate);
   ++g_launches;
   return (int)cudaGetLastError();
 }
 
 template <typename T>
 static size_t lin_smem(int max_nb, bool cost) {
-  if (cost) return 16;
-  return (size_t)6 * max_nb * SPGO_CHUNK * sizeof(T) + (size_t)8 * 32 * 6 * sizeof(T) + (size_t)8 * 32 * 2 * sizeof(int);
+  const size_t head = (sizeof(LinSmem<T>) + 15) & ~(size_t)15;
+  return cost ? head : head + (size_t)6 * max_nb * SPGO_CHUNK * sizeof(T);
 }
 
 template <typename T>

@@ -6,6 +6,9 @@
 // (src/Optimization/Solver_cuda.cu:739-753, :361-374) and updateEstimation
 // (Solver_cuda.cu:497-553).
 #include "kernels.cuh"
+#include "dfloat.cuh"
+
+#include <type_traits>
 
 namespace spgo {
 
@@ -21,82 +24,201 @@ struct FullCol {
   __device__ __forceinline__ size_t operator()(int i, int j) const { return (size_t)j * P + i; }
 };
 
-// Right-looking Cholesky S = L L^T of one problem by one CTA, then L L^T x = g_S,
-// then `refine` FP64 iterative-refinement steps r = g_S - S x, x += solve(r)
-// (used when T = float).  Matrix in shared memory (packed) when it fits, else
-// in the global scratch `fac` (full, column-major).
+constexpr int kPanel = 16;  // block width of the factorisation and the substitutions
+
+// S(r, c) of the damped reduced system for r >= c, from A (pose blocks), S_L
+// (landmark Schur term, lower tiles) and lambda:  S = A + lam diag(A) - S_L
+template <typename T>
+__device__ __forceinline__ double s_entry(const T *A, const T *SL, int P, int r, int c, double lam) {
+  const size_t k = (size_t)r * P + c;
+  double v = (double)A[k] - (double)SL[k];
+  if (r == c) v += lam * (double)A[k];
+  return v;
+}
+
+// One CTA per problem: assemble S (lower) into the factor storage, then a
+// right-looking blocked Cholesky S = L L^T with 16-column blocks: warp 0
+// factorises the 16x16 diagonal block, all threads solve the rows below it
+// (independent per row) and apply the rank-16 trailing update; three barriers
+// per block.  The substitutions are blocked the same way (two barriers per
+// block).  `refine` iterative-refinement steps form the residual g_S - S x in
+// FP64 from A and S_L.  Clears the S_L / g_L tiles it consumed.
 template <typename T, typename Idx>
-__device__ void factor_solve_body(T *Lm, Idx ix, T *y, double *x, const double *S, const double *gS, int P,
-                                  int refine, int *fail_s) {
+__device__ void factor_solve_body(T *Lm, Idx ix, T *y, double *x, float *xs, T *tmp, const T *A, T *SL,
+                                  const T *g, T *gL, double lam, int P, int refine, int *fail_s) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
-  for (int j = tid; j < P; j += nt)
-    for (int i = j; i < P; ++i) Lm[ix(i, j)] = (T)S[(size_t)i * P + j];
+  for (int c = warp; c < P; c += nw)
+    for (int r = c + lane; r < P; r += 32) Lm[ix(r, c)] = (T)s_entry(A, SL, P, r, c, lam);
+  for (int i = tid; i < P; i += nt) {
+    y[i] = g[i] - gL[i];
+    x[i] = 0.0;
+  }
   if (tid == 0) *fail_s = 0;
   __syncthreads();
-  for (int k = 0; k < P; ++k) {
-    if (tid == 0) {
-      const T d = Lm[ix(k, k)];
-      if (!(d > T(0)) || !isfinite((double)d)) *fail_s = 1;
-      else Lm[ix(k, k)] = sqrt(d);
+  for (int kb = 0; kb < P; kb += kPanel) {
+    const int ke = min(kb + kPanel, P), w = ke - kb;
+    if (warp == 0) {  // diagonal block, lane = row inside the block
+      for (int k = 0; k < w; ++k) {
+        const int col = kb + k;
+        const T d = Lm[ix(col, col)];
+        if (!(d > T(0)) || !isfinite((double)d)) {
+          if (lane == 0) *fail_s = 1;
+          break;
+        }
+        const T lkk = sqrt(d);
+        __syncwarp();
+        if (lane == 0) {
+          Lm[ix(col, col)] = lkk;
+          tmp[k] = T(1) / lkk;
+        }
+        if (lane > k && lane < w) Lm[ix(kb + lane, col)] /= lkk;
+        __syncwarp();
+        if (lane > k && lane < w) {
+          const T li = Lm[ix(kb + lane, col)];
+          for (int j = k + 1; j <= lane; ++j) Lm[ix(kb + lane, kb + j)] -= li * Lm[ix(kb + j, col)];
+        }
+        __syncwarp();
+      }
     }
     __syncthreads();
     if (*fail_s) return;
-    const T inv = T(1) / Lm[ix(k, k)];
-    for (int i = k + 1 + tid; i < P; i += nt) Lm[ix(i, k)] *= inv;
+    // rows below the block: L(i, kb:ke) = S(i, kb:ke) L_D^-T
+    for (int i = ke + tid; i < P; i += nt) {
+      T r[kPanel];
+#pragma unroll
+      for (int c = 0; c < kPanel; ++c) r[c] = c < w ? Lm[ix(i, kb + c)] : T(0);
+#pragma unroll
+      for (int c = 0; c < kPanel; ++c) {
+        if (c < w) {
+          T v = r[c];
+#pragma unroll
+          for (int m = 0; m < c; ++m) v -= r[m] * Lm[ix(kb + c, kb + m)];
+          r[c] = v * tmp[c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < kPanel; ++c)
+        if (c < w) Lm[ix(i, kb + c)] = r[c];
+    }
     __syncthreads();
-    for (int j = k + 1 + warp; j < P; j += nw) {
-      const T ljk = Lm[ix(j, k)];
-      for (int i = j + lane; i < P; i += 32) Lm[ix(i, j)] -= Lm[ix(i, k)] * ljk;
+    // trailing update with the finished block
+    for (int j = ke + warp; j < P; j += nw) {
+      T ljk[kPanel];
+#pragma unroll
+      for (int k = 0; k < kPanel; ++k) ljk[k] = k < w ? Lm[ix(j, kb + k)] : T(0);
+      for (int i = j + lane; i < P; i += 32) {
+        T acc = T(0);
+#pragma unroll
+        for (int k = 0; k < kPanel; ++k)
+          if (k < w) acc += Lm[ix(i, kb + k)] * ljk[k];
+        Lm[ix(i, j)] -= acc;
+      }
     }
     __syncthreads();
   }
-  for (int i = tid; i < P; i += nt) {
-    y[i] = (T)gS[i];
-    x[i] = 0.0;
-  }
-  __syncthreads();
   for (int it = 0; it <= refine; ++it) {
-    // forward L z = y
-    for (int k = 0; k < P; ++k) {
-      if (tid == 0) y[k] = y[k] / Lm[ix(k, k)];
+    // forward L z = y, block by block; warp 0 solves the 16x16 diagonal block with
+    // lane c owning unknown c (one shuffle per unknown)
+    for (int kb = 0; kb < P; kb += kPanel) {
+      const int ke = min(kb + kPanel, P), w = ke - kb;
+      if (warp == 0) {
+        T v = lane < w ? y[kb + lane] : T(0);
+        for (int c = 0; c < w; ++c) {
+          T yc = v / Lm[ix(kb + c, kb + c)];
+          yc = __shfl_sync(0xffffffffu, yc, c);
+          if (lane == c) v = yc;
+          if (lane > c && lane < w) v -= Lm[ix(kb + lane, kb + c)] * yc;
+        }
+        if (lane < w) y[kb + lane] = v;
+      }
       __syncthreads();
-      const T yk = y[k];
-      for (int i = k + 1 + tid; i < P; i += nt) y[i] -= Lm[ix(i, k)] * yk;
+      for (int i = ke + tid; i < P; i += nt) {
+        T v = y[i];
+        for (int c = 0; c < w; ++c) v -= Lm[ix(i, kb + c)] * y[kb + c];
+        y[i] = v;
+      }
       __syncthreads();
     }
-    // backward L^T w = z
-    for (int k = P - 1; k >= 0; --k) {
-      if (tid == 0) y[k] = y[k] / Lm[ix(k, k)];
+    // backward L^T w = z, blocks from the bottom
+    for (int kb = ((P - 1) / kPanel) * kPanel; kb >= 0; kb -= kPanel) {
+      const int ke = min(kb + kPanel, P), w = ke - kb;
+      for (int c = warp; c < w; c += nw) {
+        T acc = T(0);
+        for (int i = ke + lane; i < P; i += 32) acc += Lm[ix(i, kb + c)] * y[i];
+        acc = warp_sum(acc);
+        if (lane == 0) tmp[c] = acc;
+      }
       __syncthreads();
-      const T yk = y[k];
-      for (int i = tid; i < k; i += nt) y[i] -= Lm[ix(k, i)] * yk;
+      if (warp == 0) {
+        T v = lane < w ? y[kb + lane] - tmp[lane] : T(0);
+        for (int c = w - 1; c >= 0; --c) {
+          T xc = v / Lm[ix(kb + c, kb + c)];
+          xc = __shfl_sync(0xffffffffu, xc, c);
+          if (lane == c) v = xc;
+          if (lane < c) v -= Lm[ix(kb + c, kb + lane)] * xc;
+        }
+        if (lane < w) y[kb + lane] = v;
+      }
       __syncthreads();
     }
     for (int i = tid; i < P; i += nt) x[i] += (double)y[i];
     __syncthreads();
     if (it == refine) break;
-    // FP64 residual r = g_S - S x
+    // residual r = g_S - S x with ~48-bit accuracy: FP64 when T = double, else
+    // double-float sums on the FP32 pipes (S entries are exact in float)
+    if constexpr (std::is_same<T, float>::value) {
+      for (int j = tid; j < P; j += nt) {
+        const df xj = df_from_double(x[j]);
+        xs[2 * j] = xj.h;
+        xs[2 * j + 1] = xj.l;
+      }
+      __syncthreads();
+    }
     for (int i = warp; i < P; i += nw) {
-      double acc = 0.0;
-      for (int j = lane; j < P; j += 32) acc += S[(size_t)i * P + j] * x[j];
-      acc = warp_sum(acc);
-      if (lane == 0) y[i] = (T)(gS[i] - acc);
+      double r;
+      if constexpr (std::is_same<T, float>::value) {
+        df acc = df_make(0.f);
+        for (int j = lane; j < P; j += 32) {
+          const size_t k = i >= j ? (size_t)i * P + j : (size_t)j * P + i;
+          const df sij = df_sub(A[k], SL[k]) + (i == j ? df_from_double(lam * (double)A[k]) : df_make(0.f));
+          acc = acc + sij * df{xs[2 * j], xs[2 * j + 1]};
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const df other{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
+          acc = acc + other;
+        }
+        r = (double)g[i] - (double)gL[i] - ((double)acc.h + (double)acc.l);
+      } else {
+        double acc = 0.0;
+        for (int j = lane; j < P; j += 32) {
+          const double sij = i >= j ? s_entry(A, SL, P, i, j, lam) : s_entry(A, SL, P, j, i, lam);
+          acc += sij * x[j];
+        }
+        acc = warp_sum(acc);
+        r = (double)g[i] - (double)gL[i] - acc;
+      }
+      if (lane == 0) y[i] = (T)r;
     }
     __syncthreads();
   }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(512) k_factor_solve(PlanView pv, WorkView wv, int refine, int use_smem) {
+__global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, int refine, int use_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int fail_s;
+  __shared__ T tmp_s[kPanel];
   const int b = blockIdx.x;
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   const int N = pv.p_npose[b], P = 6 * N;
   const size_t off = pv.p_S_off[b];
   const int po = pv.p_param_off[b];
-  const double *S = wv.S + off;
-  const double *gS = wv.gS + po;
+  const T *A = reinterpret_cast<const T *>(wv.A) + off;
+  T *SL = reinterpret_cast<T *>(wv.SL) + off;
+  const T *g = reinterpret_cast<const T *>(wv.g) + po;
+  T *gL = reinterpret_cast<T *>(wv.gL) + po;
+  const double lam = wv.lm[b].lam;
   double *x;
   T *y;
   if (use_smem) {
@@ -104,17 +226,26 @@ __global__ void __launch_bounds__(512) k_factor_solve(PlanView pv, WorkView wv, 
     T *Lm = reinterpret_cast<T *>(smem_raw);
     x = reinterpret_cast<double *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15));
     y = reinterpret_cast<T *>(x + P);
-    factor_solve_body<T, PackedCol>(Lm, PackedCol{P}, y, x, S, gS, P, refine, &fail_s);
+    float *xs = reinterpret_cast<float *>(y + P);
+    factor_solve_body<T, PackedCol>(Lm, PackedCol{P}, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
   } else {
     x = reinterpret_cast<double *>(smem_raw);
     y = reinterpret_cast<T *>(x + P);
+    float *xs = reinterpret_cast<float *>(y + P);
     T *Lm = reinterpret_cast<T *>(wv.fac) + off;
-    factor_solve_body<T, FullCol>(Lm, FullCol{P}, y, x, S, gS, P, refine, &fail_s);
+    factor_solve_body<T, FullCol>(Lm, FullCol{P}, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
   }
   __syncthreads();
   const bool failed = fail_s != 0;
   for (int i = threadIdx.x; i < P; i += blockDim.x) wv.delta[po + i] = failed ? 0.0 : x[i];
   if (threadIdx.x == 0 && failed) wv.lm[b].fail = 1;
+  // clear the consumed S_L tiles (every element whose row tile >= column tile) and g_L
+  constexpr int TR = 6 * SPGO_TILE_BLOCKS;
+  for (int r = threadIdx.x >> 5; r < P; r += blockDim.x >> 5) {
+    const int cmax = min(P, (r / TR + 1) * TR);
+    for (int c = threadIdx.x & 31; c < cmax; c += 32) SL[(size_t)r * P + c] = T(0);
+  }
+  for (int i = threadIdx.x; i < P; i += blockDim.x) gL[i] = T(0);
 }
 
 static const size_t kSmemBudget = 200 * 1024;
@@ -122,13 +253,13 @@ static const size_t kSmemBudget = 200 * 1024;
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed, void *stream) {
   const int P = pv.max_P;
-  const size_t vec = (size_t)P * (sizeof(double) + sizeof(T)) + 16;
+  const size_t vec = (size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float)) + 16;
   const size_t packed = (((size_t)P * (P + 1) / 2) * sizeof(T) + 15) / 16 * 16 + vec;
   const int use_smem = packed <= kSmemBudget;
   const size_t sm = use_smem ? packed : vec;
   const int refine = mixed ? prm.refine_steps : 0;
   cudaFuncSetAttribute(k_factor_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_factor_solve<T><<<pv.B, 512, sm, (cudaStream_t)stream>>>(pv, wv, refine, use_smem);
+  k_factor_solve<T><<<pv.B, 256, sm, (cudaStream_t)stream>>>(pv, wv, refine, use_smem);
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -150,13 +281,13 @@ __global__ void k_backsub(PlanView pv, WorkView wv, Params prm, const double *al
   if (slot < cnt) {
     const int li = lm0 + slot;
     const double *dl = wv.delta + po + 6 * f0;
-    double s = 0.0;
-    for (int r = 0; r < 6 * nb; ++r) s += (double)slab[(size_t)r * SPGO_CHUNK + slot] * dl[r];
+    T s = T(0);
+    for (int r = 0; r < 6 * nb; ++r) s += slab[(size_t)r * SPGO_CHUNK + slot] * (T)dl[r];
     const double C = (double)reinterpret_cast<const T *>(wv.C)[li];
     const double ga = (double)reinterpret_cast<const T *>(wv.ga)[li];
     const double lam = wv.lm[b].lam;
     const double Dd = C * (1.0 + lam) + (double)prm.eps;
-    const double da = (ga - s) / Dd;
+    const double da = (ga - (double)s) / Dd;
     pred = da * (ga + (Dd - C) * da);
     const int u = pv.lm_user[li];
     const double an = alpha[u] + da;
@@ -177,6 +308,7 @@ int launch_backsub(const PlanView &pv, const WorkView &wv, const Params &prm, co
 }
 
 // ---- T_k <- T_k Exp(scale * delta_k) in FP64; pred += delta^T (g + lam diag(A) delta) ----
+template <typename T>
 __global__ void k_update_poses(PlanView pv, WorkView wv, const double *poses, double *out, double scale,
                                int gate) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -195,20 +327,22 @@ __global__ void k_update_poses(PlanView pv, WorkView wv, const double *poses, do
 #pragma unroll
   for (int q = 0; q < 12; ++q) out[12 * (size_t)p + q] = Tn[q];
   const double lam = wv.lm[b].lam;
-  const double *A = wv.A + pv.p_S_off[b];
+  const T *A = reinterpret_cast<const T *>(wv.A) + pv.p_S_off[b];
+  const T *g = reinterpret_cast<const T *>(wv.g);
   double pred = 0.0;
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
     const double d = wv.delta[po + q];
-    const double akk = A[(size_t)(6 * k + q) * P + 6 * k + q];
-    pred += d * (wv.g[po + q] + lam * akk * d);
+    const double akk = (double)A[(size_t)(6 * k + q) * P + 6 * k + q];
+    pred += d * ((double)g[po + q] + lam * akk * d);
   }
   atomicAdd(wv.pred_acc + b, pred);
 }
 
+template <typename T>
 int launch_update_poses(const PlanView &pv, const WorkView &wv, const double *poses, double *poses_out,
                         double scale, int direct, void *stream) {
-  k_update_poses<<<grid_for(pv.NP, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, poses, poses_out, scale,
+  k_update_poses<T><<<grid_for(pv.NP, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, poses, poses_out, scale,
                                                                        direct ? GATE_ALL : GATE_RUNNING);
   ++g_launches;
   return (int)cudaGetLastError();
@@ -362,8 +496,58 @@ int launch_export_B_n(const PlanView &pv, const WorkView &wv, int problem, int n
   return (int)cudaGetLastError();
 }
 
+// dense damped reduced system of one problem, FP64 (both triangles), from A, S_L, g, g_L
+template <typename T>
+__global__ void k_export_S(PlanView pv, WorkView wv, int b, double *S, double *gS) {
+  const int P = 6 * pv.p_npose[b];
+  const size_t off = pv.p_S_off[b];
+  const int po = pv.p_param_off[b];
+  const T *A = reinterpret_cast<const T *>(wv.A) + off;
+  T *SL = reinterpret_cast<T *>(wv.SL) + off;
+  const double lam = wv.lm[b].lam;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)P * P) return;
+  const int r = (int)(t / P), c = (int)(t % P);
+  if (c > r) return;
+  const double v = s_entry(A, SL, P, r, c, lam);
+  S[(size_t)r * P + c] = v;
+  S[(size_t)c * P + r] = v;
+  if (c == 0) {
+    T *gL = reinterpret_cast<T *>(wv.gL) + po;
+    gS[r] = (double)reinterpret_cast<const T *>(wv.g)[po + r] - (double)gL[r];
+  }
+}
+
+template <typename T>
+int launch_export_S(const PlanView &pv, const WorkView &wv, int problem, double *S, double *gS, void *stream) {
+  const long long n = (long long)pv.max_P * pv.max_P;
+  k_export_S<T><<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(pv, wv, problem, S, gS);
+  ++g_launches;
+  // the Schur pass ran for every problem: clear all of S_L / g_L for the next one
+  cudaMemsetAsync(wv.SL, 0, (size_t)pv.total_S * sizeof(T), (cudaStream_t)stream);
+  cudaMemsetAsync(wv.gL, 0, (size_t)pv.total_params * sizeof(T), (cudaStream_t)stream);
+  return (int)cudaGetLastError();
+}
+template int launch_export_S<float>(const PlanView &, const WorkView &, int, double *, double *, void *);
+template int launch_export_S<double>(const PlanView &, const WorkView &, int, double *, double *, void *);
+
+__global__ void k_to_double(const void *src, int f64, double *dst, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dst[i] = f64 ? reinterpret_cast<const double *>(src)[i] : (double)reinterpret_cast<const float *>(src)[i];
+}
+
+int launch_to_double(const void *src, int f64, double *dst, int64_t n, void *stream) {
+  if (n <= 0) return 0;
+  k_to_double<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(src, f64, dst, n);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
 template int launch_factor_solve<float>(const PlanView &, const WorkView &, const Params &, int, void *);
 template int launch_factor_solve<double>(const PlanView &, const WorkView &, const Params &, int, void *);
+template int launch_update_poses<float>(const PlanView &, const WorkView &, const double *, double *, double, int, void *);
+template int launch_update_poses<double>(const PlanView &, const WorkView &, const double *, double *, double, int, void *);
 template int launch_backsub<float>(const PlanView &, const WorkView &, const Params &, const double *, double *, int, void *);
 template int launch_backsub<double>(const PlanView &, const WorkView &, const Params &, const double *, double *, int, void *);
 template int launch_export_B_n<float>(const PlanView &, const WorkView &, int, int, double *, double *, double *, void *);

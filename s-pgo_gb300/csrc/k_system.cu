@@ -7,10 +7,13 @@
 //
 // Pose-pose blocks (incremental chain, S-PGO's parameterisation): for i <= j,
 //   A(i, j) = Ad_i^T F(i, j) Ad_j,  F(i, j) = sum_{lo <= i, hi > j} M_{lo,hi},
-// with every M shifted to the world origin in FP64 first (E_x^T M E_x), then a
-// prefix sum over lo (fixed hi) and a suffix sum over hi (fixed i), in place.
+// computed by a prefix sum over lo (fixed hi, re-centring the running sum on
+// each row's camera centre) and a suffix sum over hi (fixed i).  Every sum is
+// kept about a nearby camera centre, so the working precision (FP32 in the
+// mixed path) never sees world-sized lever arms.
 // g(i) = Ad_i^T sum_{lo <= i < hi} m_{lo,hi} is the e = 0 diagonal of the same sums.
 #include "kernels.cuh"
+#include "frames.cuh"
 
 namespace spgo {
 
@@ -18,119 +21,162 @@ __device__ __forceinline__ constexpr int t6(int i, int j) {  // symmetric 6x6 up
   return i <= j ? i * 6 - (i * (i - 1)) / 2 + (j - i) : j * 6 - (j * (j - 1)) / 2 + (i - j);
 }
 
-// shift one pair record from origin x = left centre of frame lo to the world
-// origin (FP64) and clear the accumulator for the next linearisation
+// E_z^T M E_z and E_z^T m for E_z = [[I, 0], [-[z]x, I]]: moves a pair record
+// from origin x to origin y = x - z (K^y = K^x E_{x - y}).  With Z = [z]x:
+//   P' = P - Q Z + Z Q^T - Z R Z,  Q' = Q + Z R,  R' = R,  m' = [m_w + Z m_v ; m_v]
 template <typename T>
-__global__ void k_pair_shift(PlanView pv, WorkView wv) {
-  const int b = blockIdx.y;
-  if (!problem_active(wv.lm, b, GATE_RELIN)) return;
-  const int N = pv.p_npose[b], D = pv.p_pair_D[b];
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= N * D) return;
-  const int lo = t / D, d = t % D + 1;
-  if (lo + d > N) return;
-  const size_t rec = (size_t)(pv.p_pair_off[b] + t);
-  T *src = reinterpret_cast<T *>(wv.pair_acc) + rec * 27;
-  double M[21], m[6];
-#pragma unroll
-  for (int k = 0; k < 21; ++k) { M[k] = (double)src[k]; src[k] = T(0); }
-#pragma unroll
-  for (int k = 0; k < 6; ++k) { m[k] = (double)src[21 + k]; src[21 + k] = T(0); }
-  const double *x = wv.fr_c + (size_t)(pv.p_frame_off[b] + lo) * 6;
-  const double X[9] = {0, -x[2], x[1], x[2], 0, -x[0], -x[1], x[0], 0};
-  // blocks: P = M[w w], Q = M[w v], R = M[v v]
-  double P[9], Q[9], R[9];
+__device__ __forceinline__ void shift_record(T *v, const Vec3<T> &z) {
+  const T Z[9] = {T(0), -z.z, z.y, z.z, T(0), -z.x, -z.y, z.x, T(0)};
+  T P[9], Q[9], R[9];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      P[3 * i + j] = M[t6(i, j)];
-      Q[3 * i + j] = M[t6(i, 3 + j)];
-      R[3 * i + j] = M[t6(3 + i, 3 + j)];
+      P[3 * i + j] = v[t6(i, j)];
+      Q[3 * i + j] = v[t6(i, 3 + j)];
+      R[3 * i + j] = v[t6(3 + i, 3 + j)];
     }
-  // P' = P - Q X + X Q^T - X R X ;  Q' = Q + X R ;  R' = R
-  double QX[9], XQt[9], XR[9], XRX[9];
+  T QZ[9], ZQt[9], ZR[9];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      double a = 0, bq = 0, c = 0;
+      T a = T(0), bq = T(0), c = T(0);
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        a += Q[3 * i + k] * X[3 * k + j];
-        bq += X[3 * i + k] * Q[3 * j + k];
-        c += X[3 * i + k] * R[3 * k + j];
+        a += Q[3 * i + k] * Z[3 * k + j];
+        bq += Z[3 * i + k] * Q[3 * j + k];
+        c += Z[3 * i + k] * R[3 * k + j];
       }
-      QX[3 * i + j] = a;
-      XQt[3 * i + j] = bq;
-      XR[3 * i + j] = c;
+      QZ[3 * i + j] = a;
+      ZQt[3 * i + j] = bq;
+      ZR[3 * i + j] = c;
     }
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      double a = 0;
+    for (int j = i; j < 3; ++j) {
+      T zrz = T(0);
 #pragma unroll
-      for (int k = 0; k < 3; ++k) a += XR[3 * i + k] * X[3 * k + j];
-      XRX[3 * i + j] = a;
+      for (int k = 0; k < 3; ++k) zrz += ZR[3 * i + k] * Z[3 * k + j];
+      v[t6(i, j)] = P[3 * i + j] - QZ[3 * i + j] + ZQt[3 * i + j] - zrz;
     }
-  double *dst = wv.pair64 + rec * 27;
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = i; j < 3; ++j)
-      dst[t6(i, j)] = P[3 * i + j] - QX[3 * i + j] + XQt[3 * i + j] - XRX[3 * i + j];
+    for (int j = 0; j < 3; ++j) v[t6(i, 3 + j)] = Q[3 * i + j] + ZR[3 * i + j];
+  const T mv0 = v[24], mv1 = v[25], mv2 = v[26];
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) dst[t6(i, 3 + j)] = Q[3 * i + j] + XR[3 * i + j];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = i; j < 3; ++j) dst[t6(3 + i, 3 + j)] = R[3 * i + j];
-  // m' = [m_w + X m_v ; m_v]
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-    dst[21 + i] = m[i] + X[3 * i] * m[3] + X[3 * i + 1] * m[4] + X[3 * i + 2] * m[5];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) dst[24 + i] = m[3 + i];
+  for (int i = 0; i < 3; ++i) v[21 + i] += Z[3 * i] * mv0 + Z[3 * i + 1] * mv1 + Z[3 * i + 2] * mv2;
 }
 
-// prefix over lo for fixed hi:  P(i, hi) = sum_{lo <= i} M(lo, hi), in place
-__global__ void k_pair_prefix_lo(PlanView pv, WorkView wv) {
+// component `comp` (0..26) of the record v moved by E_z (see shift_record),
+// reading the whole 27-vector from shared memory
+template <typename T>
+__device__ __forceinline__ T shifted_component(const T *v, int comp, const Vec3<T> &z) {
+  const T Z[9] = {T(0), -z.z, z.y, z.z, T(0), -z.x, -z.y, z.x, T(0)};
+  auto Pm = [&](int i, int j) { return v[t6(i, j)]; };
+  auto Qm = [&](int i, int j) { return v[t6(i, 3 + j)]; };
+  auto Rm = [&](int i, int j) { return v[t6(3 + i, 3 + j)]; };
+  if (comp >= 21) {
+    const int r = comp - 21;
+    if (r >= 3) return v[comp];
+    return v[comp] + Z[3 * r] * v[24] + Z[3 * r + 1] * v[25] + Z[3 * r + 2] * v[26];
+  }
+  // (i, j), i <= j, of the upper-triangle index
+  int i = 0, rem = comp;
+  while (rem >= 6 - i) {
+    rem -= 6 - i;
+    ++i;
+  }
+  const int j = i + rem;
+  if (i >= 3) return v[comp];
+  if (j >= 3) {  // Q' = Q + Z R
+    T acc = Qm(i, j - 3);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc += Z[3 * i + k] * Rm(k, j - 3);
+    return acc;
+  }
+  // P' = P - Q Z + Z Q^T - Z R Z
+  T acc = Pm(i, j);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    acc -= Qm(i, k) * Z[3 * k + j];
+    acc += Z[3 * i + k] * Qm(j, k);
+    T zr = T(0);
+#pragma unroll
+    for (int l = 0; l < 3; ++l) zr += Rm(k, l) * Z[3 * l + j];
+    acc -= Z[3 * i + k] * zr;
+  }
+  return acc;
+}
+
+// pass A, one warp per (problem, hi), lane = component:
+// P(i, hi) = sum_{lo <= i} M(lo, hi), each term about its own origin c_lo; the
+// running sum is re-centred from c_{lo-1} to c_lo before adding M(lo, hi), so
+// every partial sum sits at the origin of its row i and only relative centres
+// enter the arithmetic.  Reads and clears the accumulators.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pair_prefix(PlanView pv, WorkView wv) {
+  __shared__ T acc_s[8][28];
   const int b = blockIdx.y;
   if (!problem_active(wv.lm, b, GATE_RELIN)) return;
   const int N = pv.p_npose[b], D = pv.p_pair_D[b];
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= N * 27) return;
-  const int hi = 1 + t / 27, comp = t % 27;
-  double *base = wv.pair64 + (size_t)pv.p_pair_off[b] * 27 + comp;
-  double acc = 0.0;
-  for (int lo = max(0, hi - D); lo < hi; ++lo) {
-    double *p = base + ((size_t)lo * D + (hi - lo - 1)) * 27;
-    acc += *p;
-    *p = acc;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int hi = 1 + blockIdx.x * (blockDim.x >> 5) + w;
+  if (hi > N) return;
+  const int fo = pv.p_frame_off[b];
+  T *acc_base = reinterpret_cast<T *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
+  T *out_base = reinterpret_cast<T *>(wv.pairF) + (size_t)pv.p_pair_off[b] * 27;
+  T *acc = acc_s[w];
+  if (lane < 27) acc[lane] = T(0);
+  __syncwarp();
+  const int lo0 = max(0, hi - D);
+  const int cl = lane < 27 ? lane : 0;
+  T next = acc_base[((size_t)lo0 * D + (hi - lo0 - 1)) * 27 + cl];  // prefetched one record ahead
+  for (int lo = lo0; lo < hi; ++lo) {
+    const size_t rec = (size_t)lo * D + (hi - lo - 1);
+    const T cur = next;
+    if (lo + 1 < hi) next = acc_base[((size_t)(lo + 1) * D + (hi - lo - 2)) * 27 + cl];
+    if (lo > lo0) {
+      const Vec3<T> z = FramesT<T>::rel(wv, fo + lo - 1, 0, fo + lo, 0);
+      const T v = lane < 27 ? shifted_component(acc, lane, z) : T(0);
+      __syncwarp();
+      if (lane < 27) acc[lane] = v;
+      __syncwarp();
+    }
+    if (lane < 27) {
+      const T nv = acc[lane] + cur;
+      acc_base[rec * 27 + lane] = T(0);
+      acc[lane] = nv;
+      out_base[rec * 27 + lane] = nv;
+    }
+    __syncwarp();
   }
 }
 
-// suffix over hi for fixed i:  F(i, i + e) = sum_{d' > e} P(i, i + d'), in place
-__global__ void k_pair_suffix_hi(PlanView pv, WorkView wv) {
+// pass B, one thread per (problem, i, component): F(i, i + e) = sum_{d' > e} P(i, i + d')
+// (all about origin c_i), in place
+template <typename T>
+__global__ void k_pair_suffix(PlanView pv, WorkView wv) {
   const int b = blockIdx.y;
   if (!problem_active(wv.lm, b, GATE_RELIN)) return;
   const int N = pv.p_npose[b], D = pv.p_pair_D[b];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= N * 27) return;
   const int i = t / 27, comp = t % 27;
-  double *base = wv.pair64 + ((size_t)pv.p_pair_off[b] + (size_t)i * D) * 27 + comp;
-  double acc = 0.0;
+  T *base = reinterpret_cast<T *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + (size_t)i * D) * 27 + comp;
+  T acc = T(0);
   for (int dp = min(D, N - i); dp >= 1; --dp) {
-    double *p = base + (size_t)(dp - 1) * 27;
+    T *p = base + (size_t)(dp - 1) * 27;
     acc += *p;
     *p = acc;
   }
 }
 
-// A(i, j) = Ad_i^T F(i, j) Ad_j and g(i) = Ad_i^T f(i); Ad = [[R, 0], [[c]x R, R]]
+// A(i, j) = Ad_i^T F(i, j) Ad_j about origin c_i: Ad_i = diag(R_i, R_i),
+// Ad_j = [[R_j, 0], [[c_j - c_i]x R_j, R_j]];  g(i) = [R_i^T f_w ; R_i^T f_v]
+template <typename T>
 __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
   const int b = blockIdx.y;
   if (!problem_active(wv.lm, b, GATE_RELIN)) return;
@@ -142,51 +188,40 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
   const int j = i + e;
   const int P = 6 * N;
   const int fo = pv.p_frame_off[b];
-  const double *F = wv.pair64 + ((size_t)pv.p_pair_off[b] + (size_t)i * D + e) * 27;
-  const double *Ri = wv.fr_Rd + (size_t)(fo + i) * 18, *ci = wv.fr_c + (size_t)(fo + i) * 6;
-  const double *Rj = wv.fr_Rd + (size_t)(fo + j) * 18, *cj = wv.fr_c + (size_t)(fo + j) * 6;
-  // C R = [c]x R for both frames
-  double CRi[9], CRj[9];
+  const T *F = reinterpret_cast<const T *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + (size_t)i * D + e) * 27;
+  const T *Ri = FramesT<T>::R(wv, fo + i, 0);
+  const T *Rj = FramesT<T>::R(wv, fo + j, 0);
+  const Vec3<T> cji = FramesT<T>::rel(wv, fo + j, 0, fo + i, 0);
+  // C R_j with C = [c_j - c_i]x
+  T CRj[9];
   {
-    const double Xi[9] = {0, -ci[2], ci[1], ci[2], 0, -ci[0], -ci[1], ci[0], 0};
-    const double Xj[9] = {0, -cj[2], cj[1], cj[2], 0, -cj[0], -cj[1], cj[0], 0};
+    const T X[9] = {T(0), -cji.z, cji.y, cji.z, T(0), -cji.x, -cji.y, cji.x, T(0)};
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        double a = 0, bb = 0;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          a += Xi[3 * r + k] * Ri[3 * k + c];
-          bb += Xj[3 * r + k] * Rj[3 * k + c];
-        }
-        CRi[3 * r + c] = a;
-        CRj[3 * r + c] = bb;
-      }
+      for (int c = 0; c < 3; ++c)
+        CRj[3 * r + c] = X[3 * r] * Rj[c] + X[3 * r + 1] * Rj[3 + c] + X[3 * r + 2] * Rj[6 + c];
   }
-  double *A = wv.A + pv.p_S_off[b];
+  T *A = reinterpret_cast<T *>(wv.A) + pv.p_S_off[b];
   for (int col = 0; col < 6; ++col) {
-    // column `col` of Ad_j
-    double adj[6];
+    T adj[6];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      adj[r] = col < 3 ? Rj[3 * r + col] : 0.0;
+      adj[r] = col < 3 ? Rj[3 * r + col] : T(0);
       adj[3 + r] = col < 3 ? CRj[3 * r + col] : Rj[3 * r + col - 3];
     }
-    double w[6];
+    T w[6];
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-      double a = 0;
+      T a = T(0);
 #pragma unroll
       for (int k = 0; k < 6; ++k) a += F[t6(r, k)] * adj[k];
       w[r] = a;
     }
-    // out = Ad_i^T w : rows 0-2 = R_i^T w_w + (C_i R_i)^T w_v ; rows 3-5 = R_i^T w_v
-    double out[6];
+    T out[6];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      out[r] = Ri[r] * w[0] + Ri[3 + r] * w[1] + Ri[6 + r] * w[2] + CRi[r] * w[3] + CRi[3 + r] * w[4] +
-               CRi[6 + r] * w[5];
+      out[r] = Ri[r] * w[0] + Ri[3 + r] * w[1] + Ri[6 + r] * w[2];
       out[3 + r] = Ri[r] * w[3] + Ri[3 + r] * w[4] + Ri[6 + r] * w[5];
     }
 #pragma unroll
@@ -196,12 +231,11 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
     }
   }
   if (e == 0) {
-    const double *f = F + 21;
-    double *g = wv.g + pv.p_param_off[b] + 6 * i;
+    const T *f = F + 21;
+    T *g = reinterpret_cast<T *>(wv.g) + pv.p_param_off[b] + 6 * i;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      g[r] = Ri[r] * f[0] + Ri[3 + r] * f[1] + Ri[6 + r] * f[2] + CRi[r] * f[3] + CRi[3 + r] * f[4] +
-             CRi[6 + r] * f[5];
+      g[r] = Ri[r] * f[0] + Ri[3 + r] * f[1] + Ri[6 + r] * f[2];
       g[3 + r] = Ri[r] * f[3] + Ri[3 + r] * f[4] + Ri[6 + r] * f[5];
     }
   }
@@ -211,14 +245,12 @@ template <typename T>
 int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream) {
   (void)gate;
   cudaStream_t st = (cudaStream_t)stream;
+  const int nmax = pv.max_P / 6;
   const int nd = pv.max_D > 0 ? pv.max_D : 1;
-  dim3 g1(grid_for((long long)(pv.max_P / 6) * nd, 128), pv.B);
-  k_pair_shift<T><<<g1, 128, 0, st>>>(pv, wv);
-  dim3 g2(grid_for((long long)(pv.max_P / 6) * 27, 128), pv.B);
-  k_pair_prefix_lo<<<g2, 128, 0, st>>>(pv, wv);
-  k_pair_suffix_hi<<<g2, 128, 0, st>>>(pv, wv);
-  k_pairs_to_A<<<g1, 128, 0, st>>>(pv, wv);
-  g_launches += 4;
+  k_pair_prefix<T><<<dim3(grid_for(nmax, 8), pv.B), 256, 0, st>>>(pv, wv);
+  k_pair_suffix<T><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);
+  k_pairs_to_A<T><<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
+  g_launches += 3;
   return (int)cudaGetLastError();
 }
 
@@ -308,50 +340,9 @@ int launch_schur(const PlanView &pv, const WorkView &wv, const Params &prm, void
   return (int)cudaGetLastError();
 }
 
-// ---- S = A + lam diag(A) - S_L (both triangles), g_S = g - g_L; clears S_L / g_L ----
-template <typename T>
-__global__ void k_assemble(PlanView pv, WorkView wv) {
-  const int b = blockIdx.y;
-  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
-  const int N = pv.p_npose[b], P = 6 * N;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)P * P) return;
-  const int r = (int)(t / P), c = (int)(t % P);
-  constexpr int TR = 6 * SPGO_TILE_BLOCKS;
-  if (r / TR < c / TR) return;  // handled by the mirrored element
-  const double lam = wv.lm[b].lam;
-  const size_t off = pv.p_S_off[b];
-  T *SL = reinterpret_cast<T *>(wv.SL) + off;
-  const double sl = (double)SL[(size_t)r * P + c];
-  SL[(size_t)r * P + c] = T(0);
-  const double *A = wv.A + off;
-  double *S = wv.S + off;
-  double v = A[(size_t)r * P + c] - sl;
-  if (r == c) v += lam * A[(size_t)r * P + c];
-  S[(size_t)r * P + c] = v;
-  // diagonal tiles hold both halves; an off-diagonal tile also fills its mirror
-  if (r / TR != c / TR) S[(size_t)c * P + r] = v;
-  if (c == 0) {
-    const int po = pv.p_param_off[b];
-    T *gL = reinterpret_cast<T *>(wv.gL) + po;
-    wv.gS[po + r] = wv.g[po + r] - (double)gL[r];
-    gL[r] = T(0);
-  }
-}
-
-template <typename T>
-int launch_assemble(const PlanView &pv, const WorkView &wv, void *stream) {
-  dim3 g(grid_for((long long)pv.max_P * pv.max_P, 256), pv.B);
-  k_assemble<T><<<g, 256, 0, (cudaStream_t)stream>>>(pv, wv);
-  ++g_launches;
-  return (int)cudaGetLastError();
-}
-
 template int launch_system<float>(const PlanView &, const WorkView &, int, void *);
 template int launch_system<double>(const PlanView &, const WorkView &, int, void *);
 template int launch_schur<float>(const PlanView &, const WorkView &, const Params &, void *);
 template int launch_schur<double>(const PlanView &, const WorkView &, const Params &, void *);
-template int launch_assemble<float>(const PlanView &, const WorkView &, void *);
-template int launch_assemble<double>(const PlanView &, const WorkView &, void *);
 
 }  // namespace spgo

@@ -43,6 +43,7 @@ struct PlanView {                 // device pointers into the static buffer
   const float *lm_uv;     // [L][2]
   const int64_t *lm_obs;  // [L+1]
   // per observation
+  const uint8_t *obs_slot;   // landmark slot inside its chunk
   const int32_t *obs_frame;
   const float *obs_uv;    // [O][4]
   // chunks
@@ -53,6 +54,9 @@ struct PlanView {                 // device pointers into the static buffer
   // frame -> problem
   const int32_t *fr_prob;
   const int32_t *pose_prob;
+  // tensor-core Schur work items
+  const int32_t *tc_prob, *tc_row0, *tc_col0, *tc_ncols, *tc_cbeg, *tc_cend, *tc_chunks;
+  int32_t n_tc_items;
 };
 
 struct LMState {
@@ -64,18 +68,19 @@ struct LMState {
 struct WorkView {
   // frame tables: [F][2 cams] rotation (cam->world) and centre
   float *fr_Rf;     // [F][2][9]
+  float *fr_Rl;     // [F][2][9] float(R - float(R))
   double *fr_Rd;    // [F][2][9]
   double *fr_c;     // [F][2][3]
+  float *fr_ch;     // [F][2][3] float(c)
+  float *fr_cl;     // [F][2][3] float(c - float(c))
   double *poses_cand;   // [NP][12]
   double *alpha_cand;   // [L] (caller order)
-  void *pair_acc;       // [total_pairs][27] T
-  double *pair64;       // [total_pairs][27]
-  double *A;            // [total_S]
-  double *g;            // [total_params]
-  void *SL;             // [total_S] T
+  void *pair_acc;       // [total_pairs][27] T  (accumulated by the linearisation)
+  void *pairF;          // [total_pairs][27] T  (prefix / suffix sums)
+  void *A;              // [total_S] T      pose-pose blocks
+  void *g;              // [total_params] T pose gradient
+  void *SL;             // [total_S] T      landmark Schur term (lower tiles)
   void *gL;             // [total_params] T
-  double *S;            // [total_S]
-  double *gS;           // [total_params]
   void *fac;            // [total_S] T   (global-memory factor for large problems)
   double *delta;        // [total_params]
   void *C;              // [L] T
@@ -91,6 +96,7 @@ struct Params {
   float loss_scale, eps, alpha_min, alpha_max;
   double lambda0, lambda_max, tol;
   int32_t max_iters, refine_steps;
+  int32_t use_graph, use_tc;
 };
 
 // launch wrappers (defined in the .cu files); all return cudaError_t as int
@@ -103,13 +109,12 @@ int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream
 template <typename T>
 int launch_schur(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
 template <typename T>
-int launch_assemble(const PlanView &pv, const WorkView &wv, void *stream);
-template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed,
                         void *stream);
 template <typename T>
 int launch_backsub(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
                    double *alpha_out, int direct, void *stream);
+template <typename T>
 int launch_update_poses(const PlanView &pv, const WorkView &wv, const double *poses, double *poses_out,
                         double scale, int direct, void *stream);
 int launch_decide(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
@@ -119,6 +124,11 @@ int launch_reset(const PlanView &pv, const WorkView &wv, const Params &prm, doub
 template <typename T>
 int launch_export_B_n(const PlanView &pv, const WorkView &wv, int problem, int n_chunks, double *B,
                       double *C, double *ga, void *stream);
+
+int launch_schur_tc(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
+template <typename T>
+int launch_export_S(const PlanView &pv, const WorkView &wv, int problem, double *S, double *gS, void *stream);
+int launch_to_double(const void *src, int f64, double *dst, int64_t n, void *stream);
 
 // count of kernel launches made by this library in this process
 extern int64_t g_launches;

@@ -24,7 +24,7 @@ EXPORTED = [
     "spgo_plan_destroy", "spgo_plan_offsets", "spgo_solver_create", "spgo_solver_destroy", "spgo_set_params",
     "spgo_gn_step", "spgo_lm_reset", "spgo_lm_iterate", "spgo_lm_status", "spgo_lm_solve",
     "spgo_export_system", "spgo_launch_count", "spgo_profile_enable", "spgo_profile_read",
-    "spgo_cost_noalloc",
+    "spgo_cost_noalloc", "spgo_export_reduced",
 ]
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
                  "update", "bookkeeping"]
@@ -41,7 +41,7 @@ class HostProblem(C.Structure):
 class PlanSizes(C.Structure):
     _fields_ = [("n_problems", C.c_int32), ("total_poses", C.c_int32), ("total_landmarks", C.c_int32),
                 ("total_obs", C.c_int64), ("n_chunks", C.c_int32), ("n_schur_items", C.c_int32),
-                ("max_params", C.c_int32), ("reserved", C.c_int32), ("static_bytes", C.c_size_t),
+                ("max_params", C.c_int32), ("schur_chunk_tiles", C.c_int32), ("static_bytes", C.c_size_t),
                 ("workspace_bytes", C.c_size_t), ("slab_elems", C.c_int64), ("pair_records", C.c_int64)]
 
 
@@ -49,7 +49,7 @@ class Params(C.Structure):
     _fields_ = [("loss", C.c_int32), ("near_boost", C.c_int32), ("loss_scale", C.c_float), ("eps", C.c_float),
                 ("alpha_min", C.c_float), ("alpha_max", C.c_float), ("lambda0", C.c_double),
                 ("lambda_max", C.c_double), ("tol", C.c_double), ("max_iters", C.c_int32),
-                ("refine_steps", C.c_int32)]
+                ("refine_steps", C.c_int32), ("use_graph", C.c_int32), ("use_tc", C.c_int32)]
 
 
 class ProblemStatus(C.Structure):
@@ -96,6 +96,8 @@ def lib() -> C.CDLL:
     L.spgo_lm_status.argtypes = [vp, C.POINTER(ProblemStatus), vp]
     L.spgo_lm_solve.argtypes = [vp, i32, C.POINTER(C.c_int32), vp]
     L.spgo_export_system.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
+    L.spgo_export_reduced.argtypes = [vp, i32, C.c_double, vp, vp, vp]
+    L.spgo_export_reduced.restype = C.c_int
     L.spgo_profile_enable.argtypes = [vp, i32]
     L.spgo_profile_read.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), i32, vp]
     L.spgo_cost_noalloc.argtypes = [C.POINTER(DeviceProblem), vp, vp, C.POINTER(Params), vp, vp]

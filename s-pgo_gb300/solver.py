@@ -160,7 +160,7 @@ class BatchSolver:
     # -- parameters ---------------------------------------------------------------
     def set_params(self, loss: Optional[str] = None, loss_scale=None, near_boost=None, eps=None,
                    alpha_min=None, alpha_max=None, lambda0=None, lambda_max=None, tol=None, max_iters=None,
-                   refine_steps=None):
+                   refine_steps=None, use_graph=None, use_tc=None):
         p = self.params
         if loss is not None:
             p.loss = _LOSS[loss]
@@ -175,6 +175,10 @@ class BatchSolver:
             p.max_iters = int(max_iters)
         if refine_steps is not None:
             p.refine_steps = int(refine_steps)
+        if use_graph is not None:
+            p.use_graph = int(bool(use_graph))
+        if use_tc is not None:
+            p.use_tc = int(bool(use_tc))
         self._apply_params()
 
     def _apply_params(self):
@@ -223,6 +227,16 @@ class BatchSolver:
 
     def slab_floats(self) -> int:
         return int(self.sizes.slab_elems)
+
+    def export_reduced(self, b: int, lam: float) -> dict:
+        """Damped reduced camera system S = A + lam diag(A) - B D^-1 B^T and g_S of problem b (FP64)."""
+        P = 6 * int(self.problems[b].n_poses)
+        S = torch.zeros(P * P, dtype=torch.float64, device=self.device)
+        gS = torch.zeros(P, dtype=torch.float64, device=self.device)
+        nat.check(self.L.spgo_export_reduced(self._solver, int(b), float(lam), C.c_void_p(S.data_ptr()),
+                                             C.c_void_p(gS.data_ptr()), self._sp()), "export_reduced")
+        self.synchronize()
+        return dict(S=S.cpu().numpy().reshape(P, P), gS=gS.cpu().numpy())
 
     def launch_count(self) -> int:
         return int(self.L.spgo_launch_count(self._solver))

@@ -1,0 +1,58 @@
+"""Damped reduced camera system S = A + lam diag(A) - B D^-1 B^T and g_S from the
+CUDA path (SIMT and tensor-core Schur complements) against the FP64 oracle.
+Tolerances, relative to the largest entry: FP64 path 1e-9; mixed path with SIMT
+FP32 Schur 1e-4; mixed path with the tensor-core Schur (TF32 operands, 10-bit
+mantissa, FP32 accumulation) 2e-3."""
+import numpy as np
+import pytest
+
+import spgo_gb300.scenes as scenes
+from spgo_gb300.solver import BatchSolver
+from oracle import solver as S
+
+pytestmark = pytest.mark.gpu
+
+
+def f32_obs(p):
+    q = p.copy()
+    q.obs_uv = p.obs_uv.astype(np.float32).astype(np.float64)
+    q.anchor_uv = p.anchor_uv.astype(np.float32).astype(np.float64)
+    q.intrinsics = p.intrinsics.astype(np.float32).astype(np.float64)
+    return q
+
+
+def oracle_reduced(p, lam, eps=1e-4):
+    lin = S.linearize(f32_obs(p), S.Loss())
+    D = lin.C * (1.0 + lam) + eps
+    BD = lin.B / D[None, :]
+    Sm = lin.A + np.diag(lam * np.diag(lin.A)) - BD @ lin.B.T
+    return Sm, lin.g_T - BD @ lin.g_a
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.mark.parametrize("prec,use_tc,tol", [("fp64", 0, 1e-9), ("mixed", 0, 1e-4), ("mixed", 1, 2e-3)])
+def test_reduced_system_matches_oracle(built_lib, cuda_device, prec, use_tc, tol):
+    # sizes that exercise one and two 128-row tensor-core tiles and partial column ranges
+    probs = [scenes.circle_scene(s, n, l) for s, n, l in [(301, 9, 240), (302, 26, 700), (303, 14, 380)]]
+    bs = BatchSolver(probs, precision=prec)
+    bs.set_params(loss="l2", use_tc=use_tc)
+    for lam in (1e-4, 0.5):
+        for b, p in enumerate(probs):
+            got = bs.export_reduced(b, lam)
+            Sm, gS = oracle_reduced(p, lam)
+            assert rel(got["S"], Sm) < tol, (b, lam)
+            assert rel(got["gS"], gS) < max(tol, 1e-6), (b, lam)
+
+
+def test_tensor_core_solve_converges(built_lib, cuda_device):
+    """LM with the tensor-core Schur reaches the oracle's converged cost."""
+    probs = [scenes.circle_scene(s, n, l) for s, n, l in [(200, 8, 500), (205, 18, 455), (214, 31, 234)]]
+    bs = BatchSolver([f32_obs(p) for p in probs], precision="mixed")
+    bs.set_params(loss="l2", max_iters=30, tol=1e-6, use_tc=1)
+    sts = bs.solve()
+    for b, p in enumerate(probs):
+        res = S.lm_solve(f32_obs(p), S.Loss(), max_iters=30, tol=1e-6)
+        assert abs(sts[b]["cost"] - res.cost) / res.cost < 1e-6
