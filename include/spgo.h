@@ -186,6 +186,40 @@ int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, do
  * gS [P].  For parity checks of the Schur complement. */
 int spgo_export_reduced(spgo_solver *s, int32_t problem, double lambda, double *S, double *gS, void *stream);
 
+/* ---- learned damping controller (no counterpart in the reference) ---------
+ * A 16 -> 64 -> 64 -> 2 MLP (exact GELU) proposes the next LM damping from the
+ * cost, gain-ratio history, lambda, gradient and Hessian-diagonal statistics.
+ * Parameters: one flat FP32 vector of SPGO_MLP_PARAMS floats, W1 [64x16] (out x
+ * in), b1 [64], W2 [64x64], b2 [64], W3 [2x64], b3 [2].  Outputs: change of
+ * log10(lambda) and the logit that the current damping yields an accepted step. */
+#define SPGO_MLP_PARAMS 5378
+#define SPGO_MLP_INPUTS 16
+
+/* FP32 forward of n feature rows d_X [n*16] -> d_out [n*2]; d_cache [n*128]
+ * (or NULL) keeps the pre-activations for spgo_mlp_grad. */
+int spgo_mlp_forward(const float *d_params, const float *d_X, int32_t n, float *d_out, float *d_cache,
+                     void *stream);
+/* Mean loss (out0 - t0)^2 + BCE(out1, t1) over n samples with targets d_T [n*2]
+ * and its gradient d_grad [SPGO_MLP_PARAMS]; d_loss [1]; scratch d_out [n*2],
+ * d_cache [n*128]. */
+int spgo_mlp_grad(const float *d_params, const float *d_X, const float *d_T, int32_t n, float *d_grad,
+                  float *d_loss, float *d_out, float *d_cache, void *stream);
+/* One Adam step (beta 0.9 / 0.999) on the parameters; step counts from 1. */
+int spgo_mlp_adam(float *d_params, const float *d_grad, float *d_m, float *d_v, int32_t step, float lr,
+                  void *stream);
+/* Use the controller (BF16 weights, converted from d_params) in spgo_lm_iterate:
+ * after an accepted step its proposal replaces the Nielsen update when its
+ * accept logit is positive; a rejected step always falls back to Nielsen.
+ * d_params = NULL switches it off. */
+int spgo_lm_set_controller(spgo_solver *s, const float *d_params, void *stream);
+/* The controller's 16 inputs for every problem at its current state, d_feat [B*16]. */
+int spgo_lm_features(spgo_solver *s, float *d_feat, void *stream);
+/* Linearise where needed, then for each of n_factors (<= 32) damping factors f
+ * evaluate the cost of the step taken with lambda * f for every running problem,
+ * leaving the state and the LM bookkeeping unchanged; host costs [n_factors*B]
+ * (synchronises the stream). */
+int spgo_lm_probe(spgo_solver *s, int32_t n_factors, const double *factors, double *costs, void *stream);
+
 /* Count of kernel launches enqueued by this solver since creation. */
 int64_t spgo_launch_count(const spgo_solver *s);
 

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -59,7 +60,7 @@ struct spgo_plan {
   int64_t total_S = 0, total_pairs = 0, total_slab = 0;
   std::vector<int32_t> p_npose, p_frame_off, p_pose_off, p_lm_off, p_lm_cnt, p_pair_D, p_param_off, p_chunk_off,
       p_chunk_cnt, fr_prob, pose_prob;
-  std::vector<int64_t> p_S_off, p_pair_off;
+  std::vector<int64_t> p_S_off, p_pair_off, p_nres;
   std::vector<float> p_intr;
   std::vector<double> p_Trl;
   std::vector<int32_t> lm_prob, lm_host, lm_lo, lm_hi, lm_user, lm_chunk, lm_slot;
@@ -77,7 +78,7 @@ struct spgo_plan {
   size_t static_bytes = 0, ws_bytes = 0;
   // workspace segment offsets
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
-      w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred;
+      w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -98,7 +99,8 @@ static void build_layout(spgo_plan *p) {
   p->static_bytes = 0;
   add_seg(p, p->p_npose); add_seg(p, p->p_frame_off); add_seg(p, p->p_pose_off); add_seg(p, p->p_lm_off);
   add_seg(p, p->p_lm_cnt); add_seg(p, p->p_pair_D); add_seg(p, p->p_param_off); add_seg(p, p->p_chunk_off);
-  add_seg(p, p->p_chunk_cnt); add_seg(p, p->p_S_off); add_seg(p, p->p_pair_off); add_seg(p, p->p_intr);
+  add_seg(p, p->p_chunk_cnt); add_seg(p, p->p_S_off); add_seg(p, p->p_pair_off); add_seg(p, p->p_nres);
+  add_seg(p, p->p_intr);
   add_seg(p, p->p_Trl); add_seg(p, p->lm_prob); add_seg(p, p->lm_host); add_seg(p, p->lm_lo); add_seg(p, p->lm_hi);
   add_seg(p, p->lm_user); add_seg(p, p->lm_chunk); add_seg(p, p->lm_slot); add_seg(p, p->lm_uv);
   add_seg(p, p->lm_obs); add_seg(p, p->obs_frame); add_seg(p, p->obs_uv); add_seg(p, p->ch_prob);
@@ -132,15 +134,18 @@ static void build_layout(spgo_plan *p) {
   p->w_gL = take((size_t)p->total_params * ts);
   // global factor storage only when a problem is too large for the shared-memory path
   const size_t P = (size_t)p->max_P;
-  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8) + 16;
+  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8 + 4) + 16;
   p->w_fac = take(packed <= 200 * 1024 ? 0 : (size_t)p->total_S * ts);
   p->w_delta = take((size_t)p->total_params * 8);
-  p->w_C = take((size_t)p->L * ts);
+  p->w_C = take((size_t)(p->L + 64) * ts);  // + 64: the tensor-core Schur copies 16-byte aligned supersets
   p->w_ga = take((size_t)p->L * ts);
   p->w_slab = take((size_t)p->total_slab * ts);
   p->w_lm = take((size_t)p->B * sizeof(LMState));
   p->w_cost = take((size_t)p->B * 8);
   p->w_pred = take((size_t)p->B * 8);
+  p->w_lmb = take((size_t)p->B * sizeof(LMState));
+  p->w_probe = take((size_t)p->B * 32 * 8);
+  p->w_ctrl = take((size_t)SPGO_MLP_PARAMS * 2);
   p->ws_bytes = o;
 }
 
@@ -272,14 +277,13 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
           p->wk_cend.push_back((int32_t)p->wk_chunks.size());
         }
       }
-    // tensor-core Schur work list: 128-row tiles, lower-triangle columns in ranges of <= 256
+    // tensor-core Schur work list: 128 x 128 tiles of the lower triangle, <= 64 chunks each
     {
       const int P = 6 * N;
       const int kTcSplit = 64;
       for (int row0 = 0; row0 < P; row0 += 128) {
-        const int colmax = std::min(P, row0 + 128);
-        for (int col0 = 0; col0 < colmax; col0 += 256) {
-          const int ncols = ((std::min(256, colmax - col0) + 15) / 16) * 16;
+        for (int col0 = 0; col0 <= row0; col0 += 128) {
+          const int ncols = ((std::min(128, P - col0) + 15) / 16) * 16;
           std::vector<int32_t> lst;
           for (int c = ch_begin; c < ch_end; ++c) {
             const int s0 = 6 * p->ch_f0[c], s1 = 6 * (p->ch_f0[c] + p->ch_nb[c]);
@@ -310,6 +314,7 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     p->p_chunk_cnt.push_back(ch_end - ch_begin);
     p->p_S_off.push_back(S_off);
     p->p_pair_off.push_back(pair_off);
+    p->p_nres.push_back(4 * q.n_obs);
     for (int k = 0; k < 8; ++k) p->p_intr.push_back(q.intrinsics[k]);
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 4; ++c) p->p_Trl.push_back(q.T_r_to_l[4 * r + c]);
@@ -348,6 +353,7 @@ struct spgo_solver {
   double *poses, *alpha;
   unsigned char *d_static, *d_ws;
   int64_t launches0;
+  bool controller = false;  // learned damping active
   // optional per-kernel timing: event pairs recorded around each launch
   bool prof = false;
   std::vector<cudaEvent_t> ev;
@@ -412,7 +418,8 @@ static void make_views(spgo_solver *s) {
   v.p_lm_cnt = seg_ptr<int32_t>(p, st, i++); v.p_pair_D = seg_ptr<int32_t>(p, st, i++);
   v.p_param_off = seg_ptr<int32_t>(p, st, i++); v.p_chunk_off = seg_ptr<int32_t>(p, st, i++);
   v.p_chunk_cnt = seg_ptr<int32_t>(p, st, i++); v.p_S_off = seg_ptr<int64_t>(p, st, i++);
-  v.p_pair_off = seg_ptr<int64_t>(p, st, i++); v.p_intr = seg_ptr<float>(p, st, i++);
+  v.p_pair_off = seg_ptr<int64_t>(p, st, i++); v.p_nres = seg_ptr<int64_t>(p, st, i++);
+  v.p_intr = seg_ptr<float>(p, st, i++);
   v.p_Trl = seg_ptr<double>(p, st, i++); v.lm_prob = seg_ptr<int32_t>(p, st, i++);
   v.lm_host = seg_ptr<int32_t>(p, st, i++); v.lm_lo = seg_ptr<int32_t>(p, st, i++);
   v.lm_hi = seg_ptr<int32_t>(p, st, i++); v.lm_user = seg_ptr<int32_t>(p, st, i++);
@@ -456,15 +463,25 @@ static void make_views(spgo_solver *s) {
   x.lm = reinterpret_cast<LMState *>(w + p->w_lm);
   x.cost_acc = reinterpret_cast<double *>(w + p->w_cost);
   x.pred_acc = reinterpret_cast<double *>(w + p->w_pred);
+  x.lm_backup = reinterpret_cast<LMState *>(w + p->w_lmb);
+  x.probe_costs = reinterpret_cast<double *>(w + p->w_probe);
+  x.ctrl_bf16 = w + p->w_ctrl;
 }
 
 // one linearisation + reduced system (+ damping from the device-side lambda)
+// `stats`: refresh the controller's per-problem statistics; `ctrl`: let the learned
+// controller set lambda for the step about to be taken from the fresh linearisation
 template <typename T>
-static int enqueue_linearize(spgo_solver *s, cudaStream_t st) {
+static int enqueue_linearize(spgo_solver *s, cudaStream_t st, bool stats, bool ctrl) {
   { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_RELIN, st)); }
   { PROF(K_LINEARIZE); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 0, GATE_RELIN, st)); }
   { PROF(K_SYSTEM); CUDA_TRY(launch_system<T>(s->pv, s->wv, GATE_RELIN, st)); }
-  { PROF(K_BOOKKEEP); CUDA_TRY(launch_post_linearize(s->pv, s->wv, st)); }
+  {
+    PROF(K_BOOKKEEP);
+    if (stats || ctrl) CUDA_TRY(launch_lm_stats(s->pv, s->wv, std::is_same<T, double>::value, st));
+    CUDA_TRY(launch_post_linearize(s->pv, s->wv, st));
+    if (ctrl) CUDA_TRY(launch_controller(s->pv, s->wv, s->wv.ctrl_bf16, st));
+  }
   return SPGO_OK;
 }
 
@@ -485,13 +502,16 @@ static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
 template <typename T>
 static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
   int rc;
-  if ((rc = enqueue_linearize<T>(s, st)) != SPGO_OK) return rc;
+  if ((rc = enqueue_linearize<T>(s, st, s->controller, s->controller)) != SPGO_OK) return rc;
   if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
   { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st)); }
   { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
   { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, st)); }
   { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st)); }
-  { PROF(K_BOOKKEEP); CUDA_TRY(launch_decide(s->pv, s->wv, s->prm, st)); }
+  {
+    PROF(K_BOOKKEEP);
+    CUDA_TRY(launch_decide(s->pv, s->wv, s->prm, st));
+  }
   { PROF(K_BOOKKEEP); CUDA_TRY(launch_commit(s->pv, s->wv, s->poses, s->alpha, st)); }
   return SPGO_OK;
 }
@@ -501,11 +521,30 @@ static int enqueue_gn(spgo_solver *s, int iters, float step_size, cudaStream_t s
   for (int it = 0; it < iters; ++it) {
     { PROF(K_BOOKKEEP); CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, 0.0, st)); }
     int rc;
-    if ((rc = enqueue_linearize<T>(s, st)) != SPGO_OK) return rc;
+    if ((rc = enqueue_linearize<T>(s, st, false, false)) != SPGO_OK) return rc;
     if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
     { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->alpha, 1, st)); }
     { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->poses, (double)step_size, 1, st)); }
   }
+  return SPGO_OK;
+}
+
+template <typename T>
+static int enqueue_probe(spgo_solver *s, int nf, const double *factors, cudaStream_t st) {
+  int rc;
+  // the statistics feed the features of the probed states; the controller does not act
+  if ((rc = enqueue_linearize<T>(s, st, true, false)) != SPGO_OK) return rc;
+  CUDA_TRY(cudaMemcpyAsync(s->wv.lm_backup, s->wv.lm, sizeof(LMState) * s->plan->B, cudaMemcpyDeviceToDevice, st));
+  for (int j = 0; j < nf; ++j) {
+    CUDA_TRY(launch_scale_lambda(s->pv, s->wv, factors[j], st));
+    if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
+    CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st));
+    CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st));
+    CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, st));
+    CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st));
+    CUDA_TRY(launch_take_probe(s->pv, s->wv, j, st));
+  }
+  CUDA_TRY(cudaMemcpyAsync(s->wv.lm, s->wv.lm_backup, sizeof(LMState) * s->plan->B, cudaMemcpyDeviceToDevice, st));
   return SPGO_OK;
 }
 
@@ -782,7 +821,7 @@ int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, do
   const spgo_plan *p = s->plan;
   // linearise every problem at its current state (lambda untouched: reset sets lambda0)
   CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, st));
-  int rc = p->precision == SPGO_PREC_FP64 ? enqueue_linearize<double>(s, st) : enqueue_linearize<float>(s, st);
+  int rc = p->precision == SPGO_PREC_FP64 ? enqueue_linearize<double>(s, st, false, false) : enqueue_linearize<float>(s, st, false, false);
   if (rc != SPGO_OK) return rc;
   const int N = p->p_npose[problem], P = 6 * N, L = p->p_lm_cnt[problem];
   const bool f64 = p->precision == SPGO_PREC_FP64;
@@ -808,7 +847,7 @@ int spgo_export_reduced(spgo_solver *s, int32_t problem, double lambda, double *
   const spgo_plan *p = s->plan;
   const bool f64 = p->precision == SPGO_PREC_FP64;
   CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, lambda, st));
-  int rc = f64 ? enqueue_linearize<double>(s, st) : enqueue_linearize<float>(s, st);
+  int rc = f64 ? enqueue_linearize<double>(s, st, false, false) : enqueue_linearize<float>(s, st, false, false);
   if (rc != SPGO_OK) return rc;
   if (!f64 && s->prm.use_tc) {
     CUDA_TRY(launch_schur_tc(s->pv, s->wv, s->prm, st));
@@ -817,6 +856,36 @@ int spgo_export_reduced(spgo_solver *s, int32_t problem, double lambda, double *
   }
   CUDA_TRY(f64 ? launch_export_S<double>(s->pv, s->wv, problem, S, gS, st)
                : launch_export_S<float>(s->pv, s->wv, problem, S, gS, st));
+  return SPGO_OK;
+}
+
+int spgo_lm_set_controller(spgo_solver *s, const float *d_params, void *stream) {
+  if (!s) return fail(SPGO_ERR_INVALID_ARG, "null solver");
+  if (!d_params) {
+    s->controller = false;
+  } else {
+    CUDA_TRY(launch_to_bf16(d_params, s->wv.ctrl_bf16, SPGO_MLP_PARAMS, stream));
+    s->controller = true;
+  }
+  drop_graphs(s);
+  return SPGO_OK;
+}
+
+int spgo_lm_features(spgo_solver *s, float *d_feat, void *stream) {
+  if (!s || !d_feat) return fail(SPGO_ERR_INVALID_ARG, "null argument");
+  CUDA_TRY(launch_features(s->pv, s->wv, d_feat, stream));
+  return SPGO_OK;
+}
+
+int spgo_lm_probe(spgo_solver *s, int32_t n_factors, const double *factors, double *costs, void *stream) {
+  if (!s || !factors || !costs || n_factors < 1 || n_factors > 32) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = s->plan->precision == SPGO_PREC_FP64 ? enqueue_probe<double>(s, n_factors, factors, st)
+                                                : enqueue_probe<float>(s, n_factors, factors, st);
+  if (rc != SPGO_OK) return rc;
+  CUDA_TRY(cudaMemcpyAsync(costs, s->wv.probe_costs, sizeof(double) * n_factors * s->plan->B, cudaMemcpyDeviceToHost,
+                           st));
+  CUDA_TRY(cudaStreamSynchronize(st));
   return SPGO_OK;
 }
 

@@ -1,0 +1,339 @@
+// Learned LM damping controller: a 16 -> 64 -> 64 -> 2 MLP with exact GELU.
+//
+// No counterpart in the reference (S-PGO has no damping schedule at all).
+// Parameters are one flat FP32 vector: W1 [64x16] (out x in), b1 [64],
+// W2 [64x64], b2 [64], W3 [2x64], b3 [2]  (5378 floats).  Outputs: out0 =
+// proposed change of log10(lambda), out1 = logit that the current damping gives
+// an accepted step.  Training loss per sample: (out0 - t0)^2 + BCE(out1, t1),
+// averaged over the batch.
+//
+// Kernels: FP32 forward (thread per sample, weights in shared memory), fused
+// loss + backward (thread per sample, per-CTA shared-memory gradient
+// reduction, one global reduction per CTA), Adam, and the BF16 inference the LM
+// loop runs (warp per problem, FP32 accumulation).
+#include <cuda_bf16.h>
+
+#include "kernels.cuh"
+
+namespace spgo {
+
+constexpr int kIn = 16, kH = 64, kOut = 2;
+constexpr int kW1 = 0, kB1 = kW1 + kH * kIn, kW2 = kB1 + kH, kB2 = kW2 + kH * kH, kW3 = kB2 + kH,
+              kB3 = kW3 + kOut * kH, kParams = kB3 + kOut;
+static_assert(kParams == SPGO_MLP_PARAMS, "parameter count");
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * expf(-0.5f * x * x) * 0.39894228040143268f;
+}
+
+// forward; cache (optional) holds z1 [n x 64] then z2 [n x 64]
+__global__ void __launch_bounds__(128) k_mlp_fwd(const float *__restrict__ theta, const float *__restrict__ X, int n,
+                                                 float *__restrict__ out, float *__restrict__ cache) {
+  __shared__ float W[kParams];
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x) W[i] = theta[i];
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  float x[kIn];
+#pragma unroll
+  for (int k = 0; k < kIn; ++k) x[k] = X[(size_t)s * kIn + k];
+  float h1[kH];
+#pragma unroll 4
+  for (int j = 0; j < kH; ++j) {
+    float z = W[kB1 + j];
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) z += W[kW1 + j * kIn + k] * x[k];
+    if (cache) cache[(size_t)s * kH + j] = z;
+    h1[j] = gelu(z);
+  }
+  float o0 = W[kB3], o1 = W[kB3 + 1];
+  for (int j = 0; j < kH; ++j) {
+    float z = W[kB2 + j];
+#pragma unroll 8
+    for (int k = 0; k < kH; ++k) z += W[kW2 + j * kH + k] * h1[k];
+    if (cache) cache[(size_t)n * kH + (size_t)s * kH + j] = z;
+    const float h2 = gelu(z);
+    o0 += W[kW3 + j] * h2;
+    o1 += W[kW3 + kH + j] * h2;
+  }
+  out[2 * s] = o0;
+  out[2 * s + 1] = o1;
+}
+
+// loss + gradient (accumulated into grad, which the caller zeroes) for samples
+// whose forward pass left out / cache
+__global__ void __launch_bounds__(128) k_mlp_bwd(const float *__restrict__ theta, const float *__restrict__ X,
+                                                 const float *__restrict__ T, int n, const float *__restrict__ out,
+                                                 const float *__restrict__ cache, float *__restrict__ grad,
+                                                 float *__restrict__ loss) {
+  __shared__ float W[kParams];
+  __shared__ float G[kParams];
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
+    W[i] = theta[i];
+    G[i] = 0.f;
+  }
+  __syncthreads();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  float lsum = 0.f;
+  if (s < n) {
+    const float inv_n = 1.f / (float)n;
+    const float o0 = out[2 * s], o1 = out[2 * s + 1];
+    const float t0 = T[2 * s], t1 = T[2 * s + 1];
+    const float sig = 1.f / (1.f + expf(-o1));
+    lsum = (o0 - t0) * (o0 - t0) + (fmaxf(o1, 0.f) + log1pf(expf(-fabsf(o1)))) - t1 * o1;
+    const float d0 = 2.f * (o0 - t0) * inv_n, d1 = (sig - t1) * inv_n;
+    atomicAdd(&G[kB3], d0);
+    atomicAdd(&G[kB3 + 1], d1);
+    const float *z1 = cache + (size_t)s * kH;
+    const float *z2 = cache + (size_t)n * kH + (size_t)s * kH;
+    float h1[kH];
+#pragma unroll 8
+    for (int k = 0; k < kH; ++k) h1[k] = gelu(z1[k]);
+    float dh1[kH];
+#pragma unroll 8
+    for (int k = 0; k < kH; ++k) dh1[k] = 0.f;
+    for (int j = 0; j < kH; ++j) {
+      const float zj = z2[j];
+      const float h2 = gelu(zj);
+      atomicAdd(&G[kW3 + j], d0 * h2);
+      atomicAdd(&G[kW3 + kH + j], d1 * h2);
+      const float dz2 = (d0 * W[kW3 + j] + d1 * W[kW3 + kH + j]) * gelu_grad(zj);
+      atomicAdd(&G[kB2 + j], dz2);
+#pragma unroll 8
+      for (int k = 0; k < kH; ++k) {
+        atomicAdd(&G[kW2 + j * kH + k], dz2 * h1[k]);
+        dh1[k] += dz2 * W[kW2 + j * kH + k];
+      }
+    }
+    float x[kIn];
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) x[k] = X[(size_t)s * kIn + k];
+    for (int j = 0; j < kH; ++j) {
+      const float dz1 = dh1[j] * gelu_grad(z1[j]);
+      atomicAdd(&G[kB1 + j], dz1);
+#pragma unroll
+      for (int k = 0; k < kIn; ++k) atomicAdd(&G[kW1 + j * kIn + k], dz1 * x[k]);
+    }
+  }
+  lsum = warp_sum(lsum);
+  if ((threadIdx.x & 31) == 0 && lsum != 0.f) atomicAdd(loss, lsum / (float)n);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x)
+    if (G[i] != 0.f) atomicAdd(grad + i, G[i]);
+}
+
+__global__ void k_mlp_adam(float *theta, const float *grad, float *m, float *v, int step, float lr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kParams) return;
+  const float b1 = 0.9f, b2 = 0.999f, e = 1e-8f;
+  const float g = grad[i];
+  const float mi = b1 * m[i] + (1.f - b1) * g;
+  const float vi = b2 * v[i] + (1.f - b2) * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  const float mh = mi / (1.f - powf(b1, (float)step)), vh = vi / (1.f - powf(b2, (float)step));
+  theta[i] -= lr * mh / (sqrtf(vh) + e);
+}
+
+__global__ void k_to_bf16(const float *src, __nv_bfloat16 *dst, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = __float2bfloat16(src[i]);
+}
+
+// BF16-weight inference for up to one feature vector per warp; lanes split the
+// hidden units, FP32 accumulation
+__device__ void mlp_infer_warp(const __nv_bfloat16 *__restrict__ Wb, const float *x, float &o0, float &o1) {
+  const int lane = threadIdx.x & 31;
+  float h1[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int j = lane + 32 * q;
+    float z = __bfloat162float(Wb[kB1 + j]);
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) z += __bfloat162float(Wb[kW1 + j * kIn + k]) * x[k];
+    h1[q] = gelu(z);
+  }
+  float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int j = lane + 32 * q;
+    float z = __bfloat162float(Wb[kB2 + j]);
+    for (int k = 0; k < kH; ++k) {
+      const float hk = __shfl_sync(0xffffffffu, h1[k >> 5], k & 31);
+      z += __bfloat162float(Wb[kW2 + j * kH + k]) * hk;
+    }
+    const float h2 = gelu(z);
+    p0 += __bfloat162float(Wb[kW3 + j]) * h2;
+    p1 += __bfloat162float(Wb[kW3 + kH + j]) * h2;
+  }
+  o0 = warp_sum(p0) + __bfloat162float(Wb[kB3]);
+  o1 = warp_sum(p1) + __bfloat162float(Wb[kB3 + 1]);
+}
+
+__device__ __forceinline__ float feat_clip(double v) {
+  return v == v ? (float)fmin(40.0, fmax(-40.0, v)) : 0.f;
+}
+__device__ __forceinline__ double lg(double v) { return log10(fmax(v, 1e-300)); }
+
+// the controller's 16 inputs for problem b (see spgo_lm_features); each is finite
+// and clipped to [-40, 40]
+__device__ void lm_features(const PlanView &pv, const LMState &s, int b, float *f) {
+  const double nres = fmax(1.0, (double)pv.p_nres[b]);
+  f[0] = feat_clip(lg(s.cost) - log10(nres));
+  f[1] = feat_clip(lg(s.cost) - lg(s.cost0));
+  f[2] = feat_clip(fmin(2.0, fmax(-2.0, s.rho1)));
+  f[3] = feat_clip(fmin(2.0, fmax(-2.0, s.rho2)));
+  f[4] = feat_clip(fmin(2.0, fmax(-2.0, s.rho3)));
+  f[5] = feat_clip(lg(s.lam));
+  f[6] = feat_clip(lg(s.gnorm) - 0.5 * lg(s.dmean));
+  f[7] = feat_clip(lg(s.dmean) - log10(nres));
+  f[8] = feat_clip(lg(s.dmax) - lg(s.dmin));
+  f[9] = feat_clip(lg(s.cmean));
+  f[10] = feat_clip((double)s.iters / 30.0);
+  f[11] = feat_clip((double)s.last_acc);
+  f[12] = feat_clip(log10(fmax(s.last_rel, 1e-12)));
+  f[13] = feat_clip(log10(fmax(s.last_predrel, 1e-16)));
+  f[14] = feat_clip(log2(fmax(s.nu, 1.0)));
+  f[15] = feat_clip((double)s.rej_streak / 5.0);
+}
+
+// Runs once per LM iteration after the linearisation pass, before the step is
+// solved: at the first iteration and after every accepted step (the state was
+// just relinearised and the cost is current), the controller's
+// proposal lambda * 10^out0 replaces the schedule's lambda when its logit out1 > 0
+// (it predicts that deviating from the schedule gives the lower cost).  After a
+// rejected step no relinearisation happens and the Nielsen increase stands: the
+// fallback whenever a step fails the gain-ratio test.
+__global__ void k_controller(PlanView pv, WorkView wv, const __nv_bfloat16 *Wb) {
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (b >= pv.B) return;
+  LMState &s = wv.lm[b];
+  if (s.status != 0 || !(s.iters == 0 || s.last_acc)) return;
+  float x[kIn];
+  lm_features(pv, s, b, x);
+  float o0, o1;
+  mlp_infer_warp(Wb, x, o0, o1);
+  if ((threadIdx.x & 31) == 0 && o1 > 0.f) {
+    const double dl = fmin(3.0, fmax(-6.0, (double)o0));
+    s.lam = fmin(1e12, fmax(1e-14, s.lam * pow(10.0, dl)));
+  }
+}
+
+__global__ void k_features(PlanView pv, WorkView wv, float *feat) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= pv.B) return;
+  lm_features(pv, wv.lm[b], b, feat + (size_t)b * kIn);
+}
+
+// per-problem statistics of the fresh linearisation: max |g|, diag(A) mean/max/min, mean C
+template <typename T>
+__global__ void k_lm_stats(PlanView pv, WorkView wv) {
+  __shared__ double red[4][32];
+  const int b = blockIdx.x;
+  LMState &s = wv.lm[b];
+  if (s.status != 0 || !s.relin) return;
+  const int P = 6 * pv.p_npose[b];
+  const T *A = reinterpret_cast<const T *>(wv.A) + pv.p_S_off[b];
+  const T *g = reinterpret_cast<const T *>(wv.g) + pv.p_param_off[b];
+  double gmax = 0.0, dsum = 0.0, dmax = 0.0, dmin = 1e300, csum = 0.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    gmax = fmax(gmax, fabs((double)g[i]));
+    const double d = (double)A[(size_t)i * P + i];
+    dsum += d;
+    dmax = fmax(dmax, d);
+    dmin = fmin(dmin, d);
+  }
+  const int l0 = pv.p_lm_off[b], lc = pv.p_lm_cnt[b];
+  for (int i = threadIdx.x; i < lc; i += blockDim.x) csum += (double)reinterpret_cast<const T *>(wv.C)[l0 + i];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+    dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+    dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+    csum += __shfl_xor_sync(0xffffffffu, csum, o);
+  }
+  __shared__ double r5[32][5];
+  if (lane == 0) {
+    r5[w][0] = gmax; r5[w][1] = dsum; r5[w][2] = dmax; r5[w][3] = dmin; r5[w][4] = csum;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      r5[0][0] = fmax(r5[0][0], r5[k][0]);
+      r5[0][1] += r5[k][1];
+      r5[0][2] = fmax(r5[0][2], r5[k][2]);
+      r5[0][3] = fmin(r5[0][3], r5[k][3]);
+      r5[0][4] += r5[k][4];
+    }
+    s.gnorm = r5[0][0];
+    s.dmean = P ? r5[0][1] / P : 0.0;
+    s.dmax = r5[0][2];
+    s.dmin = P ? r5[0][3] : 0.0;
+    s.cmean = lc ? r5[0][4] / lc : 0.0;
+  }
+  (void)red;
+}
+
+int launch_lm_stats(const PlanView &pv, const WorkView &wv, int f64, void *stream) {
+  if (f64)
+    k_lm_stats<double><<<pv.B, 128, 0, (cudaStream_t)stream>>>(pv, wv);
+  else
+    k_lm_stats<float><<<pv.B, 128, 0, (cudaStream_t)stream>>>(pv, wv);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wb, void *stream) {
+  k_controller<<<grid_for(pv.B, 4), 128, 0, (cudaStream_t)stream>>>(pv, wv,
+                                                                   reinterpret_cast<const __nv_bfloat16 *>(Wb));
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_features(const PlanView &pv, const WorkView &wv, float *feat, void *stream) {
+  k_features<<<grid_for(pv.B, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, feat);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_to_bf16(const float *src, void *dst, int n, void *stream) {
+  k_to_bf16<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(src, reinterpret_cast<__nv_bfloat16 *>(dst), n);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+}  // namespace spgo
+
+using namespace spgo;
+
+extern "C" int spgo_mlp_forward(const float *d_params, const float *d_X, int32_t n, float *d_out, float *d_cache,
+                                void *stream) {
+  if (!d_params || !d_X || !d_out || n < 0) return SPGO_ERR_INVALID_ARG;
+  if (n == 0) return SPGO_OK;
+  k_mlp_fwd<<<grid_for(n, 128), 128, 0, (cudaStream_t)stream>>>(d_params, d_X, n, d_out, d_cache);
+  ++g_launches;
+  return cudaGetLastError() == cudaSuccess ? SPGO_OK : SPGO_ERR_CUDA;
+}
+
+extern "C" int spgo_mlp_grad(const float *d_params, const float *d_X, const float *d_T, int32_t n, float *d_grad,
+                             float *d_loss, float *d_out, float *d_cache, void *stream) {
+  if (!d_params || !d_X || !d_T || !d_grad || !d_loss || !d_out || !d_cache || n <= 0) return SPGO_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemsetAsync(d_grad, 0, sizeof(float) * kParams, st);
+  cudaMemsetAsync(d_loss, 0, sizeof(float), st);
+  k_mlp_fwd<<<grid_for(n, 128), 128, 0, st>>>(d_params, d_X, n, d_out, d_cache);
+  k_mlp_bwd<<<grid_for(n, 128), 128, 0, st>>>(d_params, d_X, d_T, n, d_out, d_cache, d_grad, d_loss);
+  g_launches += 2;
+  return cudaGetLastError() == cudaSuccess ? SPGO_OK : SPGO_ERR_CUDA;
+}
+
+extern "C" int spgo_mlp_adam(float *d_params, const float *d_grad, float *d_m, float *d_v, int32_t step, float lr,
+                             void *stream) {
+  if (!d_params || !d_grad || !d_m || !d_v || step < 1) return SPGO_ERR_INVALID_ARG;
+  k_mlp_adam<<<grid_for(kParams, 256), 256, 0, (cudaStream_t)stream>>>(d_params, d_grad, d_m, d_v, step, lr);
+  ++g_launches;
+  return cudaGetLastError() == cudaSuccess ? SPGO_OK : SPGO_ERR_CUDA;
+}

@@ -12,18 +12,10 @@
 
 namespace spgo {
 
-// storage of the factor: packed lower triangle, column-major (column j holds rows j..P-1)
-struct PackedCol {
-  int P;
-  __device__ __forceinline__ size_t operator()(int i, int j) const {
-    return (size_t)j * P - ((size_t)j * (j - 1)) / 2 + (size_t)(i - j);
-  }
-};
-struct FullCol {
-  int P;
-  __device__ __forceinline__ size_t operator()(int i, int j) const { return (size_t)j * P + i; }
-};
-
+// Storage of the factor: element (i, j), i >= j, at Lm[cb[j] + i] with per-column
+// base offsets cb in shared memory: packed lower triangle, column-major (column j
+// holds rows j..P-1; cb[j] = j P - j (j + 1) / 2) when it fits in shared memory,
+// else the full column-major matrix in global scratch (cb[j] = j P).
 constexpr int kPanel = 16;  // block width of the factorisation and the substitutions
 
 // S(r, c) of the damped reduced system for r >= c, from A (pose blocks), S_L
@@ -43,9 +35,10 @@ __device__ __forceinline__ double s_entry(const T *A, const T *SL, int P, int r,
 // per block.  The substitutions are blocked the same way (two barriers per
 // block).  `refine` iterative-refinement steps form the residual g_S - S x in
 // FP64 from A and S_L.  Clears the S_L / g_L tiles it consumed.
-template <typename T, typename Idx>
-__device__ void factor_solve_body(T *Lm, Idx ix, T *y, double *x, float *xs, T *tmp, const T *A, T *SL,
+template <typename T>
+__device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *xs, T *tmp, const T *A, T *SL,
                                   const T *g, T *gL, double lam, int P, int refine, int *fail_s) {
+#define ix(i, j) (cb[(j)] + (i))
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   for (int c = warp; c < P; c += nw)
     for (int r = c + lane; r < P; r += 32) Lm[ix(r, c)] = (T)s_entry(A, SL, P, r, c, lam);
@@ -83,10 +76,13 @@ __device__ void factor_solve_body(T *Lm, Idx ix, T *y, double *x, float *xs, T *
     __syncthreads();
     if (*fail_s) return;
     // rows below the block: L(i, kb:ke) = S(i, kb:ke) L_D^-T
+    int cbk[kPanel];
+#pragma unroll
+    for (int c = 0; c < kPanel; ++c) cbk[c] = c < w ? cb[kb + c] : 0;
     for (int i = ke + tid; i < P; i += nt) {
       T r[kPanel];
 #pragma unroll
-      for (int c = 0; c < kPanel; ++c) r[c] = c < w ? Lm[ix(i, kb + c)] : T(0);
+      for (int c = 0; c < kPanel; ++c) r[c] = c < w ? Lm[cbk[c] + i] : T(0);
 #pragma unroll
       for (int c = 0; c < kPanel; ++c) {
         if (c < w) {
@@ -98,20 +94,20 @@ __device__ void factor_solve_body(T *Lm, Idx ix, T *y, double *x, float *xs, T *
       }
 #pragma unroll
       for (int c = 0; c < kPanel; ++c)
-        if (c < w) Lm[ix(i, kb + c)] = r[c];
+        if (c < w) Lm[cbk[c] + i] = r[c];
     }
     __syncthreads();
     // trailing update with the finished block
     for (int j = ke + warp; j < P; j += nw) {
       T ljk[kPanel];
 #pragma unroll
-      for (int k = 0; k < kPanel; ++k) ljk[k] = k < w ? Lm[ix(j, kb + k)] : T(0);
+      for (int k = 0; k < kPanel; ++k) ljk[k] = k < w ? Lm[cbk[k] + j] : T(0);
+      T *colj = Lm + cb[j];
       for (int i = j + lane; i < P; i += 32) {
         T acc = T(0);
 #pragma unroll
-        for (int k = 0; k < kPanel; ++k)
-          if (k < w) acc += Lm[ix(i, kb + k)] * ljk[k];
-        Lm[ix(i, j)] -= acc;
+        for (int k = 0; k < kPanel; ++k) acc += Lm[cbk[k] + i] * ljk[k];
+        colj[i] -= acc;
       }
     }
     __syncthreads();
@@ -204,6 +200,8 @@ __device__ void factor_solve_body(T *Lm, Idx ix, T *y, double *x, float *xs, T *
   }
 }
 
+#undef ix
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, int refine, int use_smem) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -227,13 +225,19 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
     x = reinterpret_cast<double *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15));
     y = reinterpret_cast<T *>(x + P);
     float *xs = reinterpret_cast<float *>(y + P);
-    factor_solve_body<T, PackedCol>(Lm, PackedCol{P}, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
+    int *cb = reinterpret_cast<int *>(xs + 2 * P);
+    for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P - (j * (j + 1)) / 2;
+    __syncthreads();
+    factor_solve_body<T>(Lm, cb, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
   } else {
     x = reinterpret_cast<double *>(smem_raw);
     y = reinterpret_cast<T *>(x + P);
     float *xs = reinterpret_cast<float *>(y + P);
+    int *cb = reinterpret_cast<int *>(xs + 2 * P);
+    for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P;
+    __syncthreads();
     T *Lm = reinterpret_cast<T *>(wv.fac) + off;
-    factor_solve_body<T, FullCol>(Lm, FullCol{P}, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
+    factor_solve_body<T>(Lm, cb, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
   }
   __syncthreads();
   const bool failed = fail_s != 0;
@@ -253,7 +257,7 @@ static const size_t kSmemBudget = 200 * 1024;
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed, void *stream) {
   const int P = pv.max_P;
-  const size_t vec = (size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float)) + 16;
+  const size_t vec = (size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 16;
   const size_t packed = (((size_t)P * (P + 1) / 2) * sizeof(T) + 15) / 16 * 16 + vec;
   const int use_smem = packed <= kSmemBudget;
   const size_t sm = use_smem ? packed : vec;
@@ -359,6 +363,9 @@ __global__ void k_reset(PlanView pv, WorkView wv, double lam) {
   s.iters = s.accepted = s.status = 0;
   s.relin = 1;
   s.fail = s.flag = s.factor_failures = s.pad = 0;
+  s.rho1 = s.rho2 = s.rho3 = s.last_rel = s.last_predrel = 0.0;
+  s.gnorm = s.dmean = s.dmax = s.dmin = s.cmean = 0.0;
+  s.last_acc = s.rej_streak = 0;
   wv.lm[b] = s;
   wv.cost_acc[b] = 0.0;
   wv.pred_acc[b] = 0.0;
@@ -410,9 +417,16 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
   s.pred = pred;
   s.iters += 1;
   const bool ok = !s.fail && isfinite(Fn) && pred > 0.0 && Fn < F;
+  s.rho3 = s.rho2;
+  s.rho2 = s.rho1;
+  s.rho1 = s.fail ? -2.0 : (pred > 0.0 && isfinite(Fn) ? (F - Fn) / pred : -2.0);
+  s.last_acc = ok ? 1 : 0;
+  s.last_predrel = pred / fmax(F, 1e-300);
+  s.rej_streak = ok ? 0 : s.rej_streak + 1;
   if (ok) {
     const double rho = (F - Fn) / pred;
     const double rel = (F - Fn) / fmax(F, 1e-300);
+    s.last_rel = rel;
     s.accepted += 1;
     s.flag = 1;
     s.cost = Fn;
@@ -530,6 +544,31 @@ int launch_export_S(const PlanView &pv, const WorkView &wv, int problem, double 
 }
 template int launch_export_S<float>(const PlanView &, const WorkView &, int, double *, double *, void *);
 template int launch_export_S<double>(const PlanView &, const WorkView &, int, double *, double *, void *);
+
+__global__ void k_scale_lambda(PlanView pv, WorkView wv, double factor) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < pv.B) wv.lm[b].lam = wv.lm_backup[b].lam * factor;
+}
+
+__global__ void k_take_probe(PlanView pv, WorkView wv, int j) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= pv.B) return;
+  wv.probe_costs[(size_t)j * pv.B + b] = wv.lm[b].status == 0 ? wv.cost_acc[b] : 0.0;
+  wv.cost_acc[b] = 0.0;
+  wv.pred_acc[b] = 0.0;
+}
+
+int launch_scale_lambda(const PlanView &pv, const WorkView &wv, double factor, void *stream) {
+  k_scale_lambda<<<grid_for(pv.B, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, factor);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+int launch_take_probe(const PlanView &pv, const WorkView &wv, int j, void *stream) {
+  k_take_probe<<<grid_for(pv.B, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, j);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
 
 __global__ void k_to_double(const void *src, int f64, double *dst, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -36,6 +36,7 @@ struct PlanView {                 // device pointers into the static buffer
   const int32_t *p_npose, *p_frame_off, *p_pose_off, *p_lm_off, *p_lm_cnt, *p_pair_D,
       *p_param_off, *p_chunk_off, *p_chunk_cnt;
   const int64_t *p_S_off, *p_pair_off;
+  const int64_t *p_nres;   // residual rows (4 per stereo observation)
   const float *p_intr;    // [B][8]
   const double *p_Trl;    // [B][12]
   // per landmark (internal order)
@@ -62,6 +63,10 @@ struct PlanView {                 // device pointers into the static buffer
 struct LMState {
   double lam, nu, cost, cost_cand, pred, cost0, cost_lin;
   int32_t iters, accepted, status, relin, fail, flag, factor_failures, pad;
+  // history and statistics the learned damping controller reads
+  double rho1, rho2, rho3, last_rel, last_predrel;
+  double gnorm, dmean, dmax, dmin, cmean;
+  int32_t last_acc, rej_streak;
 };
 
 // per-iteration scratch (precision-dependent arrays typed at the kernel)
@@ -87,6 +92,9 @@ struct WorkView {
   void *ga;             // [L] T
   void *slab;           // [sum slab] T
   LMState *lm;          // [B]
+  LMState *lm_backup;   // [B] (lambda probes)
+  double *probe_costs;  // [32][B]
+  void *ctrl_bf16;      // [SPGO_MLP_PARAMS] bf16 controller weights
   double *cost_acc;     // [B]
   double *pred_acc;     // [B]
 };
@@ -125,6 +133,12 @@ template <typename T>
 int launch_export_B_n(const PlanView &pv, const WorkView &wv, int problem, int n_chunks, double *B,
                       double *C, double *ga, void *stream);
 
+int launch_lm_stats(const PlanView &pv, const WorkView &wv, int f64, void *stream);
+int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wb, void *stream);
+int launch_features(const PlanView &pv, const WorkView &wv, float *feat, void *stream);
+int launch_to_bf16(const float *src, void *dst, int n, void *stream);
+int launch_scale_lambda(const PlanView &pv, const WorkView &wv, double factor, void *stream);
+int launch_take_probe(const PlanView &pv, const WorkView &wv, int j, void *stream);
 int launch_schur_tc(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
 template <typename T>
 int launch_export_S(const PlanView &pv, const WorkView &wv, int problem, double *S, double *gS, void *stream);

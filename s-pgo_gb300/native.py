@@ -24,8 +24,10 @@ EXPORTED = [
     "spgo_plan_destroy", "spgo_plan_offsets", "spgo_solver_create", "spgo_solver_destroy", "spgo_set_params",
     "spgo_gn_step", "spgo_lm_reset", "spgo_lm_iterate", "spgo_lm_status", "spgo_lm_solve",
     "spgo_export_system", "spgo_launch_count", "spgo_profile_enable", "spgo_profile_read",
-    "spgo_cost_noalloc", "spgo_export_reduced",
+    "spgo_cost_noalloc", "spgo_export_reduced", "spgo_mlp_forward", "spgo_mlp_grad", "spgo_mlp_adam",
+    "spgo_lm_set_controller", "spgo_lm_features", "spgo_lm_probe",
 ]
+MLP_PARAMS, MLP_INPUTS = 5378, 16
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
                  "update", "bookkeeping"]
 
@@ -96,6 +98,15 @@ def lib() -> C.CDLL:
     L.spgo_lm_status.argtypes = [vp, C.POINTER(ProblemStatus), vp]
     L.spgo_lm_solve.argtypes = [vp, i32, C.POINTER(C.c_int32), vp]
     L.spgo_export_system.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
+    L.spgo_mlp_forward.argtypes = [vp, vp, i32, vp, vp, vp]
+    L.spgo_mlp_grad.argtypes = [vp, vp, vp, i32, vp, vp, vp, vp, vp]
+    L.spgo_mlp_adam.argtypes = [vp, vp, vp, vp, i32, C.c_float, vp]
+    L.spgo_lm_set_controller.argtypes = [vp, vp, vp]
+    L.spgo_lm_features.argtypes = [vp, vp, vp]
+    L.spgo_lm_probe.argtypes = [vp, i32, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
+    for name in ("spgo_mlp_forward", "spgo_mlp_grad", "spgo_mlp_adam", "spgo_lm_set_controller",
+                 "spgo_lm_features", "spgo_lm_probe"):
+        getattr(L, name).restype = C.c_int
     L.spgo_export_reduced.argtypes = [vp, i32, C.c_double, vp, vp, vp]
     L.spgo_export_reduced.restype = C.c_int
     L.spgo_profile_enable.argtypes = [vp, i32]

@@ -238,6 +238,27 @@ class BatchSolver:
         self.synchronize()
         return dict(S=S.cpu().numpy().reshape(P, P), gS=gS.cpu().numpy())
 
+    def features(self) -> np.ndarray:
+        """The learned controller's 16 inputs per problem at the current state."""
+        B = len(self.problems)
+        f = torch.zeros(B * nat.MLP_INPUTS, dtype=torch.float32, device=self.device)
+        nat.check(self.L.spgo_lm_features(self._solver, C.c_void_p(f.data_ptr()), self._sp()), "lm_features")
+        self.synchronize()
+        return f.cpu().numpy().reshape(B, nat.MLP_INPUTS)
+
+    def probe(self, factors) -> np.ndarray:
+        """Cost of the step taken with lambda * f, for each factor and problem ([n_f, B])."""
+        fac = np.ascontiguousarray(factors, dtype=np.float64)
+        out = np.zeros(len(fac) * len(self.problems), dtype=np.float64)
+        nat.check(self.L.spgo_lm_probe(self._solver, len(fac), fac.ctypes.data_as(C.POINTER(C.c_double)),
+                                       out.ctypes.data_as(C.POINTER(C.c_double)), self._sp()), "lm_probe")
+        return out.reshape(len(fac), len(self.problems))
+
+    def set_controller(self, params: Optional[torch.Tensor]):
+        """Learned damping (FP32 parameter tensor on the device) or None for plain Nielsen."""
+        ptr = C.c_void_p(params.data_ptr()) if params is not None else C.c_void_p(0)
+        nat.check(self.L.spgo_lm_set_controller(self._solver, ptr, self._sp()), "lm_set_controller")
+
     def launch_count(self) -> int:
         return int(self.L.spgo_launch_count(self._solver))
 

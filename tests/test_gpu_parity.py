@@ -136,7 +136,9 @@ def test_batched_equals_individual(built_lib, cuda_device):
         ref = p.copy()
         res = S.lm_solve(ref, S.Loss(), max_iters=30, tol=1e-6)
         refs.append(ref)
-        assert sts[b]["status"] == nat.STATUS_CONVERGED
+        # at the FP32 noise floor a mixed-precision problem may stop with no step
+        # lowering the FP64 cost (stalled) instead of by the relative-decrease test
+        assert sts[b]["status"] in (nat.STATUS_CONVERGED, nat.STATUS_STALLED)
         assert abs(sts[b]["cost"] - res.cost) / res.cost < 1e-6
     bs.set_params(max_iters=40, tol=1e-10)
     bs.solve()

@@ -1,8 +1,12 @@
 """Damped reduced camera system S = A + lam diag(A) - B D^-1 B^T and g_S from the
 CUDA path (SIMT and tensor-core Schur complements) against the FP64 oracle.
-Tolerances, relative to the largest entry: FP64 path 1e-9; mixed path with SIMT
-FP32 Schur 1e-4; mixed path with the tensor-core Schur (TF32 operands, 10-bit
-mantissa, FP32 accumulation) 2e-3."""
+
+S cancels most of A (on the 45-pose problem below max|A| / max|S| is ~600), so
+errors are stated relative to the largest entry of A (and of g_T for g_S), the
+scale the FP32 terms are formed at: FP64 path 1e-12; mixed path with the SIMT
+FP32 Schur 2e-6; mixed path with the tensor-core Schur (split TF32 operands,
+hi.hi + hi.lo + lo.hi, ~21-bit products, TMEM read back every 4 chunks into
+FP32 registers) 2e-6."""
 import numpy as np
 import pytest
 
@@ -26,25 +30,23 @@ def oracle_reduced(p, lam, eps=1e-4):
     D = lin.C * (1.0 + lam) + eps
     BD = lin.B / D[None, :]
     Sm = lin.A + np.diag(lam * np.diag(lin.A)) - BD @ lin.B.T
-    return Sm, lin.g_T - BD @ lin.g_a
+    return Sm, lin.g_T - BD @ lin.g_a, lin
 
 
-def rel(a, b):
-    return float(np.abs(a - b).max() / np.abs(b).max())
-
-
-@pytest.mark.parametrize("prec,use_tc,tol", [("fp64", 0, 1e-9), ("mixed", 0, 1e-4), ("mixed", 1, 2e-3)])
+@pytest.mark.parametrize("prec,use_tc,tol", [("fp64", 0, 1e-12), ("mixed", 0, 2e-6), ("mixed", 1, 2e-6)])
 def test_reduced_system_matches_oracle(built_lib, cuda_device, prec, use_tc, tol):
-    # sizes that exercise one and two 128-row tensor-core tiles and partial column ranges
-    probs = [scenes.circle_scene(s, n, l) for s, n, l in [(301, 9, 240), (302, 26, 700), (303, 14, 380)]]
+    # sizes that exercise one, two and three 128-row tensor-core tiles (P = 54, 156, 84, 270)
+    # and off-diagonal tiles with partial column ranges
+    probs = [scenes.circle_scene(s, n, l) for s, n, l in
+             [(301, 9, 240), (302, 26, 700), (303, 14, 380), (304, 45, 1200)]]
     bs = BatchSolver(probs, precision=prec)
     bs.set_params(loss="l2", use_tc=use_tc)
     for lam in (1e-4, 0.5):
         for b, p in enumerate(probs):
             got = bs.export_reduced(b, lam)
-            Sm, gS = oracle_reduced(p, lam)
-            assert rel(got["S"], Sm) < tol, (b, lam)
-            assert rel(got["gS"], gS) < max(tol, 1e-6), (b, lam)
+            Sm, gS, lin = oracle_reduced(p, lam)
+            assert np.abs(got["S"] - Sm).max() / np.abs(lin.A).max() < tol, (b, lam)
+            assert np.abs(got["gS"] - gS).max() / np.abs(lin.g_T).max() < tol, (b, lam)
 
 
 def test_tensor_core_solve_converges(built_lib, cuda_device):
