@@ -139,18 +139,31 @@ def roofline_numerator(kind: str, sizes, slab_floats: int, ts: int, probs):
     """(bound, unit, algorithmic amount per launch) for a profiled kernel kind.
 
     linearisation / cost: HBM bytes (observations 20 B, landmark record 40 B, C/g_a,
-    slab written); Schur: tensor-shaped FLOPs of the (chunk, 48x48 tile) products;
-    factor_solve: dense Cholesky + two solves + one FP64 residual per problem."""
+    slab written); Schur: FLOPs of the W D^-1 W^T chunk blocks, sum 2 (6 nb)^2 32;
+    factor_solve: dense Cholesky + two solve pairs per problem (P^3/3 + 4 P^2)."""
     O, L = sizes.total_obs, sizes.total_landmarks
     if kind == "linearize":
         return "hbm", "GB/s", 20.0 * O + 40.0 * L + 2.0 * ts * L + ts * slab_floats
     if kind == "cost":
         return "hbm", "GB/s", 20.0 * O + 40.0 * L
     if kind == "schur":
-        return "tensor", "TFLOP/s", 2.0 * 48 * 48 * 32 * sizes.schur_chunk_tiles
+        return "tensor", "TFLOP/s", float(sizes.schur_flops)
     if kind == "factor_solve":
-        return "tensor", "TFLOP/s", float(sum((6 * p.n_poses) ** 3 / 3.0 + 6 * (6 * p.n_poses) ** 2 for p in probs))
+        return "fp32", "TFLOP/s", float(sum((6 * p.n_poses) ** 3 / 3.0 + 4 * (6 * p.n_poses) ** 2 for p in probs))
     return None, None, 0.0
+
+
+def roofline_peaks(peaks: dict, tc: bool):
+    """Denominators by bound: measured HBM copy; tensor = measured cuBLAS BF16 / 2 for
+    the TF32 kind the Schur pass issues (the nominal TF32 : BF16 ratio), or the
+    BF16 figure itself; FP32 SIMT = nominal 152 SMs x 128 lanes x 2 FLOP x max clock."""
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    bf16 = float(peaks.get("bf16_tflops", 1900.0))
+    mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    src = "measured" if "hbm_gbs" in peaks else "fallback"
+    return {"hbm": (hbm, src + " hbm_gbs"),
+            "tensor": (bf16 / 2.0 if tc else bf16, src + (" bf16_tflops / 2 (tf32)" if tc else " bf16_tflops")),
+            "fp32": (152 * 128 * 2 * mhz * 1e6 / 1e12, "nominal FP32 SIMT at sm_max_mhz")}
 
 
 def run_reference(args):
@@ -216,9 +229,18 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
 
+    # learned damping: the shipped network (trained by train_controller.py), if present
+    ctl_params = None
+    if args.controller:
+        learned = importlib.import_module("spgo_gb300.learned")
+        if os.path.exists(learned.DEFAULT_WEIGHTS):
+            ctl_params = learned.Controller.load(device=dev).deployed()
+
     def make(precision):
         s = sv.BatchSolver(probs, precision=precision, device=dev, stream=stream)
         s.set_params(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4, use_tc=args.tc)
+        if ctl_params is not None:
+            s.set_controller(ctl_params)
         return s
 
     bs = make("mixed")
@@ -280,20 +302,24 @@ def run_ours(args):
         peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    pk = roofline_peaks(peaks, bool(args.tc))
     tot = sum(v[0] for v in prof.values()) or 1.0
     kernels = {k: {"ms": round(v[0], 4), "launches": v[1], "share": round(v[0] / tot, 4)} for k, v in prof.items()}
-    dom = max(prof, key=lambda k: prof[k][0])
     slab_floats = int(bs.slab_floats())
+    for k, v in prof.items():
+        b_, u_, amt = roofline_numerator(k, bs.sizes, slab_floats, 4, probs)
+        if b_ and v[1]:
+            ms_ = v[0] / v[1]
+            ach = amt / (ms_ / 1e3) / (1e9 if b_ == "hbm" else 1e12)
+            kernels[k].update(bound=b_, achieved=round(ach, 3), unit=u_, frac=round(ach / pk[b_][0], 4))
+    dom = max(prof, key=lambda k: prof[k][0])
     avg_ms = prof[dom][0] / max(1, prof[dom][1])
     bound, unit, amount = roofline_numerator(dom, bs.sizes, slab_floats, 4, probs)
-    if bound == "hbm":
-        achieved, peak = amount / (avg_ms / 1e3) / 1e9, hbm_peak
-    elif bound == "tensor":
-        achieved, peak = amount / (avg_ms / 1e3) / 1e12, float(peaks.get("bf16_tflops", 1900.0))
+    if bound:
+        achieved = amount / (avg_ms / 1e3) / (1e9 if bound == "hbm" else 1e12)
+        peak, peak_src = pk[bound]
     else:
-        achieved, peak = None, None
+        achieved, peak, peak_src = None, None, None
     roof = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": (achieved / peak) if achieved else None,
             "traffic": None, "avg_launch_ms": avg_ms, "peak_source": peak_src,
@@ -343,7 +369,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
             "data": "synthetic (seeded config-3 generator)",
             "config": {"workload": WORKLOAD, "problems_per_gpu": N_PROBLEMS, "landmarks": n_lm, "obs": n_obs,
-                       "precision": "mixed", "schur": "tcgen05 TF32" if args.tc else "SIMT FP32",
+                       "precision": "mixed", "schur": "tcgen05 split TF32" if args.tc else "SIMT FP32",
+                       "damping": "learned MLP + Nielsen fallback" if ctl_params is not None else "Nielsen",
                        "l2": "256 MB flush written between timed steps",
                        "parallelism": f"replicas x{world} (independent batches)",
                        "iterations_max": int(max(iters)), "iterations_mean": float(np.mean(iters))},
@@ -367,7 +394,8 @@ def main():
     ap.add_argument("--check-every", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--tc", type=int, default=0, help="1: tensor-core Schur complement in the mixed path")
+    ap.add_argument("--tc", type=int, default=1, help="1: tensor-core Schur complement in the mixed path, 0: SIMT")
+    ap.add_argument("--controller", type=int, default=1, help="1: learned damping (shipped weights), 0: Nielsen")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -93,6 +93,10 @@ typedef struct spgo_plan_sizes {
     size_t  workspace_bytes;     /* device buffer for per-iteration scratch       */
     int64_t slab_elems;          /* elements of the landmark-chunk slabs (W blocks) */
     int64_t pair_records;        /* (lo, hi) pose-pair accumulators               */
+    int64_t schur_flops;         /* algorithmic FLOPs of one landmark Schur pass:
+                                    sum over chunks of 2 (6 nb)^2 x 32 (W D^-1 W^T blocks) */
+    int32_t n_tc_items;          /* tensor-core Schur work items (128x128 tiles x chunk lists) */
+    int32_t tc_chunk_tiles;      /* (chunk, 128x128 tile) products per tensor-core pass */
 } spgo_plan_sizes;
 
 /* solver parameters */
@@ -110,8 +114,9 @@ typedef struct spgo_params {
     int32_t refine_steps;        /* FP64 iterative-refinement steps (mixed precision) */
     int32_t use_graph;           /* 1: spgo_lm_iterate replays a captured CUDA graph
                                     (not on the legacy default stream, not while profiling) */
-    int32_t use_tc;              /* 1: mixed path forms the landmark Schur complement on the
-                                    tensor cores (tcgen05, TF32 in / FP32 accumulate) */
+    int32_t use_tc;              /* 1 (default): mixed path forms the landmark Schur complement
+                                    on the tensor cores (tcgen05, split TF32, FP32 accumulate);
+                                    0: FP32 SIMT */
 } spgo_params;
 
 typedef struct spgo_problem_status {

@@ -134,7 +134,7 @@ static void build_layout(spgo_plan *p) {
   p->w_gL = take((size_t)p->total_params * ts);
   // global factor storage only when a problem is too large for the shared-memory path
   const size_t P = (size_t)p->max_P;
-  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8 + 4) + 16;
+  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8 + 4) + 16 + P * ts + 16;
   p->w_fac = take(packed <= 200 * 1024 ? 0 : (size_t)p->total_S * ts);
   p->w_delta = take((size_t)p->total_params * 8);
   p->w_C = take((size_t)(p->L + 64) * ts);  // + 64: the tensor-core Schur copies 16-byte aligned supersets
@@ -569,7 +569,7 @@ void spgo_default_params(spgo_params *p) {
   p->max_iters = 30;
   p->refine_steps = 1;
   p->use_graph = 1;
-  p->use_tc = 0;
+  p->use_tc = 1;
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
@@ -602,6 +602,10 @@ int spgo_plan_sizes_get(const spgo_plan *p, spgo_plan_sizes *o) {
   o->n_schur_items = (int32_t)p->wk_prob.size();
   o->max_params = p->max_P;
   o->schur_chunk_tiles = (int32_t)p->wk_chunks.size();
+  o->schur_flops = 0;
+  for (size_t c = 0; c < p->ch_nb.size(); ++c) o->schur_flops += 2LL * (6LL * p->ch_nb[c]) * (6LL * p->ch_nb[c]) * 32;
+  o->n_tc_items = (int32_t)p->tc_prob.size();
+  o->tc_chunk_tiles = (int32_t)p->tc_chunks.size();
   o->static_bytes = p->static_bytes;
   o->workspace_bytes = p->ws_bytes;
   o->slab_elems = p->total_slab;

@@ -20,11 +20,13 @@ constexpr int kPanel = 16;  // block width of the factorisation and the substitu
 
 // S(r, c) of the damped reduced system for r >= c, from A (pose blocks), S_L
 // (landmark Schur term, lower tiles) and lambda:  S = A + lam diag(A) - S_L
+// (in T: the FP32 difference A - S_L is the correctly rounded exact difference,
+// the same value an FP64 evaluation rounded to FP32 would give off the diagonal)
 template <typename T>
-__device__ __forceinline__ double s_entry(const T *A, const T *SL, int P, int r, int c, double lam) {
+__device__ __forceinline__ T s_entry(const T *A, const T *SL, int P, int r, int c, T lam) {
   const size_t k = (size_t)r * P + c;
-  double v = (double)A[k] - (double)SL[k];
-  if (r == c) v += lam * (double)A[k];
+  T v = A[k] - SL[k];
+  if (r == c) v += lam * A[k];
   return v;
 }
 
@@ -36,12 +38,13 @@ __device__ __forceinline__ double s_entry(const T *A, const T *SL, int P, int r,
 // block).  `refine` iterative-refinement steps form the residual g_S - S x in
 // FP64 from A and S_L.  Clears the S_L / g_L tiles it consumed.
 template <typename T>
-__device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *xs, T *tmp, const T *A, T *SL,
-                                  const T *g, T *gL, double lam, int P, int refine, int *fail_s) {
+__device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *xs, T *dinv, T *tmp, const T *A,
+                                  T *SL, const T *g, T *gL, double lam, int P, int refine, int *fail_s) {
 #define ix(i, j) (cb[(j)] + (i))
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
+  const T lam_t = (T)lam;
   for (int c = warp; c < P; c += nw)
-    for (int r = c + lane; r < P; r += 32) Lm[ix(r, c)] = (T)s_entry(A, SL, P, r, c, lam);
+    for (int r = c + lane; r < P; r += 32) Lm[ix(r, c)] = s_entry(A, SL, P, r, c, lam_t);
   for (int i = tid; i < P; i += nt) {
     y[i] = g[i] - gL[i];
     x[i] = 0.0;
@@ -50,28 +53,33 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
   __syncthreads();
   for (int kb = 0; kb < P; kb += kPanel) {
     const int ke = min(kb + kPanel, P), w = ke - kb;
-    if (warp == 0) {  // diagonal block, lane = row inside the block
-      for (int k = 0; k < w; ++k) {
-        const int col = kb + k;
-        const T d = Lm[ix(col, col)];
-        if (!(d > T(0)) || !isfinite((double)d)) {
-          if (lane == 0) *fail_s = 1;
-          break;
+    if (warp == 0) {
+      // diagonal block in registers: lane i < w holds row i (a[j] = L(kb+i, kb+j), j <= i);
+      // column k is finished with one shuffle of the pivot and one per later row
+      T a[kPanel];
+#pragma unroll
+      for (int j = 0; j < kPanel; ++j) a[j] = (lane < w && j <= lane) ? Lm[ix(kb + lane, kb + j)] : T(0);
+      bool bad = false;
+      // (columns k >= w of a narrow last block run on a unit pivot and are discarded)
+#pragma unroll
+      for (int k = 0; k < kPanel; ++k) {
+        const T dk = __shfl_sync(0xffffffffu, a[k], k);
+        const T d = k < w ? dk : T(1);
+        bad = bad || !(d > T(0)) || !isfinite((double)d);
+        const T lkk = sqrt(d), rinv = T(1) / lkk;
+        const T lik = lane > k ? a[k] * rinv : (lane == k ? lkk : a[k]);
+        a[k] = lik;
+#pragma unroll
+        for (int j = 0; j < kPanel; ++j) {
+          const T ljk = __shfl_sync(0xffffffffu, lik, j);
+          if (j > k && lane >= j) a[j] -= lik * ljk;
         }
-        const T lkk = sqrt(d);
-        __syncwarp();
-        if (lane == 0) {
-          Lm[ix(col, col)] = lkk;
-          tmp[k] = T(1) / lkk;
-        }
-        if (lane > k && lane < w) Lm[ix(kb + lane, col)] /= lkk;
-        __syncwarp();
-        if (lane > k && lane < w) {
-          const T li = Lm[ix(kb + lane, col)];
-          for (int j = k + 1; j <= lane; ++j) Lm[ix(kb + lane, kb + j)] -= li * Lm[ix(kb + j, col)];
-        }
-        __syncwarp();
+        if (lane == 0 && k < w) dinv[kb + k] = rinv;
       }
+#pragma unroll
+      for (int j = 0; j < kPanel; ++j)
+        if (lane < w && j <= lane) Lm[ix(kb + lane, kb + j)] = a[j];
+      if (bad && lane == 0) *fail_s = 1;
     }
     __syncthreads();
     if (*fail_s) return;
@@ -89,7 +97,7 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
           T v = r[c];
 #pragma unroll
           for (int m = 0; m < c; ++m) v -= r[m] * Lm[ix(kb + c, kb + m)];
-          r[c] = v * tmp[c];
+          r[c] = v * dinv[kb + c];
         }
       }
 #pragma unroll
@@ -97,17 +105,28 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
         if (c < w) Lm[cbk[c] + i] = r[c];
     }
     __syncthreads();
-    // trailing update with the finished block
-    for (int j = ke + warp; j < P; j += nw) {
-      T ljk[kPanel];
+    // trailing update with the finished block, kCols columns per warp pass (each
+    // loaded panel row serves kCols columns; 2 in FP64 to bound registers)
+    constexpr int kCols = sizeof(T) == 8 ? 2 : 4;
+    for (int j0 = ke + kCols * warp; j0 < P; j0 += kCols * nw) {
+      T ljk[kCols][kPanel];
 #pragma unroll
-      for (int k = 0; k < kPanel; ++k) ljk[k] = k < w ? Lm[cbk[k] + j] : T(0);
-      T *colj = Lm + cb[j];
-      for (int i = j + lane; i < P; i += 32) {
-        T acc = T(0);
+      for (int c = 0; c < kCols; ++c)
 #pragma unroll
-        for (int k = 0; k < kPanel; ++k) acc += Lm[cbk[k] + i] * ljk[k];
-        colj[i] -= acc;
+        for (int k = 0; k < kPanel; ++k) ljk[c][k] = (k < w && j0 + c < P) ? Lm[cbk[k] + j0 + c] : T(0);
+      for (int i = j0 + lane; i < P; i += 32) {
+        T li[kPanel];
+#pragma unroll
+        for (int k = 0; k < kPanel; ++k) li[k] = Lm[cbk[k] + i];
+#pragma unroll
+        for (int c = 0; c < kCols; ++c) {
+          if (j0 + c < P && i >= j0 + c) {
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < kPanel; ++k) acc += li[k] * ljk[c][k];
+            Lm[cb[j0 + c] + i] -= acc;
+          }
+        }
       }
     }
     __syncthreads();
@@ -120,7 +139,7 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
       if (warp == 0) {
         T v = lane < w ? y[kb + lane] : T(0);
         for (int c = 0; c < w; ++c) {
-          T yc = v / Lm[ix(kb + c, kb + c)];
+          T yc = v * dinv[kb + c];
           yc = __shfl_sync(0xffffffffu, yc, c);
           if (lane == c) v = yc;
           if (lane > c && lane < w) v -= Lm[ix(kb + lane, kb + c)] * yc;
@@ -148,7 +167,7 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
       if (warp == 0) {
         T v = lane < w ? y[kb + lane] - tmp[lane] : T(0);
         for (int c = w - 1; c >= 0; --c) {
-          T xc = v / Lm[ix(kb + c, kb + c)];
+          T xc = v * dinv[kb + c];
           xc = __shfl_sync(0xffffffffu, xc, c);
           if (lane == c) v = xc;
           if (lane < c) v -= Lm[ix(kb + c, kb + lane)] * xc;
@@ -188,7 +207,7 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
       } else {
         double acc = 0.0;
         for (int j = lane; j < P; j += 32) {
-          const double sij = i >= j ? s_entry(A, SL, P, i, j, lam) : s_entry(A, SL, P, j, i, lam);
+          const double sij = i >= j ? s_entry(A, SL, P, i, j, lam_t) : s_entry(A, SL, P, j, i, lam_t);
           acc += sij * x[j];
         }
         acc = warp_sum(acc);
@@ -226,18 +245,23 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
     y = reinterpret_cast<T *>(x + P);
     float *xs = reinterpret_cast<float *>(y + P);
     int *cb = reinterpret_cast<int *>(xs + 2 * P);
+    T *dinv = reinterpret_cast<T *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15) +
+                                    (((size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 15) &
+                                     ~(size_t)15));
     for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P - (j * (j + 1)) / 2;
     __syncthreads();
-    factor_solve_body<T>(Lm, cb, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
+    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
   } else {
     x = reinterpret_cast<double *>(smem_raw);
     y = reinterpret_cast<T *>(x + P);
     float *xs = reinterpret_cast<float *>(y + P);
     int *cb = reinterpret_cast<int *>(xs + 2 * P);
+    T *dinv = reinterpret_cast<T *>(smem_raw + (((size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) +
+                                                              sizeof(int)) + 15) & ~(size_t)15));
     for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P;
     __syncthreads();
     T *Lm = reinterpret_cast<T *>(wv.fac) + off;
-    factor_solve_body<T>(Lm, cb, y, x, xs, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
+    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
   }
   __syncthreads();
   const bool failed = fail_s != 0;
@@ -257,7 +281,8 @@ static const size_t kSmemBudget = 200 * 1024;
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed, void *stream) {
   const int P = pv.max_P;
-  const size_t vec = (size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 16;
+  const size_t vec = (size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 16 +
+                     (size_t)P * sizeof(T) + 16;
   const size_t packed = (((size_t)P * (P + 1) / 2) * sizeof(T) + 15) / 16 * 16 + vec;
   const int use_smem = packed <= kSmemBudget;
   const size_t sm = use_smem ? packed : vec;
@@ -523,7 +548,8 @@ __global__ void k_export_S(PlanView pv, WorkView wv, int b, double *S, double *g
   if (t >= (long long)P * P) return;
   const int r = (int)(t / P), c = (int)(t % P);
   if (c > r) return;
-  const double v = s_entry(A, SL, P, r, c, lam);
+  const size_t k = (size_t)r * P + c;
+  const double v = (double)A[k] - (double)SL[k] + (r == c ? lam * (double)A[k] : 0.0);
   S[(size_t)r * P + c] = v;
   S[(size_t)c * P + r] = v;
   if (c == 0) {

@@ -160,23 +160,37 @@ class Controller:
         self.mu = X.mean(0)
         self.sd = np.maximum(X.std(0), 1e-3)
 
+    def _grad_dev(self, dX: torch.Tensor, dT: torch.Tensor, g: torch.Tensor, loss: torch.Tensor,
+                  out: torch.Tensor, cache: torch.Tensor, st):
+        nat.check(self.L.spgo_mlp_grad(_vp(self.theta), _vp(dX), _vp(dT), int(dX.shape[0]), _vp(g), _vp(loss),
+                                       _vp(out), _vp(cache), st), "mlp_grad")
+
     def train(self, tr: Traces, epochs=60, batch=512, lr=2e-3, seed=0, fit_norm=True) -> List[float]:
+        """Adam on the mean loss; the standardised traces stay on the device and
+        every step is three kernel launches (forward, backward, Adam)."""
         if fit_norm:
             self.fit_normalization(tr.X)
-        rng = np.random.default_rng(seed)
         n = tr.X.shape[0]
-        hist = []
+        Xd = torch.tensor(self._norm(tr.X), device=self.device)
+        Td = torch.tensor(np.asarray(tr.T, np.float32), device=self.device)
+        gen = torch.Generator(device=self.device)
+        gen.manual_seed(seed)
+        g = torch.zeros(nat.MLP_PARAMS, dtype=torch.float32, device=self.device)
+        loss = torch.zeros(1, dtype=torch.float32, device=self.device)
+        out = torch.zeros(2 * batch, dtype=torch.float32, device=self.device)
+        cache = torch.zeros(128 * batch, dtype=torch.float32, device=self.device)
+        ep_loss = torch.zeros(epochs, dtype=torch.float64, device=self.device)
+        st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         for ep in range(epochs):
-            perm = rng.permutation(n)
-            tot = 0.0
+            perm = torch.randperm(n, device=self.device, generator=gen)
+            Xp, Tp = Xd[perm].contiguous(), Td[perm].contiguous()
             for s0 in range(0, n, batch):
-                idx = perm[s0:s0 + batch]
-                loss, g = self.grad(tr.X[idx], tr.T[idx])
+                m = min(batch, n - s0)
+                self._grad_dev(Xp[s0:s0 + m], Tp[s0:s0 + m], g, loss, out, cache, st)
                 self.adam_step(g, lr)
-                tot += loss * len(idx)
-            hist.append(tot / n)
+                ep_loss[ep] += loss[0].double() * m
         torch.cuda.synchronize(self.device)
-        return hist
+        return (ep_loss / n).cpu().tolist()
 
 
 def iterations_to_target(problems, controller: Optional[Controller], targets: np.ndarray, max_iters=30,

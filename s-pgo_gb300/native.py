@@ -44,7 +44,8 @@ class PlanSizes(C.Structure):
     _fields_ = [("n_problems", C.c_int32), ("total_poses", C.c_int32), ("total_landmarks", C.c_int32),
                 ("total_obs", C.c_int64), ("n_chunks", C.c_int32), ("n_schur_items", C.c_int32),
                 ("max_params", C.c_int32), ("schur_chunk_tiles", C.c_int32), ("static_bytes", C.c_size_t),
-                ("workspace_bytes", C.c_size_t), ("slab_elems", C.c_int64), ("pair_records", C.c_int64)]
+                ("workspace_bytes", C.c_size_t), ("slab_elems", C.c_int64), ("pair_records", C.c_int64),
+                ("schur_flops", C.c_int64), ("n_tc_items", C.c_int32), ("tc_chunk_tiles", C.c_int32)]
 
 
 class Params(C.Structure):

@@ -3,7 +3,7 @@ CUDA path (SIMT and tensor-core Schur complements) against the FP64 oracle.
 
 S cancels most of A (on the 45-pose problem below max|A| / max|S| is ~600), so
 errors are stated relative to the largest entry of A (and of g_T for g_S), the
-scale the FP32 terms are formed at: FP64 path 1e-12; mixed path with the SIMT
+scale the FP32 terms are formed at: FP64 path 1e-10; mixed path with the SIMT
 FP32 Schur 2e-6; mixed path with the tensor-core Schur (split TF32 operands,
 hi.hi + hi.lo + lo.hi, ~21-bit products, TMEM read back every 4 chunks into
 FP32 registers) 2e-6."""
@@ -33,7 +33,7 @@ def oracle_reduced(p, lam, eps=1e-4):
     return Sm, lin.g_T - BD @ lin.g_a, lin
 
 
-@pytest.mark.parametrize("prec,use_tc,tol", [("fp64", 0, 1e-12), ("mixed", 0, 2e-6), ("mixed", 1, 2e-6)])
+@pytest.mark.parametrize("prec,use_tc,tol", [("fp64", 0, 1e-10), ("mixed", 0, 2e-6), ("mixed", 1, 2e-6)])
 def test_reduced_system_matches_oracle(built_lib, cuda_device, prec, use_tc, tol):
     # sizes that exercise one, two and three 128-row tensor-core tiles (P = 54, 156, 84, 270)
     # and off-diagonal tiles with partial column ranges
