@@ -44,7 +44,18 @@ def _env_rank():
 
 
 def _batch_seed(rank: int) -> int:
+    """Seed of rank r's 256-problem batch (rank 0: the config-3 batch, seed 3)."""
     return 3 + 7919 * rank
+
+
+def max_over_ranks(x: float, world: int, device="cpu") -> float:
+    """The slowest rank's value (the timed region's wall time), via all_reduce MAX."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 # ---------------------------------------------------------------------------
@@ -288,10 +299,7 @@ def run_ours(args):
     prof = bs.profile_read()
     bs.profile(0)
     total_ms = float(sum(ms))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, world, dev)
     value = N_PROBLEMS * world * args.steps / (total_ms / 1e3)
     iters = [s["iterations"] for s in status]
     chosen_costs = np.array([s["cost"] for s in status])

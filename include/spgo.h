@@ -199,6 +199,7 @@ int spgo_export_reduced(spgo_solver *s, int32_t problem, double lambda, double *
  * log10(lambda) and the logit that the current damping yields an accepted step. */
 #define SPGO_MLP_PARAMS 5378
 #define SPGO_MLP_INPUTS 16
+#define SPGO_MLP_CACHE_PER_SAMPLE 386   /* floats of spgo_mlp_grad scratch per sample */
 
 /* FP32 forward of n feature rows d_X [n*16] -> d_out [n*2]; d_cache [n*128]
  * (or NULL) keeps the pre-activations for spgo_mlp_grad. */
@@ -206,7 +207,7 @@ int spgo_mlp_forward(const float *d_params, const float *d_X, int32_t n, float *
                      void *stream);
 /* Mean loss (out0 - t0)^2 + BCE(out1, t1) over n samples with targets d_T [n*2]
  * and its gradient d_grad [SPGO_MLP_PARAMS]; d_loss [1]; scratch d_out [n*2],
- * d_cache [n*128]. */
+ * d_cache [n*SPGO_MLP_CACHE_PER_SAMPLE]. */
 int spgo_mlp_grad(const float *d_params, const float *d_X, const float *d_T, int32_t n, float *d_grad,
                   float *d_loss, float *d_out, float *d_cache, void *stream);
 /* One Adam step (beta 0.9 / 0.999) on the parameters; step counts from 1. */

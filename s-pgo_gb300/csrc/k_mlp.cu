@@ -8,8 +8,8 @@
 // averaged over the batch.
 //
 // Kernels: FP32 forward (thread per sample, weights in shared memory), fused
-// loss + backward (thread per sample, per-CTA shared-memory gradient
-// reduction, one global reduction per CTA), Adam, and the BF16 inference the LM
+// loss + per-sample deltas (thread per sample), the parameter gradient as batch
+// sums (thread per parameter, no atomics), Adam, and the BF16 inference the LM
 // loop runs (warp per problem, FP32 accumulation).
 #include <cuda_bf16.h>
 
@@ -61,66 +61,88 @@ __global__ void __launch_bounds__(128) k_mlp_fwd(const float *__restrict__ theta
   out[2 * s + 1] = o1;
 }
 
-// loss + gradient (accumulated into grad, which the caller zeroes) for samples
-// whose forward pass left out / cache
-__global__ void __launch_bounds__(128) k_mlp_bwd(const float *__restrict__ theta, const float *__restrict__ X,
-                                                 const float *__restrict__ T, int n, const float *__restrict__ out,
-                                                 const float *__restrict__ cache, float *__restrict__ grad,
-                                                 float *__restrict__ loss) {
+// Backward in two passes, no atomics on the parameters:
+//   k_mlp_delta  (thread per sample): loss, and the per-sample activations and
+//                deltas h1, h2, dz1, dz2, dout into the cache;
+//   k_mlp_param  (thread per parameter): the batch sum of delta x activation,
+//                written straight into grad.
+// Cache layout (floats): [z1 | z2 | h1 | h2 | dz1 | dz2] each n x 64, then dout n x 2.
+constexpr int kCachePerSample = 6 * kH + 2;
+static_assert(kCachePerSample == SPGO_MLP_CACHE_PER_SAMPLE, "cache size");
+
+__global__ void __launch_bounds__(128) k_mlp_delta(const float *__restrict__ theta, const float *__restrict__ T, int n,
+                                                   const float *__restrict__ out, float *__restrict__ cache,
+                                                   float *__restrict__ loss) {
   __shared__ float W[kParams];
-  __shared__ float G[kParams];
-  for (int i = threadIdx.x; i < kParams; i += blockDim.x) {
-    W[i] = theta[i];
-    G[i] = 0.f;
-  }
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x) W[i] = theta[i];
   __syncthreads();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   float lsum = 0.f;
   if (s < n) {
+    const size_t nh = (size_t)n * kH;
+    const float *z1 = cache + (size_t)s * kH;
+    const float *z2 = cache + nh + (size_t)s * kH;
+    float *h1 = cache + 2 * nh + (size_t)s * kH;
+    float *h2 = cache + 3 * nh + (size_t)s * kH;
+    float *dz1 = cache + 4 * nh + (size_t)s * kH;
+    float *dz2 = cache + 5 * nh + (size_t)s * kH;
+    float *dout = cache + 6 * nh + 2 * (size_t)s;
     const float inv_n = 1.f / (float)n;
     const float o0 = out[2 * s], o1 = out[2 * s + 1];
     const float t0 = T[2 * s], t1 = T[2 * s + 1];
     const float sig = 1.f / (1.f + expf(-o1));
     lsum = (o0 - t0) * (o0 - t0) + (fmaxf(o1, 0.f) + log1pf(expf(-fabsf(o1)))) - t1 * o1;
     const float d0 = 2.f * (o0 - t0) * inv_n, d1 = (sig - t1) * inv_n;
-    atomicAdd(&G[kB3], d0);
-    atomicAdd(&G[kB3 + 1], d1);
-    const float *z1 = cache + (size_t)s * kH;
-    const float *z2 = cache + (size_t)n * kH + (size_t)s * kH;
-    float h1[kH];
-#pragma unroll 8
-    for (int k = 0; k < kH; ++k) h1[k] = gelu(z1[k]);
-    float dh1[kH];
-#pragma unroll 8
-    for (int k = 0; k < kH; ++k) dh1[k] = 0.f;
+    dout[0] = d0;
+    dout[1] = d1;
+    float g2[kH];
     for (int j = 0; j < kH; ++j) {
       const float zj = z2[j];
-      const float h2 = gelu(zj);
-      atomicAdd(&G[kW3 + j], d0 * h2);
-      atomicAdd(&G[kW3 + kH + j], d1 * h2);
-      const float dz2 = (d0 * W[kW3 + j] + d1 * W[kW3 + kH + j]) * gelu_grad(zj);
-      atomicAdd(&G[kB2 + j], dz2);
-#pragma unroll 8
-      for (int k = 0; k < kH; ++k) {
-        atomicAdd(&G[kW2 + j * kH + k], dz2 * h1[k]);
-        dh1[k] += dz2 * W[kW2 + j * kH + k];
-      }
+      h2[j] = gelu(zj);
+      g2[j] = (d0 * W[kW3 + j] + d1 * W[kW3 + kH + j]) * gelu_grad(zj);
+      dz2[j] = g2[j];
     }
-    float x[kIn];
-#pragma unroll
-    for (int k = 0; k < kIn; ++k) x[k] = X[(size_t)s * kIn + k];
-    for (int j = 0; j < kH; ++j) {
-      const float dz1 = dh1[j] * gelu_grad(z1[j]);
-      atomicAdd(&G[kB1 + j], dz1);
-#pragma unroll
-      for (int k = 0; k < kIn; ++k) atomicAdd(&G[kW1 + j * kIn + k], dz1 * x[k]);
+    for (int k = 0; k < kH; ++k) {
+      const float zk = z1[k];
+      h1[k] = gelu(zk);
+      float acc = 0.f;
+#pragma unroll 8
+      for (int j = 0; j < kH; ++j) acc += g2[j] * W[kW2 + j * kH + k];
+      dz1[k] = acc * gelu_grad(zk);
     }
   }
   lsum = warp_sum(lsum);
   if ((threadIdx.x & 31) == 0 && lsum != 0.f) atomicAdd(loss, lsum / (float)n);
-  __syncthreads();
-  for (int i = threadIdx.x; i < kParams; i += blockDim.x)
-    if (G[i] != 0.f) atomicAdd(grad + i, G[i]);
+}
+
+__global__ void __launch_bounds__(128) k_mlp_param(const float *__restrict__ X, int n, const float *__restrict__ cache,
+                                                   float *__restrict__ grad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kParams) return;
+  const size_t nh = (size_t)n * kH;
+  const float *h1 = cache + 2 * nh, *h2 = cache + 3 * nh, *dz1 = cache + 4 * nh, *dz2 = cache + 5 * nh;
+  const float *dout = cache + 6 * nh;
+  float acc = 0.f;
+  if (p < kB1) {
+    const int j = p / kIn, k = p % kIn;
+    for (int s = 0; s < n; ++s) acc += dz1[(size_t)s * kH + j] * X[(size_t)s * kIn + k];
+  } else if (p < kW2) {
+    const int j = p - kB1;
+    for (int s = 0; s < n; ++s) acc += dz1[(size_t)s * kH + j];
+  } else if (p < kB2) {
+    const int j = (p - kW2) / kH, k = (p - kW2) % kH;
+    for (int s = 0; s < n; ++s) acc += dz2[(size_t)s * kH + j] * h1[(size_t)s * kH + k];
+  } else if (p < kW3) {
+    const int j = p - kB2;
+    for (int s = 0; s < n; ++s) acc += dz2[(size_t)s * kH + j];
+  } else if (p < kB3) {
+    const int o = (p - kW3) / kH, j = (p - kW3) % kH;
+    for (int s = 0; s < n; ++s) acc += dout[2 * (size_t)s + o] * h2[(size_t)s * kH + j];
+  } else {
+    const int o = p - kB3;
+    for (int s = 0; s < n; ++s) acc += dout[2 * (size_t)s + o];
+  }
+  grad[p] = acc;
 }
 
 __global__ void k_mlp_adam(float *theta, const float *grad, float *m, float *v, int step, float lr) {
@@ -322,11 +344,11 @@ extern "C" int spgo_mlp_grad(const float *d_params, const float *d_X, const floa
                              float *d_loss, float *d_out, float *d_cache, void *stream) {
   if (!d_params || !d_X || !d_T || !d_grad || !d_loss || !d_out || !d_cache || n <= 0) return SPGO_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
-  cudaMemsetAsync(d_grad, 0, sizeof(float) * kParams, st);
   cudaMemsetAsync(d_loss, 0, sizeof(float), st);
   k_mlp_fwd<<<grid_for(n, 128), 128, 0, st>>>(d_params, d_X, n, d_out, d_cache);
-  k_mlp_bwd<<<grid_for(n, 128), 128, 0, st>>>(d_params, d_X, d_T, n, d_out, d_cache, d_grad, d_loss);
-  g_launches += 2;
+  k_mlp_delta<<<grid_for(n, 128), 128, 0, st>>>(d_params, d_T, n, d_out, d_cache, d_loss);
+  k_mlp_param<<<grid_for(kParams, 128), 128, 0, st>>>(d_X, n, d_cache, d_grad);
+  g_launches += 3;
   return cudaGetLastError() == cudaSuccess ? SPGO_OK : SPGO_ERR_CUDA;
 }
 

@@ -131,7 +131,7 @@ class Controller:
         g = torch.zeros(nat.MLP_PARAMS, dtype=torch.float32, device=self.device)
         loss = torch.zeros(1, dtype=torch.float32, device=self.device)
         out = torch.zeros(2 * n, dtype=torch.float32, device=self.device)
-        cache = torch.zeros(128 * n, dtype=torch.float32, device=self.device)
+        cache = torch.zeros(nat.MLP_CACHE_PER_SAMPLE * n, dtype=torch.float32, device=self.device)
         st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         nat.check(self.L.spgo_mlp_grad(_vp(self.theta), _vp(dX), _vp(dT), n, _vp(g), _vp(loss), _vp(out),
                                        _vp(cache), st), "mlp_grad")
@@ -178,7 +178,7 @@ class Controller:
         g = torch.zeros(nat.MLP_PARAMS, dtype=torch.float32, device=self.device)
         loss = torch.zeros(1, dtype=torch.float32, device=self.device)
         out = torch.zeros(2 * batch, dtype=torch.float32, device=self.device)
-        cache = torch.zeros(128 * batch, dtype=torch.float32, device=self.device)
+        cache = torch.zeros(nat.MLP_CACHE_PER_SAMPLE * batch, dtype=torch.float32, device=self.device)
         ep_loss = torch.zeros(epochs, dtype=torch.float64, device=self.device)
         st = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
         for ep in range(epochs):

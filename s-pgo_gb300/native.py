@@ -27,7 +27,7 @@ EXPORTED = [
     "spgo_cost_noalloc", "spgo_export_reduced", "spgo_mlp_forward", "spgo_mlp_grad", "spgo_mlp_adam",
     "spgo_lm_set_controller", "spgo_lm_features", "spgo_lm_probe",
 ]
-MLP_PARAMS, MLP_INPUTS = 5378, 16
+MLP_PARAMS, MLP_INPUTS, MLP_CACHE_PER_SAMPLE = 5378, 16, 386
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
                  "update", "bookkeeping"]
 

@@ -123,3 +123,21 @@ def test_zero_controller_is_nielsen(built_lib, cuda_device):
         assert runs[0][b]["iterations"] == runs[1][b]["iterations"]
         assert abs(runs[0][b]["cost"] - runs[1][b]["cost"]) / r.cost < 1e-12
         assert abs(runs[1][b]["cost"] - r.cost) / r.cost < 1e-6
+
+
+def test_trained_controller_beats_nielsen_on_heldout(built_lib, cuda_device):
+    """The shipped network (trained on other seeds) reaches the plain FP64 solver's
+    cost in fewer LM iterations than the plain schedule, on held-out problems."""
+    import os
+    if not os.path.exists(learned.DEFAULT_WEIGHTS):
+        pytest.fail("controller weights missing")
+    probs = scenes.config3(seed=2500, n_problems=96)
+    bs = BatchSolver(probs, precision="fp64")
+    bs.set_params(loss="l2", max_iters=30, tol=1e-6)
+    targets = np.array([s["cost"] for s in bs.solve()])
+    bs.close()
+    ctl = learned.Controller.load(device="cuda")
+    plain, _, _ = learned.iterations_to_target(probs, None, targets, precision="mixed")
+    lrn, costs, _ = learned.iterations_to_target(probs, ctl, targets, precision="mixed")
+    assert lrn.mean() < 0.9 * plain.mean(), (lrn.mean(), plain.mean())
+    assert (lrn <= 30).mean() >= (plain <= 30).mean()

@@ -101,3 +101,20 @@ def test_reference_gn_step_decreases_cost():
     c0 = S.cost(p, S.REFERENCE_GPU_LOSS)
     S.reference_gn_step(p, iterations=3, step_size=1.0)
     assert S.cost(p, S.REFERENCE_GPU_LOSS) < 0.1 * c0
+
+
+def test_mlp_oracle_gradient_fd():
+    """The controller network's FP64 reference gradient against central differences."""
+    from oracle import mlp as M
+    rng = np.random.default_rng(0)
+    theta = M.init(seed=2).astype(np.float64)
+    X = rng.normal(0.0, 1.0, (7, M.D_IN))
+    T = np.stack([rng.normal(0.0, 1.0, 7), rng.integers(0, 2, 7)], 1).astype(np.float64)
+    _, g = M.loss_and_grad(theta, X, T)
+    idx = rng.choice(M.N_PARAMS, 40, replace=False)
+    h = 1e-6
+    for i in idx:
+        e = np.zeros_like(theta)
+        e[i] = h
+        fd = (M.loss_and_grad(theta + e, X, T)[0] - M.loss_and_grad(theta - e, X, T)[0]) / (2 * h)
+        assert abs(fd - g[i]) < 1e-6 * max(1.0, abs(g[i]))
