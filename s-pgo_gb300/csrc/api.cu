@@ -138,7 +138,7 @@ static void build_layout(spgo_plan *p) {
   p->w_fac = take(packed <= 200 * 1024 ? 0 : (size_t)p->total_S * ts);
   p->w_delta = take((size_t)p->total_params * 8);
   p->w_C = take((size_t)(p->L + 64) * ts);  // + 64: the tensor-core Schur copies 16-byte aligned supersets
-  p->w_ga = take((size_t)p->L * ts);
+  p->w_ga = take((size_t)(p->L + 64) * ts);  // + 64: as C
   p->w_slab = take((size_t)p->total_slab * ts);
   p->w_lm = take((size_t)p->B * sizeof(LMState));
   p->w_cost = take((size_t)p->B * 8);
@@ -474,6 +474,8 @@ static void make_views(spgo_solver *s) {
 template <typename T>
 static int enqueue_linearize(spgo_solver *s, cudaStream_t st, bool stats, bool ctrl) {
   { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_RELIN, st)); }
+  // the cost at the first linearisation point (later ones come from the cost pass that accepted them)
+  { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 1, GATE_FIRST, st)); }
   { PROF(K_LINEARIZE); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 0, GATE_RELIN, st)); }
   { PROF(K_SYSTEM); CUDA_TRY(launch_system<T>(s->pv, s->wv, GATE_RELIN, st)); }
   {

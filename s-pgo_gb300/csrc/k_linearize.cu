@@ -104,18 +104,27 @@ struct LinSmem {
   int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
   double cost[8];
   T pair[SPGO_MAX_WINDOW + 1][27];  // (host, target) pair terms of the chunk, by target - f0
+  int key[8][32];                   // per warp: target frame of each lane's observation (-1: none)
 };
+constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [27][33]
 
 // ---- fused linearisation / cost -----------------------------------------------
 // One CTA per chunk of <= 32 landmarks.  Phase A: per-landmark anchor point.
 // Phase B: one thread per observation (both cameras): residual, robust weight,
-// inverse-depth Jacobian (C, g_a by shared atomics), pair accumulators (global
-// reductions), and the observation's s K^T j_alpha written into the slab row of
-// its frame.  Phase C: per landmark, the suffix (frames after the anchor) and
-// prefix (frames before it) sums that turn those rows into b_l(i), then
-// B_l(i) = Ad_i^T b_l(i).  COST = true runs phase B's residual part only.
+// inverse-depth Jacobian (C, g_a by shared atomics), pair accumulators, and the
+// observation's s K^T j_alpha written into the slab row of its frame.  The pair
+// terms of a warp are staged in shared memory and summed over runs of equal
+// target frame (observations are sorted by frame, and every landmark of the
+// chunk has the same host) by 27 lanes, one value each.  Phase C: per landmark,
+// the suffix (frames after the anchor) and prefix (frames before it) sums that
+// turn those rows into b_l(i), then B_l(i) = Ad_i^T b_l(i).
+// COST = true is the cost pass: residuals only, in double-float on the FP32 path
+// (FP64-accurate cost for the gain ratio).  The linearisation itself (COST =
+// false) forms residuals in plain T: they feed the gradient only, where FP32
+// rounding (~3e-5 px) is far below what moves the optimum; the cost at the
+// linearisation point always comes from a cost pass.
 template <typename T, bool COST>
-__global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Params prm,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanView pv, WorkView wv, Params prm,
                                                    const double *__restrict__ alpha_state, int gate) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
@@ -128,7 +137,8 @@ __global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Par
   const T fxs[2] = {(T)intr[0], (T)intr[4]}, fys[2] = {(T)intr[1], (T)intr[5]};
   const T cxs[2] = {(T)intr[2], (T)intr[6]}, cys[2] = {(T)intr[3], (T)intr[7]};
   LinSmem<T> &sm = *reinterpret_cast<LinSmem<T> *>(smem_raw);
-  T *slab_s = reinterpret_cast<T *>(smem_raw + ((sizeof(LinSmem<T>) + 15) & ~(size_t)15));  // [6 nb][32]
+  T *stage = reinterpret_cast<T *>(smem_raw + ((sizeof(LinSmem<T>) + 15) & ~(size_t)15));  // [8][27][33]
+  T *slab_s = stage + 8 * 27 * kStagePitch;                                                 // [6 nb][32]
   const int rows = 6 * nb;
 
   // phase A
@@ -140,7 +150,7 @@ __global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Par
     const T *Ra = FramesT<T>::R(wv, fo + a, 0);
     const Vec3<T> ta = v3<T>((ua - cxs[0]) / fxs[0] / alpha, (va - cys[0]) / fys[0] / alpha, T(1) / alpha);
     Vec3<T> X = mul(Ra, ta);
-    if constexpr (std::is_same<T, float>::value) {
+    if constexpr (COST && std::is_same<T, float>::value) {
       // the same point as a double-float, for the residuals
       const df al = df_from_double(alpha_state[pv.lm_user[li]]);
       const df t3[3] = {df_sub(pv.lm_uv[2 * li], intr[2]) / df_make(intr[0]) / al,
@@ -217,7 +227,7 @@ __global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Par
         const T fx = fxs[cam], fy = fys[cam];
         Vec3<T> t;
         T r0, r1;
-        if constexpr (std::is_same<T, float>::value) {
+        if constexpr (COST && std::is_same<T, float>::value) {
           // residual in double-float: X + (c_a - c_n), rotated, projected
           const float *ah = wv.fr_ch + (size_t)fa * 6, *al = wv.fr_cl + (size_t)fa * 6;
           const float *nh = wv.fr_ch + (size_t)fn * 6 + cam * 3, *nl = wv.fr_cl + (size_t)fn * 6 + cam * 3;
@@ -245,8 +255,10 @@ __global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Par
         const T iz = T(1) / t.z;
         T rho;
         const T w2 = boost * robust<T>(prm.loss, lscale, r0 * r0 + r1 * r1, rho);
-        cost_t += T(0.5) * boost * rho;
-        if (COST) continue;
+        if (COST) {
+          cost_t += T(0.5) * boost * rho;
+          continue;
+        }
         // dpi/dt (2x3) then u = dpi/dt R_n^T (rows u0, u1)
         const T j00 = fx * iz, j02 = -fx * t.x * iz * iz, j11 = fy * iz, j12 = -fy * t.y * iz * iz;
         const Vec3<T> u0 = v3<T>(j00 * Rn[0] + j02 * Rn[2], j00 * Rn[3] + j02 * Rn[5], j00 * Rn[6] + j02 * Rn[8]);
@@ -289,42 +301,47 @@ __global__ void __launch_bounds__(256) k_linearize(PlanView pv, WorkView wv, Par
       }
     }
     if (!COST) {
-      // segmented sum over runs of equal target frame (runs are contiguous)
+      // stage the 27 pair values, then lanes 0..26 each sum one value over the
+      // runs of equal target frame and add each run into the chunk's pair slot
+      T *st = stage + (size_t)(tid >> 5) * 27 * kStagePitch;
+      int *keys = sm.key[tid >> 5];
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const int kd = __shfl_down_sync(0xffffffffu, key, d);
-        const bool take = (lane + d < 32) && (kd == key);
+      for (int k = 0; k < 21; ++k) st[k * kStagePitch + lane] = M[k];
 #pragma unroll
-        for (int k = 0; k < 21; ++k) {
-          const T v = __shfl_down_sync(0xffffffffu, M[k], d);
-          if (take) M[k] += v;
+      for (int k = 0; k < 6; ++k) st[(21 + k) * kStagePitch + lane] = m[k];
+      keys[lane] = key;
+      __syncwarp();
+      if (__any_sync(0xffffffffu, key >= 0) && lane < 27) {
+        const T *col = st + lane * kStagePitch;
+        T acc = T(0);
+        int cur = keys[0];
+        for (int i = 0; i < 32; ++i) {
+          const int k = keys[i];
+          if (k != cur) {
+            if (cur >= 0 && acc != T(0)) atomicAdd(&sm.pair[cur - f0][lane], acc);
+            acc = T(0);
+            cur = k;
+          }
+          acc += col[i];
         }
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          const T v = __shfl_down_sync(0xffffffffu, m[k], d);
-          if (take) m[k] += v;
-        }
+        if (cur >= 0 && acc != T(0)) atomicAdd(&sm.pair[cur - f0][lane], acc);
       }
-      const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
-      if (key >= 0 && (lane == 0 || kprev != key)) {
-        T *dst = sm.pair[key - f0];
-#pragma unroll
-        for (int k = 0; k < 21; ++k) atomicAdd(dst + k, M[k]);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) atomicAdd(dst + 21 + k, m[k]);
-      }
+      __syncwarp();
     }
   }
-  // cost: warp sums, then one FP64 atomic per CTA
-  const double cost = warp_sum((double)cost_t);
-  if ((tid & 31) == 0) sm.cost[tid >> 5] = cost;
-  __syncthreads();
-  if (tid == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm.cost[w];
-    if (t != 0.0) atomicAdd(wv.cost_acc + b, t);
+  if (COST) {
+    // cost: warp sums, then one FP64 atomic per CTA
+    const double cost = warp_sum((double)cost_t);
+    if ((tid & 31) == 0) sm.cost[tid >> 5] = cost;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm.cost[w];
+      if (t != 0.0) atomicAdd(wv.cost_acc + b, t);
+    }
+    return;
   }
-  if (COST) return;
+  __syncthreads();
 
   // pair slots -> global accumulators: (lo, hi) = (min, max)(host, target)
   {
@@ -398,7 +415,7 @@ int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, in
 template <typename T>
 static size_t lin_smem(int max_nb, bool cost) {
   const size_t head = (sizeof(LinSmem<T>) + 15) & ~(size_t)15;
-  return cost ? head : head + (size_t)6 * max_nb * SPGO_CHUNK * sizeof(T);
+  return cost ? head : head + ((size_t)8 * 27 * kStagePitch + (size_t)6 * max_nb * SPGO_CHUNK) * sizeof(T);
 }
 
 template <typename T>

@@ -163,34 +163,52 @@ __global__ void k_to_bf16(const float *src, __nv_bfloat16 *dst, int n) {
   if (i < n) dst[i] = __float2bfloat16(src[i]);
 }
 
-// BF16-weight inference for up to one feature vector per warp; lanes split the
-// hidden units, FP32 accumulation
-__device__ void mlp_infer_warp(const __nv_bfloat16 *__restrict__ Wb, const float *x, float &o0, float &o1) {
+// BF16-weight inference, one feature vector per warp: the CTA stages the BF16
+// weights in shared memory as FP32 with both weight matrices transposed (lanes
+// read consecutive hidden units), lanes split the hidden units, FP32 accumulation
+struct MlpSmem {
+  float w1t[kIn][kH], b1[kH], w2t[kH][kH], b2[kH], w3[kOut][kH], b3[kOut];
+};
+
+__device__ void stage_mlp(const __nv_bfloat16 *__restrict__ Wb, MlpSmem &m) {
+  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) m.w1t[i % kIn][i / kIn] = __bfloat162float(Wb[kW1 + i]);
+  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) m.w2t[i % kH][i / kH] = __bfloat162float(Wb[kW2 + i]);
+  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
+    m.b1[i] = __bfloat162float(Wb[kB1 + i]);
+    m.b2[i] = __bfloat162float(Wb[kB2 + i]);
+    m.w3[0][i] = __bfloat162float(Wb[kW3 + i]);
+    m.w3[1][i] = __bfloat162float(Wb[kW3 + kH + i]);
+  }
+  if (threadIdx.x < kOut) m.b3[threadIdx.x] = __bfloat162float(Wb[kB3 + threadIdx.x]);
+}
+
+__device__ void mlp_infer_warp(const MlpSmem &m, const float *x, float &o0, float &o1) {
   const int lane = threadIdx.x & 31;
   float h1[2];
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
     const int j = lane + 32 * q;
-    float z = __bfloat162float(Wb[kB1 + j]);
+    float z = m.b1[j];
 #pragma unroll
-    for (int k = 0; k < kIn; ++k) z += __bfloat162float(Wb[kW1 + j * kIn + k]) * x[k];
+    for (int k = 0; k < kIn; ++k) z += m.w1t[k][j] * x[k];
     h1[q] = gelu(z);
   }
   float p0 = 0.f, p1 = 0.f;
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
     const int j = lane + 32 * q;
-    float z = __bfloat162float(Wb[kB2 + j]);
+    float z = m.b2[j];
+#pragma unroll 8
     for (int k = 0; k < kH; ++k) {
       const float hk = __shfl_sync(0xffffffffu, h1[k >> 5], k & 31);
-      z += __bfloat162float(Wb[kW2 + j * kH + k]) * hk;
+      z += m.w2t[k][j] * hk;
     }
     const float h2 = gelu(z);
-    p0 += __bfloat162float(Wb[kW3 + j]) * h2;
-    p1 += __bfloat162float(Wb[kW3 + kH + j]) * h2;
+    p0 += m.w3[0][j] * h2;
+    p1 += m.w3[1][j] * h2;
   }
-  o0 = warp_sum(p0) + __bfloat162float(Wb[kB3]);
-  o1 = warp_sum(p1) + __bfloat162float(Wb[kB3 + 1]);
+  o0 = warp_sum(p0) + m.b3[0];
+  o1 = warp_sum(p1) + m.b3[1];
 }
 
 __device__ __forceinline__ float feat_clip(double v) {
@@ -228,6 +246,9 @@ __device__ void lm_features(const PlanView &pv, const LMState &s, int b, float *
 // rejected step no relinearisation happens and the Nielsen increase stands: the
 // fallback whenever a step fails the gain-ratio test.
 __global__ void k_controller(PlanView pv, WorkView wv, const __nv_bfloat16 *Wb) {
+  __shared__ MlpSmem m;
+  stage_mlp(Wb, m);
+  __syncthreads();
   const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (b >= pv.B) return;
   LMState &s = wv.lm[b];
@@ -235,7 +256,7 @@ __global__ void k_controller(PlanView pv, WorkView wv, const __nv_bfloat16 *Wb) 
   float x[kIn];
   lm_features(pv, s, b, x);
   float o0, o1;
-  mlp_infer_warp(Wb, x, o0, o1);
+  mlp_infer_warp(m, x, o0, o1);
   if ((threadIdx.x & 31) == 0 && o1 > 0.f) {
     const double dl = fmin(3.0, fmax(-6.0, (double)o0));
     s.lam = fmin(1e12, fmax(1e-14, s.lam * pow(10.0, dl)));
@@ -309,7 +330,7 @@ int launch_lm_stats(const PlanView &pv, const WorkView &wv, int f64, void *strea
 }
 
 int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wb, void *stream) {
-  k_controller<<<grid_for(pv.B, 4), 128, 0, (cudaStream_t)stream>>>(pv, wv,
+  k_controller<<<grid_for(pv.B, 8), 256, 0, (cudaStream_t)stream>>>(pv, wv,
                                                                    reinterpret_cast<const __nv_bfloat16 *>(Wb));
   ++g_launches;
   return (int)cudaGetLastError();

@@ -18,6 +18,8 @@
 //              x = hi + lo (hi rounded to 10 mantissa bits, lo = x - hi rounded
 //              again), written in the no-swizzle K-major core-matrix layout into
 //              a double-buffered operand stage (zero rows outside the chunk);
+//              on diagonal tiles they also accumulate the g-side term
+//              g_L(row) += sum_k x_k (g_a,k s_k) = sum_k W_k g_a,k / D_k;
 //   warp 8     one thread issues 3 x 4 kind::tf32 MMAs per chunk (hi.hi + hi.lo +
 //              lo.hi, K = 8 each) into one of two 128-lane x 128-column FP32 TMEM
 //              accumulators, trimming N to the chunk's last column;
@@ -32,8 +34,7 @@
 // Every wait is bounded by the global timer; a timeout sets the problem's
 // failure flag, lets the copies and MMAs in flight finish, frees TMEM and returns.
 //
-// The g-side term g_L = sum_l B_l g_a,l / D_l is a matrix-vector product and
-// runs on the SIMT cores (k_schur_g).
+// (The SIMT Schur path in k_system.cu forms g_L the same way inside its tiles.)
 #include "kernels.cuh"
 #include "tc.cuh"
 
@@ -58,7 +59,8 @@ struct OpStage {                    // 64 KB, 1024-byte aligned
 struct RawSlot {                    // 33,024 bytes (16-byte multiple)
   float x[kTcTile * kTcK];          // tile-row slab rows [xr0, xr1), row-major
   float y[kTcTile * kTcK];          // tile-column slab rows [yr0, yr1)
-  float c[48];                      // C[cstart .. cstart + 36), cstart = lm0 & ~3
+  float c[36];                      // C[cstart .. cstart + 36), cstart = lm0 & ~3
+  float ga[36];                     // g_a over the same range
   int32_t s1, cnt, coff, xr0, xr1, yr0, yr1, pad[9];
 };
 
@@ -66,6 +68,7 @@ struct TcSmem {
   OpStage op[kOpStages];
   RawSlot raw[kRawSlots];
   float sk[2][kTcK];
+  float gs[2][kTcK];                // g_a,k s_k of the chunk being split (diagonal tiles)
   int32_t op_ncols[kOpStages];
   uint64_t raw_full[kRawSlots], raw_empty[kRawSlots], op_full[kOpStages], op_empty[kOpStages];
   uint64_t acc_full[2], acc_empty[2], fin;
@@ -84,13 +87,17 @@ __device__ __forceinline__ float tf32_round(float x) {
 }
 
 // scale one slab row (or zeros) by s and write its hi/lo parts as row r of an
-// operand in core-matrix layout; piece order rotated by r (bank-conflict free)
-__device__ __forceinline__ void split_row(const float *src, bool valid, const float *s, int r, float *h, float *l) {
+// operand in core-matrix layout; piece order rotated by r (bank-conflict free).
+// With gs != nullptr also returns sum_k x_k gs_k.
+__device__ __forceinline__ float split_row(const float *src, bool valid, const float *s, const float *gs, int r,
+                                           float *h, float *l) {
+  float gacc = 0.f;
 #pragma unroll
   for (int m = 0; m < 8; ++m) {
     const int kq = (m + r) & 7;
     float4 v = valid ? *reinterpret_cast<const float4 *>(src + 4 * kq) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float x[4] = {v.x * s[4 * kq], v.y * s[4 * kq + 1], v.z * s[4 * kq + 2], v.w * s[4 * kq + 3]};
+    if (gs) gacc += x[0] * gs[4 * kq] + x[1] * gs[4 * kq + 1] + x[2] * gs[4 * kq + 2] + x[3] * gs[4 * kq + 3];
     float hi[4], lo[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -101,6 +108,7 @@ __device__ __forceinline__ void split_row(const float *src, bool valid, const fl
     *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(h) + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
     *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(l) + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
   }
+  return gacc;
 }
 
 __device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
@@ -150,6 +158,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
     if (lane == 0) {
       const float *slab_all = reinterpret_cast<const float *>(wv.slab);
       const float *Cv = reinterpret_cast<const float *>(wv.C);
+      const float *Gv = reinterpret_cast<const float *>(wv.ga);
       int issued = 0;
       for (int i = 0; i < n; ++i) {
         const int r = i % kRawSlots, u = i / kRawSlots;
@@ -174,10 +183,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
         R.yr1 = yr1;
         const uint32_t bx = xr1 > xr0 ? (uint32_t)(xr1 - xr0) * kTcK * 4 : 0u;
         const uint32_t by = (!diag && yr1 > yr0) ? (uint32_t)(yr1 - yr0) * kTcK * 4 : 0u;
-        tc::mbar_arrive_expect_tx(&sm.raw_full[r], bx + by + 144u);
+        tc::mbar_arrive_expect_tx(&sm.raw_full[r], bx + by + (diag ? 288u : 144u));
         if (bx) tc::bulk_g2s(R.x, slab + (size_t)(xr0 - s0) * kTcK, bx, &sm.raw_full[r]);
         if (by) tc::bulk_g2s(R.y, slab + (size_t)(yr0 - s0) * kTcK, by, &sm.raw_full[r]);
         tc::bulk_g2s(R.c, Cv + cstart, 144u, &sm.raw_full[r]);
+        if (diag) tc::bulk_g2s(R.ga, Gv + cstart, 144u, &sm.raw_full[r]);
         issued = i + 1;
       }
       // let every copy in flight land before the CTA can exit
@@ -189,6 +199,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
     // ---- transform warps ----
     const float lam1 = (float)(1.0 + wv.lm[b].lam);
     const float eps = prm.eps;
+    float gl = 0.f;  // g_L of tile row tid (diagonal tiles)
+    bool done = true;
     for (int i = 0; i < n; ++i) {
       const int r = i % kRawSlots, u = i / kRawSlots, o = i % kOpStages, uo = i / kOpStages;
       bool ok = tc::mbar_wait_until(&sm.raw_full[r], u & 1, deadline, err);
@@ -196,9 +208,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
       if (!ok) *err = 1;
       const RawSlot &R = sm.raw[r];
       float *sk = sm.sk[i & 1];
-      if (warp == 0) sk[lane] = lane < R.cnt ? rsqrtf(R.c[R.coff + lane] * lam1 + eps) : 0.f;
+      float *gs = sm.gs[i & 1];
+      if (warp == 0) {
+        const float sv = lane < R.cnt ? rsqrtf(R.c[R.coff + lane] * lam1 + eps) : 0.f;
+        sk[lane] = sv;
+        if (diag) gs[lane] = lane < R.cnt ? R.ga[R.coff + lane] * sv : 0.f;
+      }
       named_sync(1, 128);
-      if (*err) break;
+      if (*err) {
+        done = false;
+        break;
+      }
       const int n_eff = (i % kGroup == 0) ? ncols : min(ncols, ((R.s1 - col0 + 15) / 16) * 16);
       if (tid == 0) sm.op_ncols[o] = n_eff;
       OpStage &S = sm.op[o];
@@ -206,17 +226,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
       {
         const int gr = row0 + t;
         const bool v = gr >= R.xr0 && gr < R.xr1;
-        split_row(R.x + (size_t)(v ? gr - R.xr0 : 0) * kTcK, v, sk, t, S.xh, S.xl);
+        gl += split_row(R.x + (size_t)(v ? gr - R.xr0 : 0) * kTcK, v, sk, diag ? gs : nullptr, t, S.xh, S.xl);
       }
       if (!diag && t < n_eff) {
         const int gc = col0 + t;
         const bool v = gc >= R.yr0 && gc < R.yr1;
-        split_row(R.y + (size_t)(v ? gc - R.yr0 : 0) * kTcK, v, sk, t, S.yh, S.yl);
+        (void)split_row(R.y + (size_t)(v ? gc - R.yr0 : 0) * kTcK, v, sk, nullptr, t, S.yh, S.yl);
       }
       tc::fence_proxy_async();
       tc::mbar_arrive(&sm.op_full[o]);
       tc::mbar_arrive(&sm.raw_empty[r]);
     }
+    if (diag && done && row0 + tid < P && gl != 0.f)
+      red_add(reinterpret_cast<float *>(wv.gL) + pv.p_param_off[b] + row0 + tid, gl);
   } else if (warp == 8) {
     // ---- MMA issue ----
     if (lane == 0) {
@@ -310,32 +332,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
   if (warp == 8) tc::tmem_dealloc(tmem, 256);
 }
 
-// g_L(rows of the chunk) += sum_k slab[row][k] g_a,k / D_k   (one CTA per chunk)
-template <typename T>
-__global__ void k_schur_g(PlanView pv, WorkView wv, Params prm, int gate) {
-  __shared__ T dg[SPGO_CHUNK];
-  const int c = blockIdx.x;
-  const int b = pv.ch_prob[c];
-  if (!problem_active(wv.lm, b, gate)) return;
-  const int f0 = pv.ch_f0[c], nb = pv.ch_nb[c], lm0 = pv.ch_lm0[c], cnt = pv.ch_cnt[c];
-  const double lam1 = 1.0 + wv.lm[b].lam;
-  if (threadIdx.x < SPGO_CHUNK) {
-    const int k = threadIdx.x;
-    dg[k] = k < cnt ? (T)((double)reinterpret_cast<const T *>(wv.ga)[lm0 + k] /
-                          ((double)reinterpret_cast<const T *>(wv.C)[lm0 + k] * lam1 + (double)prm.eps))
-                    : T(0);
-  }
-  __syncthreads();
-  const T *slab = reinterpret_cast<const T *>(wv.slab) + pv.ch_slab[c];
-  T *gL = reinterpret_cast<T *>(wv.gL) + pv.p_param_off[b] + 6 * f0;
-  for (int row = threadIdx.x; row < 6 * nb; row += blockDim.x) {
-    T s = T(0);
-#pragma unroll 8
-    for (int k = 0; k < SPGO_CHUNK; ++k) s += slab[(size_t)row * SPGO_CHUNK + k] * dg[k];
-    if (s != T(0)) red_add(gL + row, s);
-  }
-}
-
 size_t tc_smem_bytes() { return sizeof(TcSmem) + 1024; }
 
 int launch_schur_tc(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream) {
@@ -344,10 +340,6 @@ int launch_schur_tc(const PlanView &pv, const WorkView &wv, const Params &prm, v
     const size_t sm = tc_smem_bytes();
     cudaFuncSetAttribute(k_schur_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_schur_tc<<<pv.n_tc_items, kTcThreads, sm, st>>>(pv, wv, prm, GATE_RUNNING);
-    ++g_launches;
-  }
-  if (pv.n_chunks > 0) {
-    k_schur_g<float><<<pv.n_chunks, 128, 0, st>>>(pv, wv, prm, GATE_RUNNING);
     ++g_launches;
   }
   return (int)cudaGetLastError();

@@ -403,16 +403,19 @@ int launch_reset(const PlanView &pv, const WorkView &wv, const Params &prm, doub
   return (int)cudaGetLastError();
 }
 
-// after a linearisation: the cost at the linearisation point becomes the current cost
+// after a linearisation: at the first one, the cost pass's value becomes the
+// current (and initial) cost; later linearisation points are accepted candidates
+// whose cost the candidate's cost pass already set
 __global__ void k_post_linearize(PlanView pv, WorkView wv) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= pv.B) return;
   LMState &s = wv.lm[b];
   if (s.status != 0 || !s.relin) return;
-  const double c = wv.cost_acc[b];
-  s.cost_lin = c;
-  s.cost = c;
-  if (s.iters == 0) s.cost0 = c;
+  if (s.iters == 0) {
+    s.cost = wv.cost_acc[b];
+    s.cost0 = s.cost;
+  }
+  s.cost_lin = s.cost;
   s.relin = 0;
   wv.cost_acc[b] = 0.0;
 }

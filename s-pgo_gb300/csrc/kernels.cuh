@@ -11,6 +11,7 @@ __device__ __forceinline__ bool problem_active(const LMState *lm, int b, int gat
   const LMState &s = lm[b];
   if (s.status != 0) return false;
   if (gate == GATE_RELIN) return s.relin != 0;
+  if (gate == GATE_FIRST) return s.relin != 0 && s.iters == 0;
   return true;
 }
 

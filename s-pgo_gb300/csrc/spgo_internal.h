@@ -23,8 +23,9 @@
 
 namespace spgo {
 
-// which problems a kernel works on: all, those needing a relinearisation, those still running
-enum Gate { GATE_ALL = 0, GATE_RELIN = 1, GATE_RUNNING = 2 };
+// which problems a kernel works on: all, those needing a relinearisation, those still
+// running, those about to be linearised for the first time since the reset
+enum Gate { GATE_ALL = 0, GATE_RELIN = 1, GATE_RUNNING = 2, GATE_FIRST = 3 };
 
 struct PlanView {                 // device pointers into the static buffer
   int32_t B, F, NP, L;
