@@ -119,10 +119,12 @@ constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [
 // the suffix (frames after the anchor) and prefix (frames before it) sums that
 // turn those rows into b_l(i), then B_l(i) = Ad_i^T b_l(i).
 // COST = true is the cost pass: residuals only, in double-float on the FP32 path
-// (FP64-accurate cost for the gain ratio).  The linearisation itself (COST =
-// false) forms residuals in plain T: they feed the gradient only, where FP32
-// rounding (~3e-5 px) is far below what moves the optimum; the cost at the
-// linearisation point always comes from a cost pass.
+// (FP64-accurate cost for the gain ratio), which it also stores as FP32 per
+// observation.  The linearisation (COST = false) always follows a cost pass at
+// the same state (the first one after a reset, or the accepted candidate's), so
+// on the FP32 path it reads those residuals instead of forming them from
+// pixel-sized FP32 quantities (whose ~3e-5 px rounding would move the optimum
+// by ~1e-5 m), and it takes the cost from that pass too.
 template <typename T, bool COST>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanView pv, WorkView wv, Params prm,
                                                    const double *__restrict__ alpha_state, int gate) {
@@ -203,6 +205,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
       const int slot = pv.obs_slot[o];
       const int n = pv.obs_frame[o];
       const float4 z = reinterpret_cast<const float4 *>(pv.obs_uv)[o];
+      float4 rstore = make_float4(0.f, 0.f, 0.f, 0.f);  // cost pass: residuals to keep
+      float4 rlast = make_float4(0.f, 0.f, 0.f, 0.f);   // linearisation (FP32): residuals kept
+      if constexpr (!COST && std::is_same<T, float>::value) rlast = reinterpret_cast<const float4 *>(wv.res)[o];
       const int a = sm.a[slot];
       const Vec3<T> X = v3<T>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
       const int fa = fo + a, fn = fo + n;
@@ -245,12 +250,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
           r0 = df_to_float(df_make(cam ? z.z : z.x) - pu);
           r1 = df_to_float(df_make(cam ? z.w : z.y) - pv_);
           t = v3<T>(tt[0].h, tt[1].h, tt[2].h);
+          if (cam) {
+            rstore.z = r0;
+            rstore.w = r1;
+          } else {
+            rstore.x = r0;
+            rstore.y = r1;
+          }
         } else {
           const Vec3<T> d = FramesT<T>::rel(wv, fa, 0, fn, cam);
           t = mulT(Rn, v3<T>(X.x + d.x, X.y + d.y, X.z + d.z));
-          const T izr = T(1) / t.z;
-          r0 = (T)(cam ? z.z : z.x) - (fx * t.x * izr + cxs[cam]);
-          r1 = (T)(cam ? z.w : z.y) - (fy * t.y * izr + cys[cam]);
+          if constexpr (!COST && std::is_same<T, float>::value) {
+            r0 = cam ? rlast.z : rlast.x;
+            r1 = cam ? rlast.w : rlast.y;
+          } else {
+            const T izr = T(1) / t.z;
+            r0 = (T)(cam ? z.z : z.x) - (fx * t.x * izr + cxs[cam]);
+            r1 = (T)(cam ? z.w : z.y) - (fy * t.y * izr + cys[cam]);
+          }
         }
         const T iz = T(1) / t.z;
         T rho;
@@ -286,6 +303,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
           q[5] += u0.z * sj0 + u1.z * sj1;
         }
       }
+      if constexpr (COST && std::is_same<T, float>::value) reinterpret_cast<float4 *>(wv.res)[o] = rstore;
       if (!COST) {
         atomicAdd(&sm.C[slot], accC);
         atomicAdd(&sm.ga[slot], accG);

@@ -81,6 +81,7 @@ struct WorkView {
   float *fr_cl;     // [F][2][3] float(c - float(c))
   double *poses_cand;   // [NP][12]
   double *alpha_cand;   // [L] (caller order)
+  float *res;           // [O][4] residuals of the last cost pass (FP32 path): u_l, v_l, u_r, v_r
   void *pair_acc;       // [total_pairs][27] T  (accumulated by the linearisation)
   void *pairF;          // [total_pairs][27] T  (prefix / suffix sums)
   void *A;              // [total_S] T      pose-pose blocks
