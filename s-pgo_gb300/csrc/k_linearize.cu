@@ -124,7 +124,8 @@ constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [
 // the same state (the first one after a reset, or the accepted candidate's), so
 // on the FP32 path it reads those residuals instead of forming them from
 // pixel-sized FP32 quantities (whose ~3e-5 px rounding would move the optimum
-// by ~1e-5 m), and it takes the cost from that pass too.
+// by ~1e-5 m), and it takes the cost from that pass too; only the camera-frame
+// point for the Jacobian is formed there (double-float, without the projection).
 template <typename T, bool COST>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanView pv, WorkView wv, Params prm,
                                                    const double *__restrict__ alpha_state, int gate) {
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
     const T *Ra = FramesT<T>::R(wv, fo + a, 0);
     const Vec3<T> ta = v3<T>((ua - cxs[0]) / fxs[0] / alpha, (va - cys[0]) / fys[0] / alpha, T(1) / alpha);
     Vec3<T> X = mul(Ra, ta);
-    if constexpr (COST && std::is_same<T, float>::value) {
+    if constexpr (std::is_same<T, float>::value) {
       // the same point as a double-float, for the residuals
       const df al = df_from_double(alpha_state[pv.lm_user[li]]);
       const df t3[3] = {df_sub(pv.lm_uv[2 * li], intr[2]) / df_make(intr[0]) / al,
@@ -257,13 +258,29 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
             rstore.x = r0;
             rstore.y = r1;
           }
+        } else if constexpr (std::is_same<T, float>::value) {
+          // the camera-frame point for the Jacobian: X + (c_a - c_n) and the
+          // rotation in double-float, rounded once (an FP32 rotation of the
+          // rounded point measured 1e-5 relative error in the Hessian blocks
+          // on a 45-pose circle scene; this keeps them at the 1e-7 level)
+          const float *ah = wv.fr_ch + (size_t)fa * 6, *al = wv.fr_cl + (size_t)fa * 6;
+          const float *nh = wv.fr_ch + (size_t)fn * 6 + cam * 3, *nl = wv.fr_cl + (size_t)fn * 6 + cam * 3;
+          const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
+          df Xc[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + (df_sub(ah[k], nh[k]) + df_make(al[k] - nl[k]));
+          df tt[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            tt[k] = df{Rn[k], Rl[k]} * Xc[0] + df{Rn[3 + k], Rl[3 + k]} * Xc[1] + df{Rn[6 + k], Rl[6 + k]} * Xc[2];
+          t = v3<T>(tt[0].h, tt[1].h, tt[2].h);
+          r0 = cam ? rlast.z : rlast.x;
+          r1 = cam ? rlast.w : rlast.y;
         } else {
           const Vec3<T> d = FramesT<T>::rel(wv, fa, 0, fn, cam);
           t = mulT(Rn, v3<T>(X.x + d.x, X.y + d.y, X.z + d.z));
-          if constexpr (!COST && std::is_same<T, float>::value) {
-            r0 = cam ? rlast.z : rlast.x;
-            r1 = cam ? rlast.w : rlast.y;
-          } else {
+          {
             const T izr = T(1) / t.z;
             r0 = (T)(cam ? z.z : z.x) - (fx * t.x * izr + cxs[cam]);
             r1 = (T)(cam ? z.w : z.y) - (fy * t.y * izr + cys[cam]);
