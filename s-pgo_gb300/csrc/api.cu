@@ -135,7 +135,8 @@ static void build_layout(spgo_plan *p) {
   p->w_gL = take((size_t)p->total_params * ts);
   // global factor storage only when a problem is too large for the shared-memory path
   const size_t P = (size_t)p->max_P;
-  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8 + 4) + 16 + P * ts + 16;
+  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8 + 4) + 16 + P * ts + 16 +
+                        9 * 2 * P * ts + 16;
   p->w_fac = take(packed <= 200 * 1024 ? 0 : (size_t)p->total_S * ts);
   p->w_delta = take((size_t)p->total_params * 8);
   p->w_C = take((size_t)(p->L + 64) * ts);  // + 64: the tensor-core Schur copies 16-byte aligned supersets

@@ -35,16 +35,19 @@ __device__ __forceinline__ T s_entry(const T *A, const T *SL, int P, int r, int 
 // factorises the 16x16 diagonal block, all threads solve the rows below it
 // (independent per row) and apply the rank-16 trailing update; three barriers
 // per block.  The substitutions are blocked the same way (two barriers per
-// block).  `refine` iterative-refinement steps form the residual g_S - S x in
-// FP64 from A and S_L.  Clears the S_L / g_L tiles it consumed.
+// block).  `refine` iterative-refinement steps form the residual g_S - S x
+// (double-float on the FP32 path, FP64 otherwise) from A and S_L in one
+// coalesced pass over the lower triangle.  Clears the S_L / g_L tiles it consumed.
 template <typename T>
-__device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *xs, T *dinv, T *tmp, const T *A,
-                                  T *SL, const T *g, T *gL, double lam, int P, int refine, int *fail_s) {
+__device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *xs, T *dinv, T *tmp, T *colacc,
+                                  const T *A, T *SL, const T *g, T *gL, double lam, int P, int refine,
+                                  int *fail_s) {
 #define ix(i, j) (cb[(j)] + (i))
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   const T lam_t = (T)lam;
-  for (int c = warp; c < P; c += nw)
-    for (int r = c + lane; r < P; r += 32) Lm[ix(r, c)] = s_entry(A, SL, P, r, c, lam_t);
+  // assembly: rows over warps, columns over lanes (coalesced reads of A and S_L)
+  for (int r = warp; r < P; r += nw)
+    for (int c = lane; c <= r; c += 32) Lm[ix(r, c)] = s_entry(A, SL, P, r, c, lam_t);
   for (int i = tid; i < P; i += nt) {
     y[i] = g[i] - gL[i];
     x[i] = 0.0;
@@ -189,6 +192,69 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
       }
       __syncthreads();
     }
+    if (colacc) {
+      // one coalesced pass over the lower triangle, row i per warp, column j per
+      // lane: S_ij x_j feeds row i's sum (warp reduction) and S_ij x_i feeds
+      // column j's sum, kept per warp in shared memory and added up at the end.
+      // Layout: colacc[w][2 P] (float path: h, l pairs; FP64 path: P doubles),
+      // then the row sums [2 P].
+      T *rowp = colacc + (size_t)nw * 2 * P;
+      for (int k = tid; k < (nw + 1) * 2 * P; k += nt) colacc[k] = T(0);
+      __syncthreads();
+      T *mine = colacc + (size_t)warp * 2 * P;
+      for (int i = warp; i < P; i += nw) {
+        const T *Ai = A + (size_t)i * P, *Si = SL + (size_t)i * P;
+        if constexpr (std::is_same<T, float>::value) {
+          const df xi{xs[2 * i], xs[2 * i + 1]};
+          df acc = df_make(0.f);
+          for (int j = lane; j <= i; j += 32) {
+            df sij = df_sub(Ai[j], Si[j]);
+            if (j == i) sij = sij + df_from_double(lam * (double)Ai[j]);
+            acc = acc + sij * df{xs[2 * j], xs[2 * j + 1]};
+            if (j < i) {
+              const df c = df{mine[2 * j], mine[2 * j + 1]} + sij * xi;
+              mine[2 * j] = c.h;
+              mine[2 * j + 1] = c.l;
+            }
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const df other{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
+            acc = acc + other;
+          }
+          if (lane == 0) {
+            rowp[2 * i] = acc.h;
+            rowp[2 * i + 1] = acc.l;
+          }
+        } else {
+          const double xi = x[i];
+          double acc = 0.0;
+          for (int j = lane; j <= i; j += 32) {
+            double sij = (double)Ai[j] - (double)Si[j];
+            if (j == i) sij += lam * (double)Ai[j];
+            acc += sij * x[j];
+            if (j < i) mine[j] += sij * xi;
+          }
+          acc = warp_sum(acc);
+          if (lane == 0) rowp[i] = acc;
+        }
+      }
+      __syncthreads();
+      for (int i = tid; i < P; i += nt) {
+        double sx;
+        if constexpr (std::is_same<T, float>::value) {
+          df t{rowp[2 * i], rowp[2 * i + 1]};
+          for (int w = 0; w < nw; ++w) t = t + df{colacc[(size_t)w * 2 * P + 2 * i], colacc[(size_t)w * 2 * P + 2 * i + 1]};
+          sx = (double)t.h + (double)t.l;
+        } else {
+          sx = rowp[i];
+          for (int w = 0; w < nw; ++w) sx += colacc[(size_t)w * 2 * P + i];
+        }
+        y[i] = (T)((double)g[i] - (double)gL[i] - sx);
+      }
+      __syncthreads();
+      continue;
+    }
     for (int i = warp; i < P; i += nw) {
       double r;
       if constexpr (std::is_same<T, float>::value) {
@@ -248,9 +314,10 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
     T *dinv = reinterpret_cast<T *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15) +
                                     (((size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 15) &
                                      ~(size_t)15));
+    T *colacc = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(dinv) + (((size_t)P * sizeof(T) + 15) & ~(size_t)15));
     for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P - (j * (j + 1)) / 2;
     __syncthreads();
-    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
+    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, colacc, A, SL, g, gL, lam, P, refine, &fail_s);
   } else {
     x = reinterpret_cast<double *>(smem_raw);
     y = reinterpret_cast<T *>(x + P);
@@ -261,7 +328,7 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
     for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P;
     __syncthreads();
     T *Lm = reinterpret_cast<T *>(wv.fac) + off;
-    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, A, SL, g, gL, lam, P, refine, &fail_s);
+    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, nullptr, A, SL, g, gL, lam, P, refine, &fail_s);
   }
   __syncthreads();
   const bool failed = fail_s != 0;
@@ -283,7 +350,8 @@ int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &pr
   const int P = pv.max_P;
   const size_t vec = (size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 16 +
                      (size_t)P * sizeof(T) + 16;
-  const size_t packed = (((size_t)P * (P + 1) / 2) * sizeof(T) + 15) / 16 * 16 + vec;
+  const size_t colacc = (size_t)(256 / 32 + 1) * 2 * P * sizeof(T);  // residual column sums (smem path)
+  const size_t packed = (((size_t)P * (P + 1) / 2) * sizeof(T) + 15) / 16 * 16 + vec + colacc + 16;
   const int use_smem = packed <= kSmemBudget;
   const size_t sm = use_smem ? packed : vec;
   const int refine = mixed ? prm.refine_steps : 0;
