@@ -147,7 +147,7 @@ static void build_layout(spgo_plan *p) {
   p->w_pred = take((size_t)p->B * 8);
   p->w_lmb = take((size_t)p->B * sizeof(LMState));
   p->w_probe = take((size_t)p->B * 32 * 8);
-  p->w_ctrl = take((size_t)SPGO_MLP_PARAMS * 2);
+  p->w_ctrl = take(mlp_deployed_bytes());
   p->ws_bytes = o;
 }
 
@@ -468,7 +468,7 @@ static void make_views(spgo_solver *s) {
   x.pred_acc = reinterpret_cast<double *>(w + p->w_pred);
   x.lm_backup = reinterpret_cast<LMState *>(w + p->w_lmb);
   x.probe_costs = reinterpret_cast<double *>(w + p->w_probe);
-  x.ctrl_bf16 = w + p->w_ctrl;
+  x.ctrl = w + p->w_ctrl;
 }
 
 // one linearisation + reduced system (+ damping from the device-side lambda)
@@ -485,7 +485,7 @@ static int enqueue_linearize(spgo_solver *s, cudaStream_t st, bool stats, bool c
     PROF(K_BOOKKEEP);
     if (stats || ctrl) CUDA_TRY(launch_lm_stats(s->pv, s->wv, std::is_same<T, double>::value, st));
     CUDA_TRY(launch_post_linearize(s->pv, s->wv, st));
-    if (ctrl) CUDA_TRY(launch_controller(s->pv, s->wv, s->wv.ctrl_bf16, st));
+    if (ctrl) CUDA_TRY(launch_controller(s->pv, s->wv, s->wv.ctrl, st));
   }
   return SPGO_OK;
 }
@@ -873,7 +873,7 @@ int spgo_lm_set_controller(spgo_solver *s, const float *d_params, void *stream) 
   if (!d_params) {
     s->controller = false;
   } else {
-    CUDA_TRY(launch_to_bf16(d_params, s->wv.ctrl_bf16, SPGO_MLP_PARAMS, stream));
+    CUDA_TRY(launch_mlp_deploy(d_params, s->wv.ctrl, stream));
     s->controller = true;
   }
   drop_graphs(s);

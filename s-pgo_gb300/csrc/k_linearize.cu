@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
 }
 
 int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, void *stream) {
-  k_chain<<<grid_for(pv.B, 4), 128, 0, (cudaStream_t)stream>>>(pv, wv, poses, gate);
+  k_chain<<<pv.B, 32, 0, (cudaStream_t)stream>>>(pv, wv, poses, gate);  // one warp (and SM slot) per problem
   ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -158,28 +158,39 @@ __global__ void k_mlp_adam(float *theta, const float *grad, float *m, float *v, 
   theta[i] -= lr * mh / (sqrtf(vh) + e);
 }
 
-__global__ void k_to_bf16(const float *src, __nv_bfloat16 *dst, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = __float2bfloat16(src[i]);
-}
+// the controller's inference weights: each parameter rounded to BF16, stored as
+// FP32 in the shared-memory layout below (weight matrices transposed)
+__device__ __forceinline__ float bf16r(float v) { return __bfloat162float(__float2bfloat16(v)); }
 
-// BF16-weight inference, one feature vector per warp: the CTA stages the BF16
-// weights in shared memory as FP32 with both weight matrices transposed (lanes
-// read consecutive hidden units), lanes split the hidden units, FP32 accumulation
+// BF16-weight inference, one feature vector per warp: lanes split the hidden
+// units, FP32 accumulation.  The weights live in shared memory as FP32 copies of
+// the BF16-rounded parameters, both matrices transposed so that lanes read
+// consecutive hidden units; spgo_lm_set_controller writes that layout once into
+// the workspace and every controller launch copies it in with 16-byte loads.
 struct MlpSmem {
   float w1t[kIn][kH], b1[kH], w2t[kH][kH], b2[kH], w3[kOut][kH], b3[kOut];
+  float pad[2];  // 16-byte multiple
 };
+static_assert(sizeof(MlpSmem) % 16 == 0, "float4 staging");
 
-__device__ void stage_mlp(const __nv_bfloat16 *__restrict__ Wb, MlpSmem &m) {
-  for (int i = threadIdx.x; i < kH * kIn; i += blockDim.x) m.w1t[i % kIn][i / kIn] = __bfloat162float(Wb[kW1 + i]);
-  for (int i = threadIdx.x; i < kH * kH; i += blockDim.x) m.w2t[i % kH][i / kH] = __bfloat162float(Wb[kW2 + i]);
-  for (int i = threadIdx.x; i < kH; i += blockDim.x) {
-    m.b1[i] = __bfloat162float(Wb[kB1 + i]);
-    m.b2[i] = __bfloat162float(Wb[kB2 + i]);
-    m.w3[0][i] = __bfloat162float(Wb[kW3 + i]);
-    m.w3[1][i] = __bfloat162float(Wb[kW3 + kH + i]);
+__global__ void k_mlp_deploy(const float *__restrict__ theta, MlpSmem *__restrict__ m) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kH * kIn) m->w1t[i % kIn][i / kIn] = bf16r(theta[kW1 + i]);
+  if (i < kH * kH) m->w2t[i % kH][i / kH] = bf16r(theta[kW2 + i]);
+  if (i < kH) {
+    m->b1[i] = bf16r(theta[kB1 + i]);
+    m->b2[i] = bf16r(theta[kB2 + i]);
+    m->w3[0][i] = bf16r(theta[kW3 + i]);
+    m->w3[1][i] = bf16r(theta[kW3 + kH + i]);
   }
-  if (threadIdx.x < kOut) m.b3[threadIdx.x] = __bfloat162float(Wb[kB3 + threadIdx.x]);
+  if (i < kOut) m->b3[i] = bf16r(theta[kB3 + i]);
+  if (i < 2) m->pad[i] = 0.f;
+}
+
+__device__ void stage_mlp(const MlpSmem *__restrict__ src, MlpSmem &m) {
+  const float4 *s4 = reinterpret_cast<const float4 *>(src);
+  float4 *d4 = reinterpret_cast<float4 *>(&m);
+  for (int i = threadIdx.x; i < (int)(sizeof(MlpSmem) / 16); i += blockDim.x) d4[i] = s4[i];
 }
 
 __device__ void mlp_infer_warp(const MlpSmem &m, const float *x, float &o0, float &o1) {
@@ -245,9 +256,9 @@ __device__ void lm_features(const PlanView &pv, const LMState &s, int b, float *
 // (it predicts that deviating from the schedule gives the lower cost).  After a
 // rejected step no relinearisation happens and the Nielsen increase stands: the
 // fallback whenever a step fails the gain-ratio test.
-__global__ void k_controller(PlanView pv, WorkView wv, const __nv_bfloat16 *Wb) {
+__global__ void k_controller(PlanView pv, WorkView wv, const MlpSmem *Wd) {
   __shared__ MlpSmem m;
-  stage_mlp(Wb, m);
+  stage_mlp(Wd, m);
   __syncthreads();
   const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (b >= pv.B) return;
@@ -329,9 +340,8 @@ int launch_lm_stats(const PlanView &pv, const WorkView &wv, int f64, void *strea
   return (int)cudaGetLastError();
 }
 
-int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wb, void *stream) {
-  k_controller<<<grid_for(pv.B, 8), 256, 0, (cudaStream_t)stream>>>(pv, wv,
-                                                                   reinterpret_cast<const __nv_bfloat16 *>(Wb));
+int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wd, void *stream) {
+  k_controller<<<grid_for(pv.B, 8), 256, 0, (cudaStream_t)stream>>>(pv, wv, reinterpret_cast<const MlpSmem *>(Wd));
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -342,11 +352,12 @@ int launch_features(const PlanView &pv, const WorkView &wv, float *feat, void *s
   return (int)cudaGetLastError();
 }
 
-int launch_to_bf16(const float *src, void *dst, int n, void *stream) {
-  k_to_bf16<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(src, reinterpret_cast<__nv_bfloat16 *>(dst), n);
+int launch_mlp_deploy(const float *theta, void *dst, void *stream) {
+  k_mlp_deploy<<<grid_for(kH * kH, 256), 256, 0, (cudaStream_t)stream>>>(theta, reinterpret_cast<MlpSmem *>(dst));
   ++g_launches;
   return (int)cudaGetLastError();
 }
+size_t mlp_deployed_bytes() { return sizeof(MlpSmem); }
 
 }  // namespace spgo
 

@@ -375,11 +375,27 @@ __global__ void k_backsub(PlanView pv, WorkView wv, Params prm, const double *al
   const int po = pv.p_param_off[b];
   const T *slab = reinterpret_cast<const T *>(wv.slab) + pv.ch_slab[c];
   double pred = 0.0;
+  // B_l^T delta over the chunk's rows: delta comes in 32 rows at a time (one
+  // coalesced load, then shuffles), four independent accumulators
+  const double *dl = wv.delta + po + 6 * f0;
+  const int rows = 6 * nb;
+  T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+  for (int rb = 0; rb < rows; rb += 32) {
+    const T dv = rb + slot < rows ? (T)dl[rb + slot] : T(0);
+    const T *sr = slab + (size_t)rb * SPGO_CHUNK + slot;
+    const int nr = min(32, rows - rb);
+    int k = 0;
+    for (; k + 4 <= nr; k += 4) {
+      s0 += sr[(size_t)k * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k);
+      s1 += sr[(size_t)(k + 1) * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k + 1);
+      s2 += sr[(size_t)(k + 2) * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k + 2);
+      s3 += sr[(size_t)(k + 3) * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k + 3);
+    }
+    for (; k < nr; ++k) s0 += sr[(size_t)k * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k);
+  }
   if (slot < cnt) {
     const int li = lm0 + slot;
-    const double *dl = wv.delta + po + 6 * f0;
-    T s = T(0);
-    for (int r = 0; r < 6 * nb; ++r) s += slab[(size_t)r * SPGO_CHUNK + slot] * (T)dl[r];
+    const T s = (s0 + s1) + (s2 + s3);
     const double C = (double)reinterpret_cast<const T *>(wv.C)[li];
     const double ga = (double)reinterpret_cast<const T *>(wv.ga)[li];
     const double lam = wv.lm[b].lam;

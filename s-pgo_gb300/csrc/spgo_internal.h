@@ -96,7 +96,7 @@ struct WorkView {
   LMState *lm;          // [B]
   LMState *lm_backup;   // [B] (lambda probes)
   double *probe_costs;  // [32][B]
-  void *ctrl_bf16;      // [SPGO_MLP_PARAMS] bf16 controller weights
+  void *ctrl;           // deployed controller weights (BF16-rounded, inference layout)
   double *cost_acc;     // [B]
   double *pred_acc;     // [B]
 };
@@ -138,7 +138,8 @@ int launch_export_B_n(const PlanView &pv, const WorkView &wv, int problem, int n
 int launch_lm_stats(const PlanView &pv, const WorkView &wv, int f64, void *stream);
 int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wb, void *stream);
 int launch_features(const PlanView &pv, const WorkView &wv, float *feat, void *stream);
-int launch_to_bf16(const float *src, void *dst, int n, void *stream);
+int launch_mlp_deploy(const float *theta, void *dst, void *stream);
+size_t mlp_deployed_bytes();
 int launch_scale_lambda(const PlanView &pv, const WorkView &wv, double factor, void *stream);
 int launch_take_probe(const PlanView &pv, const WorkView &wv, int j, void *stream);
 int launch_schur_tc(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
