@@ -159,6 +159,21 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
   p->B = nprob;
   int32_t frame_off = 0, pose_off = 0, lm_off = 0, param_off = 0;
   int64_t S_off = 0, pair_off = 0, slab_off = 0, obs_total = 0;
+  {  // the per-landmark and per-observation arrays are sized once
+    int64_t Lt = 0, Ot = 0;
+    for (int b = 0; b < nprob; ++b) {
+      Lt += std::max(0, probs[b].n_landmarks);
+      Ot += std::max<int64_t>(0, probs[b].n_obs);
+    }
+    p->obs_frame.resize((size_t)Ot);
+    p->obs_slot.resize((size_t)Ot);
+    p->obs_uv.resize((size_t)Ot * 4);
+    for (auto *v : {&p->lm_prob, &p->lm_host, &p->lm_lo, &p->lm_hi, &p->lm_user, &p->lm_chunk, &p->lm_slot})
+      v->reserve((size_t)Lt);
+    p->lm_uv.reserve((size_t)Lt * 2);
+    p->lm_obs.reserve((size_t)Lt + 1);
+  }
+  std::vector<int32_t> fcount;  // counting sort of a chunk's observations by frame
   for (int b = 0; b < nprob; ++b) {
     const spgo_host_problem &q = probs[b];
     const int N = q.n_poses, L = q.n_landmarks;
@@ -201,20 +216,33 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     });
     const int32_t ch_begin = (int32_t)p->ch_prob.size();
     int32_t cur = -1;
-    // observations of the open chunk: (frame, slot, source index), emitted sorted by frame
-    std::vector<std::array<int64_t, 3>> pend;
-    auto close_chunk = [&]() {
+    int k_open = 0;  // first landmark (position in `order`) of the open chunk
+    // emit the open chunk's observations sorted by frame (stable: landmark order
+    // inside a frame) with a counting sort over its frame window
+    auto close_chunk = [&](int k_end) {
       if (cur < 0) return;
       slab_off += (int64_t)6 * p->ch_nb[cur] * SPGO_CHUNK;
-      std::stable_sort(pend.begin(), pend.end(),
-                       [](const std::array<int64_t, 3> &x, const std::array<int64_t, 3> &y) { return x[0] < y[0]; });
-      for (const auto &e : pend) {
-        p->obs_frame.push_back((int32_t)e[0]);
-        p->obs_slot.push_back((uint8_t)e[1]);
-        for (int c = 0; c < 4; ++c) p->obs_uv.push_back(q.obs_uv[4 * e[2] + c]);
+      const int f0 = p->ch_f0[cur], nf = p->ch_nb[cur] + 1;
+      fcount.assign((size_t)nf + 1, 0);
+      int64_t n_chunk = 0;
+      for (int k = k_open; k < k_end; ++k) {
+        const int l = order[k];
+        for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) ++fcount[(size_t)(q.obs_frame[o] - f0) + 1];
+        n_chunk += q.obs_ptr[l + 1] - q.obs_ptr[l];
       }
-      obs_total += (int64_t)pend.size();
-      pend.clear();
+      for (int f = 0; f < nf; ++f) fcount[(size_t)f + 1] += fcount[(size_t)f];
+      for (int k = k_open; k < k_end; ++k) {
+        const int l = order[k];
+        const uint8_t slot = (uint8_t)(k - k_open);
+        for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) {
+          const int n = q.obs_frame[o];
+          const size_t dst = (size_t)(obs_total + fcount[(size_t)(n - f0)]++);
+          p->obs_frame[dst] = n;
+          p->obs_slot[dst] = slot;
+          std::memcpy(&p->obs_uv[4 * dst], q.obs_uv + 4 * o, 4 * sizeof(float));
+        }
+      }
+      obs_total += n_chunk;
     };
     for (int k = 0; k < L; ++k) {
       const int l = order[k];
@@ -225,7 +253,8 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
         if (nb_new > SPGO_MAX_WINDOW) fresh = true;
       }
       if (fresh) {
-        close_chunk();
+        close_chunk(k);
+        k_open = k;
         cur = (int32_t)p->ch_prob.size();
         p->ch_prob.push_back(b);
         p->ch_f0.push_back(std::min(lo[l], N - 1));
@@ -248,10 +277,8 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
       p->lm_uv.push_back(q.anchor_uv[2 * l]);
       p->lm_uv.push_back(q.anchor_uv[2 * l + 1]);
       p->lm_obs.push_back(obs_total);
-      for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o)
-        pend.push_back({(int64_t)q.obs_frame[o], (int64_t)(p->ch_cnt[cur] - 1), o});
     }
-    close_chunk();
+    close_chunk(L);
     const int32_t ch_end = (int32_t)p->ch_prob.size();
     for (int c = ch_begin; c < ch_end; ++c) {
       if (p->ch_f0[c] < 0 || p->ch_f0[c] + p->ch_nb[c] > N)
