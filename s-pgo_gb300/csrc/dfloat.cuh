@@ -70,6 +70,25 @@ __device__ __forceinline__ df operator/(const df &a, const df &b) {
   return fast_two_sum(q1, q2);
 }
 
+// sum_j (a_j + al_j)(b_j) for three double-float b_j and double-float
+// coefficients (ah, al): the three leading products exactly (two-product), their
+// sum with two error-free additions, all cross and low terms in one float.
+// ~31 FP32 operations instead of ~46 for three products and two additions.
+__device__ __forceinline__ df df_dot3(float a0h, float a0l, float a1h, float a1l, float a2h, float a2l,
+                                      const df &b0, const df &b1, const df &b2) {
+  const df p0 = two_prod(a0h, b0.h), p1 = two_prod(a1h, b1.h), p2 = two_prod(a2h, b2.h);
+  const df s01 = two_sum(p0.h, p1.h);
+  const df s = two_sum(s01.h, p2.h);
+  float lo = ((p0.l + p1.l) + (p2.l + s01.l)) + s.l;
+  lo = fmaf(a0h, b0.l, lo);
+  lo = fmaf(a1h, b1.l, lo);
+  lo = fmaf(a2h, b2.l, lo);
+  lo = fmaf(a0l, b0.h, lo);
+  lo = fmaf(a1l, b1.h, lo);
+  lo = fmaf(a2l, b2.h, lo);
+  return fast_two_sum(s.h, lo);
+}
+
 // a - b for plain floats, exactly, as a double-float
 __device__ __forceinline__ df df_sub(float a, float b) { return two_sum(a, -b); }
 

@@ -105,6 +105,7 @@ struct LinSmem {
   double cost[8];
   T pair[SPGO_MAX_WINDOW + 1][27];  // (host, target) pair terms of the chunk, by target - f0
   int key[8][32];                   // per warp: target frame of each lane's observation (-1: none)
+  float dch[SPGO_MAX_WINDOW + 1][2][3], dcl[SPGO_MAX_WINDOW + 1][2][3];  // FP32 path: c_host - c_(f0+f, cam)
 };
 constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [27][33]
 
@@ -177,6 +178,18 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
     sm.lo[tid] = pv.lm_lo[li];
     sm.hi[tid] = pv.lm_hi[li];
   }
+  if constexpr (std::is_same<T, float>::value) {
+    // the host's left centre minus every window frame's camera centres, as double-floats
+    const int fh = fo + pv.lm_host[lm0];
+    for (int idx = tid; idx < (nb + 1) * 6; idx += blockDim.x) {
+      const int f = idx / 6, cam = (idx / 3) & 1, k = idx % 3;
+      const size_t fn = (size_t)(fo + f0 + f);
+      df d = df_sub(wv.fr_ch[(size_t)fh * 6 + k], wv.fr_ch[fn * 6 + cam * 3 + k]);
+      d = d + df_make(wv.fr_cl[(size_t)fh * 6 + k] - wv.fr_cl[fn * 6 + cam * 3 + k]);
+      sm.dch[f][cam][k] = d.h;
+      sm.dcl[f][cam][k] = d.l;
+    }
+  }
   if (!COST) {
     for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_s[i] = T(0);
     for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) (&sm.pair[0][0])[i] = T(0);
@@ -234,22 +247,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
         Vec3<T> t;
         T r0, r1;
         if constexpr (COST && std::is_same<T, float>::value) {
-          // residual in double-float: X + (c_a - c_n), rotated, projected
-          const float *ah = wv.fr_ch + (size_t)fa * 6, *al = wv.fr_cl + (size_t)fa * 6;
-          const float *nh = wv.fr_ch + (size_t)fn * 6 + cam * 3, *nl = wv.fr_cl + (size_t)fn * 6 + cam * 3;
+          // residual in double-float: X + (c_a - c_n), rotated, then projected as
+          // r = ((z - c) t_z - f t_x) / t_z (the small numerator carries the
+          // precision, the division is plain FP32)
           const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
+          const int fw = n - f0;
           df Xc[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + (df_sub(ah[k], nh[k]) + df_make(al[k] - nl[k]));
+            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{sm.dch[fw][cam][k], sm.dcl[fw][cam][k]};
           df tt[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            tt[k] = df{Rn[k], Rl[k]} * Xc[0] + df{Rn[3 + k], Rl[3 + k]} * Xc[1] + df{Rn[6 + k], Rl[6 + k]} * Xc[2];
-          const df pu = (tt[0] / tt[2]) * fx + df_make(cxs[cam]);
-          const df pv_ = (tt[1] / tt[2]) * fy + df_make(cys[cam]);
-          r0 = df_to_float(df_make(cam ? z.z : z.x) - pu);
-          r1 = df_to_float(df_make(cam ? z.w : z.y) - pv_);
+            tt[k] = df_dot3(Rn[k], Rl[k], Rn[3 + k], Rl[3 + k], Rn[6 + k], Rl[6 + k], Xc[0], Xc[1], Xc[2]);
+          const df nu = df_sub(cam ? z.z : z.x, cxs[cam]) * tt[2] - tt[0] * fx;
+          const df nv = df_sub(cam ? z.w : z.y, cys[cam]) * tt[2] - tt[1] * fy;
+          const float itz = 1.f / tt[2].h;
+          r0 = (nu.h + nu.l) * itz;
+          r1 = (nv.h + nv.l) * itz;
           t = v3<T>(tt[0].h, tt[1].h, tt[2].h);
           if (cam) {
             rstore.z = r0;
@@ -263,17 +278,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
           // rotation in double-float, rounded once (an FP32 rotation of the
           // rounded point measured 1e-5 relative error in the Hessian blocks
           // on a 45-pose circle scene; this keeps them at the 1e-7 level)
-          const float *ah = wv.fr_ch + (size_t)fa * 6, *al = wv.fr_cl + (size_t)fa * 6;
-          const float *nh = wv.fr_ch + (size_t)fn * 6 + cam * 3, *nl = wv.fr_cl + (size_t)fn * 6 + cam * 3;
           const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
+          const int fw = n - f0;
           df Xc[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + (df_sub(ah[k], nh[k]) + df_make(al[k] - nl[k]));
+            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{sm.dch[fw][cam][k], sm.dcl[fw][cam][k]};
           df tt[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            tt[k] = df{Rn[k], Rl[k]} * Xc[0] + df{Rn[3 + k], Rl[3 + k]} * Xc[1] + df{Rn[6 + k], Rl[6 + k]} * Xc[2];
+            tt[k] = df_dot3(Rn[k], Rl[k], Rn[3 + k], Rl[3 + k], Rn[6 + k], Rl[6 + k], Xc[0], Xc[1], Xc[2]);
           t = v3<T>(tt[0].h, tt[1].h, tt[2].h);
           r0 = cam ? rlast.z : rlast.x;
           r1 = cam ? rlast.w : rlast.y;
