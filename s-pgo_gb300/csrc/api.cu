@@ -309,7 +309,7 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     // tensor-core Schur work list: 128 x 128 tiles of the lower triangle, <= 64 chunks each
     {
       const int P = 6 * N;
-      const int kTcSplit = 64;
+      const int kTcSplit = SPGO_TC_SPLIT;
       for (int row0 = 0; row0 < P; row0 += 128) {
         for (int col0 = 0; col0 <= row0; col0 += 128) {
           const int ncols = ((std::min(128, P - col0) + 15) / 16) * 16;
@@ -359,6 +359,20 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     pair_off += (int64_t)N * maxw;
   }
   p->lm_obs.push_back(obs_total);
+  {  // tensor-core Schur items longest first (one CTA per SM: the last wave stays short)
+    const size_t n = p->tc_prob.size();
+    std::vector<size_t> ord(n);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t x, size_t y) {
+      return p->tc_cend[x] - p->tc_cbeg[x] > p->tc_cend[y] - p->tc_cbeg[y];
+    });
+    auto perm = [&](std::vector<int32_t> &v) {
+      std::vector<int32_t> t(n);
+      for (size_t i = 0; i < n; ++i) t[i] = v[ord[i]];
+      v.swap(t);
+    };
+    perm(p->tc_prob); perm(p->tc_row0); perm(p->tc_col0); perm(p->tc_ncols); perm(p->tc_cbeg); perm(p->tc_cend);
+  }
   p->F = frame_off;
   p->NP = pose_off;
   p->L = lm_off;

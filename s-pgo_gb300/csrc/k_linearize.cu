@@ -103,11 +103,30 @@ struct LinSmem {
   T C[SPGO_CHUNK], ga[SPGO_CHUNK];
   int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
   double cost[8];
-  T pair[SPGO_MAX_WINDOW + 1][27];  // (host, target) pair terms of the chunk, by target - f0
   int key[8][32];                   // per warp: target frame of each lane's observation (-1: none)
-  float dch[SPGO_MAX_WINDOW + 1][2][3], dcl[SPGO_MAX_WINDOW + 1][2][3];  // FP32 path: c_host - c_(f0+f, cam)
 };
 constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [27][33]
+
+// Dynamic shared memory after LinSmem, sized by the batch's widest chunk window
+// (W = max_nb + 1 frames) and the CTA's warps:
+//   dc    [W][6] float x 2   FP32 path: c_host - c_(f0 + f, cam), hi and lo
+//   pair  [W][27] T          (host, target) pair terms of the chunk, by target - f0
+//   stage [warps][27][33] T  per-warp staging of the pair terms
+//   slab  [6 (W - 1)][32] T  the chunk's slab
+// (the cost pass uses dc only)
+template <typename T>
+struct LinLayout {
+  size_t dc, pair, stage, slab, total;
+  __host__ __device__ LinLayout(int max_nb, int warps, bool cost) {
+    const size_t W = (size_t)max_nb + 1;
+    auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    dc = up(sizeof(LinSmem<T>));
+    pair = dc + up(W * 12 * sizeof(float));
+    stage = pair + up(W * 27 * sizeof(T));
+    slab = stage + up((size_t)warps * 27 * kStagePitch * sizeof(T));
+    total = cost ? pair : slab + (size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(T);
+  }
+};
 
 // ---- fused linearisation / cost -----------------------------------------------
 // One CTA per chunk of <= 32 landmarks.  Phase A: per-landmark anchor point.
@@ -141,8 +160,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
   const T fxs[2] = {(T)intr[0], (T)intr[4]}, fys[2] = {(T)intr[1], (T)intr[5]};
   const T cxs[2] = {(T)intr[2], (T)intr[6]}, cys[2] = {(T)intr[3], (T)intr[7]};
   LinSmem<T> &sm = *reinterpret_cast<LinSmem<T> *>(smem_raw);
-  T *stage = reinterpret_cast<T *>(smem_raw + ((sizeof(LinSmem<T>) + 15) & ~(size_t)15));  // [8][27][33]
-  T *slab_s = stage + 8 * 27 * kStagePitch;                                                 // [6 nb][32]
+  const LinLayout<T> lay(pv.max_nb, blockDim.x >> 5, COST);
+  float *dch = reinterpret_cast<float *>(smem_raw + lay.dc);  // [W][6] hi, then [W][6] lo
+  float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
+  T(*pair)[27] = reinterpret_cast<T(*)[27]>(smem_raw + lay.pair);
+  T *stage = reinterpret_cast<T *>(smem_raw + lay.stage);
+  T *slab_s = reinterpret_cast<T *>(smem_raw + lay.slab);
   const int rows = 6 * nb;
 
   // phase A
@@ -186,13 +209,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
       const size_t fn = (size_t)(fo + f0 + f);
       df d = df_sub(wv.fr_ch[(size_t)fh * 6 + k], wv.fr_ch[fn * 6 + cam * 3 + k]);
       d = d + df_make(wv.fr_cl[(size_t)fh * 6 + k] - wv.fr_cl[fn * 6 + cam * 3 + k]);
-      sm.dch[f][cam][k] = d.h;
-      sm.dcl[f][cam][k] = d.l;
+      dch[idx] = d.h;
+      dcl[idx] = d.l;
     }
   }
   if (!COST) {
     for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_s[i] = T(0);
-    for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) (&sm.pair[0][0])[i] = T(0);
+    for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) (&pair[0][0])[i] = T(0);
   }
   __syncthreads();
 
@@ -255,7 +278,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
           df Xc[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{sm.dch[fw][cam][k], sm.dcl[fw][cam][k]};
+            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{dch[fw * 6 + cam * 3 + k], dcl[fw * 6 + cam * 3 + k]};
           df tt[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
@@ -283,7 +306,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
           df Xc[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{sm.dch[fw][cam][k], sm.dcl[fw][cam][k]};
+            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{dch[fw * 6 + cam * 3 + k], dcl[fw * 6 + cam * 3 + k]};
           df tt[3];
 #pragma unroll
           for (int k = 0; k < 3; ++k)
@@ -367,13 +390,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
         for (int i = 0; i < 32; ++i) {
           const int k = keys[i];
           if (k != cur) {
-            if (cur >= 0 && acc != T(0)) atomicAdd(&sm.pair[cur - f0][lane], acc);
+            if (cur >= 0 && acc != T(0)) atomicAdd(&pair[cur - f0][lane], acc);
             acc = T(0);
             cur = k;
           }
           acc += col[i];
         }
-        if (cur >= 0 && acc != T(0)) atomicAdd(&sm.pair[cur - f0][lane], acc);
+        if (cur >= 0 && acc != T(0)) atomicAdd(&pair[cur - f0][lane], acc);
       }
       __syncwarp();
     }
@@ -399,7 +422,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
     for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) {
       const int sl = i / 27, comp = i % 27;
       const int n = f0 + sl;
-      const T v = sm.pair[sl][comp];
+      const T v = pair[sl][comp];
       if (n == a || v == T(0)) continue;
       const int lo = min(a, n), hi = max(a, n);
       red_add(pair_acc + ((size_t)lo * D + (hi - lo - 1)) * 27 + comp, v);
@@ -461,11 +484,8 @@ int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, in
   return (int)cudaGetLastError();
 }
 
-template <typename T>
-static size_t lin_smem(int max_nb, bool cost) {
-  const size_t head = (sizeof(LinSmem<T>) + 15) & ~(size_t)15;
-  return cost ? head : head + ((size_t)8 * 27 * kStagePitch + (size_t)6 * max_nb * SPGO_CHUNK) * sizeof(T);
-}
+constexpr int kCostThreads = 64;   // cost pass: short CTAs, many per SM (latency-bound)
+constexpr int kLinThreads = 256;
 
 template <typename T>
 int launch_linearize(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
@@ -473,11 +493,12 @@ int launch_linearize(const PlanView &pv, const WorkView &wv, const Params &prm, 
   if (pv.n_chunks == 0) return 0;
   cudaStream_t st = (cudaStream_t)stream;
   if (cost_only) {
-    k_linearize<T, true><<<pv.n_chunks, 256, lin_smem<T>(pv.max_nb, true), st>>>(pv, wv, prm, alpha, gate);
+    const size_t sm = LinLayout<T>(pv.max_nb, kCostThreads / 32, true).total;
+    k_linearize<T, true><<<pv.n_chunks, kCostThreads, sm, st>>>(pv, wv, prm, alpha, gate);
   } else {
-    const size_t sm = lin_smem<T>(pv.max_nb, false);
+    const size_t sm = LinLayout<T>(pv.max_nb, kLinThreads / 32, false).total;
     cudaFuncSetAttribute(k_linearize<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_linearize<T, false><<<pv.n_chunks, 256, sm, st>>>(pv, wv, prm, alpha, gate);
+    k_linearize<T, false><<<pv.n_chunks, kLinThreads, sm, st>>>(pv, wv, prm, alpha, gate);
   }
   ++g_launches;
   return (int)cudaGetLastError();

@@ -46,7 +46,7 @@ constexpr int kRawSlots = 3;
 constexpr int kOpStages = 2;
 constexpr int kGroup = 4;           // chunks accumulated in TMEM between readbacks
 constexpr int kTcThreads = 320;     // 10 warps, roles above
-constexpr int kTcMaxChunks = 64;    // the planner's split
+constexpr int kTcMaxChunks = SPGO_TC_SPLIT;  // the planner's split
 constexpr uint64_t kTimeoutNs = 2000000000ull;
 
 struct OpStage {                    // 64 KB, 1024-byte aligned

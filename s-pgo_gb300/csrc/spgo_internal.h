@@ -20,6 +20,7 @@
 #define SPGO_CHUNK 32          // landmarks per chunk (slab columns)
 #define SPGO_TILE_BLOCKS 8     // pose blocks per Schur output tile (48 rows)
 #define SPGO_KSPLIT 16         // chunks per Schur work item
+#define SPGO_TC_SPLIT 64       // chunks per tensor-core Schur work item
 
 namespace spgo {
 
