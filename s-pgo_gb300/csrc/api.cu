@@ -77,7 +77,7 @@ struct spgo_plan {
   std::vector<Seg> segs;
   size_t static_bytes = 0, ws_bytes = 0;
   // workspace segment offsets
-  size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pgacc, w_pgF, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
+  size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl;
 };
 
@@ -127,8 +127,6 @@ static void build_layout(spgo_plan *p) {
   p->w_pcand = take((size_t)p->NP * 12 * 8);
   p->w_acand = take((size_t)p->L * 8);
   p->w_res = take((size_t)p->O * 16);
-  p->w_pgacc = take((size_t)p->total_pairs * 6 * 8);
-  p->w_pgF = take((size_t)p->total_pairs * 6 * 8);
   p->w_pacc = take((size_t)p->total_pairs * 27 * ts);
   p->w_pF = take((size_t)p->total_pairs * 27 * ts);
   p->w_A = take((size_t)p->total_S * ts);
@@ -496,8 +494,6 @@ static void make_views(spgo_solver *s) {
   x.alpha_cand = reinterpret_cast<double *>(w + p->w_acand);
   x.res = reinterpret_cast<float *>(w + p->w_res);
   x.pair_acc = w + p->w_pacc;
-  x.pg_acc = reinterpret_cast<double *>(w + p->w_pgacc);
-  x.pg_F = reinterpret_cast<double *>(w + p->w_pgF);
   x.pairF = w + p->w_pF;
   x.A = w + p->w_A;
   x.g = w + p->w_g;

@@ -110,20 +110,18 @@ constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [
 // Dynamic shared memory after LinSmem, sized by the batch's widest chunk window
 // (W = max_nb + 1 frames) and the CTA's warps:
 //   dc    [W][6] float x 2   FP32 path: c_host - c_(f0 + f, cam), hi and lo
-//   pm    [W][6] double      FP32 path: the pair terms' gradient parts, in FP64
 //   pair  [W][27] T          (host, target) pair terms of the chunk, by target - f0
 //   stage [warps][27][33] T  per-warp staging of the pair terms
 //   slab  [6 (W - 1)][32] T  the chunk's slab
 // (the cost pass uses dc only)
 template <typename T>
 struct LinLayout {
-  size_t dc, pm, pair, stage, slab, total;
+  size_t dc, pair, stage, slab, total;
   __host__ __device__ LinLayout(int max_nb, int warps, bool cost) {
     const size_t W = (size_t)max_nb + 1;
     auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
     dc = up(sizeof(LinSmem<T>));
-    pm = dc + up(W * 12 * sizeof(float));
-    pair = pm + up(W * 6 * sizeof(double));
+    pair = dc + up(W * 12 * sizeof(float));
     stage = pair + up(W * 27 * sizeof(T));
     slab = stage + up((size_t)warps * 27 * kStagePitch * sizeof(T));
     total = cost ? pair : slab + (size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(T);
@@ -166,8 +164,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
   float *dch = reinterpret_cast<float *>(smem_raw + lay.dc);  // [W][6] hi, then [W][6] lo
   float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
   T(*pair)[27] = reinterpret_cast<T(*)[27]>(smem_raw + lay.pair);
-  double(*pm)[6] = reinterpret_cast<double(*)[6]>(smem_raw + lay.pm);
-  constexpr bool kSplitG = std::is_same<T, float>::value;  // gradient parts kept in FP64
   T *stage = reinterpret_cast<T *>(smem_raw + lay.stage);
   T *slab_s = reinterpret_cast<T *>(smem_raw + lay.slab);
   const int rows = 6 * nb;
@@ -220,8 +216,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
   if (!COST) {
     for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_s[i] = T(0);
     for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) (&pair[0][0])[i] = T(0);
-    if (kSplitG)
-      for (int i = tid; i < (nb + 1) * 6; i += blockDim.x) (&pm[0][0])[i] = 0.0;
   }
   __syncthreads();
 
@@ -390,32 +384,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
       keys[lane] = key;
       __syncwarp();
       if (__any_sync(0xffffffffu, key >= 0) && lane < 27) {
-        // compensated (Kahan) run sums; the gradient parts (lanes 21..26) go to
-        // FP64 slots on the FP32 path
         const T *col = st + lane * kStagePitch;
-        T acc = T(0), cmp = T(0);
+        T acc = T(0);
         int cur = keys[0];
-        auto flush = [&]() {
-          if (cur < 0 || acc == T(0)) return;
-          if (kSplitG && lane >= 21)
-            atomicAdd(&pm[cur - f0][lane - 21], (double)acc - (double)cmp);
-          else
-            atomicAdd(&pair[cur - f0][lane], acc - cmp);
-        };
         for (int i = 0; i < 32; ++i) {
           const int k = keys[i];
           if (k != cur) {
-            flush();
+            if (cur >= 0 && acc != T(0)) atomicAdd(&pair[cur - f0][lane], acc);
             acc = T(0);
-            cmp = T(0);
             cur = k;
           }
-          const T y = col[i] - cmp;
-          const T t = acc + y;
-          cmp = (t - acc) - y;
-          acc = t;
+          acc += col[i];
         }
-        flush();
+        if (cur >= 0 && acc != T(0)) atomicAdd(&pair[cur - f0][lane], acc);
       }
       __syncwarp();
     }
@@ -441,16 +422,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
     for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) {
       const int sl = i / 27, comp = i % 27;
       const int n = f0 + sl;
-      if (n == a) continue;
+      const T v = pair[sl][comp];
+      if (n == a || v == T(0)) continue;
       const int lo = min(a, n), hi = max(a, n);
-      const size_t rec = (size_t)lo * D + (hi - lo - 1);
-      if (kSplitG && comp >= 21) {
-        const double v = pm[sl][comp - 21];
-        if (v != 0.0) red_add(wv.pg_acc + ((size_t)pv.p_pair_off[b] + rec) * 6 + (comp - 21), v);
-      } else {
-        const T v = pair[sl][comp];
-        if (v != T(0)) red_add(pair_acc + rec * 27 + comp, v);
-      }
+      red_add(pair_acc + ((size_t)lo * D + (hi - lo - 1)) * 27 + comp, v);
     }
   }
 

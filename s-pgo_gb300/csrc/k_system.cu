@@ -15,8 +15,6 @@
 #include "kernels.cuh"
 #include "frames.cuh"
 
-#include <type_traits>
-
 namespace spgo {
 
 __device__ __forceinline__ constexpr int t6(int i, int j) {  // symmetric 6x6 upper index, any order
@@ -243,62 +241,6 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
   }
 }
 
-// FP32 path: the gradient from the FP64 pair accumulators.  Pass 1, thread per
-// (problem, hi): Pg(i, hi) = sum_{lo <= i} m(lo, hi) re-centred to c_i (running
-// sum moved c_{i-1} -> c_i: m_w += (c_{i-1} - c_i) x m_v), stored at record
-// (i, hi); reads and clears the accumulators.  Pass 2, thread per (problem, i):
-// f(i) = sum_{hi > i} Pg(i, hi), g(i) = [R_i^T f_w ; R_i^T f_v].  All in FP64:
-// near convergence g is a small difference of terms with ~10 m lever arms.
-__global__ void k_pair_g_prefix(PlanView pv, WorkView wv) {
-  const int b = blockIdx.y;
-  if (!problem_active(wv.lm, b, GATE_RELIN)) return;
-  const int N = pv.p_npose[b], D = pv.p_pair_D[b];
-  const int hi = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (hi > N) return;
-  const int fo = pv.p_frame_off[b];
-  double *acc = wv.pg_acc + (size_t)pv.p_pair_off[b] * 6;
-  double *out = wv.pg_F + (size_t)pv.p_pair_off[b] * 6;
-  double m[6] = {0, 0, 0, 0, 0, 0};
-  const int lo0 = max(0, hi - D);
-  for (int lo = lo0; lo < hi; ++lo) {
-    if (lo > lo0) {
-      const double *cp = wv.fr_c + (size_t)(fo + lo - 1) * 6, *cc = wv.fr_c + (size_t)(fo + lo) * 6;
-      const double z0 = cp[0] - cc[0], z1 = cp[1] - cc[1], z2 = cp[2] - cc[2];
-      m[0] += z1 * m[5] - z2 * m[4];
-      m[1] += z2 * m[3] - z0 * m[5];
-      m[2] += z0 * m[4] - z1 * m[3];
-    }
-    const size_t rec = ((size_t)lo * D + (hi - lo - 1)) * 6;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      m[k] += acc[rec + k];
-      acc[rec + k] = 0.0;
-      out[rec + k] = m[k];
-    }
-  }
-}
-
-template <typename T>
-__global__ void k_pair_g_sum(PlanView pv, WorkView wv) {
-  const int b = blockIdx.y;
-  if (!problem_active(wv.lm, b, GATE_RELIN)) return;
-  const int N = pv.p_npose[b], D = pv.p_pair_D[b];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const double *F = wv.pg_F + ((size_t)pv.p_pair_off[b] + (size_t)i * D) * 6;
-  double f[6] = {0, 0, 0, 0, 0, 0};
-  for (int e = 0; e < min(D, N - i); ++e)
-#pragma unroll
-    for (int k = 0; k < 6; ++k) f[k] += F[(size_t)e * 6 + k];
-  const double *R = wv.fr_Rd + (size_t)(pv.p_frame_off[b] + i) * 18;
-  T *g = reinterpret_cast<T *>(wv.g) + pv.p_param_off[b] + 6 * i;
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    g[r] = (T)(R[r] * f[0] + R[3 + r] * f[1] + R[6 + r] * f[2]);
-    g[3 + r] = (T)(R[r] * f[3] + R[3 + r] * f[4] + R[6 + r] * f[5]);
-  }
-}
-
 template <typename T>
 int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream) {
   (void)gate;
@@ -309,11 +251,6 @@ int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream
   k_pair_suffix<T><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);
   k_pairs_to_A<T><<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
   g_launches += 3;
-  if (std::is_same<T, float>::value) {  // the gradient in FP64 (replaces k_pairs_to_A's FP32 g)
-    k_pair_g_prefix<<<dim3(grid_for(nmax, 64), pv.B), 64, 0, st>>>(pv, wv);
-    k_pair_g_sum<T><<<dim3(grid_for(nmax, 64), pv.B), 64, 0, st>>>(pv, wv);
-    g_launches += 2;
-  }
   return (int)cudaGetLastError();
 }
 

@@ -85,8 +85,6 @@ struct WorkView {
   float *res;           // [O][4] residuals of the last cost pass (FP32 path): u_l, v_l, u_r, v_r
   void *pair_acc;       // [total_pairs][27] T  (accumulated by the linearisation)
   void *pairF;          // [total_pairs][27] T  (prefix / suffix sums)
-  double *pg_acc;       // [total_pairs][6]  FP32 path: the gradient parts of the pair terms, in FP64
-  double *pg_F;         // [total_pairs][6]  FP32 path: their re-centred prefix sums over lo
   void *A;              // [total_S] T      pose-pose blocks
   void *g;              // [total_params] T pose gradient
   void *SL;             // [total_S] T      landmark Schur term (lower tiles)
