@@ -25,6 +25,10 @@ LOSSES = {
     "huber": (S.Loss(S.LOSS_HUBER, 2.0), dict(loss="huber", loss_scale=2.0, near_boost=False)),
 }
 TOL = {"fp64": 1e-9, "mixed": 1e-4}
+# State parity is checked at the optimum, not at a stopping point: near a minimum a
+# relative cost decrease of 1e-10 still allows ~1e-5 m of pose motion, so both
+# solvers continue until no step lowers the cost (or OPT_ITERS iterations).
+OPT_ITERS, OPT_TOL = 80, 1e-15
 
 
 def relmax(a, b):
@@ -100,8 +104,8 @@ def pose_errors(P, Q):
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_lm_solve_matches_oracle_config0(built_lib, cuda_device, prec):
-    """Config 0 (10 LM iterations, lambda0 = 1e-4) reaches the oracle's cost; run on to a
-    1e-10 stopping rule, the states agree to 1e-5 rad / 1e-5 m (a 1e-6 rule alone leaves
+    """Config 0 (10 LM iterations, lambda0 = 1e-4) reaches the oracle's cost; run on to
+    the optimum, the states agree to 1e-5 rad / 1e-5 m (a 1e-6 rule alone leaves
     about 1e-5 m of slack along flat directions)."""
     p = f32_obs(scenes.config0())
     ref = p.copy()
@@ -116,8 +120,8 @@ def test_lm_solve_matches_oracle_config0(built_lib, cuda_device, prec):
     if prec == "fp64":
         assert st["iterations"] == res.iterations and st["accepted"] == res.accepted
     ref2 = ref.copy()
-    S.lm_solve(ref2, S.Loss(), max_iters=30, tol=1e-10)
-    bs.set_params(max_iters=30, tol=1e-10)
+    S.lm_solve(ref2, S.Loss(), max_iters=OPT_ITERS, tol=OPT_TOL)
+    bs.set_params(max_iters=OPT_ITERS, tol=OPT_TOL)
     bs.solve()
     er, et = pose_errors(bs.get_poses(0), ref2.poses)
     assert er < 1e-5 and et < 1e-5
@@ -140,10 +144,10 @@ def test_batched_equals_individual(built_lib, cuda_device):
         # lowering the FP64 cost (stalled) instead of by the relative-decrease test
         assert sts[b]["status"] in (nat.STATUS_CONVERGED, nat.STATUS_STALLED)
         assert abs(sts[b]["cost"] - res.cost) / res.cost < 1e-6
-    bs.set_params(max_iters=40, tol=1e-10)
+    bs.set_params(max_iters=OPT_ITERS, tol=OPT_TOL)
     bs.solve()
     for b, ref in enumerate(refs):
-        S.lm_solve(ref, S.Loss(), max_iters=40, tol=1e-10)
+        S.lm_solve(ref, S.Loss(), max_iters=OPT_ITERS, tol=OPT_TOL)
         er, et = pose_errors(bs.get_poses(b), ref.poses)
         assert er < 1e-5 and et < 1e-5
 
@@ -156,8 +160,8 @@ def test_huber_outliers_converge(built_lib, cuda_device):
     bs.set_params(loss="huber", loss_scale=2.0, max_iters=30, tol=1e-6)
     st = bs.solve()[0]
     assert abs(st["cost"] - res.cost) / res.cost < 1e-6
-    S.lm_solve(ref, S.Loss(S.LOSS_HUBER, 2.0), max_iters=40, tol=1e-10)
-    bs.set_params(max_iters=40, tol=1e-10)
+    S.lm_solve(ref, S.Loss(S.LOSS_HUBER, 2.0), max_iters=OPT_ITERS, tol=OPT_TOL)
+    bs.set_params(max_iters=OPT_ITERS, tol=OPT_TOL)
     bs.solve()
     er, et = pose_errors(bs.get_poses(0), ref.poses)
     assert er < 1e-5 and et < 1e-5
