@@ -17,6 +17,7 @@ namespace spgo {
 // holds rows j..P-1; cb[j] = j P - j (j + 1) / 2) when it fits in shared memory,
 // else the full column-major matrix in global scratch (cb[j] = j P).
 constexpr int kPanel = 16;  // block width of the factorisation and the substitutions
+constexpr int kRowRegs = 8; // row entries per lane held in registers by the assembly and residual (P <= 256)
 
 // S(r, c) of the damped reduced system for r >= c, from A (pose blocks), S_L
 // (landmark Schur term, lower tiles) and lambda:  S = A + lam diag(A) - S_L
@@ -45,9 +46,28 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
 #define ix(i, j) (cb[(j)] + (i))
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   const T lam_t = (T)lam;
-  // assembly: rows over warps, columns over lanes (coalesced reads of A and S_L)
-  for (int r = warp; r < P; r += nw)
-    for (int c = lane; c <= r; c += 32) Lm[ix(r, c)] = s_entry(A, SL, P, r, c, lam_t);
+  // assembly: rows over warps, columns over lanes (coalesced reads of A and S_L);
+  // up to kRowRegs columns per lane are loaded before any is used
+  if (P <= 32 * kRowRegs) {
+    for (int r = warp; r < P; r += nw) {
+      const T *Ar = A + (size_t)r * P, *Sr = SL + (size_t)r * P;
+      T av[kRowRegs], sv[kRowRegs];
+#pragma unroll
+      for (int m = 0; m < kRowRegs; ++m) {
+        const int c = lane + 32 * m;
+        av[m] = c <= r ? Ar[c] : T(0);
+        sv[m] = c <= r ? Sr[c] : T(0);
+      }
+#pragma unroll
+      for (int m = 0; m < kRowRegs; ++m) {
+        const int c = lane + 32 * m;
+        if (c <= r) Lm[ix(r, c)] = av[m] - sv[m] + (c == r ? lam_t * av[m] : T(0));
+      }
+    }
+  } else {
+    for (int r = warp; r < P; r += nw)
+      for (int c = lane; c <= r; c += 32) Lm[ix(r, c)] = s_entry(A, SL, P, r, c, lam_t);
+  }
   for (int i = tid; i < P; i += nt) {
     y[i] = g[i] - gL[i];
     x[i] = 0.0;
@@ -69,7 +89,14 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
         const T dk = __shfl_sync(0xffffffffu, a[k], k);
         const T d = k < w ? dk : T(1);
         bad = bad || !(d > T(0)) || !isfinite((double)d);
-        const T lkk = sqrt(d), rinv = T(1) / lkk;
+        T lkk, rinv;
+        if constexpr (std::is_same<T, float>::value) {  // one MUFU op on the serial pivot chain
+          rinv = rsqrtf(d);
+          lkk = d * rinv;
+        } else {
+          lkk = sqrt(d);
+          rinv = T(1) / lkk;
+        }
         const T lik = lane > k ? a[k] * rinv : (lane == k ? lkk : a[k]);
         a[k] = lik;
 #pragma unroll
@@ -140,12 +167,21 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
     for (int kb = 0; kb < P; kb += kPanel) {
       const int ke = min(kb + kPanel, P), w = ke - kb;
       if (warp == 0) {
+        // lane = unknown; its row of the diagonal block and the pivots are loaded
+        // first, so the serial chain is multiply, shuffle, FMA per unknown
+        T lr[kPanel], di[kPanel];
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c) {
+          lr[c] = (lane < w && c < lane) ? Lm[ix(kb + lane, kb + c)] : T(0);
+          di[c] = c < w ? dinv[kb + c] : T(0);
+        }
         T v = lane < w ? y[kb + lane] : T(0);
-        for (int c = 0; c < w; ++c) {
-          T yc = v * dinv[kb + c];
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c) {
+          T yc = v * di[c];
           yc = __shfl_sync(0xffffffffu, yc, c);
           if (lane == c) v = yc;
-          if (lane > c && lane < w) v -= Lm[ix(kb + lane, kb + c)] * yc;
+          v -= lr[c] * yc;
         }
         if (lane < w) y[kb + lane] = v;
       }
@@ -168,12 +204,19 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
       }
       __syncthreads();
       if (warp == 0) {
+        T lc[kPanel], di[kPanel];  // column `lane` of the diagonal block, pivots
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c) {
+          lc[c] = (c < w && lane < c) ? Lm[ix(kb + c, kb + lane)] : T(0);
+          di[c] = c < w ? dinv[kb + c] : T(0);
+        }
         T v = lane < w ? y[kb + lane] - tmp[lane] : T(0);
-        for (int c = w - 1; c >= 0; --c) {
-          T xc = v * dinv[kb + c];
+#pragma unroll
+        for (int c = kPanel - 1; c >= 0; --c) {
+          T xc = v * di[c];
           xc = __shfl_sync(0xffffffffu, xc, c);
           if (lane == c) v = xc;
-          if (lane < c) v -= Lm[ix(kb + c, kb + lane)] * xc;
+          v -= lc[c] * xc;
         }
         if (lane < w) y[kb + lane] = v;
       }
@@ -207,15 +250,30 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
         if constexpr (std::is_same<T, float>::value) {
           const df xi{xs[2 * i], xs[2 * i + 1]};
           df acc = df_make(0.f);
-          for (int j = lane; j <= i; j += 32) {
-            df sij = df_sub(Ai[j], Si[j]);
-            if (j == i) sij = sij + df_from_double(lam * (double)Ai[j]);
+          auto term = [&](int j, float a, float sl) {
+            df sij = df_sub(a, sl);
+            if (j == i) sij = sij + df_from_double(lam * (double)a);
             acc = acc + sij * df{xs[2 * j], xs[2 * j + 1]};
             if (j < i) {
               const df c = df{mine[2 * j], mine[2 * j + 1]} + sij * xi;
               mine[2 * j] = c.h;
               mine[2 * j + 1] = c.l;
             }
+          };
+          if (P <= 32 * kRowRegs) {
+            // the row's entries are loaded before use (up to kRowRegs per lane)
+            float av[kRowRegs], sv[kRowRegs];
+#pragma unroll
+            for (int m = 0; m < kRowRegs; ++m) {
+              const int j = lane + 32 * m;
+              av[m] = j <= i ? Ai[j] : 0.f;
+              sv[m] = j <= i ? Si[j] : 0.f;
+            }
+#pragma unroll
+            for (int m = 0; m < kRowRegs; ++m)
+              if (lane + 32 * m <= i) term(lane + 32 * m, av[m], sv[m]);
+          } else {
+            for (int j = lane; j <= i; j += 32) term(j, Ai[j], Si[j]);
           }
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) {
