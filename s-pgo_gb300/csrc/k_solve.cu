@@ -89,14 +89,7 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
         const T dk = __shfl_sync(0xffffffffu, a[k], k);
         const T d = k < w ? dk : T(1);
         bad = bad || !(d > T(0)) || !isfinite((double)d);
-        T lkk, rinv;
-        if constexpr (std::is_same<T, float>::value) {  // one MUFU op on the serial pivot chain
-          rinv = rsqrtf(d);
-          lkk = d * rinv;
-        } else {
-          lkk = sqrt(d);
-          rinv = T(1) / lkk;
-        }
+        const T lkk = sqrt(d), rinv = T(1) / lkk;  // correctly rounded: the refinement step relies on it
         const T lik = lane > k ? a[k] * rinv : (lane == k ? lkk : a[k]);
         a[k] = lik;
 #pragma unroll
