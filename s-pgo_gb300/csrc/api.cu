@@ -57,6 +57,8 @@ struct spgo_plan {
   int32_t B = 0, F = 0, NP = 0, L = 0;
   int64_t O = 0;
   int32_t max_P = 0, max_D = 1, max_nb = 1, total_params = 0;
+  int32_t max_P_small = 0;                 // widest problem of the batched factorisation
+  std::vector<int32_t> large;              // problems factored by k_chol_large.cu
   int64_t total_S = 0, total_pairs = 0, total_slab = 0;
   std::vector<int32_t> p_npose, p_frame_off, p_pose_off, p_lm_off, p_lm_cnt, p_pair_D, p_param_off, p_chunk_off,
       p_chunk_cnt, fr_prob, pose_prob;
@@ -77,6 +79,7 @@ struct spgo_plan {
   std::vector<Seg> segs;
   size_t static_bytes = 0, ws_bytes = 0;
   // workspace segment offsets
+  size_t w_Sx = 0, w_lg = 0;
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl;
 };
@@ -133,11 +136,11 @@ static void build_layout(spgo_plan *p) {
   p->w_g = take((size_t)p->total_params * ts);
   p->w_SL = take((size_t)p->total_S * ts);
   p->w_gL = take((size_t)p->total_params * ts);
-  // global factor storage only when a problem is too large for the shared-memory path
-  const size_t P = (size_t)p->max_P;
-  const size_t packed = ((P * (P + 1) / 2) * ts + 15) / 16 * 16 + P * (8 + ts + 8 + 4) + 16 + P * ts + 16 +
-                        9 * 2 * P * ts + 16;
-  p->w_fac = take(packed <= 200 * 1024 ? 0 : (size_t)p->total_S * ts);
+  // factor storage, exact S and vectors of the multi-CTA factorisation, when any problem needs it
+  const bool any_large = !p->large.empty();
+  p->w_fac = take(any_large ? (size_t)p->total_S * ts : 0);
+  p->w_Sx = take(any_large ? (size_t)p->total_S * 8 : 0);
+  p->w_lg = take(any_large ? (size_t)p->total_params * 8 * 6 : 0);
   p->w_delta = take((size_t)p->total_params * 8);
   p->w_C = take((size_t)(p->L + 64) * ts);  // + 64: the tensor-core Schur copies 16-byte aligned supersets
   p->w_ga = take((size_t)(p->L + 64) * ts);  // + 64: as C
@@ -381,6 +384,16 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
   p->total_S = S_off;
   p->total_pairs = pair_off;
   p->total_slab = slab_off;
+  {  // factorisation route per problem: batched in shared memory, or the multi-CTA path
+    const size_t ts = precision == SPGO_PREC_FP64 ? 8 : 4;
+    for (int b = 0; b < nprob; ++b) {
+      const int P = 6 * p->p_npose[b];
+      if (factor_packed_bytes(P, ts) <= SPGO_FACTOR_SMEM)
+        p->max_P_small = std::max(p->max_P_small, P);
+      else
+        p->large.push_back(b);
+    }
+  }
   build_layout(p);
   return SPGO_OK;
 }
@@ -482,6 +495,7 @@ static void make_views(spgo_solver *s) {
   v.tc_cbeg = seg_ptr<int32_t>(p, st, i++); v.tc_cend = seg_ptr<int32_t>(p, st, i++);
   v.tc_chunks = seg_ptr<int32_t>(p, st, i++);
   v.n_tc_items = (int32_t)p->tc_prob.size();
+  v.max_P_small = p->max_P_small;
   unsigned char *w = s->d_ws;
   WorkView &x = s->wv;
   x.fr_Rf = reinterpret_cast<float *>(w + p->w_frRf);
@@ -500,6 +514,16 @@ static void make_views(spgo_solver *s) {
   x.SL = w + p->w_SL;
   x.gL = w + p->w_gL;
   x.fac = w + p->w_fac;
+  if (!p->large.empty()) {
+    x.Sx = w + p->w_Sx;
+    double *lg = reinterpret_cast<double *>(w + p->w_lg);
+    const size_t tp = (size_t)p->total_params;
+    x.lg_g0 = lg;
+    x.lg_x = lg + tp;
+    x.lg_xs = reinterpret_cast<float *>(lg + 2 * tp);  // 2 tp floats
+    x.lg_y = lg + 3 * tp;
+    x.lg_dinv = lg + 4 * tp;
+  }
   x.delta = reinterpret_cast<double *>(w + p->w_delta);
   x.C = w + p->w_C;
   x.ga = w + p->w_ga;
@@ -541,7 +565,12 @@ static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
     PROF(K_SCHUR);
     CUDA_TRY(launch_schur<T>(s->pv, s->wv, s->prm, st));
   }
-  { PROF(K_FACTOR); CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st)); }
+  {
+    PROF(K_FACTOR);
+    CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st));
+    for (const int b : s->plan->large)
+      CUDA_TRY(launch_factor_large<T>(s->pv, s->wv, b, 6 * s->plan->p_npose[b], mixed ? s->prm.refine_steps : 0, st));
+  }
   return SPGO_OK;
 }
 

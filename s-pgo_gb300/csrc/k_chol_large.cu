@@ -1,0 +1,357 @@
+// Large reduced camera systems: problems whose packed factor does not fit in one
+// CTA's shared memory (P beyond ~300 in FP32; config 1's 600 and config 2's 3000).
+//
+// Same mathematics as k_factor_solve (S = A + lam diag(A) - S_L, Cholesky, one
+// refinement step with an exact residual), spread over the GPU instead of one CTA:
+//   k_lg_assemble  row per CTA: the FP32/T copy of S into the factor storage
+//                  (column-major, lower), the exact S (double-float / FP64,
+//                  full, row-major) for the residual, g0 = g - g_L; clears S_L, g_L
+//   per 64-column panel kb:
+//     k_lg_potrf   one CTA factors the 64x64 diagonal block in shared memory
+//     k_lg_trsm    thread per row below it: L(i, kb:) = S(i, kb:) L_kk^-T
+//     k_lg_syrk    one CTA per 64x64 tile of the trailing lower triangle,
+//                  C -= L_i L_j^T from shared-memory tiles, 4x4 outputs per thread
+//   k_lg_solve     one 512-thread CTA: blocked forward / backward substitution
+//                  (32-unknown shuffle chains inside each 64-block, parallel
+//                  row and column updates), x += solution
+//   k_lg_resid     warp per row: g0 - S x from the exact S (between two solves)
+// Replaces, for such problems, the reference's libtorch Cholesky of the dense
+// reduced system (src/Optimization/linear_solvers.cu:195-218).
+#include "kernels.cuh"
+#include "dfloat.cuh"
+
+#include <type_traits>
+
+namespace spgo {
+
+constexpr int kLgNB = 64;
+
+template <typename T> struct ExactS;
+template <> struct ExactS<float> { using type = float2; };  // (hi, lo) double-float
+template <> struct ExactS<double> { using type = double; };
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lg_assemble(PlanView pv, WorkView wv, int b) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  const int P = 6 * pv.p_npose[b], r = blockIdx.x;
+  if (r >= P) return;
+  const size_t off = pv.p_S_off[b];
+  const T *A = reinterpret_cast<const T *>(wv.A) + off;
+  T *SL = reinterpret_cast<T *>(wv.SL) + off;
+  T *fac = reinterpret_cast<T *>(wv.fac) + off;
+  auto *Sx = reinterpret_cast<typename ExactS<T>::type *>(wv.Sx) + off;
+  const double lam = wv.lm[b].lam;
+  // S_L may hold entries up to the end of the row's 48-wide SIMT tile (both Schur paths clear here)
+  constexpr int TR = 6 * SPGO_TILE_BLOCKS;
+  const int cmax = min(P, (r / TR + 1) * TR);
+  for (int c = threadIdx.x; c < cmax; c += blockDim.x) {
+    if (c <= r) {
+      const T a = A[(size_t)r * P + c], sl = SL[(size_t)r * P + c];
+      T v = a - sl;
+      if (c == r) v += (T)lam * a;
+      fac[(size_t)c * P + r] = v;
+      if constexpr (std::is_same<T, float>::value) {
+        df e = df_sub(a, sl);
+        if (c == r) e = e + df_from_double(lam * (double)a);
+        Sx[(size_t)r * P + c] = make_float2(e.h, e.l);
+        if (c < r) Sx[(size_t)c * P + r] = make_float2(e.h, e.l);
+      } else {
+        const double e = (double)a - (double)sl + (c == r ? lam * (double)a : 0.0);
+        Sx[(size_t)r * P + c] = e;
+        if (c < r) Sx[(size_t)c * P + r] = e;
+      }
+    }
+    SL[(size_t)r * P + c] = T(0);
+  }
+  if (threadIdx.x == 0) {
+    const int po = pv.p_param_off[b];
+    T *gL = reinterpret_cast<T *>(wv.gL) + po;
+    wv.lg_g0[po + r] = (double)reinterpret_cast<const T *>(wv.g)[po + r] - (double)gL[r];
+    gL[r] = T(0);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lg_potrf(PlanView pv, WorkView wv, int b, int kb) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  __shared__ T D[kLgNB][kLgNB + 1];
+  __shared__ T rinv_s;
+  __shared__ int bad;
+  const int P = 6 * pv.p_npose[b], nb = min(kLgNB, P - kb), tid = threadIdx.x;
+  T *fac = reinterpret_cast<T *>(wv.fac) + pv.p_S_off[b];
+  T *dinv = reinterpret_cast<T *>(wv.lg_dinv) + pv.p_param_off[b];
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int i = idx % nb, j = idx / nb;
+    if (i >= j) D[i][j] = fac[(size_t)(kb + j) * P + kb + i];
+  }
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (tid == 0) {
+      const T d = D[k][k];
+      if (!(d > T(0)) || !isfinite((double)d)) bad = 1;
+      const T lkk = sqrt(d);
+      D[k][k] = lkk;
+      rinv_s = T(1) / lkk;
+      dinv[kb + k] = rinv_s;
+    }
+    __syncthreads();
+    for (int i = k + 1 + tid; i < nb; i += blockDim.x) D[i][k] *= rinv_s;
+    __syncthreads();
+    const int m = nb - k - 1;
+    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+      const int ii = k + 1 + idx % m, jj = k + 1 + idx / m;
+      if (ii >= jj) D[ii][jj] -= D[ii][k] * D[jj][k];
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && bad) wv.lm[b].fail = 1;
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int i = idx % nb, j = idx / nb;
+    if (i >= j) fac[(size_t)(kb + j) * P + kb + i] = D[i][j];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_lg_trsm(PlanView pv, WorkView wv, int b, int kb) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  __shared__ T D[kLgNB][kLgNB + 1];
+  __shared__ T di[kLgNB];
+  const int P = 6 * pv.p_npose[b], nb = min(kLgNB, P - kb), ke = kb + nb, tid = threadIdx.x;
+  const T *fac_c = reinterpret_cast<const T *>(wv.fac) + pv.p_S_off[b];
+  T *fac = reinterpret_cast<T *>(wv.fac) + pv.p_S_off[b];
+  const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + pv.p_param_off[b];
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int i = idx % nb, j = idx / nb;
+    D[i][j] = i > j ? fac_c[(size_t)(kb + j) * P + kb + i] : T(0);
+  }
+  for (int j = tid; j < nb; j += blockDim.x) di[j] = dinv[kb + j];
+  __syncthreads();
+  const int i = ke + blockIdx.x * blockDim.x + tid;
+  if (i >= P) return;
+  T x[kLgNB];
+#pragma unroll
+  for (int j = 0; j < kLgNB; ++j) x[j] = j < nb ? fac_c[(size_t)(kb + j) * P + i] : T(0);
+#pragma unroll
+  for (int j = 0; j < kLgNB; ++j) {
+    T v = x[j];
+#pragma unroll
+    for (int m = 0; m < j; ++m) v -= x[m] * D[j][m];
+    x[j] = j < nb ? v * di[j] : T(0);
+  }
+#pragma unroll
+  for (int j = 0; j < kLgNB; ++j)
+    if (j < nb) fac[(size_t)(kb + j) * P + i] = x[j];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lg_syrk(PlanView pv, WorkView wv, int b, int kb) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  __shared__ T LR[kLgNB][kLgNB + 1];
+  __shared__ T LC[kLgNB][kLgNB + 1];
+  const int P = 6 * pv.p_npose[b], nb = min(kLgNB, P - kb), ke = kb + nb, tid = threadIdx.x;
+  // tile t -> (ti >= tj) of the trailing lower triangle
+  const int t = blockIdx.x;
+  int ti = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+  while (ti * (ti + 1) / 2 > t) --ti;
+  const int tj = t - ti * (ti + 1) / 2;
+  const int R0 = ke + kLgNB * ti, C0 = ke + kLgNB * tj;
+  T *fac = reinterpret_cast<T *>(wv.fac) + pv.p_S_off[b];
+  for (int idx = tid; idx < nb * kLgNB; idx += blockDim.x) {
+    const int r = idx % kLgNB, k = idx / kLgNB;
+    LR[k][r] = R0 + r < P ? fac[(size_t)(kb + k) * P + R0 + r] : T(0);
+    LC[k][r] = C0 + r < P ? fac[(size_t)(kb + k) * P + C0 + r] : T(0);
+  }
+  __syncthreads();
+  const int tx = tid % 16, ty = tid / 16;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  for (int k = 0; k < nb; ++k) {
+    T a[4], c[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      a[i] = LR[k][tx + 16 * i];
+      c[i] = LC[k][ty + 16 * i];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * c[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = R0 + tx + 16 * i, c = C0 + ty + 16 * j;
+      if (r < P && c < P && r >= c) fac[(size_t)c * P + r] -= acc[i][j];
+    }
+}
+
+// Blocked substitutions with the factor in global memory, one 512-thread CTA.
+// first: start from g0 (x = 0); else from the residual in lg_y.  last: write
+// delta (zero if the factorisation failed); else keep x and its double-float
+// split for the residual.
+template <typename T>
+__global__ void __launch_bounds__(512) k_lg_solve(PlanView pv, WorkView wv, int b, int first, int last) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ T tmp[kLgNB];
+  const int P = 6 * pv.p_npose[b], po = pv.p_param_off[b];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
+  T *y = reinterpret_cast<T *>(smem_raw);
+  const T *L = reinterpret_cast<const T *>(wv.fac) + pv.p_S_off[b];
+  const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + po;
+  T *ly = reinterpret_cast<T *>(wv.lg_y) + po;
+  for (int i = tid; i < P; i += blockDim.x) y[i] = first ? (T)wv.lg_g0[po + i] : ly[i];
+  __syncthreads();
+  auto Lat = [&](int i, int j) { return L[(size_t)j * P + i]; };  // L(i, j), i >= j
+  // forward L z = y
+  for (int kb = 0; kb < P; kb += kLgNB) {
+    const int nb = min(kLgNB, P - kb), ke = kb + nb;
+    if (warp == 0) {
+      for (int h = 0; h < nb; h += 32) {
+        const int w = min(32, nb - h), u = kb + h + lane;  // lane = unknown u
+        T v = lane < w ? y[u] : T(0);
+        if (h > 0 && lane < w)  // the first half's unknowns are final
+          for (int c = 0; c < h; ++c) v -= Lat(u, kb + c) * y[kb + c];
+        T lr[32], di[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          lr[c] = (lane < w && c < lane) ? Lat(u, kb + h + c) : T(0);
+          di[c] = c < w ? dinv[kb + h + c] : T(0);
+        }
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          T yc = v * di[c];
+          yc = __shfl_sync(0xffffffffu, yc, c);
+          if (lane == c) v = yc;
+          v -= lr[c] * yc;
+        }
+        if (lane < w) y[u] = v;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    for (int i = ke + tid; i < P; i += blockDim.x) {
+      T v = y[i];
+      for (int c = 0; c < nb; ++c) v -= Lat(i, kb + c) * y[kb + c];
+      y[i] = v;
+    }
+    __syncthreads();
+  }
+  // backward L^T w = z, blocks from the bottom
+  for (int kb = ((P - 1) / kLgNB) * kLgNB; kb >= 0; kb -= kLgNB) {
+    const int nb = min(kLgNB, P - kb), ke = kb + nb;
+    for (int c = warp; c < nb; c += nw) {
+      T acc = T(0);
+      for (int i = ke + lane; i < P; i += 32) acc += Lat(i, kb + c) * y[i];
+      acc = warp_sum(acc);
+      if (lane == 0) tmp[c] = acc;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int h = ((nb - 1) / 32) * 32; h >= 0; h -= 32) {
+        const int w = min(32, nb - h), u = kb + h + lane;
+        T v = lane < w ? y[u] - tmp[h + lane] : T(0);
+        if (lane < w)  // the later half's unknowns are final
+          for (int m = h + w; m < nb; ++m) v -= Lat(kb + m, u) * y[kb + m];
+        T lc[32], di[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) {
+          lc[c] = (c < w && lane < c) ? Lat(kb + h + c, u) : T(0);
+          di[c] = c < w ? dinv[kb + h + c] : T(0);
+        }
+#pragma unroll
+        for (int c = 31; c >= 0; --c) {
+          T xc = v * di[c];
+          xc = __shfl_sync(0xffffffffu, xc, c);
+          if (lane == c) v = xc;
+          v -= lc[c] * xc;
+        }
+        if (lane < w) y[u] = v;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+  const bool failed = wv.lm[b].fail != 0;
+  for (int i = tid; i < P; i += blockDim.x) {
+    const double xi = (first ? 0.0 : wv.lg_x[po + i]) + (double)y[i];
+    if (last) {
+      wv.delta[po + i] = failed ? 0.0 : xi;
+    } else {
+      wv.lg_x[po + i] = xi;
+      const df s = df_from_double(xi);
+      wv.lg_xs[2 * (po + i)] = s.h;
+      wv.lg_xs[2 * (po + i) + 1] = s.l;
+    }
+  }
+}
+
+// residual y = g0 - S x from the exact S, warp per row
+template <typename T>
+__global__ void __launch_bounds__(256) k_lg_resid(PlanView pv, WorkView wv, int b) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  const int P = 6 * pv.p_npose[b], po = pv.p_param_off[b];
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= P) return;
+  const auto *Sx = reinterpret_cast<const typename ExactS<T>::type *>(wv.Sx) + pv.p_S_off[b] + (size_t)i * P;
+  double r;
+  if constexpr (std::is_same<T, float>::value) {
+    const float *xs = wv.lg_xs + 2 * (size_t)po;
+    df acc = df_make(0.f);
+    for (int j = lane; j < P; j += 32) {
+      const float2 s = Sx[j];
+      acc = acc + df{s.x, s.y} * df{xs[2 * j], xs[2 * j + 1]};
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const df other{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
+      acc = acc + other;
+    }
+    r = (double)acc.h + (double)acc.l;
+  } else {
+    double acc = 0.0;
+    for (int j = lane; j < P; j += 32) acc += Sx[j] * wv.lg_x[po + j];
+    r = warp_sum(acc);
+  }
+  if (lane == 0) reinterpret_cast<T *>(wv.lg_y)[po + i] = (T)(wv.lg_g0[po + i] - r);
+}
+
+template <typename T>
+int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int refine, void *stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  k_lg_assemble<T><<<P, 256, 0, st>>>(pv, wv, b);
+  int n = 1;
+  for (int kb = 0; kb < P; kb += kLgNB) {
+    const int ke = min(P, kb + kLgNB);
+    k_lg_potrf<T><<<1, 256, 0, st>>>(pv, wv, b, kb);
+    ++n;
+    if (ke < P) {
+      const int M = P - ke, nt = (M + kLgNB - 1) / kLgNB;
+      k_lg_trsm<T><<<(M + 127) / 128, 128, 0, st>>>(pv, wv, b, kb);
+      k_lg_syrk<T><<<nt * (nt + 1) / 2, 256, 0, st>>>(pv, wv, b, kb);
+      n += 2;
+    }
+  }
+  const size_t sm = (size_t)P * sizeof(T);
+  cudaFuncSetAttribute(k_lg_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_lg_solve<T><<<1, 512, sm, st>>>(pv, wv, b, 1, refine == 0);
+  ++n;
+  for (int it = 0; it < refine; ++it) {
+    k_lg_resid<T><<<(P + 7) / 8, 256, 0, st>>>(pv, wv, b);
+    k_lg_solve<T><<<1, 512, sm, st>>>(pv, wv, b, 0, it == refine - 1);
+    n += 2;
+  }
+  g_launches += n;
+  return (int)cudaGetLastError();
+}
+
+template int launch_factor_large<float>(const PlanView &, const WorkView &, int, int, int, void *);
+template int launch_factor_large<double>(const PlanView &, const WorkView &, int, int, int, void *);
+
+}  // namespace spgo

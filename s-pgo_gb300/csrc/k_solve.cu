@@ -228,109 +228,79 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
       }
       __syncthreads();
     }
-    if (colacc) {
-      // one coalesced pass over the lower triangle, row i per warp, column j per
-      // lane: S_ij x_j feeds row i's sum (warp reduction) and S_ij x_i feeds
-      // column j's sum, kept per warp in shared memory and added up at the end.
-      // Layout: colacc[w][2 P] (float path: h, l pairs; FP64 path: P doubles),
-      // then the row sums [2 P].
-      T *rowp = colacc + (size_t)nw * 2 * P;
-      for (int k = tid; k < (nw + 1) * 2 * P; k += nt) colacc[k] = T(0);
-      __syncthreads();
-      T *mine = colacc + (size_t)warp * 2 * P;
-      for (int i = warp; i < P; i += nw) {
-        const T *Ai = A + (size_t)i * P, *Si = SL + (size_t)i * P;
-        if constexpr (std::is_same<T, float>::value) {
-          const df xi{xs[2 * i], xs[2 * i + 1]};
-          df acc = df_make(0.f);
-          auto term = [&](int j, float a, float sl) {
-            df sij = df_sub(a, sl);
-            if (j == i) sij = sij + df_from_double(lam * (double)a);
-            acc = acc + sij * df{xs[2 * j], xs[2 * j + 1]};
-            if (j < i) {
-              const df c = df{mine[2 * j], mine[2 * j + 1]} + sij * xi;
-              mine[2 * j] = c.h;
-              mine[2 * j + 1] = c.l;
-            }
-          };
-          if (P <= 32 * kRowRegs) {
-            // the row's entries are loaded before use (up to kRowRegs per lane)
-            float av[kRowRegs], sv[kRowRegs];
-#pragma unroll
-            for (int m = 0; m < kRowRegs; ++m) {
-              const int j = lane + 32 * m;
-              av[m] = j <= i ? Ai[j] : 0.f;
-              sv[m] = j <= i ? Si[j] : 0.f;
-            }
-#pragma unroll
-            for (int m = 0; m < kRowRegs; ++m)
-              if (lane + 32 * m <= i) term(lane + 32 * m, av[m], sv[m]);
-          } else {
-            for (int j = lane; j <= i; j += 32) term(j, Ai[j], Si[j]);
-          }
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            const df other{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
-            acc = acc + other;
-          }
-          if (lane == 0) {
-            rowp[2 * i] = acc.h;
-            rowp[2 * i + 1] = acc.l;
-          }
-        } else {
-          const double xi = x[i];
-          double acc = 0.0;
-          for (int j = lane; j <= i; j += 32) {
-            double sij = (double)Ai[j] - (double)Si[j];
-            if (j == i) sij += lam * (double)Ai[j];
-            acc += sij * x[j];
-            if (j < i) mine[j] += sij * xi;
-          }
-          acc = warp_sum(acc);
-          if (lane == 0) rowp[i] = acc;
-        }
-      }
-      __syncthreads();
-      for (int i = tid; i < P; i += nt) {
-        double sx;
-        if constexpr (std::is_same<T, float>::value) {
-          df t{rowp[2 * i], rowp[2 * i + 1]};
-          for (int w = 0; w < nw; ++w) t = t + df{colacc[(size_t)w * 2 * P + 2 * i], colacc[(size_t)w * 2 * P + 2 * i + 1]};
-          sx = (double)t.h + (double)t.l;
-        } else {
-          sx = rowp[i];
-          for (int w = 0; w < nw; ++w) sx += colacc[(size_t)w * 2 * P + i];
-        }
-        y[i] = (T)((double)g[i] - (double)gL[i] - sx);
-      }
-      __syncthreads();
-      continue;
-    }
+    // one coalesced pass over the lower triangle, row i per warp, column j per
+    // lane: S_ij x_j feeds row i's sum (warp reduction) and S_ij x_i feeds
+    // column j's sum, kept per warp in shared memory and added up at the end.
+    // Layout: colacc[w][2 P] (float path: h, l pairs; FP64 path: P doubles),
+    // then the row sums [2 P].
+    T *rowp = colacc + (size_t)nw * 2 * P;
+    for (int k = tid; k < (nw + 1) * 2 * P; k += nt) colacc[k] = T(0);
+    __syncthreads();
+    T *mine = colacc + (size_t)warp * 2 * P;
     for (int i = warp; i < P; i += nw) {
-      double r;
+      const T *Ai = A + (size_t)i * P, *Si = SL + (size_t)i * P;
       if constexpr (std::is_same<T, float>::value) {
+        const df xi{xs[2 * i], xs[2 * i + 1]};
         df acc = df_make(0.f);
-        for (int j = lane; j < P; j += 32) {
-          const size_t k = i >= j ? (size_t)i * P + j : (size_t)j * P + i;
-          const df sij = df_sub(A[k], SL[k]) + (i == j ? df_from_double(lam * (double)A[k]) : df_make(0.f));
+        auto term = [&](int j, float a, float sl) {
+          df sij = df_sub(a, sl);
+          if (j == i) sij = sij + df_from_double(lam * (double)a);
           acc = acc + sij * df{xs[2 * j], xs[2 * j + 1]};
+          if (j < i) {
+            const df c = df{mine[2 * j], mine[2 * j + 1]} + sij * xi;
+            mine[2 * j] = c.h;
+            mine[2 * j + 1] = c.l;
+          }
+        };
+        if (P <= 32 * kRowRegs) {
+          // the row's entries are loaded before use (up to kRowRegs per lane)
+          float av[kRowRegs], sv[kRowRegs];
+#pragma unroll
+          for (int m = 0; m < kRowRegs; ++m) {
+            const int j = lane + 32 * m;
+            av[m] = j <= i ? Ai[j] : 0.f;
+            sv[m] = j <= i ? Si[j] : 0.f;
+          }
+#pragma unroll
+          for (int m = 0; m < kRowRegs; ++m)
+            if (lane + 32 * m <= i) term(lane + 32 * m, av[m], sv[m]);
+        } else {
+          for (int j = lane; j <= i; j += 32) term(j, Ai[j], Si[j]);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
           const df other{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
           acc = acc + other;
         }
-        r = (double)g[i] - (double)gL[i] - ((double)acc.h + (double)acc.l);
+        if (lane == 0) {
+          rowp[2 * i] = acc.h;
+          rowp[2 * i + 1] = acc.l;
+        }
       } else {
+        const double xi = x[i];
         double acc = 0.0;
-        for (int j = lane; j < P; j += 32) {
-          const double sij = i >= j ? s_entry(A, SL, P, i, j, lam_t) : s_entry(A, SL, P, j, i, lam_t);
+        for (int j = lane; j <= i; j += 32) {
+          double sij = (double)Ai[j] - (double)Si[j];
+          if (j == i) sij += lam * (double)Ai[j];
           acc += sij * x[j];
+          if (j < i) mine[j] += sij * xi;
         }
         acc = warp_sum(acc);
-        r = (double)g[i] - (double)gL[i] - acc;
+        if (lane == 0) rowp[i] = acc;
       }
-      if (lane == 0) y[i] = (T)r;
+    }
+    __syncthreads();
+    for (int i = tid; i < P; i += nt) {
+      double sx;
+      if constexpr (std::is_same<T, float>::value) {
+        df t{rowp[2 * i], rowp[2 * i + 1]};
+        for (int w = 0; w < nw; ++w) t = t + df{colacc[(size_t)w * 2 * P + 2 * i], colacc[(size_t)w * 2 * P + 2 * i + 1]};
+        sx = (double)t.h + (double)t.l;
+      } else {
+        sx = rowp[i];
+        for (int w = 0; w < nw; ++w) sx += colacc[(size_t)w * 2 * P + i];
+      }
+      y[i] = (T)((double)g[i] - (double)gL[i] - sx);
     }
     __syncthreads();
   }
@@ -339,13 +309,14 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
 #undef ix
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, int refine, int use_smem) {
+__global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, int refine) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int fail_s;
   __shared__ T tmp_s[kPanel];
   const int b = blockIdx.x;
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   const int N = pv.p_npose[b], P = 6 * N;
+  if (P > pv.max_P_small) return;  // a large system: k_chol_large.cu
   const size_t off = pv.p_S_off[b];
   const int po = pv.p_param_off[b];
   const T *A = reinterpret_cast<const T *>(wv.A) + off;
@@ -355,32 +326,19 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
   const double lam = wv.lm[b].lam;
   double *x;
   T *y;
-  if (use_smem) {
-    const size_t npk = (size_t)P * (P + 1) / 2;
-    T *Lm = reinterpret_cast<T *>(smem_raw);
-    x = reinterpret_cast<double *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15));
-    y = reinterpret_cast<T *>(x + P);
-    float *xs = reinterpret_cast<float *>(y + P);
-    int *cb = reinterpret_cast<int *>(xs + 2 * P);
-    T *dinv = reinterpret_cast<T *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15) +
-                                    (((size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 15) &
-                                     ~(size_t)15));
-    T *colacc = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(dinv) + (((size_t)P * sizeof(T) + 15) & ~(size_t)15));
-    for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P - (j * (j + 1)) / 2;
-    __syncthreads();
-    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, colacc, A, SL, g, gL, lam, P, refine, &fail_s);
-  } else {
-    x = reinterpret_cast<double *>(smem_raw);
-    y = reinterpret_cast<T *>(x + P);
-    float *xs = reinterpret_cast<float *>(y + P);
-    int *cb = reinterpret_cast<int *>(xs + 2 * P);
-    T *dinv = reinterpret_cast<T *>(smem_raw + (((size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) +
-                                                              sizeof(int)) + 15) & ~(size_t)15));
-    for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P;
-    __syncthreads();
-    T *Lm = reinterpret_cast<T *>(wv.fac) + off;
-    factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, nullptr, A, SL, g, gL, lam, P, refine, &fail_s);
-  }
+  const size_t npk = (size_t)P * (P + 1) / 2;
+  T *Lm = reinterpret_cast<T *>(smem_raw);
+  x = reinterpret_cast<double *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15));
+  y = reinterpret_cast<T *>(x + P);
+  float *xs = reinterpret_cast<float *>(y + P);
+  int *cb = reinterpret_cast<int *>(xs + 2 * P);
+  T *dinv = reinterpret_cast<T *>(smem_raw + ((npk * sizeof(T) + 15) & ~(size_t)15) +
+                                  (((size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 15) &
+                                   ~(size_t)15));
+  T *colacc = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(dinv) + (((size_t)P * sizeof(T) + 15) & ~(size_t)15));
+  for (int j = threadIdx.x; j < P; j += blockDim.x) cb[j] = j * P - (j * (j + 1)) / 2;
+  __syncthreads();
+  factor_solve_body<T>(Lm, cb, y, x, xs, dinv, tmp_s, colacc, A, SL, g, gL, lam, P, refine, &fail_s);
   __syncthreads();
   const bool failed = fail_s != 0;
   for (int i = threadIdx.x; i < P; i += blockDim.x) wv.delta[po + i] = failed ? 0.0 : x[i];
@@ -394,20 +352,21 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
   for (int i = threadIdx.x; i < P; i += blockDim.x) gL[i] = T(0);
 }
 
-static const size_t kSmemBudget = 200 * 1024;
+// dynamic shared memory of k_factor_solve for a P-wide problem: the packed factor,
+// the vectors, the pivots and the residual's column sums
+size_t factor_packed_bytes(int P, size_t ts) {
+  const size_t vec = (size_t)P * (sizeof(double) + ts + 2 * sizeof(float) + sizeof(int)) + 16 + (size_t)P * ts + 16;
+  const size_t colacc = (size_t)(256 / 32 + 1) * 2 * P * ts;
+  return (((size_t)P * (P + 1) / 2) * ts + 15) / 16 * 16 + vec + colacc + 16;
+}
 
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed, void *stream) {
-  const int P = pv.max_P;
-  const size_t vec = (size_t)P * (sizeof(double) + sizeof(T) + 2 * sizeof(float) + sizeof(int)) + 16 +
-                     (size_t)P * sizeof(T) + 16;
-  const size_t colacc = (size_t)(256 / 32 + 1) * 2 * P * sizeof(T);  // residual column sums (smem path)
-  const size_t packed = (((size_t)P * (P + 1) / 2) * sizeof(T) + 15) / 16 * 16 + vec + colacc + 16;
-  const int use_smem = packed <= kSmemBudget;
-  const size_t sm = use_smem ? packed : vec;
+  if (pv.max_P_small <= 0) return 0;
+  const size_t sm = factor_packed_bytes(pv.max_P_small, sizeof(T));
   const int refine = mixed ? prm.refine_steps : 0;
   cudaFuncSetAttribute(k_factor_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_factor_solve<T><<<pv.B, 256, sm, (cudaStream_t)stream>>>(pv, wv, refine, use_smem);
+  k_factor_solve<T><<<pv.B, 256, sm, (cudaStream_t)stream>>>(pv, wv, refine);
   ++g_launches;
   return (int)cudaGetLastError();
 }

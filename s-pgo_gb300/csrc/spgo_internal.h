@@ -21,6 +21,7 @@
 #define SPGO_TILE_BLOCKS 8     // pose blocks per Schur output tile (48 rows)
 #define SPGO_KSPLIT 16         // chunks per Schur work item
 #define SPGO_TC_SPLIT 64       // chunks per tensor-core Schur work item
+#define SPGO_FACTOR_SMEM (200 * 1024)  // shared-memory budget of the batched factorisation
 
 namespace spgo {
 
@@ -60,6 +61,7 @@ struct PlanView {                 // device pointers into the static buffer
   // tensor-core Schur work items
   const int32_t *tc_prob, *tc_row0, *tc_col0, *tc_ncols, *tc_cbeg, *tc_cend, *tc_chunks;
   int32_t n_tc_items;
+  int32_t max_P_small;    // widest problem the batched (shared-memory) factorisation takes
 };
 
 struct LMState {
@@ -98,6 +100,11 @@ struct WorkView {
   LMState *lm_backup;   // [B] (lambda probes)
   double *probe_costs;  // [32][B]
   void *ctrl;           // deployed controller weights (BF16-rounded, inference layout)
+  // large reduced systems (k_chol_large.cu), allocated when the batch has any
+  void *Sx;             // [total_S] exact S: (hi, lo) float pairs on the FP32 path, doubles on FP64
+  double *lg_g0, *lg_x; // [total_params] g - g_L; the solution so far
+  float *lg_xs;         // [2 total_params] its double-float split
+  void *lg_y, *lg_dinv; // [total_params] T: right-hand side / residual; 1 / L_kk
   double *cost_acc;     // [B]
   double *pred_acc;     // [B]
 };
@@ -119,6 +126,9 @@ template <typename T>
 int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream);
 template <typename T>
 int launch_schur(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
+size_t factor_packed_bytes(int P, size_t ts);  // shared memory of the batched factorisation
+template <typename T>
+int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int refine, void *stream);
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed,
                         void *stream);

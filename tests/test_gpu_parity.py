@@ -291,3 +291,27 @@ def test_graph_replay_matches_direct_launches(built_lib, cuda_device):
     # the run-to-run spread of the solver, not bit for bit
     assert np.allclose(out[0][0], out[1][0], rtol=1e-6, atol=0)
     assert np.abs(out[0][2] - out[1][2]).max() < 1e-4
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 2e-4)])
+def test_large_system_path_matches_oracle(built_lib, cuda_device, prec, tol):
+    """A 54-pose window (P = 324: the packed factor exceeds one CTA's shared memory)
+    goes through the multi-CTA factorisation; batched with a small problem, both
+    match the oracle's GN step, and an LM solve reaches the oracle's cost."""
+    big = f32_obs(scenes.corridor_scene(61, 54, 500))
+    small = f32_obs(scenes.circle_scene(62, 7, 90))
+    refs = [q.copy() for q in (big, small)]
+    for r in refs:
+        S.reference_gn_step(r, iterations=2, step_size=1.0)
+    bs = BatchSolver([big, small], precision=prec)
+    bs.set_params(loss="cauchy", loss_scale=3.0, near_boost=True, eps=1e-4)
+    bs.gn_step(2, 1.0)
+    for b, r in enumerate(refs):
+        assert np.abs(bs.get_poses(b) - r.poses).max() < tol
+        assert relmax(bs.get_alpha(b), r.alpha) < tol
+    bs.close()
+    bs = BatchSolver([big], precision=prec)
+    bs.set_params(loss="l2", max_iters=8, tol=1e-9)
+    st = bs.solve()[0]
+    res = S.lm_solve(big.copy(), S.Loss(), max_iters=8, tol=1e-9)
+    assert abs(st["cost"] - res.cost) / res.cost < 1e-6
