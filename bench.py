@@ -362,8 +362,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         s2 = make("mixed")
         s2.solve(check_every=args.check_every)
-        poses = [s2.get_poses(b) for b in range(len(probs))]
-        alphas = [s2.get_alpha(b) for b in range(len(probs))]
+        poses, alphas = s2.get_state()
         torch.cuda.synchronize(dev)
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
         h2d = int(s2.sizes.static_bytes + 8 * (12 * s2.sizes.total_poses + s2.sizes.total_landmarks))

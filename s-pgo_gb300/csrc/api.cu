@@ -15,6 +15,8 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <thread>
+#include <atomic>
 #include <type_traits>
 #include <stdexcept>
 #include <string>
@@ -154,29 +156,182 @@ static void build_layout(spgo_plan *p) {
   p->ws_bytes = o;
 }
 
+// One problem's share of the plan.  Landmark and observation records go straight
+// into the plan's pre-sized arrays at the problem's offsets (lm_chunk holds the
+// problem-local chunk index until the merge); chunk and work lists are local.
+struct ProbPlan {
+  int code = SPGO_OK;
+  std::string err;
+  int32_t maxw = 1, max_nb = 1;
+  int64_t slab = 0;  // slab elements of the problem
+  std::vector<int32_t> ch_f0, ch_nb, ch_lm0, ch_cnt;
+  std::vector<int64_t> ch_slab;  // problem-local slab offsets
+  std::vector<int32_t> wk_ti, wk_tj, wk_cbeg, wk_cend, wk_chunks;
+  std::vector<int32_t> tc_row0, tc_col0, tc_ncols, tc_cbeg, tc_cend, tc_chunks;
+};
+
+static void plan_problem(const spgo_host_problem &q, int b, int64_t lm_base, int64_t obs_base, spgo_plan *p,
+                         ProbPlan &o) {
+  auto bad = [&](const std::string &m) {
+    o.code = SPGO_ERR_INVALID_ARG;
+    o.err = m;
+  };
+  const int N = q.n_poses, L = q.n_landmarks;
+  // per-landmark window [lo, hi) of pose blocks
+  std::vector<int32_t> lo(L), hi(L);
+  for (int l = 0; l < L; ++l) {
+    const int a = q.host[l];
+    if (a < 0 || a > N) return bad("landmark " + std::to_string(l) + ": host out of range");
+    if (q.obs_ptr[l + 1] < q.obs_ptr[l]) return bad("obs_ptr decreasing");
+    int32_t mn = a, mx = a, prev = -1;
+    for (int64_t ob = q.obs_ptr[l]; ob < q.obs_ptr[l + 1]; ++ob) {
+      const int n = q.obs_frame[ob];
+      if (n < 0 || n > N) return bad("observation frame out of range");
+      if (n <= prev) return bad("frames must ascend strictly inside a landmark");
+      prev = n;
+      mn = std::min(mn, n);
+      mx = std::max(mx, n);
+    }
+    lo[l] = mn;
+    hi[l] = mx;
+    if (mx - mn > SPGO_MAX_WINDOW) {
+      o.code = SPGO_ERR_UNSUPPORTED;
+      o.err = "landmark " + std::to_string(l) + " spans more than SPGO_MAX_WINDOW poses";
+      return;
+    }
+    o.maxw = std::max(o.maxw, mx - mn);
+  }
+  // order landmarks by host frame, then window; a chunk holds <= 32 landmarks of ONE
+  // host, so all its pose-pair contributions (host, target) are indexed by the target
+  std::vector<int32_t> order(L);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    if (q.host[x] != q.host[y]) return q.host[x] < q.host[y];
+    return lo[x] != lo[y] ? lo[x] < lo[y] : hi[x] < hi[y];
+  });
+  std::vector<int32_t> fcount;  // counting sort of a chunk's observations by frame
+  int32_t cur = -1;
+  int k_open = 0;          // first landmark (position in `order`) of the open chunk
+  int64_t obs_local = 0;   // observations emitted so far
+  // emit the open chunk's observations sorted by frame (stable: landmark order
+  // inside a frame) with a counting sort over its frame window
+  auto close_chunk = [&](int k_end) {
+    if (cur < 0) return;
+    o.slab += (int64_t)6 * o.ch_nb[cur] * SPGO_CHUNK;
+    const int f0 = o.ch_f0[cur], nf = o.ch_nb[cur] + 1;
+    fcount.assign((size_t)nf + 1, 0);
+    int64_t n_chunk = 0;
+    for (int k = k_open; k < k_end; ++k) {
+      const int l = order[k];
+      for (int64_t ob = q.obs_ptr[l]; ob < q.obs_ptr[l + 1]; ++ob) ++fcount[(size_t)(q.obs_frame[ob] - f0) + 1];
+      n_chunk += q.obs_ptr[l + 1] - q.obs_ptr[l];
+    }
+    for (int f = 0; f < nf; ++f) fcount[(size_t)f + 1] += fcount[(size_t)f];
+    for (int k = k_open; k < k_end; ++k) {
+      const int l = order[k];
+      const uint8_t slot = (uint8_t)(k - k_open);
+      for (int64_t ob = q.obs_ptr[l]; ob < q.obs_ptr[l + 1]; ++ob) {
+        const int n = q.obs_frame[ob];
+        const size_t dst = (size_t)(obs_base + obs_local + fcount[(size_t)(n - f0)]++);
+        p->obs_frame[dst] = n;
+        p->obs_slot[dst] = slot;
+        std::memcpy(&p->obs_uv[4 * dst], q.obs_uv + 4 * ob, 4 * sizeof(float));
+      }
+    }
+    obs_local += n_chunk;
+  };
+  int32_t host_prev = -1;
+  for (int k = 0; k < L; ++k) {
+    const int l = order[k];
+    bool fresh = cur < 0 || o.ch_cnt[cur] == SPGO_CHUNK || host_prev != q.host[l];
+    if (!fresh) {
+      const int f0 = o.ch_f0[cur];
+      const int nb_new = std::max(o.ch_f0[cur] + o.ch_nb[cur], hi[l]) - f0;
+      if (nb_new > SPGO_MAX_WINDOW) fresh = true;
+    }
+    if (fresh) {
+      close_chunk(k);
+      k_open = k;
+      cur = (int32_t)o.ch_f0.size();
+      o.ch_f0.push_back(std::min(lo[l], N - 1));
+      o.ch_nb.push_back(1);
+      o.ch_lm0.push_back((int32_t)(lm_base + k));
+      o.ch_cnt.push_back(0);
+      o.ch_slab.push_back(o.slab);
+    }
+    host_prev = q.host[l];
+    const int f0 = o.ch_f0[cur];
+    o.ch_nb[cur] = std::max(o.ch_nb[cur], hi[l] - f0);
+    o.ch_cnt[cur] += 1;
+    // internal landmark lm_base + k; lm_obs holds the start of its CHUNK's observations
+    const size_t li = (size_t)(lm_base + k);
+    p->lm_prob[li] = b;
+    p->lm_host[li] = q.host[l];
+    p->lm_lo[li] = lo[l];
+    p->lm_hi[li] = hi[l];
+    p->lm_user[li] = (int32_t)(lm_base + l);
+    p->lm_chunk[li] = cur;  // problem-local until the merge
+    p->lm_slot[li] = o.ch_cnt[cur] - 1;
+    p->lm_uv[2 * li] = q.anchor_uv[2 * l];
+    p->lm_uv[2 * li + 1] = q.anchor_uv[2 * l + 1];
+    p->lm_obs[li] = obs_base + obs_local;
+  }
+  close_chunk(L);
+  const int nch = (int)o.ch_f0.size();
+  for (int c = 0; c < nch; ++c) {
+    if (o.ch_f0[c] < 0 || o.ch_f0[c] + o.ch_nb[c] > N) return bad("internal: chunk window outside the problem");
+    o.max_nb = std::max(o.max_nb, o.ch_nb[c]);
+  }
+  // Schur work list: every (ti >= tj) tile pair a chunk's window touches
+  const int ntile = (N + SPGO_TILE_BLOCKS - 1) / SPGO_TILE_BLOCKS;
+  std::vector<std::vector<int32_t>> lists((size_t)ntile * ntile);
+  for (int c = 0; c < nch; ++c) {
+    const int t0 = o.ch_f0[c] / SPGO_TILE_BLOCKS;
+    const int t1 = std::min(ntile - 1, (o.ch_f0[c] + o.ch_nb[c] - 1) / SPGO_TILE_BLOCKS);
+    for (int ti = t0; ti <= t1; ++ti)
+      for (int tj = t0; tj <= ti; ++tj) lists[(size_t)ti * ntile + tj].push_back(c);
+  }
+  for (int ti = 0; ti < ntile; ++ti)
+    for (int tj = 0; tj <= ti; ++tj) {
+      const auto &lst = lists[(size_t)ti * ntile + tj];
+      for (size_t s0 = 0; s0 < lst.size(); s0 += SPGO_KSPLIT) {
+        o.wk_ti.push_back(ti);
+        o.wk_tj.push_back(tj);
+        o.wk_cbeg.push_back((int32_t)o.wk_chunks.size());
+        for (size_t k = s0; k < std::min(lst.size(), s0 + SPGO_KSPLIT); ++k) o.wk_chunks.push_back(lst[k]);
+        o.wk_cend.push_back((int32_t)o.wk_chunks.size());
+      }
+    }
+  // tensor-core Schur work list: 128 x 128 tiles of the lower triangle, <= SPGO_TC_SPLIT chunks each
+  const int P = 6 * N;
+  for (int row0 = 0; row0 < P; row0 += 128) {
+    for (int col0 = 0; col0 <= row0; col0 += 128) {
+      const int ncols = ((std::min(128, P - col0) + 15) / 16) * 16;
+      std::vector<int32_t> lst;
+      for (int c = 0; c < nch; ++c) {
+        const int s0 = 6 * o.ch_f0[c], s1 = 6 * (o.ch_f0[c] + o.ch_nb[c]);
+        if (s1 > row0 && s0 < row0 + 128 && s1 > col0 && s0 < col0 + ncols) lst.push_back(c);
+      }
+      for (size_t st = 0; st < lst.size(); st += SPGO_TC_SPLIT) {
+        o.tc_row0.push_back(row0);
+        o.tc_col0.push_back(col0);
+        o.tc_ncols.push_back(ncols);
+        o.tc_cbeg.push_back((int32_t)o.tc_chunks.size());
+        for (size_t k = st; k < std::min(lst.size(), st + SPGO_TC_SPLIT); ++k) o.tc_chunks.push_back(lst[k]);
+        o.tc_cend.push_back((int32_t)o.tc_chunks.size());
+      }
+    }
+  }
+}
+
 static int plan_build(const spgo_host_problem *probs, int nprob, int precision, spgo_plan *p) {
   if (nprob <= 0 || !probs) return fail(SPGO_ERR_INVALID_ARG, "no problems");
   if (precision != SPGO_PREC_MIXED && precision != SPGO_PREC_FP64)
     return fail(SPGO_ERR_INVALID_ARG, "unknown precision");
   p->precision = precision;
   p->B = nprob;
-  int32_t frame_off = 0, pose_off = 0, lm_off = 0, param_off = 0;
-  int64_t S_off = 0, pair_off = 0, slab_off = 0, obs_total = 0;
-  {  // the per-landmark and per-observation arrays are sized once
-    int64_t Lt = 0, Ot = 0;
-    for (int b = 0; b < nprob; ++b) {
-      Lt += std::max(0, probs[b].n_landmarks);
-      Ot += std::max<int64_t>(0, probs[b].n_obs);
-    }
-    p->obs_frame.resize((size_t)Ot);
-    p->obs_slot.resize((size_t)Ot);
-    p->obs_uv.resize((size_t)Ot * 4);
-    for (auto *v : {&p->lm_prob, &p->lm_host, &p->lm_lo, &p->lm_hi, &p->lm_user, &p->lm_chunk, &p->lm_slot})
-      v->reserve((size_t)Lt);
-    p->lm_uv.reserve((size_t)Lt * 2);
-    p->lm_obs.reserve((size_t)Lt + 1);
-  }
-  std::vector<int32_t> fcount;  // counting sort of a chunk's observations by frame
+  // sizes, pointers and CSR shape first; the per-problem work then runs in parallel
+  std::vector<int64_t> lm_base(nprob + 1, 0), obs_base(nprob + 1, 0);
   for (int b = 0; b < nprob; ++b) {
     const spgo_host_problem &q = probs[b];
     const int N = q.n_poses, L = q.n_landmarks;
@@ -187,154 +342,76 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
       return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": null array");
     if (L > 0 && (q.obs_ptr[0] != 0 || q.obs_ptr[L] != q.n_obs))
       return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": obs_ptr is not a CSR over n_obs");
-    // per-landmark window [lo, hi) of pose blocks
-    std::vector<int32_t> lo(L), hi(L);
-    int32_t maxw = 1;
-    for (int l = 0; l < L; ++l) {
-      const int a = q.host[l];
-      if (a < 0 || a > N) return fail(SPGO_ERR_INVALID_ARG, "landmark " + std::to_string(l) + ": host out of range");
-      if (q.obs_ptr[l + 1] < q.obs_ptr[l]) return fail(SPGO_ERR_INVALID_ARG, "obs_ptr decreasing");
-      int32_t mn = a, mx = a, prev = -1;
-      for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) {
-        const int n = q.obs_frame[o];
-        if (n < 0 || n > N) return fail(SPGO_ERR_INVALID_ARG, "observation frame out of range");
-        if (n <= prev) return fail(SPGO_ERR_INVALID_ARG, "frames must ascend strictly inside a landmark");
-        prev = n;
-        mn = std::min(mn, n);
-        mx = std::max(mx, n);
-      }
-      lo[l] = mn;
-      hi[l] = mx;
-      if (mx - mn > SPGO_MAX_WINDOW)
-        return fail(SPGO_ERR_UNSUPPORTED, "landmark " + std::to_string(l) + " spans more than SPGO_MAX_WINDOW poses");
-      maxw = std::max(maxw, mx - mn);
-    }
-    // order landmarks by host frame, then window; a chunk holds <= 32 landmarks of ONE
-    // host, so all its pose-pair contributions (host, target) are indexed by the target
-    std::vector<int32_t> order(L);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-      if (q.host[x] != q.host[y]) return q.host[x] < q.host[y];
-      return lo[x] != lo[y] ? lo[x] < lo[y] : hi[x] < hi[y];
-    });
-    const int32_t ch_begin = (int32_t)p->ch_prob.size();
-    int32_t cur = -1;
-    int k_open = 0;  // first landmark (position in `order`) of the open chunk
-    // emit the open chunk's observations sorted by frame (stable: landmark order
-    // inside a frame) with a counting sort over its frame window
-    auto close_chunk = [&](int k_end) {
-      if (cur < 0) return;
-      slab_off += (int64_t)6 * p->ch_nb[cur] * SPGO_CHUNK;
-      const int f0 = p->ch_f0[cur], nf = p->ch_nb[cur] + 1;
-      fcount.assign((size_t)nf + 1, 0);
-      int64_t n_chunk = 0;
-      for (int k = k_open; k < k_end; ++k) {
-        const int l = order[k];
-        for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) ++fcount[(size_t)(q.obs_frame[o] - f0) + 1];
-        n_chunk += q.obs_ptr[l + 1] - q.obs_ptr[l];
-      }
-      for (int f = 0; f < nf; ++f) fcount[(size_t)f + 1] += fcount[(size_t)f];
-      for (int k = k_open; k < k_end; ++k) {
-        const int l = order[k];
-        const uint8_t slot = (uint8_t)(k - k_open);
-        for (int64_t o = q.obs_ptr[l]; o < q.obs_ptr[l + 1]; ++o) {
-          const int n = q.obs_frame[o];
-          const size_t dst = (size_t)(obs_total + fcount[(size_t)(n - f0)]++);
-          p->obs_frame[dst] = n;
-          p->obs_slot[dst] = slot;
-          std::memcpy(&p->obs_uv[4 * dst], q.obs_uv + 4 * o, 4 * sizeof(float));
-        }
-      }
-      obs_total += n_chunk;
+    if (L == 0 && q.n_obs != 0)
+      return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": observations without landmarks");
+    lm_base[b + 1] = lm_base[b] + L;
+    obs_base[b + 1] = obs_base[b] + q.n_obs;
+  }
+  const int64_t Lt = lm_base[nprob], Ot = obs_base[nprob];
+  p->obs_frame.resize((size_t)Ot);
+  p->obs_slot.resize((size_t)Ot);
+  p->obs_uv.resize((size_t)Ot * 4);
+  for (auto *v : {&p->lm_prob, &p->lm_host, &p->lm_lo, &p->lm_hi, &p->lm_user, &p->lm_chunk, &p->lm_slot})
+    v->resize((size_t)Lt);
+  p->lm_uv.resize((size_t)Lt * 2);
+  p->lm_obs.resize((size_t)Lt + 1);
+  std::vector<ProbPlan> pp((size_t)nprob);
+  {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nthr = (int)std::min<unsigned>(std::min<unsigned>(hw, 16u), (unsigned)nprob);
+    std::atomic<int> next(0);
+    auto work = [&]() {
+      for (int b; (b = next.fetch_add(1)) < nprob;) plan_problem(probs[b], b, lm_base[b], obs_base[b], p, pp[b]);
     };
-    for (int k = 0; k < L; ++k) {
-      const int l = order[k];
-      bool fresh = cur < 0 || p->ch_cnt[cur] == SPGO_CHUNK || p->lm_host.back() != q.host[l];
-      if (!fresh) {
-        const int f0 = p->ch_f0[cur];
-        const int nb_new = std::max(p->ch_f0[cur] + p->ch_nb[cur], hi[l]) - f0;
-        if (nb_new > SPGO_MAX_WINDOW) fresh = true;
-      }
-      if (fresh) {
-        close_chunk(k);
-        k_open = k;
-        cur = (int32_t)p->ch_prob.size();
-        p->ch_prob.push_back(b);
-        p->ch_f0.push_back(std::min(lo[l], N - 1));
-        p->ch_nb.push_back(1);
-        p->ch_lm0.push_back(lm_off + k);
-        p->ch_cnt.push_back(0);
-        p->ch_slab.push_back(slab_off);
-      }
-      const int f0 = p->ch_f0[cur];
-      p->ch_nb[cur] = std::max(p->ch_nb[cur], hi[l] - f0);
-      p->ch_cnt[cur] += 1;
-      // internal landmark lm_off + k; lm_obs holds the start of its CHUNK's observations
-      p->lm_prob.push_back(b);
-      p->lm_host.push_back(q.host[l]);
-      p->lm_lo.push_back(lo[l]);
-      p->lm_hi.push_back(hi[l]);
-      p->lm_user.push_back(lm_off + l);
-      p->lm_chunk.push_back(cur);
-      p->lm_slot.push_back(p->ch_cnt[cur] - 1);
-      p->lm_uv.push_back(q.anchor_uv[2 * l]);
-      p->lm_uv.push_back(q.anchor_uv[2 * l + 1]);
-      p->lm_obs.push_back(obs_total);
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthr; ++t) th.emplace_back(work);
+    work();
+    for (auto &t : th) t.join();
+  }
+  // merge in problem order: global chunk indices, slab offsets, work lists, records
+  int32_t frame_off = 0, pose_off = 0, lm_off = 0, param_off = 0;
+  int64_t S_off = 0, pair_off = 0, slab_off = 0;
+  for (int b = 0; b < nprob; ++b) {
+    const spgo_host_problem &q = probs[b];
+    const ProbPlan &o = pp[b];
+    if (o.code != SPGO_OK) return fail(o.code, "problem " + std::to_string(b) + ": " + o.err);
+    const int N = q.n_poses, L = q.n_landmarks, P = 6 * N;
+    const int32_t ch_begin = (int32_t)p->ch_prob.size();
+    const int nch = (int)o.ch_f0.size();
+    for (int c = 0; c < nch; ++c) {
+      p->ch_prob.push_back(b);
+      p->ch_f0.push_back(o.ch_f0[c]);
+      p->ch_nb.push_back(o.ch_nb[c]);
+      p->ch_lm0.push_back(o.ch_lm0[c]);
+      p->ch_cnt.push_back(o.ch_cnt[c]);
+      p->ch_slab.push_back(slab_off + o.ch_slab[c]);
     }
-    close_chunk(L);
-    const int32_t ch_end = (int32_t)p->ch_prob.size();
-    for (int c = ch_begin; c < ch_end; ++c) {
-      if (p->ch_f0[c] < 0 || p->ch_f0[c] + p->ch_nb[c] > N)
-        return fail(SPGO_ERR_INVALID_ARG, "internal: chunk window outside the problem");
-      p->max_nb = std::max(p->max_nb, p->ch_nb[c]);
-    }
-    // Schur work list: every (ti >= tj) tile pair a chunk's window touches
-    const int ntile = (N + SPGO_TILE_BLOCKS - 1) / SPGO_TILE_BLOCKS;
-    std::vector<std::vector<int32_t>> lists((size_t)ntile * ntile);
-    for (int c = ch_begin; c < ch_end; ++c) {
-      const int t0 = p->ch_f0[c] / SPGO_TILE_BLOCKS;
-      const int t1 = std::min(ntile - 1, (p->ch_f0[c] + p->ch_nb[c] - 1) / SPGO_TILE_BLOCKS);
-      for (int ti = t0; ti <= t1; ++ti)
-        for (int tj = t0; tj <= ti; ++tj) lists[(size_t)ti * ntile + tj].push_back(c);
-    }
-    for (int ti = 0; ti < ntile; ++ti)
-      for (int tj = 0; tj <= ti; ++tj) {
-        const auto &lst = lists[(size_t)ti * ntile + tj];
-        for (size_t s = 0; s < lst.size(); s += SPGO_KSPLIT) {
-          p->wk_prob.push_back(b);
-          p->wk_ti.push_back(ti);
-          p->wk_tj.push_back(tj);
-          p->wk_cbeg.push_back((int32_t)p->wk_chunks.size());
-          for (size_t k = s; k < std::min(lst.size(), s + SPGO_KSPLIT); ++k) p->wk_chunks.push_back(lst[k]);
-          p->wk_cend.push_back((int32_t)p->wk_chunks.size());
-        }
-      }
-    // tensor-core Schur work list: 128 x 128 tiles of the lower triangle, <= 64 chunks each
+    p->max_nb = std::max(p->max_nb, o.max_nb);
+    for (int64_t k = lm_base[b]; k < lm_base[b + 1]; ++k) p->lm_chunk[(size_t)k] += ch_begin;
     {
-      const int P = 6 * N;
-      const int kTcSplit = SPGO_TC_SPLIT;
-      for (int row0 = 0; row0 < P; row0 += 128) {
-        for (int col0 = 0; col0 <= row0; col0 += 128) {
-          const int ncols = ((std::min(128, P - col0) + 15) / 16) * 16;
-          std::vector<int32_t> lst;
-          for (int c = ch_begin; c < ch_end; ++c) {
-            const int s0 = 6 * p->ch_f0[c], s1 = 6 * (p->ch_f0[c] + p->ch_nb[c]);
-            if (s1 > row0 && s0 < row0 + 128 && s1 > col0 && s0 < col0 + ncols) lst.push_back(c);
-          }
-          for (size_t st = 0; st < lst.size(); st += kTcSplit) {
-            p->tc_prob.push_back(b);
-            p->tc_row0.push_back(row0);
-            p->tc_col0.push_back(col0);
-            p->tc_ncols.push_back(ncols);
-            p->tc_cbeg.push_back((int32_t)p->tc_chunks.size());
-            for (size_t k = st; k < std::min(lst.size(), st + kTcSplit); ++k) p->tc_chunks.push_back(lst[k]);
-            p->tc_cend.push_back((int32_t)p->tc_chunks.size());
-          }
-        }
+      const int32_t base = (int32_t)p->wk_chunks.size();
+      for (size_t i = 0; i < o.wk_ti.size(); ++i) {
+        p->wk_prob.push_back(b);
+        p->wk_ti.push_back(o.wk_ti[i]);
+        p->wk_tj.push_back(o.wk_tj[i]);
+        p->wk_cbeg.push_back(base + o.wk_cbeg[i]);
+        p->wk_cend.push_back(base + o.wk_cend[i]);
       }
+      for (const int32_t c : o.wk_chunks) p->wk_chunks.push_back(ch_begin + c);
     }
-    // per-problem records
-    const int P = 6 * N;
+    {
+      const int32_t base = (int32_t)p->tc_chunks.size();
+      for (size_t i = 0; i < o.tc_row0.size(); ++i) {
+        p->tc_prob.push_back(b);
+        p->tc_row0.push_back(o.tc_row0[i]);
+        p->tc_col0.push_back(o.tc_col0[i]);
+        p->tc_ncols.push_back(o.tc_ncols[i]);
+        p->tc_cbeg.push_back(base + o.tc_cbeg[i]);
+        p->tc_cend.push_back(base + o.tc_cend[i]);
+      }
+      for (const int32_t c : o.tc_chunks) p->tc_chunks.push_back(ch_begin + c);
+    }
+    const int32_t maxw = o.maxw;
     p->p_npose.push_back(N);
     p->p_frame_off.push_back(frame_off);
     p->p_pose_off.push_back(pose_off);
@@ -343,7 +420,7 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     p->p_pair_D.push_back(maxw);
     p->p_param_off.push_back(param_off);
     p->p_chunk_off.push_back(ch_begin);
-    p->p_chunk_cnt.push_back(ch_end - ch_begin);
+    p->p_chunk_cnt.push_back(nch);
     p->p_S_off.push_back(S_off);
     p->p_pair_off.push_back(pair_off);
     p->p_nres.push_back(4 * q.n_obs);
@@ -360,8 +437,10 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     param_off += P;
     S_off += (int64_t)P * P;
     pair_off += (int64_t)N * maxw;
+    slab_off += o.slab;
   }
-  p->lm_obs.push_back(obs_total);
+  const int64_t obs_total = Ot;
+  p->lm_obs[(size_t)Lt] = obs_total;
   {  // tensor-core Schur items longest first (one CTA per SM: the last wave stays short)
     const size_t n = p->tc_prob.size();
     std::vector<size_t> ord(n);

@@ -142,6 +142,20 @@ class BatchSolver:
         o = int(self.lm_off[b])
         return self.alpha[o:o + self.problems[b].n_landmarks].cpu().numpy().copy()
 
+    def get_state(self):
+        """Every problem's poses ([N, 4, 4]) and inverse depths, from one device-to-host
+        copy of each state array (the batched form of get_poses / get_alpha)."""
+        self.synchronize()
+        P = _to44(self.poses[:12 * int(self.sizes.total_poses)].cpu().numpy().reshape(-1, 12))
+        A = self.alpha[:int(self.sizes.total_landmarks)].cpu().numpy()
+        poses, alphas = [], []
+        for b, p in enumerate(self.problems):
+            o, N = int(self.pose_off[b]), int(p.n_poses)
+            poses.append(P[o:o + N])
+            lo = int(self.lm_off[b])
+            alphas.append(A[lo:lo + p.n_landmarks].copy())
+        return poses, alphas
+
     def set_poses(self, b: int, poses: np.ndarray):
         N = int(self.problems[b].n_poses)
         o = int(self.pose_off[b])

@@ -177,6 +177,17 @@ def test_huber_outliers_converge(built_lib, cuda_device, prec, opt_cost_tol, pos
     assert er < pose_tol and et < pose_tol
 
 
+def test_batched_readback_matches_per_problem(built_lib, cuda_device):
+    probs = [scenes.circle_scene(s, n, l) for s, n, l in [(71, 6, 80), (72, 9, 150), (73, 5, 60)]]
+    bs = BatchSolver(probs, precision="mixed")
+    bs.set_params(loss="l2", max_iters=3)
+    bs.solve()
+    poses, alphas = bs.get_state()
+    for b in range(len(probs)):
+        assert np.array_equal(poses[b], bs.get_poses(b))
+        assert np.array_equal(alphas[b], bs.get_alpha(b))
+
+
 def test_cudasolver_dropin_flow(built_lib, cuda_device):
     """CUDAmanager.py-style use: calibration, writeObservations, identity poses, step(k)."""
     truth = scenes.circle_scene(41, 5, 60)
