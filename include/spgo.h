@@ -117,6 +117,8 @@ typedef struct spgo_params {
     int32_t use_tc;              /* 1 (default): mixed path forms the landmark Schur complement
                                     on the tensor cores (tcgen05, split TF32, FP32 accumulate);
                                     0: FP32 SIMT */
+    int32_t cost_block;          /* threads per CTA of the cost pass (0: 64; else 32..256, x32) */
+    int32_t lin_block;           /* threads per CTA of the Jacobian pass (0: 256; else 32..256, x32) */
 } spgo_params;
 
 typedef struct spgo_problem_status {
@@ -176,6 +178,15 @@ int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream);
  * status check every `check_every` iterations.  Returns the iteration count
  * in *iters_done (max over problems). */
 int spgo_lm_solve(spgo_solver *s, int32_t check_every, int32_t *iters_done, void *stream);
+
+/* Autotuner (no reference counterpart): times the launch shapes that can change
+ * without re-planning on this solver's own batch -- cost-pass CTA size {64, 128,
+ * 256}, Jacobian-pass CTA size {128, 256}, and (mixed precision) the Schur path
+ * {tensor cores, SIMT} -- over a reset plus two LM iterations each (CUDA graphs
+ * off, events on), keeps the fastest of each, and applies them.  The poses and
+ * inverse depths are restored afterwards; the LM state is reset; profiling is
+ * switched off.  `chosen` (optional) receives the resulting parameters. */
+int spgo_autotune(spgo_solver *s, spgo_params *chosen, void *stream);
 
 /* Linearise at the current state and export one problem's dense system into
  * caller-owned DEVICE buffers (any pointer may be NULL):

@@ -864,6 +864,9 @@ int spgo_set_params(spgo_solver *s, const spgo_params *p) {
   if (!(p->loss_scale > 0) || !(p->eps >= 0) || !(p->alpha_min < p->alpha_max) || p->max_iters < 0 ||
       p->refine_steps < 0 || !(p->lambda0 >= 0))
     return fail(SPGO_ERR_INVALID_ARG, "parameter out of range");
+  for (const int32_t blk : {p->cost_block, p->lin_block})
+    if (blk != 0 && (blk < 32 || blk > 256 || blk % 32 != 0))
+      return fail(SPGO_ERR_INVALID_ARG, "CTA size must be 0 or a multiple of 32 in [32, 256]");
   static_assert(sizeof(Params) == sizeof(spgo_params), "params layout");
   std::memcpy(&s->prm, p, sizeof(Params));
   drop_graphs(s);  // captured launches carry the old parameters
@@ -970,6 +973,66 @@ int spgo_lm_solve(spgo_solver *s, int32_t check_every, int32_t *iters_done, void
     *iters_done = mx;
   }
   return SPGO_OK;
+}
+
+int spgo_autotune(spgo_solver *s, spgo_params *chosen, void *stream) {
+  if (!s) return fail(SPGO_ERR_INVALID_ARG, "null solver");
+  cudaStream_t st = (cudaStream_t)stream;
+  const spgo_plan *p = s->plan;
+  const bool f64 = p->precision == SPGO_PREC_FP64;
+  const size_t np = (size_t)p->NP * 12, nl = (size_t)p->L;
+  double *save = nullptr;
+  CUDA_TRY(cudaMalloc(&save, sizeof(double) * (np + nl + 1)));
+  CUDA_TRY(cudaMemcpyAsync(save, s->poses, sizeof(double) * np, cudaMemcpyDeviceToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(save + np, s->alpha, sizeof(double) * nl, cudaMemcpyDeviceToDevice, st));
+  const Params base = s->prm;
+  struct Cand {
+    int cost_block, lin_block, use_tc;
+  };
+  // every value of each dimension appears at least once; the dimensions time different kernels
+  const Cand cands[] = {{64, 256, 1}, {64, 256, 1}, {128, 128, 0}, {256, 256, 1}};
+  double t_cost[257] = {}, t_lin[257] = {}, t_schur[2] = {1e30, 1e30};
+  for (int k = 0; k < 257; ++k) t_cost[k] = t_lin[k] = 1e30;
+  int rc = SPGO_OK;
+  rc = spgo_profile_enable(s, 4096);
+  for (size_t ci = 0; rc == SPGO_OK && ci < sizeof(cands) / sizeof(cands[0]); ++ci) {
+    s->prm = base;
+    s->prm.use_graph = 0;
+    s->prm.cost_block = cands[ci].cost_block;
+    s->prm.lin_block = cands[ci].lin_block;
+    s->prm.use_tc = cands[ci].use_tc;
+    rc = launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, st);
+    for (int it = 0; rc == SPGO_OK && it < 2; ++it)
+      rc = f64 ? enqueue_lm_iteration<double>(s, st) : enqueue_lm_iteration<float>(s, st);
+    double ms[K_NKINDS];
+    int64_t cnt[K_NKINDS];
+    if (rc == SPGO_OK) rc = spgo_profile_read(s, ms, cnt, K_NKINDS, stream);
+    if (rc == SPGO_OK && ci > 0) {  // the first run warms up
+      t_cost[cands[ci].cost_block] = std::min(t_cost[cands[ci].cost_block], ms[K_COST]);
+      t_lin[cands[ci].lin_block] = std::min(t_lin[cands[ci].lin_block], ms[K_LINEARIZE]);
+      t_schur[cands[ci].use_tc] = std::min(t_schur[cands[ci].use_tc], ms[K_SCHUR]);
+    }
+    cudaMemcpyAsync(s->poses, save, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(s->alpha, save + np, sizeof(double) * nl, cudaMemcpyDeviceToDevice, st);
+  }
+  s->prm = base;
+  if (rc == SPGO_OK) {
+    int best_c = 64, best_l = 256;
+    for (const int c : {64, 128, 256})
+      if (t_cost[c] < t_cost[best_c]) best_c = c;
+    for (const int l : {128, 256})
+      if (t_lin[l] < t_lin[best_l]) best_l = l;
+    s->prm.cost_block = best_c;
+    s->prm.lin_block = best_l;
+    if (!f64) s->prm.use_tc = t_schur[1] <= t_schur[0] ? 1 : 0;
+  }
+  spgo_profile_enable(s, 0);
+  drop_graphs(s);
+  cudaStreamSynchronize(st);
+  cudaFree(save);
+  if (rc == SPGO_OK) rc = launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, st) == 0 ? SPGO_OK : SPGO_ERR_CUDA;
+  if (rc == SPGO_OK && chosen) std::memcpy(chosen, &s->prm, sizeof(Params));
+  return rc;
 }
 
 int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, double *B, double *C, double *g_a,

@@ -493,12 +493,14 @@ int launch_linearize(const PlanView &pv, const WorkView &wv, const Params &prm, 
   if (pv.n_chunks == 0) return 0;
   cudaStream_t st = (cudaStream_t)stream;
   if (cost_only) {
-    const size_t sm = LinLayout<T>(pv.max_nb, kCostThreads / 32, true).total;
-    k_linearize<T, true><<<pv.n_chunks, kCostThreads, sm, st>>>(pv, wv, prm, alpha, gate);
+    const int nt = prm.cost_block > 0 ? prm.cost_block : kCostThreads;
+    const size_t sm = LinLayout<T>(pv.max_nb, nt / 32, true).total;
+    k_linearize<T, true><<<pv.n_chunks, nt, sm, st>>>(pv, wv, prm, alpha, gate);
   } else {
-    const size_t sm = LinLayout<T>(pv.max_nb, kLinThreads / 32, false).total;
+    const int nt = prm.lin_block > 0 ? prm.lin_block : kLinThreads;
+    const size_t sm = LinLayout<T>(pv.max_nb, nt / 32, false).total;
     cudaFuncSetAttribute(k_linearize<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_linearize<T, false><<<pv.n_chunks, kLinThreads, sm, st>>>(pv, wv, prm, alpha, gate);
+    k_linearize<T, false><<<pv.n_chunks, nt, sm, st>>>(pv, wv, prm, alpha, gate);
   }
   ++g_launches;
   return (int)cudaGetLastError();

@@ -115,6 +115,7 @@ struct Params {
   double lambda0, lambda_max, tol;
   int32_t max_iters, refine_steps;
   int32_t use_graph, use_tc;
+  int32_t cost_block, lin_block;
 };
 
 // launch wrappers (defined in the .cu files); all return cudaError_t as int

@@ -25,7 +25,7 @@ EXPORTED = [
     "spgo_gn_step", "spgo_lm_reset", "spgo_lm_iterate", "spgo_lm_status", "spgo_lm_solve",
     "spgo_export_system", "spgo_launch_count", "spgo_profile_enable", "spgo_profile_read",
     "spgo_cost_noalloc", "spgo_export_reduced", "spgo_mlp_forward", "spgo_mlp_grad", "spgo_mlp_adam",
-    "spgo_lm_set_controller", "spgo_lm_features", "spgo_lm_probe",
+    "spgo_lm_set_controller", "spgo_lm_features", "spgo_lm_probe", "spgo_autotune",
 ]
 MLP_PARAMS, MLP_INPUTS, MLP_CACHE_PER_SAMPLE = 5378, 16, 386
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
@@ -52,7 +52,8 @@ class Params(C.Structure):
     _fields_ = [("loss", C.c_int32), ("near_boost", C.c_int32), ("loss_scale", C.c_float), ("eps", C.c_float),
                 ("alpha_min", C.c_float), ("alpha_max", C.c_float), ("lambda0", C.c_double),
                 ("lambda_max", C.c_double), ("tol", C.c_double), ("max_iters", C.c_int32),
-                ("refine_steps", C.c_int32), ("use_graph", C.c_int32), ("use_tc", C.c_int32)]
+                ("refine_steps", C.c_int32), ("use_graph", C.c_int32), ("use_tc", C.c_int32),
+                ("cost_block", C.c_int32), ("lin_block", C.c_int32)]
 
 
 class ProblemStatus(C.Structure):
@@ -105,6 +106,8 @@ def lib() -> C.CDLL:
     L.spgo_lm_set_controller.argtypes = [vp, vp, vp]
     L.spgo_lm_features.argtypes = [vp, vp, vp]
     L.spgo_lm_probe.argtypes = [vp, i32, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
+    L.spgo_autotune.argtypes = [vp, C.POINTER(Params), vp]
+    L.spgo_autotune.restype = C.c_int
     for name in ("spgo_mlp_forward", "spgo_mlp_grad", "spgo_mlp_adam", "spgo_lm_set_controller",
                  "spgo_lm_features", "spgo_lm_probe"):
         getattr(L, name).restype = C.c_int

@@ -174,7 +174,7 @@ class BatchSolver:
     # -- parameters ---------------------------------------------------------------
     def set_params(self, loss: Optional[str] = None, loss_scale=None, near_boost=None, eps=None,
                    alpha_min=None, alpha_max=None, lambda0=None, lambda_max=None, tol=None, max_iters=None,
-                   refine_steps=None, use_graph=None, use_tc=None):
+                   refine_steps=None, use_graph=None, use_tc=None, cost_block=None, lin_block=None):
         p = self.params
         if loss is not None:
             p.loss = _LOSS[loss]
@@ -193,6 +193,10 @@ class BatchSolver:
             p.use_graph = int(bool(use_graph))
         if use_tc is not None:
             p.use_tc = int(bool(use_tc))
+        if cost_block is not None:
+            p.cost_block = int(cost_block)
+        if lin_block is not None:
+            p.lin_block = int(lin_block)
         self._apply_params()
 
     def _apply_params(self):
@@ -217,6 +221,14 @@ class BatchSolver:
         it = C.c_int32()
         nat.check(self.L.spgo_lm_solve(self._solver, int(check_every), C.byref(it), self._sp()), "lm_solve")
         return self.status()
+
+    def autotune(self) -> dict:
+        """Time the run-time launch shapes on this batch and keep the fastest
+        (``spgo_autotune``); returns the choices."""
+        out = nat.Params()
+        nat.check(self.L.spgo_autotune(self._solver, C.byref(out), self._sp()), "autotune")
+        self.params = out
+        return dict(cost_block=out.cost_block, lin_block=out.lin_block, use_tc=out.use_tc)
 
     def gn_step(self, iterations: int = 1, step_size: float = 1.0):
         nat.check(self.L.spgo_gn_step(self._solver, int(iterations), float(step_size), self._sp()), "gn_step")

@@ -58,3 +58,20 @@ def test_tensor_core_solve_converges(built_lib, cuda_device):
     for b, p in enumerate(probs):
         res = S.lm_solve(f32_obs(p), S.Loss(), max_iters=30, tol=1e-6)
         assert abs(sts[b]["cost"] - res.cost) / res.cost < 1e-6
+
+
+def test_autotune_picks_valid_shapes_and_restores_state(built_lib, cuda_device):
+    """The autotuner returns shapes from its candidate sets, leaves the poses and
+    inverse depths untouched, and the tuned solve reaches the untuned cost."""
+    probs = [scenes.circle_scene(s, n, l) for s, n, l in [(401, 12, 600), (402, 20, 900), (403, 30, 400)]]
+    bs = BatchSolver(probs, precision="mixed")
+    bs.set_params(loss="l2", max_iters=30, tol=1e-6)
+    base = [s["cost"] for s in bs.solve()]
+    bs.load_state()
+    p0, a0 = bs.poses.clone(), bs.alpha.clone()
+    tuned = bs.autotune()
+    assert tuned["cost_block"] in (64, 128, 256) and tuned["lin_block"] in (128, 256) and tuned["use_tc"] in (0, 1)
+    assert bool((bs.poses == p0).all()) and bool((bs.alpha == a0).all())
+    after = [s["cost"] for s in bs.solve()]
+    for c0, c1 in zip(base, after):
+        assert abs(c1 - c0) / c0 < 1e-6
