@@ -88,7 +88,7 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
       for (int k = 0; k < kPanel; ++k) {
         const T dk = __shfl_sync(0xffffffffu, a[k], k);
         const T d = k < w ? dk : T(1);
-        bad = bad || !(d > T(0)) || !isfinite((double)d);
+        bad = bad || !(d > T(0)) || !(d < T(INFINITY));  // (no FP64 conversion on the pivot chain)
         const T lkk = sqrt(d), rinv = T(1) / lkk;  // correctly rounded: the refinement step relies on it
         const T lik = lane > k ? a[k] * rinv : (lane == k ? lkk : a[k]);
         a[k] = lik;
@@ -144,10 +144,13 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
 #pragma unroll
         for (int c = 0; c < kCols; ++c) {
           if (j0 + c < P && i >= j0 + c) {
-            T acc = T(0);
+            T a0 = T(0), a1 = T(0);  // two half-length FMA chains per output
 #pragma unroll
-            for (int k = 0; k < kPanel; ++k) acc += li[k] * ljk[c][k];
-            Lm[cb[j0 + c] + i] -= acc;
+            for (int k = 0; k < kPanel; k += 2) {
+              a0 += li[k] * ljk[c][k];
+              a1 += li[k + 1] * ljk[c][k + 1];
+            }
+            Lm[cb[j0 + c] + i] -= a0 + a1;
           }
         }
       }
