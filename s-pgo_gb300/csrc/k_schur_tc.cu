@@ -14,8 +14,7 @@
 //   warp 9     copy: 1-D bulk copies (cp.async.bulk) of the chunk's slab rows that
 //              fall in the tile's row range (and column range, off the diagonal)
 //              plus a 16-byte aligned superset of its C values, into a 3-slot ring;
-//   warps 0-7  transform (each thread half of one tile row's pieces): scale by
-//              s_k and split each value into TF32 parts,
+//   warps 0-3  transform: scale by s_k and split each value into TF32 parts,
 //              x = hi + lo (hi rounded to 10 mantissa bits, lo = x - hi rounded
 //              again), written in the no-swizzle K-major core-matrix layout into
 //              a double-buffered operand stage (zero rows outside the chunk);
@@ -24,10 +23,10 @@
 //   warp 8     one thread issues 3 x 4 kind::tf32 MMAs per chunk (hi.hi + hi.lo +
 //              lo.hi, K = 8 each) into one of two 128-lane x 128-column FP32 TMEM
 //              accumulators, trimming N to the chunk's last column;
-//   warps 4-7  also, every 4 chunks, read the finished accumulator with
-//              tcgen05.ld and add it into FP32 registers (one tile row per
-//              thread); at the end they stage the tile in shared memory and add
-//              its lower triangle into S_L with coalesced reductions.
+//   warps 4-7  every 4 chunks read the finished accumulator with tcgen05.ld and
+//              add it into FP32 registers (one tile row per thread), then stage
+//              the tile in shared memory and add its lower triangle into S_L with
+//              coalesced reductions.
 // The split product carries ~21 mantissa bits.  Reading the accumulator back
 // every 4 chunks keeps the tensor core's own accumulation short: accumulating a
 // whole chunk list in TMEM loses ~25x more than FP32 SIMT on wide problems,
@@ -87,16 +86,14 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
-// scale four of one slab row's eight 16-byte pieces (or zeros) by s and write
-// their hi/lo parts into row r of an operand in core-matrix layout; piece order
-// rotated by r (bank-conflict free).  With gs != nullptr also returns the pieces'
-// share of sum_k x_k gs_k.
+// scale one slab row (or zeros) by s and write its hi/lo parts as row r of an
+// operand in core-matrix layout; piece order rotated by r (bank-conflict free).
+// With gs != nullptr also returns sum_k x_k gs_k.
 __device__ __forceinline__ float split_row(const float *src, bool valid, const float *s, const float *gs, int r,
-                                           float *h, float *l, int mbeg) {
+                                           float *h, float *l) {
   float gacc = 0.f;
 #pragma unroll
-  for (int mm = 0; mm < 4; ++mm) {
-    const int m = mbeg + mm;  // pieces mbeg .. mbeg + 3 of the row's 8
+  for (int m = 0; m < 8; ++m) {
     const int kq = (m + r) & 7;
     float4 v = valid ? *reinterpret_cast<const float4 *>(src + 4 * kq) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float x[4] = {v.x * s[4 * kq], v.y * s[4 * kq + 1], v.z * s[4 * kq + 2], v.w * s[4 * kq + 3]};
@@ -133,10 +130,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
   if (tid == 0) {
     for (int i = 0; i < kRawSlots; ++i) {
       tc::mbar_init(&sm.raw_full[i], 1);
-      tc::mbar_init(&sm.raw_empty[i], 256);
+      tc::mbar_init(&sm.raw_empty[i], 128);
     }
     for (int i = 0; i < kOpStages; ++i) {
-      tc::mbar_init(&sm.op_full[i], 256);
+      tc::mbar_init(&sm.op_full[i], 128);
       tc::mbar_init(&sm.op_empty[i], 1);
     }
     for (int i = 0; i < 2; ++i) {
@@ -198,40 +195,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
         (void)tc::mbar_wait_until(&sm.raw_full[i % kRawSlots], (i / kRawSlots) & 1, deadline + kTimeoutNs,
                                   &sm.zero);
     }
-  } else if (warp < 8) {
-    // ---- transform warps 0-7; warps 4-7 also read the accumulators back ----
+  } else if (warp < 4) {
+    // ---- transform warps ----
     const float lam1 = (float)(1.0 + wv.lm[b].lam);
     const float eps = prm.eps;
-    const int t = tid & 127, mbeg = 4 * (tid >> 7);  // tile row; which half of its pieces
-    const bool accw = warp >= 4;
-    const int q = warp & 3;
-    if (accw) {
-#pragma unroll
-      for (int c = 0; c < kTcTile; ++c) acc[c] = 0.f;
-    }
-    int jr = 0;  // next accumulator group to read back (warps 4-7)
-    auto readback = [&]() {
-      const int a = jr & 1;
-      if (!tc::mbar_wait_until(&sm.acc_full[a], (jr >> 1) & 1, deadline, err)) {
-        *err = 1;
-        return;
-      }
-      tc::fence_after_sync();
-#pragma unroll
-      for (int cc = 0; cc < kTcTile / 32; ++cc) {
-        if (32 * cc < ncols) {
-          uint32_t v[32];
-          tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * kTcTile + 32 * cc), v);
-          tc::tmem_wait_ld();
-#pragma unroll
-          for (int k = 0; k < 32; ++k) acc[32 * cc + k] += __uint_as_float(v[k]);
-        }
-      }
-      tc::fence_before_sync();
-      tc::mbar_arrive(&sm.acc_empty[a]);
-      ++jr;
-    };
-    float gl = 0.f;  // this thread's share of g_L for tile row t (diagonal tiles)
+    float gl = 0.f;  // g_L of tile row tid (diagonal tiles)
     bool done = true;
     for (int i = 0; i < n; ++i) {
       const int r = i % kRawSlots, u = i / kRawSlots, o = i % kOpStages, uo = i / kOpStages;
@@ -246,7 +214,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
         sk[lane] = sv;
         if (diag) gs[lane] = lane < R.cnt ? R.ga[R.coff + lane] * sv : 0.f;
       }
-      named_sync(1, 256);
+      named_sync(1, 128);
       if (*err) {
         done = false;
         break;
@@ -254,26 +222,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
       const int n_eff = (i % kGroup == 0) ? ncols : min(ncols, ((R.s1 - col0 + 15) / 16) * 16);
       if (tid == 0) sm.op_ncols[o] = n_eff;
       OpStage &S = sm.op[o];
+      const int t = tid;  // tile row (and column row) of this thread
       {
         const int gr = row0 + t;
         const bool v = gr >= R.xr0 && gr < R.xr1;
-        gl += split_row(R.x + (size_t)(v ? gr - R.xr0 : 0) * kTcK, v, sk, diag ? gs : nullptr, t, S.xh, S.xl, mbeg);
+        gl += split_row(R.x + (size_t)(v ? gr - R.xr0 : 0) * kTcK, v, sk, diag ? gs : nullptr, t, S.xh, S.xl);
       }
       if (!diag && t < n_eff) {
         const int gc = col0 + t;
         const bool v = gc >= R.yr0 && gc < R.yr1;
-        (void)split_row(R.y + (size_t)(v ? gc - R.yr0 : 0) * kTcK, v, sk, nullptr, t, S.yh, S.yl, mbeg);
+        (void)split_row(R.y + (size_t)(v ? gc - R.yr0 : 0) * kTcK, v, sk, nullptr, t, S.yh, S.yl);
       }
       tc::fence_proxy_async();
       tc::mbar_arrive(&sm.op_full[o]);
       tc::mbar_arrive(&sm.raw_empty[r]);
-      // the group before this chunk's is complete once this chunk could be issued
-      if (accw && i % kGroup == 0 && i >= kGroup) readback();
     }
-    if (accw)
-      while (jr < ngroups && !*err) readback();
-    if (diag && done && row0 + t < P && gl != 0.f)
-      red_add(reinterpret_cast<float *>(wv.gL) + pv.p_param_off[b] + row0 + t, gl);
+    if (diag && done && row0 + tid < P && gl != 0.f)
+      red_add(reinterpret_cast<float *>(wv.gL) + pv.p_param_off[b] + row0 + tid, gl);
   } else if (warp == 8) {
     // ---- MMA issue ----
     if (lane == 0) {
@@ -309,6 +274,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
       // every MMA issued has completed once this commit arrives
       tc::commit(&sm.fin);
       (void)tc::mbar_wait_until(&sm.fin, 0, deadline + kTimeoutNs, &sm.zero);
+    }
+  } else {
+    // ---- accumulator warps 4-7 ----
+    const int q = warp - 4;
+#pragma unroll
+    for (int c = 0; c < kTcTile; ++c) acc[c] = 0.f;
+    for (int j = 0; j < ngroups; ++j) {
+      const int a = j & 1;
+      if (!tc::mbar_wait_until(&sm.acc_full[a], (j >> 1) & 1, deadline, err)) {
+        *err = 1;
+        break;
+      }
+      tc::fence_after_sync();
+#pragma unroll
+      for (int cc = 0; cc < kTcTile / 32; ++cc) {
+        if (32 * cc < ncols) {
+          uint32_t v[32];
+          tc::tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * kTcTile + 32 * cc), v);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int k = 0; k < 32; ++k) acc[32 * cc + k] += __uint_as_float(v[k]);
+        }
+      }
+      tc::fence_before_sync();
+      tc::mbar_arrive(&sm.acc_empty[a]);
     }
   }
 
