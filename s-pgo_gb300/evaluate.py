@@ -1,0 +1,110 @@
+"""Evaluation harness: estimation-error metrics and the divergence-rate study.
+
+Metrics (the reference's, restated):
+- incremental-pose error: ||Log_SE3(inv(T_true) T_est)|| per incremental pose, summed
+  over the window (CUDAmanager.py:100-109, PythonUtils/Manager.py:76-80);
+- depth error: |1 / alpha_est - 1 / alpha_true| per landmark, summed
+  (PythonUtils/Manager.py:82-95).
+
+Divergence-rate study (ConvegenceTests.py:17-63): many seeded windows, each
+stepped with the reference's undamped Gauss-Newton `step(1)` (pose step size 0.5)
+for a number of steps, recording the summed pose error after every step; a run
+counts as diverged when its final error exceeds 0.5.  Here every trial of the
+study is one problem of a single batch, so one batched launch sequence steps all
+of them at once; `mode="lm"` runs the Nielsen LM iteration instead.
+
+    python s-pgo_gb300/evaluate.py [--trials 100] [--steps 50] [--mode gn|lm]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+import time
+from typing import Dict, List
+
+import numpy as np
+
+
+def _pkg():
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if repo not in sys.path:
+        sys.path.insert(0, repo)
+    import __graft_entry__
+    return __graft_entry__.load_package()
+
+
+def incremental_pose_errors(est: np.ndarray, true: np.ndarray) -> np.ndarray:
+    """||Log_SE3(inv(T_true) T_est)|| for each incremental pose ([N, 4, 4] each)."""
+    _pkg()
+    from spgo_gb300 import se3
+    return np.array([np.linalg.norm(se3.log_se3(se3.inv(t) @ e)) for e, t in zip(est, true)])
+
+
+def depth_errors(alpha_est: np.ndarray, alpha_true: np.ndarray) -> np.ndarray:
+    """|1 / alpha_est - 1 / alpha_true| per landmark."""
+    return np.abs(1.0 / np.asarray(alpha_est, np.float64) - 1.0 / np.asarray(alpha_true, np.float64))
+
+
+def convergence_study(trials: int = 100, steps: int = 50, n_poses: int = 10, landmarks_per_frame: int = 96,
+                      step_size: float = 0.5, seed: int = 0, mode: str = "gn", precision: str = "mixed",
+                      threshold: float = 0.5, device="cuda") -> Dict:
+    """Batched divergence-rate study; returns the error matrix [trials, steps], the
+    per-step wall time of the batched step, and the divergence rate."""
+    _pkg()
+    import torch
+    from spgo_gb300 import scenes
+    from spgo_gb300.solver import BatchSolver
+    rng = np.random.Generator(np.random.PCG64(seed))
+    seeds = rng.integers(0, 2**31 - 1, trials)
+    probs = [scenes.circle_scene(int(s), n_poses, n_poses * landmarks_per_frame, name=f"trial{t}")
+             for t, s in enumerate(seeds)]
+    bs = BatchSolver(probs, precision=precision, device=device)
+    if mode == "gn":
+        bs.set_params(loss="cauchy", loss_scale=3.0, near_boost=True, eps=1e-4)
+    else:
+        bs.set_params(loss="l2", max_iters=steps, tol=0.0, use_graph=0)
+        bs.reset()
+    errors = np.zeros((trials, steps))
+    depth = np.zeros(trials)
+    times = np.zeros(steps)
+    for k in range(steps):
+        torch.cuda.synchronize(bs.device)
+        t0 = time.perf_counter()
+        if mode == "gn":
+            bs.gn_step(1, step_size)
+        else:
+            bs.iterate(1)
+        torch.cuda.synchronize(bs.device)
+        times[k] = time.perf_counter() - t0
+        poses, alphas = bs.get_state()
+        for t, p in enumerate(probs):
+            errors[t, k] = incremental_pose_errors(poses[t], p.gt_poses).sum()
+            if k == steps - 1:
+                depth[t] = depth_errors(alphas[t], p.gt_alpha).sum()
+    bs.close()
+    diverged = errors[:, -1] > threshold
+    return {"errors": errors, "step_seconds": times, "depth_error_sum": depth, "diverged": diverged,
+            "divergence_rate": float(diverged.mean())}
+
+
+def main(argv: List[str] | None = None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--trials", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--mode", choices=["gn", "lm"], default="gn")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args(argv)
+    r = convergence_study(args.trials, args.steps, mode=args.mode, precision=args.precision, seed=args.seed)
+    e = r["errors"]
+    print(json.dumps({"trials": args.trials, "steps": args.steps, "mode": args.mode, "precision": args.precision,
+                      "divergence_rate": r["divergence_rate"], "final_error_median": float(np.median(e[:, -1])),
+                      "first_error_median": float(np.median(e[:, 0])),
+                      "depth_error_sum_median": float(np.median(r["depth_error_sum"])),
+                      "ms_per_batched_step": float(1e3 * np.median(r["step_seconds"]))}))
+
+
+if __name__ == "__main__":
+    main()

@@ -42,6 +42,20 @@ def log_so3(R):
     return th * axis
 
 
+def log_se3(T):
+    """Twist (psi, rho) with Exp_SE3(psi, rho) = T: rho = J_l(psi)^-1 t."""
+    T = np.asarray(T, dtype=np.float64)
+    psi = log_so3(T[:3, :3])
+    th = float(np.linalg.norm(psi))
+    S = skew(psi)
+    if th < 1e-4:
+        c = 1.0 / 12.0 + th * th / 720.0
+    else:
+        c = (1.0 - th * np.sin(th) / (2.0 * (1.0 - np.cos(th)))) / (th * th)
+    Jinv = np.eye(3) - 0.5 * S + c * (S @ S)
+    return np.concatenate([psi, Jinv @ T[:3, 3]])
+
+
 def inv(T):
     T = np.asarray(T, dtype=np.float64)
     Ti = np.zeros_like(T)

@@ -327,3 +327,14 @@ def test_large_system_path_matches_oracle(built_lib, cuda_device, prec, tol):
     st = bs.solve()[0]
     res = S.lm_solve(big.copy(), S.Loss(), max_iters=8, tol=1e-9)
     assert abs(st["cost"] - res.cost) / res.cost < 1e-6
+
+
+def test_divergence_study_runs_batched(built_lib, cuda_device):
+    """The divergence-rate study (the reference's convergence test) as one batch:
+    errors recorded per step, GN steps reduce the median pose error."""
+    from spgo_gb300 import evaluate
+    r = evaluate.convergence_study(trials=12, steps=8, seed=5)
+    e = r["errors"]
+    assert e.shape == (12, 8) and np.isfinite(e).all()
+    assert np.median(e[:, -1]) < np.median(e[:, 0])
+    assert 0.0 <= r["divergence_rate"] <= 1.0

@@ -56,3 +56,22 @@ def test_cudasolver_staging_matches_reference_layout():
     p.validate()
     assert p.n_landmarks == 6 and list(p.host) == [0, 0, 1, 1, 2, 2]
     assert np.allclose(p.anchor_uv[3], s.getObservation(1, 3)[0][:2, 0])
+
+
+def test_evaluation_metrics():
+    """Pose error = ||Log_SE3(inv(T_true) T_est)|| (the reference's metric) and the
+    summed depth error, on known perturbations."""
+    from spgo_gb300 import evaluate, se3
+    from oracle import lie
+    rng = np.random.default_rng(3)
+    true = np.stack([lie.exp_se3(rng.normal(0, 0.3, 6)) for _ in range(4)])
+    xis = rng.normal(0, 0.05, (4, 6))
+    est = np.stack([t @ lie.exp_se3(x) for t, x in zip(true, xis)])
+    e = evaluate.incremental_pose_errors(est, true)
+    assert np.allclose(e, np.linalg.norm(xis, axis=1), rtol=1e-9, atol=1e-12)
+    assert np.allclose(evaluate.incremental_pose_errors(true, true), 0.0, atol=1e-12)
+    a = np.array([0.5, 0.25, 0.1])
+    assert np.allclose(evaluate.depth_errors(a, a * 2.0), [1.0, 2.0, 5.0])
+    for _ in range(5):
+        xi = rng.normal(0, 0.8, 6)
+        assert np.abs(se3.log_se3(lie.exp_se3(xi)) - xi).max() < 1e-12
