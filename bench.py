@@ -259,7 +259,10 @@ def run_ours(args):
         return s
 
     bs = make("mixed")
-    tuned = bs.autotune()  # launch shapes timed on this batch (untimed, before the warm-up)
+    if args.autotune:
+        tuned = bs.autotune()  # launch shapes timed on this batch (untimed, before the warm-up)
+    else:
+        tuned = dict(cost_block=bs.params.cost_block, lin_block=bs.params.lin_block, use_tc=bs.params.use_tc)
     p0, a0 = bs.poses.clone(), bs.alpha.clone()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
@@ -409,6 +412,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--tc", type=int, default=1, help="1: tensor-core Schur complement in the mixed path, 0: SIMT")
     ap.add_argument("--controller", type=int, default=1, help="1: learned damping (shipped weights), 0: Nielsen")
+    ap.add_argument("--autotune", type=int, default=1, help="1: time the run-time launch shapes first")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
