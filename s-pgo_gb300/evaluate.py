@@ -11,9 +11,13 @@ stepped with the reference's undamped Gauss-Newton `step(1)` (pose step size 0.5
 for a number of steps, recording the summed pose error after every step; a run
 counts as diverged when its final error exceeds 0.5.  Here every trial of the
 study is one problem of a single batch, so one batched launch sequence steps all
-of them at once; `mode="lm"` runs the Nielsen LM iteration instead.
+of them at once; `mode="lm"` runs the Nielsen LM iteration instead.  The windows
+come from the reference's own scene distribution (`scene="reference"`:
+`scenes.reference_scene`, identity initial poses, inverse depth 1, noise-free
+pixels, as the reference feeder sets them up) or from the project's circle scenes
+(`scene="circle"`: 1 px noise, perturbed ground truth).
 
-    python s-pgo_gb300/evaluate.py [--trials 100] [--steps 50] [--mode gn|lm]
+    python s-pgo_gb300/evaluate.py [--trials 100] [--steps 50] [--mode gn|lm] [--scene reference|circle]
 """
 from __future__ import annotations
 
@@ -49,7 +53,7 @@ def depth_errors(alpha_est: np.ndarray, alpha_true: np.ndarray) -> np.ndarray:
 
 def convergence_study(trials: int = 100, steps: int = 50, n_poses: int = 10, landmarks_per_frame: int = 96,
                       step_size: float = 0.5, seed: int = 0, mode: str = "gn", precision: str = "mixed",
-                      threshold: float = 0.5, device="cuda") -> Dict:
+                      threshold: float = 0.5, scene: str = "reference", device="cuda") -> Dict:
     """Batched divergence-rate study; returns the error matrix [trials, steps], the
     per-step wall time of the batched step, and the divergence rate."""
     _pkg()
@@ -58,8 +62,14 @@ def convergence_study(trials: int = 100, steps: int = 50, n_poses: int = 10, lan
     from spgo_gb300.solver import BatchSolver
     rng = np.random.Generator(np.random.PCG64(seed))
     seeds = rng.integers(0, 2**31 - 1, trials)
-    probs = [scenes.circle_scene(int(s), n_poses, n_poses * landmarks_per_frame, name=f"trial{t}")
-             for t, s in enumerate(seeds)]
+    if scene == "reference":
+        probs = [scenes.reference_scene(int(s), n_poses, landmarks_per_frame, name=f"trial{t}")
+                 for t, s in enumerate(seeds)]
+    elif scene == "circle":
+        probs = [scenes.circle_scene(int(s), n_poses, n_poses * landmarks_per_frame, name=f"trial{t}")
+                 for t, s in enumerate(seeds)]
+    else:
+        raise ValueError(f"unknown scene {scene!r}")
     bs = BatchSolver(probs, precision=precision, device=device)
     if mode == "gn":
         bs.set_params(loss="cauchy", loss_scale=3.0, near_boost=True, eps=1e-4)
@@ -96,10 +106,13 @@ def main(argv: List[str] | None = None):
     ap.add_argument("--mode", choices=["gn", "lm"], default="gn")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--scene", choices=["reference", "circle"], default="reference")
     args = ap.parse_args(argv)
-    r = convergence_study(args.trials, args.steps, mode=args.mode, precision=args.precision, seed=args.seed)
+    r = convergence_study(args.trials, args.steps, mode=args.mode, precision=args.precision, seed=args.seed,
+                          scene=args.scene)
     e = r["errors"]
     print(json.dumps({"trials": args.trials, "steps": args.steps, "mode": args.mode, "precision": args.precision,
+                      "scene": args.scene,
                       "divergence_rate": r["divergence_rate"], "final_error_median": float(np.median(e[:, -1])),
                       "first_error_median": float(np.median(e[:, 0])),
                       "depth_error_sum_median": float(np.median(r["depth_error_sum"])),

@@ -230,3 +230,157 @@ def config3(seed: int = 3, n_problems: int = 256):
     seeds = rng.integers(0, 2**31 - 1, n_problems)
     return [circle_scene(int(s), int(n), int(l), name=f"config3[{i}]")
             for i, (n, l, s) in enumerate(zip(Ns, Ls, seeds))]
+
+
+# ---------------------------------------------------------------------------
+# The reference's own scene distribution, restated with a seeded generator.
+# ---------------------------------------------------------------------------
+
+REF_WIDTH, REF_HEIGHT = 640.0, 512.0
+REF_INTR = np.array([320.0, 320.0, 320.0, 240.0, 320.0, 320.0, 320.0, 240.0])
+REF_BASELINE_M = 0.2
+REF_MIN_DEPTH = 0.2
+
+
+def reference_camera_poses(rng, n_frames: int, axis_draw=None) -> np.ndarray:
+    """Camera-to-world poses of ``SamplePoses.create_samples`` (PythonUtils/utils.py:19-80).
+
+    A random walk on a sphere: the polar and azimuth angles each grow by
+    U(0, 20 deg) per frame, the radius is U(2.5, 3.5) and each position component
+    is scaled by U(0.9, 1.1).  The camera looks at the origin (columns right,
+    up, forward; the up hint is (U(0, 0.2), U(0, 0.2), 1)), then a 10 deg
+    orientation noise about a random axis is applied the way the reference does
+    it: the axis-angle rotation acts on the quaternion's vector part
+    (``pp.SO3 * tensor`` is a point action on the homogeneous 4-vector), which
+    turns R into Rn R Rn^T.
+
+    ``rng`` needs ``uniform`` and ``normal``; the uniform draws come in the
+    reference's order, so ``numpy.random.RandomState(s)`` reproduces the
+    reference's stream after ``numpy.random.seed(s)``.  ``axis_draw()`` returns
+    the noise axis (the reference draws it from torch's generator); the default
+    is ``rng.normal(size=3)``."""
+    W = np.zeros((n_frames, 4, 4))
+    theta = phi = 0.0
+    for k in range(n_frames):
+        r = rng.uniform(2.5, 3.5)
+        theta += abs(rng.uniform(0.0, 20.0) * np.pi / 180.0)
+        phi += abs(rng.uniform(0.0, 20.0) * np.pi / 180.0)
+        sx = rng.uniform(0.9, 1.1)
+        sy = rng.uniform(0.9, 1.1)
+        sz = rng.uniform(0.9, 1.1)
+        pos = np.array([r * np.sin(phi) * np.cos(theta) * sx, r * np.sin(phi) * np.sin(theta) * sy,
+                        r * np.cos(phi) * sz])
+        fwd = -pos / np.linalg.norm(pos)
+        ux = rng.uniform(0.0, 0.2)
+        uy = rng.uniform(0.0, 0.2)
+        up = np.array([ux, uy, 1.0])
+        up /= np.linalg.norm(up)
+        right = np.cross(up, fwd)
+        right /= np.linalg.norm(right)
+        up = np.cross(fwd, right)
+        R = np.stack([right, up, fwd], 1)
+        axis = np.asarray(axis_draw() if axis_draw is not None else rng.normal(size=3), np.float64)
+        axis /= np.linalg.norm(axis)
+        Rn = se3.exp_so3((10.0 * np.pi / 180.0) * axis)
+        W[k] = np.eye(4)
+        W[k, :3, :3] = Rn @ R @ Rn.T
+        W[k, :3, 3] = pos
+    return W
+
+
+def reference_points(rng, m: int) -> np.ndarray:
+    """``get_point_samples`` (PythonUtils/utils.py:133-152): per point a radius
+    U(0, 2.5), then a uniform direction (azimuth U(0, 2 pi), cos(polar) U(-1, 1)),
+    drawn in the reference's order."""
+    pts = np.zeros((m, 3))
+    for l in range(m):
+        r = rng.uniform(0.0, 2.5)
+        az = rng.uniform(0.0, 2.0 * np.pi)
+        pol = np.arccos(rng.uniform(-1.0, 1.0))
+        pts[l] = r * np.array([np.sin(pol) * np.cos(az), np.sin(pol) * np.sin(az), np.cos(pol)])
+    return pts
+
+
+def reference_scene(seed: int, n_poses: int = 10, landmarks_per_frame: int = 96, pixel_noise: float = 0.0,
+                    name: str = "") -> Problem:
+    """One window of the reference's divergence study (``CUDAmanager.Manager(n, m)``):
+    ``Simulator(n + 1 frames, n * m landmarks)`` (PythonUtils/Simulator.py:12-35) with
+    every draw from ``numpy.random.Generator(PCG64(seed))``; see
+    ``reference_scene_from`` for the observation and initial-state rules."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    N = int(n_poses)
+    W = reference_camera_poses(rng, N + 1)
+    pts = reference_points(rng, N * int(landmarks_per_frame))
+    return reference_scene_from(W, pts, noise_rng=rng if pixel_noise > 0 else None, pixel_noise=pixel_noise,
+                                name=name or f"reference(N={N},m={landmarks_per_frame},seed={seed})")
+
+
+def reference_scene_from(W: np.ndarray, pts: np.ndarray, noise_rng=None, pixel_noise: float = 0.0,
+                         name: str = "") -> Problem:
+    """The reference feeder's problem for camera-to-world poses ``W`` [N+1, 4, 4] and
+    world points ``pts`` [M, 3].
+
+    - StereoSetup (PythonUtils/StereoSetup.py:8-35): fx = fy = 320, cx = 320,
+      cy = 240, 640x512, right camera 0.2 m along +x (camera-to-world W T_r_l).
+    - An observation is valid when depth >= 0.2 m, u <= 640 and v <= 512 (no lower
+      bound on u, v: Simulator.py:53-57), and is fed only when valid in both
+      cameras (CUDAmanager.py:69-79).
+    - Landmark l is anchored in frame ``map_value_to_index(l, M, N)`` and fed for
+      every frame from its anchor to N (CUDAmanager.py:71-73).
+    - The anchor pixel is what the reference kernel reads from its observation
+      tensor (Solver_cuda.cu:147): the anchor frame's left observation when it was
+      fed, else the tensor's initial (0, 0) (include/Solver.hpp:33).
+    - The feeder passes the noise-free projections (``simulator.observations``);
+      ``pixel_noise`` > 0 adds N(0, pixel_noise) from ``noise_rng`` instead, as the
+      simulator's noisy copy does (std 2 px there).
+    - Initial state: identity incremental poses and inverse depth 1 (the CUDA
+      solver's initial tensors, include/Solver.hpp:36-44).
+    """
+    W = np.asarray(W, np.float64)
+    pts = np.asarray(pts, np.float64)
+    F = W.shape[0]
+    N = F - 1
+    M = pts.shape[0]
+    T_rl = np.eye(4)
+    T_rl[0, 3] = REF_BASELINE_M
+    # general inverses, as the reference takes them (its poses come out of float32
+    # and are orthonormal only to float32 rounding)
+    Tcw_l = np.linalg.inv(W)
+    Tcw_r = np.linalg.inv(np.einsum('fij,jk->fik', W, T_rl))
+    K = REF_INTR
+
+    def project(Tcw, fx, fy, cx, cy):
+        pc = np.einsum('fij,lj->lfi', Tcw[:, :3, :3], pts) + Tcw[None, :, :3, 3]
+        z = pc[..., 2]
+        return fx * pc[..., 0] / z + cx, fy * pc[..., 1] / z + cy, z
+
+    ul, vl, zl = project(Tcw_l, *K[:4])
+    ur, vr, zr = project(Tcw_r, *K[4:])
+    ok_l = (zl >= REF_MIN_DEPTH) & (ul <= REF_WIDTH) & (vl <= REF_HEIGHT)
+    ok_r = (zr >= REF_MIN_DEPTH) & (ur <= REF_WIDTH) & (vr <= REF_HEIGHT)
+    uv = np.stack([ul, vl, ur, vr], -1)                      # [M, F, 4]
+    if pixel_noise > 0:
+        uv = uv + noise_rng.normal(0.0, pixel_noise, uv.shape)
+    host = np.array([anchor_frame(l, M, N) for l in range(M)], np.int64)
+    fed = ok_l & ok_r & (np.arange(F)[None, :] >= host[:, None])
+    cnt = fed.sum(1)
+    obs_ptr = np.zeros(M + 1, np.int64)
+    obs_ptr[1:] = np.cumsum(cnt)
+    lm_of, fr_of = np.nonzero(fed)                            # landmark-major, frames ascending
+    obs_frame = fr_of.astype(np.int32)
+    obs_uv = uv[lm_of, fr_of].astype(np.float64)
+    li = np.arange(M)
+    anchor_uv = np.where(fed[li, host][:, None], uv[li, host, :2], 0.0)
+    gt_inc = np.stack([np.linalg.inv(W[k + 1]) @ W[k] for k in range(N)])   # Simulator.py:67-78
+    gt_alpha = 1.0 / zl[li, host]
+    return Problem(n_poses=N, intrinsics=K.copy(), T_rl=T_rl, host=host.astype(np.int32),
+                   anchor_uv=anchor_uv, obs_ptr=obs_ptr, obs_frame=obs_frame, obs_uv=obs_uv,
+                   poses=np.broadcast_to(np.eye(4), (N, 4, 4)).copy(), alpha=np.ones(M),
+                   gt_poses=gt_inc, gt_alpha=gt_alpha, name=name)
+
+
+def anchor_frame(v: int, x: int, n: int) -> int:
+    """``map_value_to_index`` (PythonUtils/Optimizer.py:12-18): value v of [0, x] to a
+    frame index in [0, n - 1]."""
+    vc = max(0, min(v, x))
+    return min(int((vc / x) * n), n - 1)

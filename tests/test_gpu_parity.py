@@ -329,11 +329,35 @@ def test_large_system_path_matches_oracle(built_lib, cuda_device, prec, tol):
     assert abs(st["cost"] - res.cost) / res.cost < 1e-6
 
 
-def test_divergence_study_runs_batched(built_lib, cuda_device):
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 2e-4)])
+def test_gn_step_on_reference_scene(built_lib, cuda_device, prec, tol):
+    """A window of the reference's own scene distribution (identity start, inverse
+    depth 1, noise-free pixels, (0, 0) anchor pixels where the anchor observation was
+    not fed), plus one landmark with no observation at all, stepped as the
+    reference's study steps it, against the oracle."""
+    p = f32_obs(scenes.reference_scene(11, n_poses=10, landmarks_per_frame=96))
+    cnt = np.diff(p.obs_ptr)
+    keep = np.ones(p.n_obs, bool)
+    keep[p.obs_ptr[5]:p.obs_ptr[6]] = False
+    cnt[5] = 0
+    p.obs_frame, p.obs_uv, p.obs_ptr = p.obs_frame[keep], p.obs_uv[keep], np.r_[0, np.cumsum(cnt)]
+    assert np.any(np.all(p.anchor_uv == 0.0, axis=1))
+    ref = p.copy()
+    S.reference_gn_step(ref, iterations=3, step_size=0.5)
+    bs = BatchSolver([p], precision=prec)
+    bs.set_params(loss="cauchy", loss_scale=3.0, near_boost=True, eps=1e-4)
+    bs.gn_step(3, 0.5)
+    assert np.abs(bs.get_poses(0) - ref.poses).max() < tol
+    assert relmax(bs.get_alpha(0), ref.alpha) < tol
+    assert bs.get_alpha(0)[5] == 1.0
+
+
+@pytest.mark.parametrize("scene", ["reference", "circle"])
+def test_divergence_study_runs_batched(built_lib, cuda_device, scene):
     """The divergence-rate study (the reference's convergence test) as one batch:
     errors recorded per step, GN steps reduce the median pose error."""
     from spgo_gb300 import evaluate
-    r = evaluate.convergence_study(trials=12, steps=8, seed=5)
+    r = evaluate.convergence_study(trials=12, steps=8, seed=5, scene=scene)
     e = r["errors"]
     assert e.shape == (12, 8) and np.isfinite(e).all()
     assert np.median(e[:, -1]) < np.median(e[:, 0])
