@@ -77,6 +77,11 @@ typedef struct spgo_host_problem {
     const int64_t *obs_ptr;      /* [L+1]                                     */
     const int32_t *obs_frame;    /* [O]                                       */
     const float   *obs_uv;       /* [O*4] uL, vL, uR, vR                      */
+    /* Optional FP64 pixels: when non-null they are read instead of anchor_uv /
+     * obs_uv (which may then be null) and rounded to float as the plan is built,
+     * so a caller holding double pixels needs no conversion pass of its own. */
+    const double  *anchor_uv_f64; /* [L*2] or NULL */
+    const double  *obs_uv_f64;    /* [O*4] or NULL */
 } spgo_host_problem;
 
 /* sizes a plan needs (bytes unless noted) */

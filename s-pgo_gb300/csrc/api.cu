@@ -14,6 +14,9 @@
 #include <array>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <mutex>
+#include <cstdlib>
 #include <numeric>
 #include <thread>
 #include <atomic>
@@ -51,8 +54,76 @@ static int fail(int code, const std::string &msg) {
 struct Seg {
   size_t off;
   size_t bytes;
-  const void *src;
 };
+
+// ---- page-locked host staging, reused across plans ----------------------------
+// A plan's static data (every array the kernels read) is written straight into
+// host blocks laid out like the device buffer, so the upload is two DMA copies
+// from page-locked memory.  Blocks come from a small process-wide cache: a caller
+// that plans batch after batch reuses the same locked pages (no page faults, no
+// re-locking).  Without a CUDA device the blocks are ordinary heap memory.
+struct HostBlock {
+  unsigned char *ptr = nullptr;
+  size_t cap = 0;
+  bool pinned = false;
+};
+
+static std::mutex g_arena_mu;
+static std::vector<HostBlock> g_arena_free;
+constexpr size_t kArenaKeep = 6;              // cached blocks at most
+constexpr size_t kArenaKeepBytes = 2ull << 30;  // and bytes at most
+
+static void block_free(HostBlock &b) {
+  if (!b.ptr) return;
+  if (b.pinned)
+    cudaFreeHost(b.ptr);
+  else
+    std::free(b.ptr);
+  b = HostBlock();
+}
+
+static HostBlock arena_get(size_t bytes) {
+  bytes = std::max<size_t>(bytes, 256);
+  {
+    std::lock_guard<std::mutex> lk(g_arena_mu);
+    size_t best = g_arena_free.size();
+    for (size_t i = 0; i < g_arena_free.size(); ++i) {
+      const size_t c = g_arena_free[i].cap;
+      if (c >= bytes && c <= 2 * bytes && (best == g_arena_free.size() || c < g_arena_free[best].cap)) best = i;
+    }
+    if (best < g_arena_free.size()) {
+      HostBlock b = g_arena_free[best];
+      g_arena_free.erase(g_arena_free.begin() + (std::ptrdiff_t)best);
+      return b;
+    }
+  }
+  HostBlock b;
+  b.cap = (bytes + (1u << 20) - 1) & ~(size_t)((1u << 20) - 1);
+  void *q = nullptr;
+  if (cudaHostAlloc(&q, b.cap, cudaHostAllocPortable) == cudaSuccess) {  // locked for every context
+    b.ptr = (unsigned char *)q;
+    b.pinned = true;
+  } else {
+    cudaGetLastError();  // no device (planning on a CPU-only host): not an error of this library
+    b.ptr = (unsigned char *)std::malloc(b.cap);
+    if (!b.ptr) throw std::runtime_error("host allocation of " + std::to_string(b.cap) + " bytes failed");
+  }
+  return b;
+}
+
+static void arena_put(HostBlock &b) {
+  if (!b.ptr) return;
+  std::lock_guard<std::mutex> lk(g_arena_mu);
+  g_arena_free.push_back(b);
+  b = HostBlock();
+  size_t total = 0;
+  for (const HostBlock &x : g_arena_free) total += x.cap;
+  while (g_arena_free.size() > kArenaKeep || (total > kArenaKeepBytes && g_arena_free.size() > 1)) {
+    total -= g_arena_free.front().cap;  // the oldest goes
+    block_free(g_arena_free.front());
+    g_arena_free.erase(g_arena_free.begin());
+  }
+}
 
 struct spgo_plan {
   int32_t precision = SPGO_PREC_MIXED;
@@ -67,12 +138,17 @@ struct spgo_plan {
   std::vector<int64_t> p_S_off, p_pair_off, p_nres;
   std::vector<float> p_intr;
   std::vector<double> p_Trl;
-  std::vector<int32_t> lm_prob, lm_host, lm_lo, lm_hi, lm_user, lm_chunk, lm_slot;
-  std::vector<float> lm_uv;
-  std::vector<int64_t> lm_obs;
-  std::vector<int32_t> obs_frame;
-  std::vector<float> obs_uv;
-  std::vector<uint8_t> obs_slot;
+  // per-landmark and per-observation arrays: written by the planner directly into
+  // the big block, at their offsets in the device buffer
+  int32_t *lm_prob = nullptr, *lm_host = nullptr, *lm_lo = nullptr, *lm_hi = nullptr, *lm_user = nullptr,
+          *lm_chunk = nullptr, *lm_slot = nullptr;
+  float *lm_uv = nullptr;
+  int64_t *lm_obs = nullptr;
+  int32_t *obs_frame = nullptr;
+  float *obs_uv = nullptr;
+  uint8_t *obs_slot = nullptr;
+  size_t off_lm[7] = {}, off_lm_uv = 0, off_lm_obs = 0, off_obs_frame = 0, off_obs_uv = 0, off_obs_slot = 0;
+  size_t big_bytes = 0;
   std::vector<int32_t> ch_prob, ch_f0, ch_nb, ch_lm0, ch_cnt;
   std::vector<int64_t> ch_slab;
   std::vector<int32_t> wk_prob, wk_ti, wk_tj, wk_cbeg, wk_cend, wk_chunks;
@@ -80,41 +156,105 @@ struct spgo_plan {
   std::vector<int32_t> tc_prob, tc_row0, tc_col0, tc_ncols, tc_cbeg, tc_cend, tc_chunks;
   std::vector<Seg> segs;
   size_t static_bytes = 0, ws_bytes = 0;
+  // host staging: [0, big_bytes) of the device buffer, then the small arrays
+  HostBlock big, small;
+  mutable cudaEvent_t uploaded = nullptr;  // the last upload from the blocks
   // workspace segment offsets
   size_t w_Sx = 0, w_lg = 0;
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl;
+
+  ~spgo_plan() {
+    if (uploaded) {  // the blocks go back to the cache only once no copy reads them
+      cudaEventSynchronize(uploaded);
+      cudaEventDestroy(uploaded);
+    }
+    arena_put(big);
+    arena_put(small);
+  }
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// a small array: packed after the big block (copied into the small block later)
 template <typename V>
 static void add_seg(spgo_plan *p, const V &v) {
   Seg s;
   s.off = p->static_bytes;
   s.bytes = v.size() * sizeof(typename V::value_type);
-  s.src = v.data();
   p->segs.push_back(s);
   p->static_bytes = align256(p->static_bytes + s.bytes);
 }
 
+// a big array at its fixed offset in the big block
+static void add_big(spgo_plan *p, size_t off, size_t bytes) {
+  Seg s;
+  s.off = off;
+  s.bytes = bytes;
+  p->segs.push_back(s);
+}
+
+// offsets of the per-landmark and per-observation arrays, then the big block
+static void layout_big(spgo_plan *p, int64_t Lt, int64_t Ot) {
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t r = o;
+    o = align256(o + bytes);
+    return r;
+  };
+  for (int k = 0; k < 7; ++k) p->off_lm[k] = take((size_t)Lt * 4);
+  p->off_lm_uv = take((size_t)Lt * 8);
+  p->off_lm_obs = take((size_t)(Lt + 1) * 8);
+  p->off_obs_frame = take((size_t)Ot * 4);
+  p->off_obs_uv = take((size_t)Ot * 16);
+  p->off_obs_slot = take((size_t)Ot);
+  p->big_bytes = o;
+  p->big = arena_get(o);
+  unsigned char *b = p->big.ptr;
+  int32_t **lm[7] = {&p->lm_prob, &p->lm_host, &p->lm_lo, &p->lm_hi, &p->lm_user, &p->lm_chunk, &p->lm_slot};
+  for (int k = 0; k < 7; ++k) *lm[k] = reinterpret_cast<int32_t *>(b + p->off_lm[k]);
+  p->lm_uv = reinterpret_cast<float *>(b + p->off_lm_uv);
+  p->lm_obs = reinterpret_cast<int64_t *>(b + p->off_lm_obs);
+  p->obs_frame = reinterpret_cast<int32_t *>(b + p->off_obs_frame);
+  p->obs_uv = reinterpret_cast<float *>(b + p->off_obs_uv);
+  p->obs_slot = reinterpret_cast<uint8_t *>(b + p->off_obs_slot);
+}
+
 static void build_layout(spgo_plan *p) {
   // static segments, in PlanView order (see make_views)
+  // static segments, in PlanView order (see make_views): the big arrays sit at their
+  // offsets in the big block, the small ones are packed after it
   p->segs.clear();
-  p->static_bytes = 0;
-  add_seg(p, p->p_npose); add_seg(p, p->p_frame_off); add_seg(p, p->p_pose_off); add_seg(p, p->p_lm_off);
-  add_seg(p, p->p_lm_cnt); add_seg(p, p->p_pair_D); add_seg(p, p->p_param_off); add_seg(p, p->p_chunk_off);
-  add_seg(p, p->p_chunk_cnt); add_seg(p, p->p_S_off); add_seg(p, p->p_pair_off); add_seg(p, p->p_nres);
-  add_seg(p, p->p_intr);
-  add_seg(p, p->p_Trl); add_seg(p, p->lm_prob); add_seg(p, p->lm_host); add_seg(p, p->lm_lo); add_seg(p, p->lm_hi);
-  add_seg(p, p->lm_user); add_seg(p, p->lm_chunk); add_seg(p, p->lm_slot); add_seg(p, p->lm_uv);
-  add_seg(p, p->lm_obs); add_seg(p, p->obs_frame); add_seg(p, p->obs_uv); add_seg(p, p->ch_prob);
-  add_seg(p, p->ch_f0); add_seg(p, p->ch_nb); add_seg(p, p->ch_lm0); add_seg(p, p->ch_cnt); add_seg(p, p->ch_slab);
-  add_seg(p, p->wk_prob); add_seg(p, p->wk_ti); add_seg(p, p->wk_tj); add_seg(p, p->wk_cbeg);
-  add_seg(p, p->wk_cend); add_seg(p, p->wk_chunks); add_seg(p, p->fr_prob); add_seg(p, p->pose_prob);
-  add_seg(p, p->obs_slot);
-  add_seg(p, p->tc_prob); add_seg(p, p->tc_row0); add_seg(p, p->tc_col0); add_seg(p, p->tc_ncols);
-  add_seg(p, p->tc_cbeg); add_seg(p, p->tc_cend); add_seg(p, p->tc_chunks);
+  p->static_bytes = p->big_bytes;
+  const int64_t Lt = p->L, Ot = p->O;
+  std::vector<const void *> small_src;
+  auto small = [&](const auto &v) {
+    add_seg(p, v);
+    small_src.push_back(v.data());
+  };
+  auto big = [&](size_t off, size_t bytes) {
+    add_big(p, off, bytes);
+    small_src.push_back(nullptr);
+  };
+  small(p->p_npose); small(p->p_frame_off); small(p->p_pose_off); small(p->p_lm_off);
+  small(p->p_lm_cnt); small(p->p_pair_D); small(p->p_param_off); small(p->p_chunk_off);
+  small(p->p_chunk_cnt); small(p->p_S_off); small(p->p_pair_off); small(p->p_nres);
+  small(p->p_intr);
+  small(p->p_Trl);
+  for (int k = 0; k < 7; ++k) big(p->off_lm[k], (size_t)Lt * 4);  // lm_prob .. lm_slot
+  big(p->off_lm_uv, (size_t)Lt * 8);
+  big(p->off_lm_obs, (size_t)(Lt + 1) * 8); big(p->off_obs_frame, (size_t)Ot * 4); big(p->off_obs_uv, (size_t)Ot * 16);
+  small(p->ch_prob);
+  small(p->ch_f0); small(p->ch_nb); small(p->ch_lm0); small(p->ch_cnt); small(p->ch_slab);
+  small(p->wk_prob); small(p->wk_ti); small(p->wk_tj); small(p->wk_cbeg);
+  small(p->wk_cend); small(p->wk_chunks); small(p->fr_prob); small(p->pose_prob);
+  big(p->off_obs_slot, (size_t)Ot);
+  small(p->tc_prob); small(p->tc_row0); small(p->tc_col0); small(p->tc_ncols);
+  small(p->tc_cbeg); small(p->tc_cend); small(p->tc_chunks);
+  p->small = arena_get(p->static_bytes - p->big_bytes);
+  for (size_t i = 0; i < p->segs.size(); ++i)
+    if (small_src[i] && p->segs[i].bytes)
+      std::memcpy(p->small.ptr + (p->segs[i].off - p->big_bytes), small_src[i], p->segs[i].bytes);
   // workspace
   const size_t ts = p->precision == SPGO_PREC_FP64 ? 8 : 4;
   size_t o = 0;
@@ -235,7 +375,10 @@ static void plan_problem(const spgo_host_problem &q, int b, int64_t lm_base, int
         const size_t dst = (size_t)(obs_base + obs_local + fcount[(size_t)(n - f0)]++);
         p->obs_frame[dst] = n;
         p->obs_slot[dst] = slot;
-        std::memcpy(&p->obs_uv[4 * dst], q.obs_uv + 4 * ob, 4 * sizeof(float));
+        if (q.obs_uv_f64)
+          for (int j = 0; j < 4; ++j) p->obs_uv[4 * dst + j] = (float)q.obs_uv_f64[4 * ob + j];
+        else
+          std::memcpy(&p->obs_uv[4 * dst], q.obs_uv + 4 * ob, 4 * sizeof(float));
       }
     }
     obs_local += n_chunk;
@@ -272,8 +415,8 @@ static void plan_problem(const spgo_host_problem &q, int b, int64_t lm_base, int
     p->lm_user[li] = (int32_t)(lm_base + l);
     p->lm_chunk[li] = cur;  // problem-local until the merge
     p->lm_slot[li] = o.ch_cnt[cur] - 1;
-    p->lm_uv[2 * li] = q.anchor_uv[2 * l];
-    p->lm_uv[2 * li + 1] = q.anchor_uv[2 * l + 1];
+    p->lm_uv[2 * li] = q.anchor_uv_f64 ? (float)q.anchor_uv_f64[2 * l] : q.anchor_uv[2 * l];
+    p->lm_uv[2 * li + 1] = q.anchor_uv_f64 ? (float)q.anchor_uv_f64[2 * l + 1] : q.anchor_uv[2 * l + 1];
     p->lm_obs[li] = obs_base + obs_local;
   }
   close_chunk(L);
@@ -337,8 +480,8 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     const int N = q.n_poses, L = q.n_landmarks;
     if (N < 1) return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": n_poses < 1");
     if (L < 0 || q.n_obs < 0) return fail(SPGO_ERR_INVALID_ARG, "negative size");
-    if (!q.intrinsics || !q.T_r_to_l || (L > 0 && (!q.host || !q.anchor_uv || !q.obs_ptr)) ||
-        (q.n_obs > 0 && (!q.obs_frame || !q.obs_uv)))
+    if (!q.intrinsics || !q.T_r_to_l || (L > 0 && (!q.host || (!q.anchor_uv && !q.anchor_uv_f64) || !q.obs_ptr)) ||
+        (q.n_obs > 0 && (!q.obs_frame || (!q.obs_uv && !q.obs_uv_f64))))
       return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": null array");
     if (L > 0 && (q.obs_ptr[0] != 0 || q.obs_ptr[L] != q.n_obs))
       return fail(SPGO_ERR_INVALID_ARG, "problem " + std::to_string(b) + ": obs_ptr is not a CSR over n_obs");
@@ -348,17 +491,16 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
     obs_base[b + 1] = obs_base[b] + q.n_obs;
   }
   const int64_t Lt = lm_base[nprob], Ot = obs_base[nprob];
-  p->obs_frame.resize((size_t)Ot);
-  p->obs_slot.resize((size_t)Ot);
-  p->obs_uv.resize((size_t)Ot * 4);
-  for (auto *v : {&p->lm_prob, &p->lm_host, &p->lm_lo, &p->lm_hi, &p->lm_user, &p->lm_chunk, &p->lm_slot})
-    v->resize((size_t)Lt);
-  p->lm_uv.resize((size_t)Lt * 2);
-  p->lm_obs.resize((size_t)Lt + 1);
+  p->L = (int32_t)Lt;
+  p->O = Ot;
+  layout_big(p, Lt, Ot);
   std::vector<ProbPlan> pp((size_t)nprob);
   {
+    // up to 16 threads, leaving two cores to the threads that drive the GPU (a caller
+    // plans the next batch while the current one solves)
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int nthr = (int)std::min<unsigned>(std::min<unsigned>(hw, 16u), (unsigned)nprob);
+    const unsigned use = std::max(1u, std::min(hw, 16u) - std::min(hw - 1, 2u));
+    const int nthr = (int)std::min<unsigned>(use, (unsigned)nprob);
     std::atomic<int> next(0);
     auto work = [&]() {
       for (int b; (b = next.fetch_add(1)) < nprob;) plan_problem(probs[b], b, lm_base[b], obs_base[b], p, pp[b]);
@@ -619,8 +761,13 @@ static void make_views(spgo_solver *s) {
 // `stats`: refresh the controller's per-problem statistics; `ctrl`: let the learned
 // controller set lambda for the step about to be taken from the fresh linearisation
 template <typename T>
+constexpr int kF64 = std::is_same<T, double>::value ? 1 : 0;
+
+template <typename T>
 static int enqueue_linearize(spgo_solver *s, cudaStream_t st, bool stats, bool ctrl) {
-  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_RELIN, st)); }
+  // frame tables of the state: computed here at the first linearisation after a reset;
+  // later the accepted candidate's tables (its cost pass read them) are the state's
+  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_FIRST, kF64<T>, st)); }
   // the cost at the first linearisation point (later ones come from the cost pass that accepted them)
   { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 1, GATE_FIRST, st)); }
   { PROF(K_LINEARIZE); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 0, GATE_RELIN, st)); }
@@ -660,7 +807,7 @@ static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
   if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
   { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st)); }
   { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
-  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, st)); }
+  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, kF64<T>, st)); }
   { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st)); }
   {
     PROF(K_BOOKKEEP);
@@ -694,11 +841,13 @@ static int enqueue_probe(spgo_solver *s, int nf, const double *factors, cudaStre
     if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
     CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st));
     CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st));
-    CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, st));
+    CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, kF64<T>, st));
     CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st));
     CUDA_TRY(launch_take_probe(s->pv, s->wv, j, st));
   }
   CUDA_TRY(cudaMemcpyAsync(s->wv.lm, s->wv.lm_backup, sizeof(LMState) * s->plan->B, cudaMemcpyDeviceToDevice, st));
+  // the probes overwrote the frame tables: back to the state's
+  CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_RUNNING, kF64<T>, st));
   return SPGO_OK;
 }
 
@@ -802,14 +951,21 @@ int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_byte
   spgo_default_params(&dp);
   std::memcpy(&s->prm, &dp, sizeof(Params));
   cudaStream_t st = (cudaStream_t)stream;
-  for (const Seg &g : plan->segs)
-    if (g.bytes) {
-      cudaError_t e = cudaMemcpyAsync(s->d_static + g.off, g.src, g.bytes, cudaMemcpyHostToDevice, st);
-      if (e != cudaSuccess) {
-        delete s;
-        return fail(SPGO_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
-      }
+  {  // two copies from the page-locked staging blocks; the event keeps the blocks
+     // out of the cache until the copies have read them
+    cudaError_t e = cudaSuccess;
+    if (plan->big_bytes)
+      e = cudaMemcpyAsync(s->d_static, plan->big.ptr, plan->big_bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && plan->static_bytes > plan->big_bytes)
+      e = cudaMemcpyAsync(s->d_static + plan->big_bytes, plan->small.ptr, plan->static_bytes - plan->big_bytes,
+                          cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !plan->uploaded) e = cudaEventCreateWithFlags(&plan->uploaded, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(plan->uploaded, st);
+    if (e != cudaSuccess) {
+      delete s;
+      return fail(SPGO_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
     }
+  }
   cudaError_t e = cudaMemsetAsync(s->d_ws, 0, plan->ws_bytes, st);
   if (e != cudaSuccess) {
     delete s;

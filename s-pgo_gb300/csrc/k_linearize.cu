@@ -146,8 +146,11 @@ struct LinLayout {
 // pixel-sized FP32 quantities (whose ~3e-5 px rounding would move the optimum
 // by ~1e-5 m), and it takes the cost from that pass too; only the camera-frame
 // point for the Jacobian is formed there (double-float, without the projection).
+// Register caps (FP32 path): 64 for the cost pass, a latency-bound stream over the
+// observations that runs in small CTAs and gains from the extra resident warps
+// (16 instead of 12 64-thread CTAs per SM); 85 for the Jacobian pass.
 template <typename T, bool COST>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanView pv, WorkView wv, Params prm,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_linearize(PlanView pv, WorkView wv, Params prm,
                                                    const double *__restrict__ alpha_state, int gate) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
@@ -478,8 +481,101 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_linearize(PlanV
   }
 }
 
-int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, void *stream) {
-  k_chain<<<pv.B, 32, 0, (cudaStream_t)stream>>>(pv, wv, poses, gate);  // one warp (and SM slot) per problem
+// ---- the FP32 path's pose chain in double-float ----
+// The same scan with 3x4 products in double-float (~48 significant bits, the
+// precision of the FP32 path's frame tables: fr_Rf + fr_Rl, fr_ch + fr_cl), on the
+// FP32 pipes instead of FP64 (which runs at a small fraction of their rate on
+// this GPU).  Writes only the tables the FP32 kernels read.
+__device__ __forceinline__ void compose34_df(const df *A, const df *B, df *C) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      df v = df_dot3(A[4 * i].h, A[4 * i].l, A[4 * i + 1].h, A[4 * i + 1].l, A[4 * i + 2].h, A[4 * i + 2].l,
+                     B[j], B[4 + j], B[8 + j]);
+      if (j == 3) v = v + A[4 * i + 3];
+      C[4 * i + j] = v;
+    }
+  }
+}
+
+__device__ __forceinline__ void write_frame_df(const WorkView &wv, size_t f, const df *G, const df *Trl) {
+  df Gr[12];
+  compose34_df(G, Trl, Gr);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      wv.fr_Rf[f * 18 + 3 * i + j] = G[4 * i + j].h;
+      wv.fr_Rf[f * 18 + 9 + 3 * i + j] = Gr[4 * i + j].h;
+      wv.fr_Rl[f * 18 + 3 * i + j] = G[4 * i + j].l;
+      wv.fr_Rl[f * 18 + 9 + 3 * i + j] = Gr[4 * i + j].l;
+    }
+    wv.fr_ch[f * 6 + i] = G[4 * i + 3].h;
+    wv.fr_ch[f * 6 + 3 + i] = Gr[4 * i + 3].h;
+    wv.fr_cl[f * 6 + i] = G[4 * i + 3].l;
+    wv.fr_cl[f * 6 + 3 + i] = Gr[4 * i + 3].l;
+  }
+}
+
+__global__ void k_chain_df(PlanView pv, WorkView wv, const double *__restrict__ poses, int gate) {
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= pv.B) return;
+  if (!problem_active(wv.lm, b, gate)) return;
+  const int N = pv.p_npose[b], fo = pv.p_frame_off[b], po = pv.p_pose_off[b];
+  df Trl[12], carry[12];
+#pragma unroll
+  for (int q = 0; q < 12; ++q) {
+    Trl[q] = df_from_double(pv.p_Trl[12 * b + q]);
+    carry[q] = df_make((q == 0 || q == 5 || q == 10) ? 1.f : 0.f);
+  }
+  if (lane == 0) write_frame_df(wv, (size_t)fo, carry, Trl);
+  for (int s = 0; s < N; s += 32) {
+    const int k = s + lane;
+    df M[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) M[q] = df_make((q == 0 || q == 5 || q == 10) ? 1.f : 0.f);
+    if (k < N) {  // inverse of the incremental pose: [R^T, -R^T t]
+      const double *T = poses + 12 * (size_t)(po + k);
+      df Td[12];
+#pragma unroll
+      for (int q = 0; q < 12; ++q) Td[q] = df_from_double(T[q]);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) M[4 * i + j] = Td[4 * j + i];
+        M[4 * i + 3] = -df_dot3(Td[i].h, Td[i].l, Td[4 + i].h, Td[4 + i].l, Td[8 + i].h, Td[8 + i].l, Td[3], Td[7],
+                                Td[11]);
+      }
+    }
+    // inclusive scan: M_k <- M_0 M_1 ... M_k (earlier factors on the left)
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      df P[12];
+#pragma unroll
+      for (int q = 0; q < 12; ++q)
+        P[q] = df{__shfl_up_sync(0xffffffffu, M[q].h, d), __shfl_up_sync(0xffffffffu, M[q].l, d)};
+      if (lane >= d) {
+        df C[12];
+        compose34_df(P, M, C);
+#pragma unroll
+        for (int q = 0; q < 12; ++q) M[q] = C[q];
+      }
+    }
+    df G[12];
+    compose34_df(carry, M, G);
+    if (k < N) write_frame_df(wv, (size_t)(fo + k + 1), G, Trl);
+#pragma unroll
+    for (int q = 0; q < 12; ++q) carry[q] = df{__shfl_sync(0xffffffffu, G[q].h, 31), __shfl_sync(0xffffffffu, G[q].l, 31)};
+  }
+}
+
+int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, int f64, void *stream) {
+  if (f64)
+    k_chain<<<pv.B, 32, 0, (cudaStream_t)stream>>>(pv, wv, poses, gate);  // one warp (and SM slot) per problem
+  else
+    k_chain_df<<<pv.B, 32, 0, (cudaStream_t)stream>>>(pv, wv, poses, gate);
   ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -14,6 +14,9 @@
 #include <cuda_bf16.h>
 
 #include "kernels.cuh"
+#include "dfloat.cuh"
+
+#include <type_traits>
 
 namespace spgo {
 
@@ -227,25 +230,49 @@ __device__ __forceinline__ float feat_clip(double v) {
 }
 __device__ __forceinline__ double lg(double v) { return log10(fmax(v, 1e-300)); }
 
-// the controller's 16 inputs for problem b (see spgo_lm_features); each is finite
-// and clipped to [-40, 40]
-__device__ void lm_features(const PlanView &pv, const LMState &s, int b, float *f) {
+// The controller's 16 inputs for problem b (see spgo_lm_features), each finite and
+// clipped to [-40, 40], computed by one warp: the twelve logarithms they take
+// (FP64, which this GPU runs at a small fraction of its FP32 rate) are spread over
+// the lanes, one per lane, and broadcast; every lane then holds all 16 features.
+// log2(nu) comes out as log10(nu) / log10(2) rounded: nu is a power of two.
+__device__ void lm_features_warp(const PlanView &pv, const LMState &s, int b, float *f) {
+  const int lane = threadIdx.x & 31;
   const double nres = fmax(1.0, (double)pv.p_nres[b]);
-  f[0] = feat_clip(lg(s.cost) - log10(nres));
-  f[1] = feat_clip(lg(s.cost) - lg(s.cost0));
+  double arg = 1.0;
+  switch (lane) {
+    case 0: arg = fmax(s.cost, 1e-300); break;
+    case 1: arg = nres; break;
+    case 2: arg = fmax(s.cost0, 1e-300); break;
+    case 3: arg = fmax(s.lam, 1e-300); break;
+    case 4: arg = fmax(s.gnorm, 1e-300); break;
+    case 5: arg = fmax(s.dmean, 1e-300); break;
+    case 6: arg = fmax(s.dmax, 1e-300); break;
+    case 7: arg = fmax(s.dmin, 1e-300); break;
+    case 8: arg = fmax(s.cmean, 1e-300); break;
+    case 9: arg = fmax(s.last_rel, 1e-12); break;
+    case 10: arg = fmax(s.last_predrel, 1e-16); break;
+    case 11: arg = fmax(s.nu, 1.0); break;
+    default: break;
+  }
+  const double mine = log10(arg);
+  double Lg[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) Lg[k] = __shfl_sync(0xffffffffu, mine, k);
+  f[0] = feat_clip(Lg[0] - Lg[1]);
+  f[1] = feat_clip(Lg[0] - Lg[2]);
   f[2] = feat_clip(fmin(2.0, fmax(-2.0, s.rho1)));
   f[3] = feat_clip(fmin(2.0, fmax(-2.0, s.rho2)));
   f[4] = feat_clip(fmin(2.0, fmax(-2.0, s.rho3)));
-  f[5] = feat_clip(lg(s.lam));
-  f[6] = feat_clip(lg(s.gnorm) - 0.5 * lg(s.dmean));
-  f[7] = feat_clip(lg(s.dmean) - log10(nres));
-  f[8] = feat_clip(lg(s.dmax) - lg(s.dmin));
-  f[9] = feat_clip(lg(s.cmean));
+  f[5] = feat_clip(Lg[3]);
+  f[6] = feat_clip(Lg[4] - 0.5 * Lg[5]);
+  f[7] = feat_clip(Lg[5] - Lg[1]);
+  f[8] = feat_clip(Lg[6] - Lg[7]);
+  f[9] = feat_clip(Lg[8]);
   f[10] = feat_clip((double)s.iters / 30.0);
   f[11] = feat_clip((double)s.last_acc);
-  f[12] = feat_clip(log10(fmax(s.last_rel, 1e-12)));
-  f[13] = feat_clip(log10(fmax(s.last_predrel, 1e-16)));
-  f[14] = feat_clip(log2(fmax(s.nu, 1.0)));
+  f[12] = feat_clip(Lg[9]);
+  f[13] = feat_clip(Lg[10]);
+  f[14] = feat_clip(rint(Lg[11] / 0.30102999566398120));  // log2 of a power of two
   f[15] = feat_clip((double)s.rej_streak / 5.0);
 }
 
@@ -265,19 +292,70 @@ __global__ void k_controller(PlanView pv, WorkView wv, const MlpSmem *Wd) {
   LMState &s = wv.lm[b];
   if (s.status != 0 || !(s.iters == 0 || s.last_acc)) return;
   float x[kIn];
-  lm_features(pv, s, b, x);
+  lm_features_warp(pv, s, b, x);
   float o0, o1;
   mlp_infer_warp(m, x, o0, o1);
   if ((threadIdx.x & 31) == 0 && o1 > 0.f) {
     const double dl = fmin(3.0, fmax(-6.0, (double)o0));
-    s.lam = fmin(1e12, fmax(1e-14, s.lam * pow(10.0, dl)));
+    s.lam = fmin(1e12, fmax(1e-14, s.lam * exp10(dl)));
   }
 }
 
 __global__ void k_features(PlanView pv, WorkView wv, float *feat) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);  // warp per problem
   if (b >= pv.B) return;
-  lm_features(pv, wv.lm[b], b, feat + (size_t)b * kIn);
+  float x[kIn];
+  lm_features_warp(pv, wv.lm[b], b, x);
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < kIn; ++k) feat[(size_t)b * kIn + k] = x[k];
+}
+
+// FP32 path of k_lm_stats: the maxima and minimum are exact in float and the sums
+// run in double-float, on the FP32 pipes (FP64 runs at a small fraction of their
+// rate on this GPU).  One CTA, blockDim a multiple of 32.
+__device__ void lm_stats_f32(const PlanView &pv, const WorkView &wv, LMState &s, int b, int P, const float *A,
+                             const float *g) {
+  float gmx = 0.f, dmx = 0.f, dmn = INFINITY;
+  df ds = df_make(0.f), cs = df_make(0.f);
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    gmx = fmaxf(gmx, fabsf(g[i]));
+    const float d = A[(size_t)i * P + i];
+    ds = ds + df_make(d);
+    dmx = fmaxf(dmx, d);
+    dmn = fminf(dmn, d);
+  }
+  const int l0 = pv.p_lm_off[b], lc = pv.p_lm_cnt[b];
+  const float *C = reinterpret_cast<const float *>(wv.C) + l0;
+  for (int i = threadIdx.x; i < lc; i += blockDim.x) cs = cs + df_make(C[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    gmx = fmaxf(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
+    dmx = fmaxf(dmx, __shfl_xor_sync(0xffffffffu, dmx, o));
+    dmn = fminf(dmn, __shfl_xor_sync(0xffffffffu, dmn, o));
+    ds = ds + df{__shfl_xor_sync(0xffffffffu, ds.h, o), __shfl_xor_sync(0xffffffffu, ds.l, o)};
+    cs = cs + df{__shfl_xor_sync(0xffffffffu, cs.h, o), __shfl_xor_sync(0xffffffffu, cs.l, o)};
+  }
+  __shared__ float r7[32][7];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    r7[w][0] = gmx; r7[w][1] = ds.h; r7[w][2] = ds.l; r7[w][3] = dmx; r7[w][4] = dmn;
+    r7[w][5] = cs.h; r7[w][6] = cs.l;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      gmx = fmaxf(gmx, r7[k][0]);
+      ds = ds + df{r7[k][1], r7[k][2]};
+      dmx = fmaxf(dmx, r7[k][3]);
+      dmn = fminf(dmn, r7[k][4]);
+      cs = cs + df{r7[k][5], r7[k][6]};
+    }
+    s.gnorm = (double)gmx;
+    s.dmean = P ? ((double)ds.h + (double)ds.l) / P : 0.0;
+    s.dmax = (double)dmx;
+    s.dmin = P ? (double)dmn : 0.0;
+    s.cmean = lc ? ((double)cs.h + (double)cs.l) / lc : 0.0;
+  }
 }
 
 // per-problem statistics of the fresh linearisation: max |g|, diag(A) mean/max/min, mean C
@@ -290,6 +368,10 @@ __global__ void k_lm_stats(PlanView pv, WorkView wv) {
   const int P = 6 * pv.p_npose[b];
   const T *A = reinterpret_cast<const T *>(wv.A) + pv.p_S_off[b];
   const T *g = reinterpret_cast<const T *>(wv.g) + pv.p_param_off[b];
+  if constexpr (std::is_same<T, float>::value) {
+    lm_stats_f32(pv, wv, s, b, P, A, g);
+    return;
+  }
   double gmax = 0.0, dsum = 0.0, dmax = 0.0, dmin = 1e300, csum = 0.0;
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
     gmax = fmax(gmax, fabs((double)g[i]));
@@ -347,7 +429,7 @@ int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wd, vo
 }
 
 int launch_features(const PlanView &pv, const WorkView &wv, float *feat, void *stream) {
-  k_features<<<grid_for(pv.B, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, feat);
+  k_features<<<grid_for(pv.B, 4), 128, 0, (cudaStream_t)stream>>>(pv, wv, feat);
   ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -119,7 +119,7 @@ struct Params {
 };
 
 // launch wrappers (defined in the .cu files); all return cudaError_t as int
-int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, void *stream);
+int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, int f64, void *stream);
 template <typename T>
 int launch_linearize(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
                      int cost_only, int gate, void *stream);

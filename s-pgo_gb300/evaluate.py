@@ -107,13 +107,20 @@ def main(argv: List[str] | None = None):
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--scene", choices=["reference", "circle"], default="reference")
+    ap.add_argument("--save", default="", help="prefix: <prefix>_errors.txt ([trials, steps] summed pose "
+                    "errors, as the reference's study writes them) and <prefix>_timing.txt (ns per batched "
+                    "step: one step of every trial together)")
     args = ap.parse_args(argv)
     r = convergence_study(args.trials, args.steps, mode=args.mode, precision=args.precision, seed=args.seed,
                           scene=args.scene)
     e = r["errors"]
+    if args.save:
+        np.savetxt(args.save + "_errors.txt", e)
+        np.savetxt(args.save + "_timing.txt", 1e9 * r["step_seconds"])
     print(json.dumps({"trials": args.trials, "steps": args.steps, "mode": args.mode, "precision": args.precision,
                       "scene": args.scene,
-                      "divergence_rate": r["divergence_rate"], "final_error_median": float(np.median(e[:, -1])),
+                      "divergence_rate": r["divergence_rate"], "diverged": np.nonzero(r["diverged"])[0].tolist(),
+                      "final_error_median": float(np.median(e[:, -1])),
                       "first_error_median": float(np.median(e[:, 0])),
                       "depth_error_sum_median": float(np.median(r["depth_error_sum"])),
                       "ms_per_batched_step": float(1e3 * np.median(r["step_seconds"]))}))

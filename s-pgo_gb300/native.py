@@ -33,11 +33,15 @@ PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble
 
 
 class HostProblem(C.Structure):
+    """``spgo_host_problem``; the array fields are addresses (``ndarray.ctypes.data``):
+    intrinsics float32[8], T_r_to_l float64[16], host int32[L], anchor_uv float32[2L],
+    obs_ptr int64[L+1], obs_frame int32[O], obs_uv float32[4O], and the optional
+    FP64 pixel arrays anchor_uv_f64 float64[2L], obs_uv_f64 float64[4O]."""
     _fields_ = [("n_poses", C.c_int32), ("n_landmarks", C.c_int32), ("n_obs", C.c_int64),
-                ("intrinsics", C.POINTER(C.c_float)), ("T_r_to_l", C.POINTER(C.c_double)),
-                ("host", C.POINTER(C.c_int32)), ("anchor_uv", C.POINTER(C.c_float)),
-                ("obs_ptr", C.POINTER(C.c_int64)), ("obs_frame", C.POINTER(C.c_int32)),
-                ("obs_uv", C.POINTER(C.c_float))]
+                ("intrinsics", C.c_void_p), ("T_r_to_l", C.c_void_p),
+                ("host", C.c_void_p), ("anchor_uv", C.c_void_p),
+                ("obs_ptr", C.c_void_p), ("obs_frame", C.c_void_p),
+                ("obs_uv", C.c_void_p), ("anchor_uv_f64", C.c_void_p), ("obs_uv_f64", C.c_void_p)]
 
 
 class PlanSizes(C.Structure):
@@ -63,8 +67,7 @@ class ProblemStatus(C.Structure):
 
 class DeviceProblem(C.Structure):
     """spgo_device_problem: HostProblem's fields, device pointers."""
-    _fields_ = [(n, t if not n.startswith(("intr", "T_r", "host", "anchor", "obs_p", "obs_f", "obs_u")) else C.c_void_p)
-                for n, t in HostProblem._fields_]
+    _fields_ = [(n, t) for n, t in HostProblem._fields_ if not n.endswith("_f64")]
 
 
 class SpgoError(RuntimeError):

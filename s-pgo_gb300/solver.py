@@ -12,7 +12,8 @@
 from __future__ import annotations
 
 import ctypes as C
-from typing import List, Optional, Sequence
+from concurrent.futures import ThreadPoolExecutor
+from typing import Iterable, Iterator, List, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
@@ -40,46 +41,76 @@ def _to44(p34: np.ndarray) -> np.ndarray:
     return out
 
 
-class BatchSolver:
-    """Solve a batch of independent problems with one set of kernel launches."""
+class HostPlan:
+    """The host half of a ``BatchSolver``: the problems marshalled and planned
+    (``spgo_plan_create``: sorting, chunking and the static arrays, written into
+    page-locked staging).  It needs no device work, so it can be built on another
+    thread while an earlier batch solves (the planner releases the GIL)."""
 
-    def __init__(self, problems: Sequence[Problem], precision: str = "mixed", device="cuda",
-                 stream: Optional[torch.cuda.Stream] = None):
+    def __init__(self, problems: Sequence[Problem], precision: str = "mixed"):
         self.L = nat.lib()
         self.problems = list(problems)
         if not self.problems:
             raise ValueError("no problems")
         self.precision = precision
+        # host arrays must stay alive until the plan is built (the library copies them);
+        # FP64 pixels go in as they are (the planner rounds them while it sorts)
+        keep = []
+        hp = (nat.HostProblem * len(self.problems))()
+        for i, p in enumerate(self.problems):
+            arrs = (np.ascontiguousarray(p.intrinsics, dtype=np.float32),
+                    np.ascontiguousarray(p.T_rl, dtype=np.float64),
+                    np.ascontiguousarray(p.host, dtype=np.int32),
+                    np.ascontiguousarray(p.anchor_uv, dtype=np.float64),
+                    np.ascontiguousarray(p.obs_ptr, dtype=np.int64),
+                    np.ascontiguousarray(p.obs_frame, dtype=np.int32),
+                    np.ascontiguousarray(p.obs_uv, dtype=np.float64))
+            keep.append(arrs)
+            h = hp[i]
+            h.n_poses = int(p.n_poses)
+            h.n_landmarks = int(arrs[2].shape[0])
+            h.n_obs = int(arrs[5].shape[0])
+            h.intrinsics = arrs[0].ctypes.data
+            h.T_r_to_l = arrs[1].ctypes.data
+            h.host = arrs[2].ctypes.data
+            h.anchor_uv_f64 = arrs[3].ctypes.data
+            h.obs_ptr = arrs[4].ctypes.data
+            h.obs_frame = arrs[5].ctypes.data
+            h.obs_uv_f64 = arrs[6].ctypes.data
+        plan = C.c_void_p()
+        nat.check(self.L.spgo_plan_create(hp, len(self.problems), _PREC[precision], C.byref(plan)), "plan_create")
+        self.handle = plan
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.L.spgo_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchSolver:
+    """Solve a batch of independent problems with one set of kernel launches."""
+
+    def __init__(self, problems: Optional[Sequence[Problem]] = None, precision: str = "mixed", device="cuda",
+                 stream: Optional[torch.cuda.Stream] = None, plan: Optional[HostPlan] = None):
+        """``problems`` are planned here, or ``plan`` (a ``HostPlan``, whose
+        ownership passes to this solver) was planned beforehand."""
+        self.L = nat.lib()
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError("BatchSolver runs on a CUDA device only")
         self._stream = stream
-        # host arrays must stay alive until the plan is built (the library copies them)
-        keep = []
-        hp = (nat.HostProblem * len(self.problems))()
-        for i, p in enumerate(self.problems):
-            arrs = dict(
-                intr=np.ascontiguousarray(p.intrinsics, dtype=np.float32),
-                trl=np.ascontiguousarray(p.T_rl, dtype=np.float64).reshape(16),
-                host=np.ascontiguousarray(p.host, dtype=np.int32),
-                auv=np.ascontiguousarray(p.anchor_uv, dtype=np.float32).reshape(-1),
-                ptr=np.ascontiguousarray(p.obs_ptr, dtype=np.int64),
-                fr=np.ascontiguousarray(p.obs_frame, dtype=np.int32),
-                uv=np.ascontiguousarray(p.obs_uv, dtype=np.float32).reshape(-1),
-            )
-            keep.append(arrs)
-            hp[i].n_poses = int(p.n_poses)
-            hp[i].n_landmarks = p.n_landmarks
-            hp[i].n_obs = p.n_obs
-            hp[i].intrinsics = _ptr(arrs["intr"], C.c_float)
-            hp[i].T_r_to_l = _ptr(arrs["trl"], C.c_double)
-            hp[i].host = _ptr(arrs["host"], C.c_int32)
-            hp[i].anchor_uv = _ptr(arrs["auv"], C.c_float)
-            hp[i].obs_ptr = _ptr(arrs["ptr"], C.c_int64)
-            hp[i].obs_frame = _ptr(arrs["fr"], C.c_int32)
-            hp[i].obs_uv = _ptr(arrs["uv"], C.c_float)
-        plan = C.c_void_p()
-        nat.check(self.L.spgo_plan_create(hp, len(self.problems), _PREC[precision], C.byref(plan)), "plan_create")
+        if plan is None:
+            plan = HostPlan(problems if problems is not None else [], precision)
+        self._host_plan = plan
+        self.problems = plan.problems
+        self.precision = plan.precision
+        plan = plan.handle
         self._plan = plan
         sz = nat.PlanSizes()
         nat.check(self.L.spgo_plan_sizes_get(plan, C.byref(sz)), "plan_sizes")
@@ -102,8 +133,7 @@ class BatchSolver:
                                             C.c_void_p(self._addr(self.d_ws)), sz.workspace_bytes,
                                             C.c_void_p(self.poses.data_ptr()), C.c_void_p(self.alpha.data_ptr()),
                                             self._sp(), C.byref(solver)), "solver_create")
-        self._solver = solver
-        self.synchronize()  # the plan's host arrays are read by the async upload
+        self._solver = solver  # (the upload runs on the stream; the plan outlives it)
         self.params = nat.default_params()
         self._apply_params()
 
@@ -305,8 +335,9 @@ class BatchSolver:
             self.synchronize()
             self.L.spgo_solver_destroy(self._solver)
             self._solver = None
-        if getattr(self, "_plan", None):
-            self.L.spgo_plan_destroy(self._plan)
+        if getattr(self, "_host_plan", None):
+            self._host_plan.close()
+            self._host_plan = None
             self._plan = None
 
     def __del__(self):
@@ -314,6 +345,44 @@ class BatchSolver:
             self.close()
         except Exception:
             pass
+
+
+def _plan_on(device: torch.device, problems, precision):
+    torch.cuda.set_device(device)  # page-locked staging is allocated in this device's context
+    return HostPlan(problems, precision)
+
+
+def solve_stream(batches: Iterable[Sequence[Problem]], precision: str = "mixed", params: Optional[dict] = None,
+                 controller: Optional[torch.Tensor] = None, device="cuda",
+                 stream: Optional[torch.cuda.Stream] = None,
+                 check_every: int = 4) -> Iterator[Tuple[List[dict], list, list]]:
+    """Solve batch after batch (each a sequence of ``Problem``) with Nielsen LM (or
+    the learned controller), yielding ``(statuses, poses, inverse_depths)`` per batch
+    in order.  Batch k + 1 is planned on a worker thread while batch k solves, so the
+    host's share of a batch (marshalling, sorting, chunking) hides behind the device's;
+    every batch still has its own upload and readback."""
+    dev = torch.device(device)
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    it = iter(batches)
+    with ThreadPoolExecutor(1) as ex:
+        first = next(it, None)
+        fut = ex.submit(_plan_on, dev, first, precision) if first is not None else None
+        while fut is not None:
+            hp = fut.result()
+            nxt = next(it, None)
+            fut = ex.submit(_plan_on, dev, nxt, precision) if nxt is not None else None
+            bs = BatchSolver(device=dev, stream=stream, plan=hp)
+            try:
+                if params:
+                    bs.set_params(**params)
+                if controller is not None:
+                    bs.set_controller(controller)
+                st = bs.solve(check_every=check_every)
+                poses, alphas = bs.get_state()
+            finally:
+                bs.close()
+            yield st, poses, alphas
 
 
 class CudaSolver:

@@ -141,3 +141,25 @@ def test_trained_controller_beats_nielsen_on_heldout(built_lib, cuda_device):
     lrn, costs, _ = learned.iterations_to_target(probs, ctl, targets, precision="mixed")
     # mean LM iterations until the plain FP64 cost is reached (a miss counts 31)
     assert lrn.mean() < 0.9 * plain.mean(), (lrn.mean(), plain.mean())
+
+
+def test_controller_features_match_the_lm_state(built_lib, cuda_device):
+    """The 16 inputs (one warp per problem, the logarithms spread over the lanes)
+    against what the status read-back implies: log cost per residual, log of the
+    cost ratio, log lambda, the iteration index; all finite and inside [-40, 40]."""
+    probs = [scenes.circle_scene(s, n, l) for s, n, l in [(91, 6, 80), (92, 9, 150), (93, 12, 300)]]
+    bs = BatchSolver(probs, precision="mixed")
+    bs.set_params(loss="l2", max_iters=30, tol=1e-6)
+    bs.reset()
+    bs.iterate(3)
+    F = bs.features()
+    st = bs.status()
+    assert np.isfinite(F).all() and np.abs(F).max() <= 40.0
+    for b, p in enumerate(probs):
+        s = st[b]
+        assert F[b, 0] == pytest.approx(np.log10(s["cost"]) - np.log10(4 * p.n_obs), abs=1e-5)
+        assert F[b, 1] == pytest.approx(np.log10(s["cost"]) - np.log10(s["cost0"]), abs=1e-5)
+        assert F[b, 5] == pytest.approx(np.log10(s["lam"]), abs=1e-5)
+        assert F[b, 10] == pytest.approx(s["iterations"] / 30.0, abs=1e-6)
+        assert F[b, 14] == np.rint(F[b, 14]) and F[b, 14] >= 1.0   # log2 of nu, a power of two
+    bs.close()

@@ -152,15 +152,17 @@ def test_batched_equals_individual(built_lib, cuda_device):
         assert er < 1e-5 and et < 1e-5
 
 
-@pytest.mark.parametrize("prec,opt_cost_tol,pose_tol", [("fp64", 1e-9, 1e-5), ("mixed", 1e-7, 5e-5)])
+@pytest.mark.parametrize("prec,opt_cost_tol,pose_tol", [("fp64", 1e-9, 1e-5), ("mixed", 1e-7, 2e-4)])
 def test_huber_outliers_converge(built_lib, cuda_device, prec, opt_cost_tol, pose_tol):
     """Corridor with 5 % outliers under Huber (delta = 2 px): the LM cost matches the
     oracle's at 1e-6; run on to the optimum, the costs agree to opt_cost_tol and the
     states to pose_tol.  This scene's weakest reduced-system directions change the
-    cost by only ~1.6e-10 relative for a 2e-5 m move; the mixed path's FP32 gradient
-    stops 1.4e-9 to 1.1e-8 (relative cost, run to run) above the FP64 optimum,
-    1-2e-5 m away along them, so it is held to 1e-7 / 5e-5 m here; the FP64 path
-    holds 1e-9 / 1e-5 rad, 1e-5 m."""
+    cost by only ~1.6e-10 relative for a 2e-5 m move.  The mixed path's FP32
+    gradient stops where its rounding noise balances that curvature, and FP32
+    atomics make the noise differ run to run: over 8 runs it stopped 1.6e-10 to
+    1.4e-8 (relative cost) above the FP64 optimum and 1.4e-5 to 8.8e-5 m (3.5e-6 to
+    1.5e-5 rad) away from it, so it is held to 1e-7 / 2e-4 here; the FP64 path holds
+    1e-9 / 1e-5 rad, 1e-5 m."""
     p = f32_obs(scenes.corridor_scene(7, 40, 1500, window=20, outlier_frac=0.05))
     ref = p.copy()
     loss = S.Loss(S.LOSS_HUBER, 2.0)
@@ -362,3 +364,24 @@ def test_divergence_study_runs_batched(built_lib, cuda_device, scene):
     assert e.shape == (12, 8) and np.isfinite(e).all()
     assert np.median(e[:, -1]) < np.median(e[:, 0])
     assert 0.0 <= r["divergence_rate"] <= 1.0
+
+
+def test_solve_stream_matches_batch_solver(built_lib, cuda_device):
+    """solve_stream plans batch k + 1 on a worker thread while batch k solves: the
+    batches come back in order with the results of one BatchSolver each."""
+    from spgo_gb300.solver import solve_stream
+    batches = [[scenes.circle_scene(s, n, l) for s, n, l in [(81 + 3 * k, 6, 80), (82 + 3 * k, 9, 150)]]
+               for k in range(3)]
+    # (run to the optimum: FP32 atomics make LM paths differ run to run before it)
+    params = dict(loss="l2", max_iters=OPT_ITERS, tol=OPT_TOL)
+    got = list(solve_stream(batches, "mixed", params, device=cuda_device))
+    assert len(got) == 3
+    for batch, (st, poses, alphas) in zip(batches, got):
+        bs = BatchSolver(batch, precision="mixed")
+        bs.set_params(**params)
+        ref = bs.solve()
+        for b, p in enumerate(batch):
+            assert abs(st[b]["cost"] - ref[b]["cost"]) <= 1e-7 * ref[b]["cost"]
+            assert poses[b].shape == (p.n_poses, 4, 4) and alphas[b].shape == (p.n_landmarks,)
+            assert np.abs(poses[b] - bs.get_poses(b)).max() < 1e-4
+        bs.close()

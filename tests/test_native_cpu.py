@@ -28,7 +28,7 @@ def test_exports_every_declared_symbol(built_lib):
     assert built_lib.spgo_version() == 1
 
 
-def host_problem(p, keep):
+def host_problem(p, keep, f64=False):
     arrs = dict(intr=np.ascontiguousarray(p.intrinsics, np.float32),
                 trl=np.ascontiguousarray(p.T_rl, np.float64).reshape(16),
                 host=np.ascontiguousarray(p.host, np.int32),
@@ -39,27 +39,34 @@ def host_problem(p, keep):
     keep.append(arrs)
     h = nat.HostProblem()
     h.n_poses, h.n_landmarks, h.n_obs = int(p.n_poses), p.n_landmarks, p.n_obs
-    h.intrinsics = arrs["intr"].ctypes.data_as(C.POINTER(C.c_float))
-    h.T_r_to_l = arrs["trl"].ctypes.data_as(C.POINTER(C.c_double))
-    h.host = arrs["host"].ctypes.data_as(C.POINTER(C.c_int32))
-    h.anchor_uv = arrs["auv"].ctypes.data_as(C.POINTER(C.c_float))
-    h.obs_ptr = arrs["ptr"].ctypes.data_as(C.POINTER(C.c_int64))
-    h.obs_frame = arrs["fr"].ctypes.data_as(C.POINTER(C.c_int32))
-    h.obs_uv = arrs["uv"].ctypes.data_as(C.POINTER(C.c_float))
+    h.intrinsics = arrs["intr"].ctypes.data
+    h.T_r_to_l = arrs["trl"].ctypes.data
+    h.host = arrs["host"].ctypes.data
+    h.obs_ptr = arrs["ptr"].ctypes.data
+    h.obs_frame = arrs["fr"].ctypes.data
+    if f64:  # the optional FP64 pixel arrays instead of the float ones
+        arrs["auv64"] = np.ascontiguousarray(p.anchor_uv, np.float64).reshape(-1)
+        arrs["uv64"] = np.ascontiguousarray(p.obs_uv, np.float64).reshape(-1)
+        h.anchor_uv_f64 = arrs["auv64"].ctypes.data
+        h.obs_uv_f64 = arrs["uv64"].ctypes.data
+    else:
+        h.anchor_uv = arrs["auv"].ctypes.data
+        h.obs_uv = arrs["uv"].ctypes.data
     return h
 
 
-def plan(problems, prec=nat.PREC_MIXED):
+def plan(problems, prec=nat.PREC_MIXED, f64=False):
     keep = []
-    arr = (nat.HostProblem * len(problems))(*[host_problem(p, keep) for p in problems])
+    arr = (nat.HostProblem * len(problems))(*[host_problem(p, keep, f64) for p in problems])
     out = C.c_void_p()
     rc = nat.lib().spgo_plan_create(arr, len(problems), prec, C.byref(out))
     return rc, out
 
 
-def test_plan_sizes(built_lib):
+@pytest.mark.parametrize("f64", [False, True])
+def test_plan_sizes(built_lib, f64):
     ps = [scenes.circle_scene(s, 8 + s, 100 + 37 * s) for s in range(5)]
-    rc, pl = plan(ps)
+    rc, pl = plan(ps, f64=f64)
     assert rc == 0
     sz = nat.PlanSizes()
     assert built_lib.spgo_plan_sizes_get(pl, C.byref(sz)) == 0
@@ -107,3 +114,21 @@ def test_plan_rejects_too_wide_window(built_lib):
     p.obs_frame[s:e] = np.linspace(0, 120, e - s).astype(np.int32)
     if e - s >= 2:
         assert plan([p])[0] == -2
+
+
+def test_host_plan_on_a_worker_thread(built_lib):
+    """The planner needs no device: HostPlan builds on another thread (as
+    solve_stream does) and reports the same sizes as a plan built here."""
+    from concurrent.futures import ThreadPoolExecutor
+    from spgo_gb300.solver import HostPlan
+    ps = [scenes.circle_scene(s, 5 + s, 60 + 11 * s) for s in range(3)]
+    with ThreadPoolExecutor(1) as ex:
+        hp = ex.submit(HostPlan, ps, "mixed").result()
+    rc, pl = plan(ps)
+    assert rc == 0
+    a, b = nat.PlanSizes(), nat.PlanSizes()
+    assert built_lib.spgo_plan_sizes_get(hp.handle, C.byref(a)) == 0
+    assert built_lib.spgo_plan_sizes_get(pl, C.byref(b)) == 0
+    assert (a.static_bytes, a.workspace_bytes, a.n_chunks) == (b.static_bytes, b.workspace_bytes, b.n_chunks)
+    hp.close()
+    built_lib.spgo_plan_destroy(pl)
