@@ -47,21 +47,32 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31, nw = nt >> 5;
   const T lam_t = (T)lam;
   // assembly: rows over warps, columns over lanes (coalesced reads of A and S_L);
-  // up to kRowRegs columns per lane are loaded before any is used
+  // each warp loads kAsmRows rows (up to kRowRegs columns per lane) before it stores
+  // any, so a warp waits for one memory round trip per kAsmRows rows
   if (P <= 32 * kRowRegs) {
-    for (int r = warp; r < P; r += nw) {
-      const T *Ar = A + (size_t)r * P, *Sr = SL + (size_t)r * P;
-      T av[kRowRegs], sv[kRowRegs];
+    constexpr int kAsmRows = sizeof(T) == 4 ? 4 : 2;
+    for (int r0 = warp; r0 < P; r0 += kAsmRows * nw) {
+      T av[kAsmRows][kRowRegs], sv[kAsmRows][kRowRegs];
 #pragma unroll
-      for (int m = 0; m < kRowRegs; ++m) {
-        const int c = lane + 32 * m;
-        av[m] = c <= r ? Ar[c] : T(0);
-        sv[m] = c <= r ? Sr[c] : T(0);
+      for (int q = 0; q < kAsmRows; ++q) {
+        const int r = r0 + q * nw;
+        const T *Ar = A + (size_t)r * P, *Sr = SL + (size_t)r * P;
+#pragma unroll
+        for (int m = 0; m < kRowRegs; ++m) {
+          const int c = lane + 32 * m;
+          const bool ok = r < P && c <= r;
+          av[q][m] = ok ? Ar[c] : T(0);
+          sv[q][m] = ok ? Sr[c] : T(0);
+        }
       }
 #pragma unroll
-      for (int m = 0; m < kRowRegs; ++m) {
-        const int c = lane + 32 * m;
-        if (c <= r) Lm[ix(r, c)] = av[m] - sv[m] + (c == r ? lam_t * av[m] : T(0));
+      for (int q = 0; q < kAsmRows; ++q) {
+        const int r = r0 + q * nw;
+#pragma unroll
+        for (int m = 0; m < kRowRegs; ++m) {
+          const int c = lane + 32 * m;
+          if (r < P && c <= r) Lm[ix(r, c)] = av[q][m] - sv[q][m] + (c == r ? lam_t * av[q][m] : T(0));
+        }
       }
     }
   } else {
@@ -240,46 +251,64 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
     for (int k = tid; k < (nw + 1) * 2 * P; k += nt) colacc[k] = T(0);
     __syncthreads();
     T *mine = colacc + (size_t)warp * 2 * P;
-    for (int i = warp; i < P; i += nw) {
-      const T *Ai = A + (size_t)i * P, *Si = SL + (size_t)i * P;
+    // (the FP32 path takes two rows per warp pass: both rows' entries are loaded
+    // before either is used, so a warp waits for one round trip per two rows)
+    constexpr int kResRows = std::is_same<T, float>::value ? 2 : 1;
+    for (int i0 = warp; i0 < P; i0 += kResRows * nw) {
       if constexpr (std::is_same<T, float>::value) {
-        const df xi{xs[2 * i], xs[2 * i + 1]};
-        df acc = df_make(0.f);
-        auto term = [&](int j, float a, float sl) {
-          df sij = df_sub(a, sl);
-          if (j == i) sij = sij + df_from_double(lam * (double)a);
-          acc = acc + sij * df{xs[2 * j], xs[2 * j + 1]};
-          if (j < i) {
-            const df c = df{mine[2 * j], mine[2 * j + 1]} + sij * xi;
-            mine[2 * j] = c.h;
-            mine[2 * j + 1] = c.l;
-          }
-        };
-        if (P <= 32 * kRowRegs) {
-          // the row's entries are loaded before use (up to kRowRegs per lane)
-          float av[kRowRegs], sv[kRowRegs];
+        float av[kResRows][kRowRegs], sv[kResRows][kRowRegs];
+        const bool regs = P <= 32 * kRowRegs;
+        if (regs) {
 #pragma unroll
-          for (int m = 0; m < kRowRegs; ++m) {
-            const int j = lane + 32 * m;
-            av[m] = j <= i ? Ai[j] : 0.f;
-            sv[m] = j <= i ? Si[j] : 0.f;
-          }
+          for (int q = 0; q < kResRows; ++q) {
+            const int i = i0 + q * nw;
+            const float *Ai = A + (size_t)i * P, *Si = SL + (size_t)i * P;
 #pragma unroll
-          for (int m = 0; m < kRowRegs; ++m)
-            if (lane + 32 * m <= i) term(lane + 32 * m, av[m], sv[m]);
-        } else {
-          for (int j = lane; j <= i; j += 32) term(j, Ai[j], Si[j]);
+            for (int m = 0; m < kRowRegs; ++m) {
+              const int j = lane + 32 * m;
+              const bool ok = i < P && j <= i;
+              av[q][m] = ok ? Ai[j] : 0.f;
+              sv[q][m] = ok ? Si[j] : 0.f;
+            }
+          }
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const df other{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
-          acc = acc + other;
-        }
-        if (lane == 0) {
-          rowp[2 * i] = acc.h;
-          rowp[2 * i + 1] = acc.l;
+        for (int q = 0; q < kResRows; ++q) {
+          const int i = i0 + q * nw;
+          if (i >= P) break;
+          const float *Ai = A + (size_t)i * P, *Si = SL + (size_t)i * P;
+          const df xi{xs[2 * i], xs[2 * i + 1]};
+          df acc = df_make(0.f);
+          auto term = [&](int j, float a, float sl) {
+            df sij = df_sub(a, sl);
+            if (j == i) sij = sij + df_from_double(lam * (double)a);
+            acc = acc + sij * df{xs[2 * j], xs[2 * j + 1]};
+            if (j < i) {
+              const df c = df{mine[2 * j], mine[2 * j + 1]} + sij * xi;
+              mine[2 * j] = c.h;
+              mine[2 * j + 1] = c.l;
+            }
+          };
+          if (regs) {
+#pragma unroll
+            for (int m = 0; m < kRowRegs; ++m)
+              if (lane + 32 * m <= i) term(lane + 32 * m, av[q][m], sv[q][m]);
+          } else {
+            for (int j = lane; j <= i; j += 32) term(j, Ai[j], Si[j]);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const df other{__shfl_xor_sync(0xffffffffu, acc.h, o), __shfl_xor_sync(0xffffffffu, acc.l, o)};
+            acc = acc + other;
+          }
+          if (lane == 0) {
+            rowp[2 * i] = acc.h;
+            rowp[2 * i + 1] = acc.l;
+          }
         }
       } else {
+        const int i = i0;
+        const T *Ai = A + (size_t)i * P, *Si = SL + (size_t)i * P;
         const double xi = x[i];
         double acc = 0.0;
         for (int j = lane; j <= i; j += 32) {
