@@ -167,6 +167,14 @@ def roofline_numerator(kind: str, sizes, slab_floats: int, ts: int, probs):
     return None, None, 0.0
 
 
+# DRAM bytes (read + write) per launch of the profiled kernels on this workload
+# (256-problem batch, mixed precision): one ncu capture, dram__bytes_read.sum +
+# dram__bytes_write.sum, profiles/ncu_kernels_config3_batch.md
+NCU_TRAFFIC = {"cost": 119.63e6, "linearize": 251.86e6, "schur": 224.55e6, "factor_solve": 24.00e6,
+               "backsub": 207.06e6}
+NCU_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/ncu_kernels_config3_batch.md"
+
+
 def roofline_peaks(peaks: dict, tc: bool):
     """Denominators by bound: measured HBM copy; tensor = measured cuBLAS BF16 / 2 for
     the TF32 kind the Schur pass issues (the nominal TF32 : BF16 ratio), or the
@@ -341,7 +349,9 @@ def run_ours(args):
         achieved, peak, peak_src = None, None, None
     roof = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": (achieved / peak) if achieved else None,
-            "traffic": None, "avg_launch_ms": avg_ms, "peak_source": peak_src,
+            "traffic": NCU_TRAFFIC.get(dom),
+            "traffic_source": NCU_TRAFFIC_SOURCE, "algorithmic_per_launch": amount,
+            "avg_launch_ms": avg_ms, "peak_source": peak_src,
             "note": "algorithmic bytes per launch / CUDA-event launch duration (profiled step after the "
                     "timed region, CUDA graphs off)"}
 
