@@ -145,7 +145,11 @@ void        spgo_default_params(spgo_params *p);
 
 /* Host-side planning: validates the problems, orders landmarks by Jacobian
  * window, groups them into 32-landmark chunks and builds the Schur tile work
- * list.  Allocates host memory only. */
+ * list, on up to 16 host threads (two cores are left to other threads).  No
+ * device work: the static tables are written into page-locked host staging
+ * (ordinary heap memory without a CUDA device) taken from a small process-wide
+ * cache, so it may run on any thread, e.g. for the next batch while the
+ * current one solves.  Thread-safe. */
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems,
                      int32_t precision, spgo_plan **out);
 int spgo_plan_sizes_get(const spgo_plan *plan, spgo_plan_sizes *out);
@@ -155,11 +159,12 @@ int spgo_plan_destroy(spgo_plan *plan);
  * ([n_problems]) and the pose offset ([n_problems]) into the state buffers. */
 int spgo_plan_offsets(const spgo_plan *plan, int32_t *lm_off, int32_t *pose_off);
 
-/* Binds caller-owned device memory and uploads the plan (asynchronous H2D on
- * `stream`; the plan must outlive the copy, i.e. synchronise before
- * destroying it).  State buffers: poses [total_poses*12] (3x4 row-major
- * incremental T_curr_to_next, FP64) and alpha [total_landmarks] (FP64), both
- * in the caller's problem/landmark order. */
+/* Binds caller-owned device memory and uploads the plan: two asynchronous DMA
+ * copies on `stream` from the plan's page-locked staging (spgo_plan_destroy
+ * waits for them before the staging is reused).  The solver keeps reading the
+ * plan's host tables, so the plan must outlive the solver.  State buffers:
+ * poses [total_poses*12] (3x4 row-major incremental T_curr_to_next, FP64) and
+ * alpha [total_landmarks] (FP64), both in the caller's problem/landmark order. */
 int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_bytes,
                        void *d_workspace, size_t workspace_bytes,
                        double *d_poses, double *d_alpha, void *stream, spgo_solver **out);
