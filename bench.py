@@ -11,9 +11,9 @@ of the whole batch from its initial state.
   inputs resident in HBM; L2 is flushed (256 MB write) between timed steps.
 * ``e2e``: the same metric through the public API per step: marshal and plan
   the host problems, upload, solve, read back poses and inverse depths.  The
-  headline runs batches through ``solver.solve_stream`` (the next batch is
-  planned on a worker thread while this one solves); ``serial_value`` is one
-  ``BatchSolver`` after another.
+  headline runs batches through ``solver.solve_stream`` (batches planned on a
+  worker thread ahead of their solve, ``--inflight`` batches solving at once on
+  their own CUDA streams); ``serial_value`` is one ``BatchSolver`` after another.
 * ``plain_fp64``: the plain FP64 GPU solver (problems one at a time), its
   solves/s and how many chosen-form costs reach its converged cost (rel 1e-6).
 * ``cpu_baseline``: the FP64 CPU oracle on a bounded sample of the batch.
@@ -378,8 +378,8 @@ def run_ours(args):
 
     # end-to-end through the public API with host buffers: every batch is marshalled,
     # planned, uploaded, solved and read back.  Serially (one BatchSolver after
-    # another), and as a stream (solve_stream: batch k + 1 is planned on a worker
-    # thread while batch k solves), which is the headline.
+    # another), and as a stream (solve_stream: batches planned on a worker thread
+    # ahead of their solve, --inflight batches solving at once), which is the headline.
     e2e_ms, h2d, d2h = [], 0, 0
     for k in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize(dev)
@@ -394,12 +394,12 @@ def run_ours(args):
         s2.close()
         del poses, alphas
     serial_val = N_PROBLEMS * world / (float(np.mean(e2e_ms)) / 1e3)
-    n_stream = max(3, min(args.steps, 6))
+    n_stream = max(8, args.steps)
     stream_params = {**dict(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4, use_tc=args.tc), **(tuned or {})}
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     for _st, _poses, _alphas in sv.solve_stream([probs] * n_stream, "mixed", stream_params, ctl_params, device=dev,
-                                                stream=stream, check_every=args.check_every):
+                                                inflight=args.inflight, check_every=args.check_every):
         pass
     torch.cuda.synchronize(dev)
     stream_ms = 1e3 * (time.perf_counter() - t0) / n_stream
@@ -419,8 +419,10 @@ def run_ours(args):
             "roofline": roof, "kernels": kernels, "gpu_launches": int(launches), "clocks": clk,
             "cpu_baseline": cpu, "plain_fp64": plain,
             "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": stream_ms, "steps": n_stream, "api": "solver.solve_stream (planning of the "
-                    "next batch overlaps this batch's solve)", "serial_value": serial_val,
+                    "ms_per_step": stream_ms, "steps": n_stream, "inflight": args.inflight,
+                    "api": "solver.solve_stream: batches planned on a worker thread ahead of their solve, "
+                           f"{args.inflight} batches solving at once on their own CUDA streams",
+                    "serial_value": serial_val,
                     "serial_ms_per_step": float(np.mean(e2e_ms))}}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -441,6 +443,7 @@ def main():
     ap.add_argument("--tc", type=int, default=1, help="1: tensor-core Schur complement in the mixed path, 0: SIMT")
     ap.add_argument("--controller", type=int, default=1, help="1: learned damping (shipped weights), 0: Nielsen")
     ap.add_argument("--autotune", type=int, default=1, help="1: time the run-time launch shapes first")
+    ap.add_argument("--inflight", type=int, default=2, help="e2e: batches solving at once in solve_stream")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

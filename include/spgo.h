@@ -247,7 +247,9 @@ int spgo_lm_features(spgo_solver *s, float *d_feat, void *stream);
  * (synchronises the stream). */
 int spgo_lm_probe(spgo_solver *s, int32_t n_factors, const double *factors, double *costs, void *stream);
 
-/* Count of kernel launches enqueued by this solver since creation. */
+/* Count of kernel launches enqueued since the solver was created, graph replays
+ * included, by the calling thread (drive a solver from one thread at a time;
+ * solvers on other threads do not count here). */
 int64_t spgo_launch_count(const spgo_solver *s);
 
 /* Optional per-kernel timing with CUDA events on the launching stream.

@@ -30,7 +30,7 @@
 static thread_local std::string g_err;
 
 namespace spgo {
-int64_t g_launches = 0;
+thread_local int64_t g_launches = 0;
 void set_last_error(const char *msg) { g_err = msg; }
 }  // namespace spgo
 
@@ -70,7 +70,7 @@ struct HostBlock {
 
 static std::mutex g_arena_mu;
 static std::vector<HostBlock> g_arena_free;
-constexpr size_t kArenaKeep = 6;              // cached blocks at most
+constexpr size_t kArenaKeep = 16;             // cached blocks at most
 constexpr size_t kArenaKeepBytes = 2ull << 30;  // and bytes at most
 
 static void block_free(HostBlock &b) {
@@ -82,14 +82,19 @@ static void block_free(HostBlock &b) {
   b = HostBlock();
 }
 
+static size_t arena_cap(size_t bytes) {  // blocks come in whole MiB
+  return (std::max<size_t>(bytes, 256) + (1u << 20) - 1) & ~(size_t)((1u << 20) - 1);
+}
+
 static HostBlock arena_get(size_t bytes) {
   bytes = std::max<size_t>(bytes, 256);
   {
     std::lock_guard<std::mutex> lk(g_arena_mu);
     size_t best = g_arena_free.size();
-    for (size_t i = 0; i < g_arena_free.size(); ++i) {
+    for (size_t i = 0; i < g_arena_free.size(); ++i) {  // smallest cached block that fits, at most 2x
       const size_t c = g_arena_free[i].cap;
-      if (c >= bytes && c <= 2 * bytes && (best == g_arena_free.size() || c < g_arena_free[best].cap)) best = i;
+      if (c >= bytes && c <= 2 * arena_cap(bytes) && (best == g_arena_free.size() || c < g_arena_free[best].cap))
+        best = i;
     }
     if (best < g_arena_free.size()) {
       HostBlock b = g_arena_free[best];
@@ -98,7 +103,7 @@ static HostBlock arena_get(size_t bytes) {
     }
   }
   HostBlock b;
-  b.cap = (bytes + (1u << 20) - 1) & ~(size_t)((1u << 20) - 1);
+  b.cap = arena_cap(bytes);
   void *q = nullptr;
   if (cudaHostAlloc(&q, b.cap, cudaHostAllocPortable) == cudaSuccess) {  // locked for every context
     b.ptr = (unsigned char *)q;
@@ -643,6 +648,10 @@ struct spgo_solver {
     int64_t kernels;  // kernel nodes, for the launch count
   };
   std::vector<Graph> graphs;
+  // page-locked copy of the per-problem LM states for status reads: a copy into
+  // pageable memory would hold the driver until the stream drains, stalling the
+  // API calls of threads that drive other solvers
+  HostBlock h_lm;  // from the staging cache (freeing page-locked memory synchronises the device)
 };
 
 static void drop_graphs(spgo_solver *s) {
@@ -972,6 +981,12 @@ int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_byte
     return fail(SPGO_ERR_CUDA, std::string("workspace clear: ") + cudaGetErrorString(e));
   }
   make_views(s);
+  try {
+    s->h_lm = arena_get(sizeof(LMState) * (size_t)std::max(1, plan->B));
+  } catch (const std::exception &ex) {
+    delete s;
+    return fail(SPGO_ERR_INVALID_ARG, ex.what());
+  }
   s->launches0 = g_launches;
   *out = s;
   return SPGO_OK;
@@ -981,6 +996,7 @@ int spgo_solver_destroy(spgo_solver *s) {
   if (s) {
     for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
     drop_graphs(s);
+    arena_put(s->h_lm);
   }
   delete s;
   return SPGO_OK;
@@ -1091,8 +1107,8 @@ int spgo_lm_iterate(spgo_solver *s, int32_t n_iters, void *stream) {
 
 int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream) {
   if (!s || !out) return fail(SPGO_ERR_INVALID_ARG, "null argument");
-  std::vector<LMState> h(s->plan->B);
-  CUDA_TRY(cudaMemcpyAsync(h.data(), s->wv.lm, h.size() * sizeof(LMState), cudaMemcpyDeviceToHost,
+  LMState *h = reinterpret_cast<LMState *>(s->h_lm.ptr);
+  CUDA_TRY(cudaMemcpyAsync(h, s->wv.lm, sizeof(LMState) * (size_t)s->plan->B, cudaMemcpyDeviceToHost,
                            (cudaStream_t)stream));
   CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
   for (int b = 0; b < s->plan->B; ++b) {

@@ -134,12 +134,22 @@ __global__ void __launch_bounds__(256) k_pair_prefix(PlanView pv, WorkView wv) {
   const int lo0 = max(0, hi - D);
   const int cl = lane < 27 ? lane : 0;
   T next = acc_base[((size_t)lo0 * D + (hi - lo0 - 1)) * 27 + cl];  // prefetched one record ahead
+  // the re-centring offsets z(lo) = c(lo - 1) - c(lo) of the next 32 steps, one per
+  // lane, handed out by shuffles: the step chain does not wait on their loads
+  Vec3<T> zb = v3<T>(T(0), T(0), T(0));
+  if (lo0 + 1 + lane < hi) zb = FramesT<T>::rel(wv, fo + lo0 + lane, 0, fo + lo0 + 1 + lane, 0);
   for (int lo = lo0; lo < hi; ++lo) {
     const size_t rec = (size_t)lo * D + (hi - lo - 1);
     const T cur = next;
     if (lo + 1 < hi) next = acc_base[((size_t)(lo + 1) * D + (hi - lo - 2)) * 27 + cl];
     if (lo > lo0) {
-      const Vec3<T> z = FramesT<T>::rel(wv, fo + lo - 1, 0, fo + lo, 0);
+      const int s = (lo - lo0 - 1) & 31;
+      const Vec3<T> z = v3<T>(__shfl_sync(0xffffffffu, zb.x, s), __shfl_sync(0xffffffffu, zb.y, s),
+                              __shfl_sync(0xffffffffu, zb.z, s));
+      if (s == 31) {  // the next batch
+        const int ll = lo + 1 + lane;
+        zb = ll < hi ? FramesT<T>::rel(wv, fo + ll - 1, 0, fo + ll, 0) : v3<T>(T(0), T(0), T(0));
+      }
       const T v = lane < 27 ? shifted_component(acc, lane, z) : T(0);
       __syncwarp();
       if (lane < 27) acc[lane] = v;
@@ -167,7 +177,18 @@ __global__ void k_pair_suffix(PlanView pv, WorkView wv) {
   const int i = t / 27, comp = t % 27;
   T *base = reinterpret_cast<T *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + (size_t)i * D) * 27 + comp;
   T acc = T(0);
-  for (int dp = min(D, N - i); dp >= 1; --dp) {
+  int dp = min(D, N - i);
+  for (; dp >= 4; dp -= 4) {  // four records loaded before any is summed
+    T v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = base[(size_t)(dp - 1 - q) * 27];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      acc += v[q];
+      base[(size_t)(dp - 1 - q) * 27] = acc;
+    }
+  }
+  for (; dp >= 1; --dp) {
     T *p = base + (size_t)(dp - 1) * 27;
     acc += *p;
     *p = acc;

@@ -159,8 +159,9 @@ template <typename T>
 int launch_export_S(const PlanView &pv, const WorkView &wv, int problem, double *S, double *gS, void *stream);
 int launch_to_double(const void *src, int f64, double *dst, int64_t n, void *stream);
 
-// count of kernel launches made by this library in this process
-extern int64_t g_launches;
+// count of kernel launches made by this library on the calling thread (a solver is
+// driven by one thread at a time; several solvers may run on several threads)
+extern thread_local int64_t g_launches;
 // sets the message spgo_last_error returns (thread-local)
 void set_last_error(const char *msg);
 

@@ -12,6 +12,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import collections
 from concurrent.futures import ThreadPoolExecutor
 from typing import Iterable, Iterator, List, Optional, Sequence, Tuple
 
@@ -352,37 +353,70 @@ def _plan_on(device: torch.device, problems, precision):
     return HostPlan(problems, precision)
 
 
+def _drive(device: torch.device, stream: torch.cuda.Stream, plan_future, params, controller, check_every):
+    """One batch on one CUDA stream: bind, solve, read back, release."""
+    hp = plan_future.result()
+    torch.cuda.set_device(device)
+    with torch.cuda.stream(stream):
+        bs = BatchSolver(device=device, stream=stream, plan=hp)
+        try:
+            if params:
+                bs.set_params(**params)
+            if controller is not None:
+                bs.set_controller(controller)
+            st = bs.solve(check_every=check_every)
+            poses, alphas = bs.get_state()
+        finally:
+            bs.close()
+    return st, poses, alphas
+
+
 def solve_stream(batches: Iterable[Sequence[Problem]], precision: str = "mixed", params: Optional[dict] = None,
-                 controller: Optional[torch.Tensor] = None, device="cuda",
-                 stream: Optional[torch.cuda.Stream] = None,
+                 controller: Optional[torch.Tensor] = None, device="cuda", inflight: int = 2,
                  check_every: int = 4) -> Iterator[Tuple[List[dict], list, list]]:
     """Solve batch after batch (each a sequence of ``Problem``) with Nielsen LM (or
     the learned controller), yielding ``(statuses, poses, inverse_depths)`` per batch
-    in order.  Batch k + 1 is planned on a worker thread while batch k solves, so the
-    host's share of a batch (marshalling, sorting, chunking) hides behind the device's;
-    every batch still has its own upload and readback."""
+    in order.
+
+    ``inflight`` batches solve at once, each on its own CUDA stream driven by its own
+    host thread, so one batch's latency-bound launches fill the SMs another leaves
+    idle; one more thread plans the upcoming batches (marshalling, sorting, chunking:
+    the planner releases the GIL).  Every batch still has its own upload and
+    readback.  Up to ``inflight + 1`` batches are planned ahead of the solving ones."""
     dev = torch.device(device)
     if dev.index is None:
         dev = torch.device("cuda", torch.cuda.current_device())
+    inflight = max(1, int(inflight))
+    streams = [torch.cuda.Stream(device=dev) for _ in range(inflight)]
     it = iter(batches)
-    with ThreadPoolExecutor(1) as ex:
-        first = next(it, None)
-        fut = ex.submit(_plan_on, dev, first, precision) if first is not None else None
-        while fut is not None:
-            hp = fut.result()
-            nxt = next(it, None)
-            fut = ex.submit(_plan_on, dev, nxt, precision) if nxt is not None else None
-            bs = BatchSolver(device=dev, stream=stream, plan=hp)
-            try:
-                if params:
-                    bs.set_params(**params)
-                if controller is not None:
-                    bs.set_controller(controller)
-                st = bs.solve(check_every=check_every)
-                poses, alphas = bs.get_state()
-            finally:
-                bs.close()
-            yield st, poses, alphas
+    plans: collections.deque = collections.deque()    # planned, not yet solving
+    pending: collections.deque = collections.deque()  # solving, in batch order
+    with ThreadPoolExecutor(1) as planner, ThreadPoolExecutor(inflight) as drivers:
+        k = 0
+
+        def plan_ahead():
+            while len(plans) < inflight + 1:
+                nxt = next(it, None)
+                if nxt is None:
+                    return
+                plans.append(planner.submit(_plan_on, dev, nxt, precision))
+
+        def start_one():
+            nonlocal k
+            if plans:
+                pending.append(drivers.submit(_drive, dev, streams[k % inflight], plans.popleft(), params,
+                                              controller, check_every))
+                k += 1
+
+        plan_ahead()
+        for _ in range(inflight):
+            start_one()
+        plan_ahead()
+        while pending:
+            res = pending.popleft().result()
+            start_one()  # the next batch takes the stream of the batch just finished
+            plan_ahead()
+            yield res
 
 
 class CudaSolver:
