@@ -7,7 +7,8 @@
 //                  (column-major, lower), the exact S (double-float / FP64,
 //                  full, row-major) for the residual, g0 = g - g_L; clears S_L, g_L
 //   per 64-column panel kb:
-//     k_lg_potrf   one CTA factors the 64x64 diagonal block in shared memory
+//     k_lg_potrf   one CTA factors the 64x64 diagonal block in shared memory,
+//                  16 columns at a time (register-resident 16x16 blocks)
 //     k_lg_trsm    thread per row below it: L(i, kb:) = S(i, kb:) L_kk^-T
 //     k_lg_syrk    one CTA per 64x64 tile of the trailing lower triangle,
 //                  C -= L_i L_j^T from shared-memory tiles, 4x4 outputs per thread
@@ -71,13 +72,20 @@ __global__ void __launch_bounds__(256) k_lg_assemble(PlanView pv, WorkView wv, i
   }
 }
 
+// One CTA factors the 64x64 diagonal block in shared memory, 16 columns at a time:
+// warp 0 factors each 16x16 diagonal sub-block in registers (lane = row; column k
+// takes one shuffle of the pivot and one per later row), then all threads solve
+// the panel rows below it and update the rest of the panel's lower triangle:
+// three barriers per 16 columns.
 template <typename T>
 __global__ void __launch_bounds__(256) k_lg_potrf(PlanView pv, WorkView wv, int b, int kb) {
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  constexpr int kSub = 16;
   __shared__ T D[kLgNB][kLgNB + 1];
-  __shared__ T rinv_s;
+  __shared__ T di[kLgNB];
   __shared__ int bad;
   const int P = 6 * pv.p_npose[b], nb = min(kLgNB, P - kb), tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
   T *fac = reinterpret_cast<T *>(wv.fac) + pv.p_S_off[b];
   T *dinv = reinterpret_cast<T *>(wv.lg_dinv) + pv.p_param_off[b];
   for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
@@ -86,32 +94,77 @@ __global__ void __launch_bounds__(256) k_lg_potrf(PlanView pv, WorkView wv, int 
   }
   if (tid == 0) bad = 0;
   __syncthreads();
-  for (int k = 0; k < nb; ++k) {
-    if (tid == 0) {
-      const T d = D[k][k];
-      if (!(d > T(0)) || !isfinite((double)d)) bad = 1;
-      const T lkk = sqrt(d);
-      D[k][k] = lkk;
-      rinv_s = T(1) / lkk;
-      dinv[kb + k] = rinv_s;
+  for (int s0 = 0; s0 < nb; s0 += kSub) {
+    const int w = min(kSub, nb - s0), se = s0 + w;
+    if (warp == 0) {
+      T a[kSub];
+#pragma unroll
+      for (int j = 0; j < kSub; ++j) a[j] = (lane < w && j <= lane) ? D[s0 + lane][s0 + j] : T(0);
+      bool badl = false;
+      // (columns k >= w of a narrow last sub-block run on a unit pivot and are discarded)
+#pragma unroll
+      for (int k = 0; k < kSub; ++k) {
+        const T dk = __shfl_sync(0xffffffffu, a[k], k);
+        const T d = k < w ? dk : T(1);
+        badl = badl || !(d > T(0)) || !(d < T(INFINITY));
+        const T lkk = sqrt(d), rinv = T(1) / lkk;
+        const T lik = lane > k ? a[k] * rinv : (lane == k ? lkk : a[k]);
+        a[k] = lik;
+#pragma unroll
+        for (int j = 0; j < kSub; ++j) {
+          const T ljk = __shfl_sync(0xffffffffu, lik, j);
+          if (j > k && lane >= j) a[j] -= lik * ljk;
+        }
+        if (lane == 0 && k < w) di[s0 + k] = rinv;
+      }
+#pragma unroll
+      for (int j = 0; j < kSub; ++j)
+        if (lane < w && j <= lane) D[s0 + lane][s0 + j] = a[j];
+      if (badl && lane == 0) bad = 1;
     }
     __syncthreads();
-    for (int i = k + 1 + tid; i < nb; i += blockDim.x) D[i][k] *= rinv_s;
+    // panel rows below the sub-block: L(i, s0:se) = D(i, s0:se) L_sub^-T (right-looking)
+    for (int i = se + tid; i < nb; i += blockDim.x) {
+      T x[kSub];
+#pragma unroll
+      for (int c = 0; c < kSub; ++c) x[c] = c < w ? D[i][s0 + c] : T(0);
+#pragma unroll
+      for (int c = 0; c < kSub; ++c) {
+        x[c] = c < w ? x[c] * di[s0 + c] : T(0);
+#pragma unroll
+        for (int m = c + 1; m < kSub; ++m)
+          if (m < w) x[m] -= x[c] * D[s0 + m][s0 + c];
+      }
+#pragma unroll
+      for (int c = 0; c < kSub; ++c)
+        if (c < w) D[i][s0 + c] = x[c];
+    }
     __syncthreads();
-    const int m = nb - k - 1;
+    // the rest of the panel: D(i, j) -= sum_c L(i, c) L(j, c) for se <= j <= i < nb
+    const int m = nb - se;
     for (int idx = tid; idx < m * m; idx += blockDim.x) {
-      const int ii = k + 1 + idx % m, jj = k + 1 + idx / m;
-      if (ii >= jj) D[ii][jj] -= D[ii][k] * D[jj][k];
+      const int ii = se + idx % m, jj = se + idx / m;
+      if (ii >= jj) {
+        T acc = T(0);
+#pragma unroll
+        for (int c = 0; c < kSub; ++c)
+          if (c < w) acc += D[ii][s0 + c] * D[jj][s0 + c];
+        D[ii][jj] -= acc;
+      }
     }
     __syncthreads();
   }
   if (tid == 0 && bad) wv.lm[b].fail = 1;
+  for (int k = tid; k < nb; k += blockDim.x) dinv[kb + k] = di[k];
   for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
     const int i = idx % nb, j = idx / nb;
     if (i >= j) fac[(size_t)(kb + j) * P + kb + i] = D[i][j];
   }
 }
 
+// thread per row below the panel: L(i, kb:ke) = S(i, kb:ke) L_kk^-T, right-looking
+// (once x_j is final it is removed from every later column: independent updates
+// instead of one dependent chain per column)
 template <typename T>
 __global__ void __launch_bounds__(128) k_lg_trsm(PlanView pv, WorkView wv, int b, int kb) {
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
@@ -121,11 +174,20 @@ __global__ void __launch_bounds__(128) k_lg_trsm(PlanView pv, WorkView wv, int b
   const T *fac_c = reinterpret_cast<const T *>(wv.fac) + pv.p_S_off[b];
   T *fac = reinterpret_cast<T *>(wv.fac) + pv.p_S_off[b];
   const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + pv.p_param_off[b];
-  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
-    const int i = idx % nb, j = idx / nb;
-    D[i][j] = i > j ? fac_c[(size_t)(kb + j) * P + kb + i] : T(0);
+  for (int idx0 = tid; idx0 < kLgNB * kLgNB; idx0 += 8 * blockDim.x) {
+    T v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {  // loads first
+      const int idx = idx0 + q * blockDim.x, i = idx % kLgNB, j = idx / kLgNB;
+      v[q] = (idx < kLgNB * kLgNB && i > j && i < nb) ? fac_c[(size_t)(kb + j) * P + kb + i] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = idx0 + q * blockDim.x;
+      if (idx < kLgNB * kLgNB) D[idx % kLgNB][idx / kLgNB] = v[q];
+    }
   }
-  for (int j = tid; j < nb; j += blockDim.x) di[j] = dinv[kb + j];
+  for (int j = tid; j < kLgNB; j += blockDim.x) di[j] = j < nb ? dinv[kb + j] : T(0);
   __syncthreads();
   const int i = ke + blockIdx.x * blockDim.x + tid;
   if (i >= P) return;
@@ -134,10 +196,9 @@ __global__ void __launch_bounds__(128) k_lg_trsm(PlanView pv, WorkView wv, int b
   for (int j = 0; j < kLgNB; ++j) x[j] = j < nb ? fac_c[(size_t)(kb + j) * P + i] : T(0);
 #pragma unroll
   for (int j = 0; j < kLgNB; ++j) {
-    T v = x[j];
+    x[j] *= di[j];
 #pragma unroll
-    for (int m = 0; m < j; ++m) v -= x[m] * D[j][m];
-    x[j] = j < nb ? v * di[j] : T(0);
+    for (int m = j + 1; m < kLgNB; ++m) x[m] -= x[j] * D[m][j];
   }
 #pragma unroll
   for (int j = 0; j < kLgNB; ++j)
