@@ -297,19 +297,40 @@ __global__ void __launch_bounds__(512) k_lg_solve(PlanView pv, WorkView wv, int 
       }
     }
     __syncthreads();
+    // rows below: all 64 loads of a row are issued before the sums (four chains)
     for (int i = ke + tid; i < P; i += blockDim.x) {
-      T v = y[i];
-      for (int c = 0; c < nb; ++c) v -= Lat(i, kb + c) * y[kb + c];
-      y[i] = v;
+      T lv[kLgNB];
+#pragma unroll
+      for (int c = 0; c < kLgNB; ++c) lv[c] = c < nb ? Lat(i, kb + c) : T(0);
+      T v0 = y[i], v1 = T(0), v2 = T(0), v3 = T(0);
+#pragma unroll
+      for (int c = 0; c < kLgNB; c += 4) {
+        v0 -= lv[c] * y[kb + c];
+        v1 -= lv[c + 1] * y[kb + c + 1];
+        v2 -= lv[c + 2] * y[kb + c + 2];
+        v3 -= lv[c + 3] * y[kb + c + 3];
+      }
+      y[i] = (v0 + v1) + (v2 + v3);
     }
     __syncthreads();
   }
   // backward L^T w = z, blocks from the bottom
   for (int kb = ((P - 1) / kLgNB) * kLgNB; kb >= 0; kb -= kLgNB) {
     const int nb = min(kLgNB, P - kb), ke = kb + nb;
-    for (int c = warp; c < nb; c += nw) {
-      T acc = T(0);
-      for (int i = ke + lane; i < P; i += 32) acc += Lat(i, kb + c) * y[i];
+    for (int c = warp; c < nb; c += nw) {  // eight rows in flight per lane
+      T a[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) a[q] = T(0);
+      int i = ke + lane;
+      for (; i + 7 * 32 < P; i += 8 * 32) {
+        T lv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) lv[q] = Lat(i + 32 * q, kb + c);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] += lv[q] * y[i + 32 * q];
+      }
+      for (; i < P; i += 32) a[0] += Lat(i, kb + c) * y[i];
+      T acc = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
       acc = warp_sum(acc);
       if (lane == 0) tmp[c] = acc;
     }
