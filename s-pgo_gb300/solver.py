@@ -247,7 +247,7 @@ class BatchSolver:
         return [dict(cost0=s.cost0, cost=s.cost, lam=s.lambda_, iterations=s.iterations, accepted=s.accepted,
                      status=s.status, factor_failures=s.factor_failures) for s in out]
 
-    def solve(self, check_every: int = 4) -> List[dict]:
+    def solve(self, check_every: int = 8) -> List[dict]:
         """Reset and run Nielsen LM until every problem stops (see ``spgo_lm_solve``)."""
         it = C.c_int32()
         nat.check(self.L.spgo_lm_solve(self._solver, int(check_every), C.byref(it), self._sp()), "lm_solve")
@@ -373,7 +373,7 @@ def _drive(device: torch.device, stream: torch.cuda.Stream, plan_future, params,
 
 def solve_stream(batches: Iterable[Sequence[Problem]], precision: str = "mixed", params: Optional[dict] = None,
                  controller: Optional[torch.Tensor] = None, device="cuda", inflight: int = 2,
-                 check_every: int = 4) -> Iterator[Tuple[List[dict], list, list]]:
+                 check_every: int = 8) -> Iterator[Tuple[List[dict], list, list]]:
     """Solve batch after batch (each a sequence of ``Problem``) with Nielsen LM (or
     the learned controller), yielding ``(statuses, poses, inverse_depths)`` per batch
     in order.
