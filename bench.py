@@ -394,7 +394,7 @@ def run_ours(args):
         s2.close()
         del poses, alphas
     serial_val = N_PROBLEMS * world / (float(np.mean(e2e_ms)) / 1e3)
-    n_stream = max(8, args.steps)
+    n_stream = max(12, args.steps)
     stream_params = {**dict(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4, use_tc=args.tc), **(tuned or {})}
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -443,7 +443,7 @@ def main():
     ap.add_argument("--tc", type=int, default=1, help="1: tensor-core Schur complement in the mixed path, 0: SIMT")
     ap.add_argument("--controller", type=int, default=1, help="1: learned damping (shipped weights), 0: Nielsen")
     ap.add_argument("--autotune", type=int, default=1, help="1: time the run-time launch shapes first")
-    ap.add_argument("--inflight", type=int, default=2, help="e2e: batches solving at once in solve_stream")
+    ap.add_argument("--inflight", type=int, default=4, help="e2e: batches solving at once in solve_stream")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
