@@ -163,16 +163,17 @@ struct spgo_plan {
   size_t static_bytes = 0, ws_bytes = 0;
   // host staging: [0, big_bytes) of the device buffer, then the small arrays
   HostBlock big, small;
-  mutable cudaEvent_t uploaded = nullptr;  // the last upload from the blocks
+  mutable std::vector<cudaEvent_t> uploads;  // one per upload from the blocks
+  mutable std::mutex upload_mu;              // solvers bound from several threads
   // workspace segment offsets
   size_t w_Sx = 0, w_lg = 0;
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl;
 
   ~spgo_plan() {
-    if (uploaded) {  // the blocks go back to the cache only once no copy reads them
-      cudaEventSynchronize(uploaded);
-      cudaEventDestroy(uploaded);
+    for (cudaEvent_t e : uploads) {  // the blocks go back to the cache only once no copy reads them
+      cudaEventSynchronize(e);
+      cudaEventDestroy(e);
     }
     arena_put(big);
     arena_put(small);
@@ -962,14 +963,19 @@ int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_byte
   cudaStream_t st = (cudaStream_t)stream;
   {  // two copies from the page-locked staging blocks; the event keeps the blocks
      // out of the cache until the copies have read them
+    std::lock_guard<std::mutex> lk(plan->upload_mu);
     cudaError_t e = cudaSuccess;
     if (plan->big_bytes)
       e = cudaMemcpyAsync(s->d_static, plan->big.ptr, plan->big_bytes, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && plan->static_bytes > plan->big_bytes)
       e = cudaMemcpyAsync(s->d_static + plan->big_bytes, plan->small.ptr, plan->static_bytes - plan->big_bytes,
                           cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && !plan->uploaded) e = cudaEventCreateWithFlags(&plan->uploaded, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventRecord(plan->uploaded, st);
+    cudaEvent_t ev = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) {
+      plan->uploads.push_back(ev);
+      e = cudaEventRecord(ev, st);
+    }
     if (e != cudaSuccess) {
       delete s;
       return fail(SPGO_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
