@@ -184,6 +184,16 @@ int spgo_gn_step(spgo_solver *s, int32_t iterations, float step_size, void *stre
 int spgo_lm_reset(spgo_solver *s, void *stream);
 int spgo_lm_iterate(spgo_solver *s, int32_t n_iters, void *stream);
 int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream);
+/* Per-iteration trace of every problem since the last reset (the cost trace the
+ * reference's callers build by reading poses back after each step()): for
+ * iteration k < min(iterations, SPGO_TRACE_MAX) of problem b, host arrays indexed
+ * [b * capacity + k] receive the cost after the iteration (the candidate's when it
+ * was accepted, else unchanged), the lambda the step was solved with, and 1 / 0
+ * for accepted / rejected.  n_iters[b] = iterations recorded.  Synchronises the
+ * stream.  Any output pointer may be NULL. */
+#define SPGO_TRACE_MAX 128
+int spgo_lm_trace(spgo_solver *s, int32_t capacity, double *cost, double *lambda, int32_t *accepted,
+                  int32_t *n_iters, void *stream);
 /* Convenience: reset, iterate until every problem stops or max_iters, with a
  * status check every `check_every` iterations.  Returns the iteration count
  * in *iters_done (max over problems). */

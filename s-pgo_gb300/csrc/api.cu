@@ -168,7 +168,7 @@ struct spgo_plan {
   // workspace segment offsets
   size_t w_Sx = 0, w_lg = 0;
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
-      w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl;
+      w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl, w_trace;
 
   ~spgo_plan() {
     for (cudaEvent_t e : uploads) {  // the blocks go back to the cache only once no copy reads them
@@ -299,6 +299,7 @@ static void build_layout(spgo_plan *p) {
   p->w_lmb = take((size_t)p->B * sizeof(LMState));
   p->w_probe = take((size_t)p->B * 32 * 8);
   p->w_ctrl = take(mlp_deployed_bytes());
+  p->w_trace = take((size_t)p->B * SPGO_TRACE_MAX * 3 * 8);
   p->ws_bytes = o;
 }
 
@@ -764,6 +765,7 @@ static void make_views(spgo_solver *s) {
   x.pred_acc = reinterpret_cast<double *>(w + p->w_pred);
   x.lm_backup = reinterpret_cast<LMState *>(w + p->w_lmb);
   x.probe_costs = reinterpret_cast<double *>(w + p->w_probe);
+  x.trace = reinterpret_cast<double *>(w + p->w_trace);
   x.ctrl = w + p->w_ctrl;
 }
 
@@ -1112,12 +1114,12 @@ int spgo_lm_iterate(spgo_solver *s, int32_t n_iters, void *stream) {
 }
 
 int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream) {
-  if (!s || !out) return fail(SPGO_ERR_INVALID_ARG, "null argument");
+  if (!s) return fail(SPGO_ERR_INVALID_ARG, "null argument");
   LMState *h = reinterpret_cast<LMState *>(s->h_lm.ptr);
   CUDA_TRY(cudaMemcpyAsync(h, s->wv.lm, sizeof(LMState) * (size_t)s->plan->B, cudaMemcpyDeviceToHost,
                            (cudaStream_t)stream));
   CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
-  for (int b = 0; b < s->plan->B; ++b) {
+  for (int b = 0; out && b < s->plan->B; ++b) {
     out[b].cost0 = h[b].cost0;
     out[b].cost = h[b].cost;
     out[b].lambda = h[b].lam;
@@ -1125,6 +1127,29 @@ int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream) {
     out[b].accepted = h[b].accepted;
     out[b].status = h[b].status;
     out[b].factor_failures = h[b].factor_failures;
+  }
+  return SPGO_OK;
+}
+
+int spgo_lm_trace(spgo_solver *s, int32_t capacity, double *cost, double *lambda, int32_t *accepted,
+                  int32_t *n_iters, void *stream) {
+  if (!s || capacity < 0) return fail(SPGO_ERR_INVALID_ARG, "bad argument");
+  const int B = s->plan->B;
+  std::vector<double> h((size_t)B * SPGO_TRACE_MAX * 3);
+  CUDA_TRY(cudaMemcpyAsync(h.data(), s->wv.trace, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                           (cudaStream_t)stream));
+  int rc = spgo_lm_status(s, nullptr, stream);  // (synchronises; fills the status cache)
+  if (rc != SPGO_OK) return rc;
+  const LMState *st = reinterpret_cast<const LMState *>(s->h_lm.ptr);
+  for (int b = 0; b < B; ++b) {
+    const int n = std::min(std::min((int)st[b].iters, (int)SPGO_TRACE_MAX), capacity);
+    if (n_iters) n_iters[b] = n;
+    for (int k = 0; k < n; ++k) {
+      const double *t = &h[((size_t)b * SPGO_TRACE_MAX + k) * 3];
+      if (cost) cost[(size_t)b * capacity + k] = t[0];
+      if (lambda) lambda[(size_t)b * capacity + k] = t[1];
+      if (accepted) accepted[(size_t)b * capacity + k] = t[2] != 0.0 ? 1 : 0;
+    }
   }
   return SPGO_OK;
 }

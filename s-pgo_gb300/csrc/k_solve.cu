@@ -565,6 +565,8 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
   const double F = s.cost;
   const double Fn = wv.cost_acc[b];
   const double pred = 0.5 * wv.pred_acc[b];
+  const int it = s.iters;
+  const double lam_used = s.lam;
   wv.cost_acc[b] = 0.0;
   wv.pred_acc[b] = 0.0;
   s.cost_cand = Fn;
@@ -599,6 +601,12 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
   }
   s.fail = 0;
   if (s.status == 0 && s.iters >= prm.max_iters) s.status = SPGO_STATUS_MAX_ITERS;
+  if (it < SPGO_TRACE_MAX) {
+    double *t = wv.trace + ((size_t)b * SPGO_TRACE_MAX + it) * 3;
+    t[0] = s.cost;
+    t[1] = lam_used;
+    t[2] = ok ? 1.0 : 0.0;
+  }
 }
 
 int launch_decide(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream) {

@@ -99,6 +99,7 @@ struct WorkView {
   LMState *lm;          // [B]
   LMState *lm_backup;   // [B] (lambda probes)
   double *probe_costs;  // [32][B]
+  double *trace;        // [B][SPGO_TRACE_MAX][3]: cost after the iteration, lambda used, accepted
   void *ctrl;           // deployed controller weights (BF16-rounded, inference layout)
   // large reduced systems (k_chol_large.cu), allocated when the batch has any
   void *Sx;             // [total_S] exact S: (hi, lo) float pairs on the FP32 path, doubles on FP64

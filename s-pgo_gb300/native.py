@@ -25,8 +25,9 @@ EXPORTED = [
     "spgo_gn_step", "spgo_lm_reset", "spgo_lm_iterate", "spgo_lm_status", "spgo_lm_solve",
     "spgo_export_system", "spgo_launch_count", "spgo_profile_enable", "spgo_profile_read",
     "spgo_cost_noalloc", "spgo_export_reduced", "spgo_mlp_forward", "spgo_mlp_grad", "spgo_mlp_adam",
-    "spgo_lm_set_controller", "spgo_lm_features", "spgo_lm_probe", "spgo_autotune",
+    "spgo_lm_set_controller", "spgo_lm_features", "spgo_lm_probe", "spgo_autotune", "spgo_lm_trace",
 ]
+TRACE_MAX = 128
 MLP_PARAMS, MLP_INPUTS, MLP_CACHE_PER_SAMPLE = 5378, 16, 386
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
                  "update", "bookkeeping"]
@@ -109,6 +110,8 @@ def lib() -> C.CDLL:
     L.spgo_lm_set_controller.argtypes = [vp, vp, vp]
     L.spgo_lm_features.argtypes = [vp, vp, vp]
     L.spgo_lm_probe.argtypes = [vp, i32, C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
+    L.spgo_lm_trace.argtypes = [vp, i32, vp, vp, vp, vp, vp]
+    L.spgo_lm_trace.restype = C.c_int
     L.spgo_autotune.argtypes = [vp, C.POINTER(Params), vp]
     L.spgo_autotune.restype = C.c_int
     for name in ("spgo_mlp_forward", "spgo_mlp_grad", "spgo_mlp_adam", "spgo_lm_set_controller",

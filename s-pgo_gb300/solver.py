@@ -247,6 +247,24 @@ class BatchSolver:
         return [dict(cost0=s.cost0, cost=s.cost, lam=s.lambda_, iterations=s.iterations, accepted=s.accepted,
                      status=s.status, factor_failures=s.factor_failures) for s in out]
 
+    def trace(self) -> List[dict]:
+        """Per problem, the LM iterations since the last reset (up to ``native.TRACE_MAX``):
+        ``cost`` after each iteration, the ``lam`` its step was solved with, and whether
+        it was ``accepted`` (``spgo_lm_trace``)."""
+        B, cap = len(self.problems), nat.TRACE_MAX
+        cost = np.zeros(B * cap)
+        lam = np.zeros(B * cap)
+        acc = np.zeros(B * cap, dtype=np.int32)
+        n = np.zeros(B, dtype=np.int32)
+        nat.check(self.L.spgo_lm_trace(self._solver, cap, cost.ctypes.data, lam.ctypes.data, acc.ctypes.data,
+                                       n.ctypes.data, self._sp()), "lm_trace")
+        out = []
+        for b in range(B):
+            k = int(n[b])
+            sl = slice(b * cap, b * cap + k)
+            out.append(dict(cost=cost[sl].copy(), lam=lam[sl].copy(), accepted=acc[sl].astype(bool)))
+        return out
+
     def solve(self, check_every: int = 8) -> List[dict]:
         """Reset and run Nielsen LM until every problem stops (see ``spgo_lm_solve``)."""
         it = C.c_int32()

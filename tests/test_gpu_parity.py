@@ -385,3 +385,27 @@ def test_solve_stream_matches_batch_solver(built_lib, cuda_device):
             assert poses[b].shape == (p.n_poses, 4, 4) and alphas[b].shape == (p.n_landmarks,)
             assert np.abs(poses[b] - bs.get_poses(b)).max() < 1e-4
         bs.close()
+
+
+def test_lm_trace_matches_status(built_lib, cuda_device):
+    """spgo_lm_trace: one record per LM iteration; the cost never rises, it changes only
+    on accepted steps, its last value is the status cost; with the FP64 path the trace
+    equals the oracle's iteration by iteration."""
+    probs = [f32_obs(scenes.circle_scene(s, n, l)) for s, n, l in [(95, 6, 90), (96, 9, 160)]]
+    bs = BatchSolver(probs, precision="fp64")
+    bs.set_params(loss="l2", max_iters=12, tol=1e-9, lambda0=1e-4)
+    st = bs.solve()
+    tr = bs.trace()
+    for b, p in enumerate(probs):
+        t = tr[b]
+        assert len(t["cost"]) == st[b]["iterations"] and int(t["accepted"].sum()) == st[b]["accepted"]
+        assert t["cost"][-1] == st[b]["cost"]
+        prev = st[b]["cost0"]
+        for c, a in zip(t["cost"], t["accepted"]):
+            assert (c < prev) if a else (c == prev)
+            prev = c
+        res = S.lm_solve(p.copy(), S.Loss(), max_iters=12, tol=1e-9, lam0=1e-4)
+        ref_cost = [x["cand"] if x["rho"] > 0 else x["cost"] for x in res.trace]
+        assert np.allclose(t["cost"], ref_cost, rtol=1e-9, atol=0)
+        assert np.allclose(t["lam"], [x["lam"] for x in res.trace], rtol=1e-9, atol=0)
+    bs.close()
