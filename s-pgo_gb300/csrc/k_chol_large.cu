@@ -277,8 +277,20 @@ __global__ void __launch_bounds__(512) k_lg_solve(PlanView pv, WorkView wv, int 
       for (int h = 0; h < nb; h += 32) {
         const int w = min(32, nb - h), u = kb + h + lane;  // lane = unknown u
         T v = lane < w ? y[u] : T(0);
-        if (h > 0 && lane < w)  // the first half's unknowns are final
-          for (int c = 0; c < h; ++c) v -= Lat(u, kb + c) * y[kb + c];
+        if (h > 0) {  // the first half's unknowns are final (h = 32): loads first, four chains
+          T lq[32];
+#pragma unroll
+          for (int c = 0; c < 32; ++c) lq[c] = lane < w ? Lat(u, kb + c) : T(0);
+          T v1 = T(0), v2 = T(0), v3 = T(0);
+#pragma unroll
+          for (int c = 0; c < 32; c += 4) {
+            v -= lq[c] * y[kb + c];
+            v1 -= lq[c + 1] * y[kb + c + 1];
+            v2 -= lq[c + 2] * y[kb + c + 2];
+            v3 -= lq[c + 3] * y[kb + c + 3];
+          }
+          v += (v1 + v2) + v3;
+        }
         T lr[32], di[32];
 #pragma unroll
         for (int c = 0; c < 32; ++c) {
@@ -339,8 +351,20 @@ __global__ void __launch_bounds__(512) k_lg_solve(PlanView pv, WorkView wv, int 
       for (int h = ((nb - 1) / 32) * 32; h >= 0; h -= 32) {
         const int w = min(32, nb - h), u = kb + h + lane;
         T v = lane < w ? y[u] - tmp[h + lane] : T(0);
-        if (lane < w)  // the later half's unknowns are final
-          for (int m = h + w; m < nb; ++m) v -= Lat(kb + m, u) * y[kb + m];
+        if (h + w < nb) {  // the later half's unknowns are final (h = 0, w = 32): loads first
+          T lq[32];
+#pragma unroll
+          for (int c = 0; c < 32; ++c) lq[c] = (lane < w && 32 + c < nb) ? Lat(kb + 32 + c, u) : T(0);
+          T v1 = T(0), v2 = T(0), v3 = T(0);
+#pragma unroll
+          for (int c = 0; c < 32; c += 4) {
+            v -= lq[c] * (32 + c < nb ? y[kb + 32 + c] : T(0));
+            v1 -= lq[c + 1] * (33 + c < nb ? y[kb + 33 + c] : T(0));
+            v2 -= lq[c + 2] * (34 + c < nb ? y[kb + 34 + c] : T(0));
+            v3 -= lq[c + 3] * (35 + c < nb ? y[kb + 35 + c] : T(0));
+          }
+          v += (v1 + v2) + v3;
+        }
         T lc[32], di[32];
 #pragma unroll
         for (int c = 0; c < 32; ++c) {
