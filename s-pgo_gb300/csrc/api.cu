@@ -166,7 +166,7 @@ struct spgo_plan {
   mutable std::vector<cudaEvent_t> uploads;  // one per upload from the blocks
   mutable std::mutex upload_mu;              // solvers bound from several threads
   // workspace segment offsets
-  size_t w_Sx = 0, w_lg = 0;
+  size_t w_Sx = 0, w_lg = 0, w_lgflag = 0;
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl, w_trace;
 
@@ -289,6 +289,7 @@ static void build_layout(spgo_plan *p) {
   p->w_fac = take(any_large ? (size_t)p->total_S * ts : 0);
   p->w_Sx = take(any_large ? (size_t)p->total_S * 8 : 0);
   p->w_lg = take(any_large ? (size_t)p->total_params * 8 * 6 : 0);
+  p->w_lgflag = take(any_large ? (size_t)p->total_params * 2 * sizeof(int) : 0);
   p->w_delta = take((size_t)p->total_params * 8);
   p->w_C = take((size_t)(p->L + 64) * ts);  // + 64: the tensor-core Schur copies 16-byte aligned supersets
   p->w_ga = take((size_t)(p->L + 64) * ts);  // + 64: as C
@@ -755,6 +756,7 @@ static void make_views(spgo_solver *s) {
     x.lg_xs = reinterpret_cast<float *>(lg + 2 * tp);  // 2 tp floats
     x.lg_y = lg + 3 * tp;
     x.lg_dinv = lg + 4 * tp;
+    x.lg_flag = reinterpret_cast<int *>(w + p->w_lgflag);
   }
   x.delta = reinterpret_cast<double *>(w + p->w_delta);
   x.C = w + p->w_C;
@@ -807,7 +809,8 @@ static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
     PROF(K_FACTOR);
     CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st));
     for (const int b : s->plan->large)
-      CUDA_TRY(launch_factor_large<T>(s->pv, s->wv, b, 6 * s->plan->p_npose[b], mixed ? s->prm.refine_steps : 0, st));
+      CUDA_TRY(launch_factor_large<T>(s->pv, s->wv, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b],
+                                      mixed ? s->prm.refine_steps : 0, st));
   }
   return SPGO_OK;
 }

@@ -12,9 +12,9 @@
 //     k_lg_trsm    thread per row below it: L(i, kb:) = S(i, kb:) L_kk^-T
 //     k_lg_syrk    one CTA per 64x64 tile of the trailing lower triangle,
 //                  C -= L_i L_j^T from shared-memory tiles, 4x4 outputs per thread
-//   k_lg_solve     one 512-thread CTA: blocked forward / backward substitution
-//                  (32-unknown shuffle chains inside each 64-block, parallel
-//                  row and column updates), x += solution
+//   k_lg_fwd/bwd   forward / backward substitution with one CTA per 64-row block,
+//                  chained by per-block flags (32-unknown shuffle chains inside each
+//                  diagonal block), x += solution
 //   k_lg_resid     warp per row: g0 - S x from the exact S (between two solves)
 // Replaces, for such problems, the reference's libtorch Cholesky of the dense
 // reduced system (src/Optimization/linear_solvers.cu:195-218).
@@ -252,150 +252,225 @@ __global__ void __launch_bounds__(256) k_lg_syrk(PlanView pv, WorkView wv, int b
     }
 }
 
-// Blocked substitutions with the factor in global memory, one 512-thread CTA.
-// first: start from g0 (x = 0); else from the residual in lg_y.  last: write
-// delta (zero if the factorisation failed); else keep x and its double-float
-// split for the residual.
+// ---- substitutions spread over the GPU: one CTA per 64-row block ----
+// Forward L z = r: the CTA of block k adds up L(k, j) z_j for every earlier block j
+// as soon as that block's flag is up, then solves its diagonal block and raises its
+// own flag; backward L^T x = z the same from the bottom (the CTA of block k waits
+// only for blocks finished by lower-numbered CTAs, so the chain never waits on a CTA
+// that has not started).  Thread (r, q) handles unknown r of the block and a 16-wide
+// quarter q of each other block.  Every wait is bounded (2 s); a timeout marks the
+// problem failed (the step is rejected) and the CTA carries on.
+constexpr uint64_t kLgWaitNs = 2000000000ull;
+
+__device__ __forceinline__ uint64_t lg_clock_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool lg_wait_flag(const int *flag, uint64_t deadline) {
+  for (int it = 0;; ++it) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+    if (v) return true;
+    if ((it & 63) == 63 && lg_clock_ns() > deadline) return false;
+    __nanosleep(100);
+  }
+}
+
+__device__ __forceinline__ void lg_set_flag(int *flag) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(flag), "r"(1) : "memory");
+}
+
 template <typename T>
-__global__ void __launch_bounds__(512) k_lg_solve(PlanView pv, WorkView wv, int b, int first, int last) {
+__global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b, int first) {
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ T tmp[kLgNB];
+  __shared__ T part[4][kLgNB];
+  __shared__ T zs[kLgNB];
+  __shared__ int timed_out;
   const int P = 6 * pv.p_npose[b], po = pv.p_param_off[b];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
-  T *y = reinterpret_cast<T *>(smem_raw);
+  const int k = blockIdx.x, kb = k * kLgNB, nb = min(kLgNB, P - kb);
+  const int tid = threadIdx.x, r = tid & 63, q = tid >> 6, warp = tid >> 5, lane = tid & 31;
   const T *L = reinterpret_cast<const T *>(wv.fac) + pv.p_S_off[b];
-  const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + po;
-  T *ly = reinterpret_cast<T *>(wv.lg_y) + po;
-  for (int i = tid; i < P; i += blockDim.x) y[i] = first ? (T)wv.lg_g0[po + i] : ly[i];
-  __syncthreads();
   auto Lat = [&](int i, int j) { return L[(size_t)j * P + i]; };  // L(i, j), i >= j
-  // forward L z = y
-  for (int kb = 0; kb < P; kb += kLgNB) {
-    const int nb = min(kLgNB, P - kb), ke = kb + nb;
-    if (warp == 0) {
-      for (int h = 0; h < nb; h += 32) {
-        const int w = min(32, nb - h), u = kb + h + lane;  // lane = unknown u
-        T v = lane < w ? y[u] : T(0);
-        if (h > 0) {  // the first half's unknowns are final (h = 32): loads first, four chains
-          T lq[32];
-#pragma unroll
-          for (int c = 0; c < 32; ++c) lq[c] = lane < w ? Lat(u, kb + c) : T(0);
-          T v1 = T(0), v2 = T(0), v3 = T(0);
-#pragma unroll
-          for (int c = 0; c < 32; c += 4) {
-            v -= lq[c] * y[kb + c];
-            v1 -= lq[c + 1] * y[kb + c + 1];
-            v2 -= lq[c + 2] * y[kb + c + 2];
-            v3 -= lq[c + 3] * y[kb + c + 3];
-          }
-          v += (v1 + v2) + v3;
-        }
-        T lr[32], di[32];
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          lr[c] = (lane < w && c < lane) ? Lat(u, kb + h + c) : T(0);
-          di[c] = c < w ? dinv[kb + h + c] : T(0);
-        }
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          T yc = v * di[c];
-          yc = __shfl_sync(0xffffffffu, yc, c);
-          if (lane == c) v = yc;
-          v -= lr[c] * yc;
-        }
-        if (lane < w) y[u] = v;
-        __syncwarp();
-      }
-    }
+  const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + po;
+  T *z = reinterpret_cast<T *>(wv.lg_y) + po;  // in place: this block's right-hand side in, z out
+  int *flag = wv.lg_flag + po;
+  const uint64_t deadline = lg_clock_ns() + kLgWaitNs;
+  if (tid == 0) timed_out = 0;
+  __syncthreads();
+  T acc = T(0);
+  for (int j = 0; j < k; ++j) {  // earlier blocks are full 64-wide
+    if (tid == 0 && !timed_out && !lg_wait_flag(flag + j, deadline)) timed_out = 1;
     __syncthreads();
-    // rows below: all 64 loads of a row are issued before the sums (four chains)
-    for (int i = ke + tid; i < P; i += blockDim.x) {
-      T lv[kLgNB];
+    if (r < nb) {
+      const int c0 = j * kLgNB + 16 * q;
+      T lv[16], zv[16];
 #pragma unroll
-      for (int c = 0; c < kLgNB; ++c) lv[c] = c < nb ? Lat(i, kb + c) : T(0);
-      T v0 = y[i], v1 = T(0), v2 = T(0), v3 = T(0);
-#pragma unroll
-      for (int c = 0; c < kLgNB; c += 4) {
-        v0 -= lv[c] * y[kb + c];
-        v1 -= lv[c + 1] * y[kb + c + 1];
-        v2 -= lv[c + 2] * y[kb + c + 2];
-        v3 -= lv[c + 3] * y[kb + c + 3];
+      for (int c = 0; c < 16; ++c) {
+        lv[c] = Lat(kb + r, c0 + c);
+        zv[c] = __ldcg(z + c0 + c);
       }
-      y[i] = (v0 + v1) + (v2 + v3);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc += lv[c] * zv[c];
     }
-    __syncthreads();
   }
-  // backward L^T w = z, blocks from the bottom
-  for (int kb = ((P - 1) / kLgNB) * kLgNB; kb >= 0; kb -= kLgNB) {
-    const int nb = min(kLgNB, P - kb), ke = kb + nb;
-    for (int c = warp; c < nb; c += nw) {  // eight rows in flight per lane
-      T a[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) a[q] = T(0);
-      int i = ke + lane;
-      for (; i + 7 * 32 < P; i += 8 * 32) {
-        T lv[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) lv[q] = Lat(i + 32 * q, kb + c);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) a[q] += lv[q] * y[i + 32 * q];
-      }
-      for (; i < P; i += 32) a[0] += Lat(i, kb + c) * y[i];
-      T acc = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-      acc = warp_sum(acc);
-      if (lane == 0) tmp[c] = acc;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      for (int h = ((nb - 1) / 32) * 32; h >= 0; h -= 32) {
-        const int w = min(32, nb - h), u = kb + h + lane;
-        T v = lane < w ? y[u] - tmp[h + lane] : T(0);
-        if (h + w < nb) {  // the later half's unknowns are final (h = 0, w = 32): loads first
-          T lq[32];
-#pragma unroll
-          for (int c = 0; c < 32; ++c) lq[c] = (lane < w && 32 + c < nb) ? Lat(kb + 32 + c, u) : T(0);
-          T v1 = T(0), v2 = T(0), v3 = T(0);
-#pragma unroll
-          for (int c = 0; c < 32; c += 4) {
-            v -= lq[c] * (32 + c < nb ? y[kb + 32 + c] : T(0));
-            v1 -= lq[c + 1] * (33 + c < nb ? y[kb + 33 + c] : T(0));
-            v2 -= lq[c + 2] * (34 + c < nb ? y[kb + 34 + c] : T(0));
-            v3 -= lq[c + 3] * (35 + c < nb ? y[kb + 35 + c] : T(0));
-          }
-          v += (v1 + v2) + v3;
-        }
-        T lc[32], di[32];
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          lc[c] = (c < w && lane < c) ? Lat(kb + h + c, u) : T(0);
-          di[c] = c < w ? dinv[kb + h + c] : T(0);
-        }
-#pragma unroll
-        for (int c = 31; c >= 0; --c) {
-          T xc = v * di[c];
-          xc = __shfl_sync(0xffffffffu, xc, c);
-          if (lane == c) v = xc;
-          v -= lc[c] * xc;
-        }
-        if (lane < w) y[u] = v;
-        __syncwarp();
-      }
-    }
-    __syncthreads();
+  part[q][r] = acc;
+  __syncthreads();
+  if (tid < nb) {
+    const T rhs = first ? (T)wv.lg_g0[po + kb + tid] : z[kb + tid];
+    zs[tid] = rhs - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
   }
-  const bool failed = wv.lm[b].fail != 0;
-  for (int i = tid; i < P; i += blockDim.x) {
-    const double xi = (first ? 0.0 : wv.lg_x[po + i]) + (double)y[i];
+  __syncthreads();
+  if (warp == 0) {  // L_kk z_k = zs: two 32-unknown halves, lane = unknown
+    for (int h = 0; h < nb; h += 32) {
+      const int w = min(32, nb - h), u = kb + h + lane;
+      T v = lane < w ? zs[h + lane] : T(0);
+      if (h > 0) {  // the first half is final: loads first, four chains
+        T lq[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) lq[c] = lane < w ? Lat(u, kb + c) : T(0);
+        T v1 = T(0), v2 = T(0), v3 = T(0);
+#pragma unroll
+        for (int c = 0; c < 32; c += 4) {
+          v -= lq[c] * zs[c];
+          v1 -= lq[c + 1] * zs[c + 1];
+          v2 -= lq[c + 2] * zs[c + 2];
+          v3 -= lq[c + 3] * zs[c + 3];
+        }
+        v += (v1 + v2) + v3;
+      }
+      T lr[32], di[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        lr[c] = (lane < w && c < lane) ? Lat(u, kb + h + c) : T(0);
+        di[c] = c < w ? dinv[kb + h + c] : T(0);
+      }
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        T yc = v * di[c];
+        yc = __shfl_sync(0xffffffffu, yc, c);
+        if (lane == c) v = yc;
+        v -= lr[c] * yc;
+      }
+      if (lane < w) zs[h + lane] = v;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (tid < nb) z[kb + tid] = zs[tid];
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    lg_set_flag(flag + k);
+    if (timed_out) wv.lm[b].fail = 1;
+  }
+}
+
+// backward L^T x = z (z in place in lg_y); then x is added to the solution so far
+// (first: x itself) and written to delta (last) or to lg_x and its split
+template <typename T>
+__global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b, int first, int last) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  __shared__ T part[4][kLgNB];
+  __shared__ T zs[kLgNB];
+  __shared__ int timed_out;
+  const int P = 6 * pv.p_npose[b], po = pv.p_param_off[b];
+  const int nblk = (P + kLgNB - 1) / kLgNB, k = nblk - 1 - (int)blockIdx.x;
+  const int kb = k * kLgNB, nb = min(kLgNB, P - kb);
+  const int tid = threadIdx.x, r = tid & 63, q = tid >> 6, warp = tid >> 5, lane = tid & 31;
+  const T *L = reinterpret_cast<const T *>(wv.fac) + pv.p_S_off[b];
+  auto Lat = [&](int i, int j) { return L[(size_t)j * P + i]; };
+  const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + po;
+  T *x = reinterpret_cast<T *>(wv.lg_y) + po;
+  int *flag = wv.lg_flag + pv.total_params + po;
+  const uint64_t deadline = lg_clock_ns() + kLgWaitNs;
+  if (tid == 0) timed_out = 0;
+  __syncthreads();
+  T acc = T(0);
+  for (int j = nblk - 1; j > k; --j) {  // later blocks, finished by lower-numbered CTAs
+    if (tid == 0 && !timed_out && !lg_wait_flag(flag + j, deadline)) timed_out = 1;
+    __syncthreads();
+    const int jb = j * kLgNB, nbj = min(kLgNB, P - jb);
+    if (r < nb) {
+      T lv[16], xv[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int i = 16 * q + c;
+        lv[c] = i < nbj ? Lat(jb + i, kb + r) : T(0);  // column kb + r: contiguous per thread
+        xv[c] = i < nbj ? __ldcg(x + jb + i) : T(0);
+      }
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc += lv[c] * xv[c];
+    }
+  }
+  part[q][r] = acc;
+  __syncthreads();
+  if (tid < nb) zs[tid] = x[kb + tid] - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+  __syncthreads();
+  if (warp == 0) {  // L_kk^T x_k = zs, halves from the bottom
+    for (int h = ((nb - 1) / 32) * 32; h >= 0; h -= 32) {
+      const int w = min(32, nb - h), u = kb + h + lane;
+      T v = lane < w ? zs[h + lane] : T(0);
+      if (h + w < nb) {  // the later half is final (h = 0): loads first
+        T lq[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) lq[c] = (lane < w && 32 + c < nb) ? Lat(kb + 32 + c, u) : T(0);
+        T v1 = T(0), v2 = T(0), v3 = T(0);
+#pragma unroll
+        for (int c = 0; c < 32; c += 4) {
+          v -= lq[c] * (32 + c < nb ? zs[32 + c] : T(0));
+          v1 -= lq[c + 1] * (33 + c < nb ? zs[33 + c] : T(0));
+          v2 -= lq[c + 2] * (34 + c < nb ? zs[34 + c] : T(0));
+          v3 -= lq[c + 3] * (35 + c < nb ? zs[35 + c] : T(0));
+        }
+        v += (v1 + v2) + v3;
+      }
+      T lc[32], di[32];  // column `lane` of the diagonal block, pivots
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        lc[c] = (c < w && lane < c) ? Lat(kb + h + c, u) : T(0);
+        di[c] = c < w ? dinv[kb + h + c] : T(0);
+      }
+#pragma unroll
+      for (int c = 31; c >= 0; --c) {
+        T xc = v * di[c];
+        xc = __shfl_sync(0xffffffffu, xc, c);
+        if (lane == c) v = xc;
+        v -= lc[c] * xc;
+      }
+      if (lane < w) zs[h + lane] = v;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (tid < nb) x[kb + tid] = zs[tid];
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    lg_set_flag(flag + k);
+    if (timed_out) wv.lm[b].fail = 1;
+  }
+  if (tid < nb) {
+    const int i = kb + tid;
+    const double xi = (first ? 0.0 : wv.lg_x[po + i]) + (double)zs[tid];
     if (last) {
-      wv.delta[po + i] = failed ? 0.0 : xi;
+      wv.delta[po + i] = xi;  // (a failed factorisation zeroes delta after the solve)
     } else {
       wv.lg_x[po + i] = xi;
-      const df s = df_from_double(xi);
-      wv.lg_xs[2 * (po + i)] = s.h;
-      wv.lg_xs[2 * (po + i) + 1] = s.l;
+      const df sp = df_from_double(xi);
+      wv.lg_xs[2 * (po + i)] = sp.h;
+      wv.lg_xs[2 * (po + i) + 1] = sp.l;
     }
   }
+}
+
+// a failed factorisation (or a timed-out substitution) leaves no step
+__global__ void k_lg_zero_failed(PlanView pv, WorkView wv, int b) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  if (!wv.lm[b].fail) return;
+  const int P = 6 * pv.p_npose[b], po = pv.p_param_off[b];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) wv.delta[po + i] = 0.0;
 }
 
 // residual y = g0 - S x from the exact S, warp per row
@@ -429,7 +504,8 @@ __global__ void __launch_bounds__(256) k_lg_resid(PlanView pv, WorkView wv, int 
 }
 
 template <typename T>
-int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int refine, void *stream) {
+int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, int refine,
+                        void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
   k_lg_assemble<T><<<P, 256, 0, st>>>(pv, wv, b);
   int n = 1;
@@ -444,20 +520,28 @@ int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, in
       n += 2;
     }
   }
-  const size_t sm = (size_t)P * sizeof(T);
-  cudaFuncSetAttribute(k_lg_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_lg_solve<T><<<1, 512, sm, st>>>(pv, wv, b, 1, refine == 0);
-  ++n;
-  for (int it = 0; it < refine; ++it) {
-    k_lg_resid<T><<<(P + 7) / 8, 256, 0, st>>>(pv, wv, b);
-    k_lg_solve<T><<<1, 512, sm, st>>>(pv, wv, b, 0, it == refine - 1);
+  const int nblk = (P + kLgNB - 1) / kLgNB;
+  int *ff = wv.lg_flag + param_off, *fb = wv.lg_flag + pv.total_params + param_off;
+  for (int it = 0; it <= refine; ++it) {
+    if (it > 0) {
+      k_lg_resid<T><<<(P + 7) / 8, 256, 0, st>>>(pv, wv, b);
+      ++n;
+    }
+    cudaError_t e = cudaMemsetAsync(ff, 0, sizeof(int) * (size_t)nblk, st);
+    if (e != cudaSuccess) return (int)e;
+    k_lg_fwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0);
+    e = cudaMemsetAsync(fb, 0, sizeof(int) * (size_t)nblk, st);
+    if (e != cudaSuccess) return (int)e;
+    k_lg_bwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0, it == refine);
     n += 2;
   }
+  k_lg_zero_failed<<<grid_for(P, 256), 256, 0, st>>>(pv, wv, b);
+  ++n;
   g_launches += n;
   return (int)cudaGetLastError();
 }
 
-template int launch_factor_large<float>(const PlanView &, const WorkView &, int, int, int, void *);
-template int launch_factor_large<double>(const PlanView &, const WorkView &, int, int, int, void *);
+template int launch_factor_large<float>(const PlanView &, const WorkView &, int, int, int, int, void *);
+template int launch_factor_large<double>(const PlanView &, const WorkView &, int, int, int, int, void *);
 
 }  // namespace spgo

@@ -106,6 +106,7 @@ struct WorkView {
   double *lg_g0, *lg_x; // [total_params] g - g_L; the solution so far
   float *lg_xs;         // [2 total_params] its double-float split
   void *lg_y, *lg_dinv; // [total_params] T: right-hand side / residual; 1 / L_kk
+  int *lg_flag;         // [2 total_params]: block-done flags of the multi-CTA substitutions
   double *cost_acc;     // [B]
   double *pred_acc;     // [B]
 };
@@ -130,7 +131,8 @@ template <typename T>
 int launch_schur(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
 size_t factor_packed_bytes(int P, size_t ts);  // shared memory of the batched factorisation
 template <typename T>
-int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int refine, void *stream);
+int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, int refine,
+                        void *stream);
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed,
                         void *stream);
