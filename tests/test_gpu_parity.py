@@ -366,16 +366,18 @@ def test_divergence_study_runs_batched(built_lib, cuda_device, scene):
     assert 0.0 <= r["divergence_rate"] <= 1.0
 
 
-def test_solve_stream_matches_batch_solver(built_lib, cuda_device):
-    """solve_stream plans batch k + 1 on a worker thread while batch k solves: the
-    batches come back in order with the results of one BatchSolver each."""
+@pytest.mark.parametrize("inflight", [1, 3])
+def test_solve_stream_matches_batch_solver(built_lib, cuda_device, inflight):
+    """solve_stream plans batches on a worker thread ahead of their solve and keeps
+    `inflight` of them solving at once on their own streams: the batches come back in
+    order with the results of one BatchSolver each."""
     from spgo_gb300.solver import solve_stream
     batches = [[scenes.circle_scene(s, n, l) for s, n, l in [(81 + 3 * k, 6, 80), (82 + 3 * k, 9, 150)]]
-               for k in range(3)]
+               for k in range(4)]
     # (run to the optimum: FP32 atomics make LM paths differ run to run before it)
     params = dict(loss="l2", max_iters=OPT_ITERS, tol=OPT_TOL)
-    got = list(solve_stream(batches, "mixed", params, device=cuda_device))
-    assert len(got) == 3
+    got = list(solve_stream(batches, "mixed", params, device=cuda_device, inflight=inflight))
+    assert len(got) == 4
     for batch, (st, poses, alphas) in zip(batches, got):
         bs = BatchSolver(batch, precision="mixed")
         bs.set_params(**params)
