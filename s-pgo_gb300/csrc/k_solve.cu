@@ -426,26 +426,29 @@ __global__ void k_backsub(PlanView pv, WorkView wv, Params prm, const double *al
     const T dv = rb + slot < rows ? (T)dl[rb + slot] : T(0);
     const T *sr = slab + (size_t)rb * SPGO_CHUNK + slot;
     const int nr = min(32, rows - rb);
-    int k = 0;
-    for (; k + 4 <= nr; k += 4) {
-      s0 += sr[(size_t)k * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k);
-      s1 += sr[(size_t)(k + 1) * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k + 1);
-      s2 += sr[(size_t)(k + 2) * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k + 2);
-      s3 += sr[(size_t)(k + 3) * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k + 3);
+    T v[32];  // the block's 32 slab rows loaded before any is used
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = k < nr ? sr[(size_t)k * SPGO_CHUNK] : T(0);
+#pragma unroll
+    for (int k = 0; k < 32; k += 4) {
+      s0 += v[k] * __shfl_sync(0xffffffffu, dv, k);
+      s1 += v[k + 1] * __shfl_sync(0xffffffffu, dv, k + 1);
+      s2 += v[k + 2] * __shfl_sync(0xffffffffu, dv, k + 2);
+      s3 += v[k + 3] * __shfl_sync(0xffffffffu, dv, k + 3);
     }
-    for (; k < nr; ++k) s0 += sr[(size_t)k * SPGO_CHUNK] * __shfl_sync(0xffffffffu, dv, k);
   }
   if (slot < cnt) {
     const int li = lm0 + slot;
     const T s = (s0 + s1) + (s2 + s3);
-    const double C = (double)reinterpret_cast<const T *>(wv.C)[li];
-    const double ga = (double)reinterpret_cast<const T *>(wv.ga)[li];
+    const T C = reinterpret_cast<const T *>(wv.C)[li];
+    const T ga = reinterpret_cast<const T *>(wv.ga)[li];
     const double lam = wv.lm[b].lam;
-    const double Dd = C * (1.0 + lam) + (double)prm.eps;
-    const double da = (ga - (double)s) / Dd;
-    pred = da * (ga + (Dd - C) * da);
+    // the per-landmark update in T (its inputs are T already); the state update in FP64
+    const T Dd = C * (T)(1.0 + lam) + (T)prm.eps;
+    const T da = (ga - s) / Dd;
+    pred = (double)(da * (ga + (Dd - C) * da));
     const int u = pv.lm_user[li];
-    const double an = alpha[u] + da;
+    const double an = alpha[u] + (double)da;
     alpha_out[u] = fmin(fmax(an, (double)prm.alpha_min), (double)prm.alpha_max);
   }
   pred = warp_sum(pred);
