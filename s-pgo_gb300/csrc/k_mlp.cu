@@ -193,7 +193,20 @@ __global__ void k_mlp_deploy(const float *__restrict__ theta, MlpSmem *__restric
 __device__ void stage_mlp(const MlpSmem *__restrict__ src, MlpSmem &m) {
   const float4 *s4 = reinterpret_cast<const float4 *>(src);
   float4 *d4 = reinterpret_cast<float4 *>(&m);
-  for (int i = threadIdx.x; i < (int)(sizeof(MlpSmem) / 16); i += blockDim.x) d4[i] = s4[i];
+  constexpr int n = (int)(sizeof(MlpSmem) / 16);
+  for (int i0 = threadIdx.x; i0 < n; i0 += 8 * blockDim.x) {  // eight 16-byte loads in flight
+    float4 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int i = i0 + q * blockDim.x;
+      if (i < n) v[q] = s4[i];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int i = i0 + q * blockDim.x;
+      if (i < n) d4[i] = v[q];
+    }
+  }
 }
 
 __device__ void mlp_infer_warp(const MlpSmem &m, const float *x, float &o0, float &o1) {
@@ -326,7 +339,16 @@ __device__ void lm_stats_f32(const PlanView &pv, const WorkView &wv, LMState &s,
   }
   const int l0 = pv.p_lm_off[b], lc = pv.p_lm_cnt[b];
   const float *C = reinterpret_cast<const float *>(wv.C) + l0;
-  for (int i = threadIdx.x; i < lc; i += blockDim.x) cs = cs + df_make(C[i]);
+  for (int i0 = threadIdx.x; i0 < lc; i0 += 8 * blockDim.x) {  // eight loads in flight
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int i = i0 + q * blockDim.x;
+      v[q] = i < lc ? C[i] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) cs = cs + df_make(v[q]);
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     gmx = fmaxf(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
