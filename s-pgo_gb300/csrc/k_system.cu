@@ -209,9 +209,19 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
   const int j = i + e;
   const int P = 6 * N;
   const int fo = pv.p_frame_off[b];
-  const T *F = reinterpret_cast<const T *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + (size_t)i * D + e) * 27;
-  const T *Ri = FramesT<T>::R(wv, fo + i, 0);
-  const T *Rj = FramesT<T>::R(wv, fo + j, 0);
+  // the record and both rotations in registers first (the A stores below could
+  // otherwise alias them and force reloads)
+  const T *Fg = reinterpret_cast<const T *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + (size_t)i * D + e) * 27;
+  const T *Rig = FramesT<T>::R(wv, fo + i, 0);
+  const T *Rjg = FramesT<T>::R(wv, fo + j, 0);
+  T F[27], Ri[9], Rj[9];
+#pragma unroll
+  for (int k = 0; k < 27; ++k) F[k] = Fg[k];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    Ri[k] = Rig[k];
+    Rj[k] = Rjg[k];
+  }
   const Vec3<T> cji = FramesT<T>::rel(wv, fo + j, 0, fo + i, 0);
   // C R_j with C = [c_j - c_i]x
   T CRj[9];
@@ -224,6 +234,7 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
         CRj[3 * r + c] = X[3 * r] * Rj[c] + X[3 * r + 1] * Rj[3 + c] + X[3 * r + 2] * Rj[6 + c];
   }
   T *A = reinterpret_cast<T *>(wv.A) + pv.p_S_off[b];
+#pragma unroll
   for (int col = 0; col < 6; ++col) {
     T adj[6];
 #pragma unroll
