@@ -560,11 +560,11 @@ int launch_post_linearize(const PlanView &pv, const WorkView &wv, void *stream) 
 __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= pv.B) return;
-  LMState &s = wv.lm[b];
-  if (s.status != 0) {
-    s.flag = 0;
+  if (wv.lm[b].status != 0) {
+    wv.lm[b].flag = 0;
     return;
   }
+  LMState s = wv.lm[b];  // one read of the record, one write at the end
   const double F = s.cost;
   const double Fn = wv.cost_acc[b];
   const double pred = 0.5 * wv.pred_acc[b];
@@ -604,6 +604,7 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
   }
   s.fail = 0;
   if (s.status == 0 && s.iters >= prm.max_iters) s.status = SPGO_STATUS_MAX_ITERS;
+  wv.lm[b] = s;
   if (it < SPGO_TRACE_MAX) {
     double *t = wv.trace + ((size_t)b * SPGO_TRACE_MAX + it) * 3;
     t[0] = s.cost;
@@ -624,8 +625,11 @@ __global__ void k_commit(PlanView pv, WorkView wv, double *poses, double *alpha)
   if (t < pv.NP) {
     const int b = pv.pose_prob[t];
     if (wv.lm[b].flag) {
+      double v[12];  // all loads before the stores (the two buffers may alias as far as the compiler knows)
 #pragma unroll
-      for (int q = 0; q < 12; ++q) poses[12 * t + q] = wv.poses_cand[12 * t + q];
+      for (int q = 0; q < 12; ++q) v[q] = wv.poses_cand[12 * t + q];
+#pragma unroll
+      for (int q = 0; q < 12; ++q) poses[12 * t + q] = v[q];
     }
   }
   if (t < pv.L) {
