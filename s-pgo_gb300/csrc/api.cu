@@ -655,6 +655,10 @@ struct spgo_solver {
   // pageable memory would hold the driver until the stream drains, stalling the
   // API calls of threads that drive other solvers
   HostBlock h_lm;  // from the staging cache (freeing page-locked memory synchronises the device)
+  // status reads poll this event and yield the core between polls: several solver
+  // threads and the planner's share the host cores, and a spinning wait would take
+  // one from them, while a sleeping wait would wake up late and leave the GPU idle
+  cudaEvent_t status_ev = nullptr;
 };
 
 static void drop_graphs(spgo_solver *s) {
@@ -998,6 +1002,14 @@ int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_byte
     delete s;
     return fail(SPGO_ERR_INVALID_ARG, ex.what());
   }
+  {
+    cudaError_t e = cudaEventCreateWithFlags(&s->status_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      arena_put(s->h_lm);
+      delete s;
+      return fail(SPGO_ERR_CUDA, std::string("status event: ") + cudaGetErrorString(e));
+    }
+  }
   s->launches0 = g_launches;
   *out = s;
   return SPGO_OK;
@@ -1008,6 +1020,7 @@ int spgo_solver_destroy(spgo_solver *s) {
     for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
     drop_graphs(s);
     arena_put(s->h_lm);
+    if (s->status_ev) cudaEventDestroy(s->status_ev);
   }
   delete s;
   return SPGO_OK;
@@ -1121,7 +1134,12 @@ int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream) {
   LMState *h = reinterpret_cast<LMState *>(s->h_lm.ptr);
   CUDA_TRY(cudaMemcpyAsync(h, s->wv.lm, sizeof(LMState) * (size_t)s->plan->B, cudaMemcpyDeviceToHost,
                            (cudaStream_t)stream));
-  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  CUDA_TRY(cudaEventRecord(s->status_ev, (cudaStream_t)stream));
+  {
+    cudaError_t e;
+    while ((e = cudaEventQuery(s->status_ev)) == cudaErrorNotReady) std::this_thread::yield();
+    if (e != cudaSuccess) return fail(SPGO_ERR_CUDA, std::string("status wait: ") + cudaGetErrorString(e));
+  }
   for (int b = 0; out && b < s->plan->B; ++b) {
     out[b].cost0 = h[b].cost0;
     out[b].cost = h[b].cost;
