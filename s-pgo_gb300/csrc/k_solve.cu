@@ -476,12 +476,70 @@ __global__ void k_update_poses(PlanView pv, WorkView wv, const double *poses, do
   const int k = p - pv.p_pose_off[b];
   const int P = 6 * pv.p_npose[b];
   const int po = pv.p_param_off[b] + 6 * k;
-  double xi[6];
+  double xi[6], T0[12];
 #pragma unroll
   for (int q = 0; q < 6; ++q) xi[q] = scale * wv.delta[po + q];
-  double E[12], Tn[12];
-  exp_se3(xi, E);
-  compose34(poses + 12 * (size_t)p, E, Tn);
+#pragma unroll
+  for (int q = 0; q < 12; ++q) T0[q] = poses[12 * (size_t)p + q];
+  double Tn[12];
+  if constexpr (std::is_same<T, float>::value) {
+    // FP32 path: T_new = T + T (Exp(xi) - I), the increment Exp(xi) - I formed in FP32
+    // (relative precision of the increment itself) and the sum in double-float, so
+    // FP64 (a small fraction of the FP32 rate here) is left with the conversions
+    const float px = (float)xi[0], py = (float)xi[1], pz = (float)xi[2];
+    const float t2 = px * px + py * py + pz * pz, th = sqrtf(t2);
+    float a, b, c;
+    if (th < 0.5f) {  // series, truncation below 1e-10 relative at 0.5
+      const float t4 = t2 * t2, t6 = t4 * t2, t8 = t4 * t4;
+      a = 1.f - t2 / 6.f + t4 / 120.f - t6 / 5040.f + t8 / 362880.f;
+      b = 0.5f - t2 / 24.f + t4 / 720.f - t6 / 40320.f + t8 / 3628800.f;
+      c = 1.f / 6.f - t2 / 120.f + t4 / 5040.f - t6 / 362880.f + t8 / 39916800.f;
+    } else {
+      float sn, cs;
+      sincosf(th, &sn, &cs);
+      const float sh = sinf(0.5f * th);
+      a = sn / th;
+      b = 2.f * sh * sh / t2;
+      c = (th - sn) / (t2 * th);
+    }
+    const float S[9] = {0.f, -pz, py, pz, 0.f, -px, -py, px, 0.f};
+    float S2[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        S2[3 * i + j] = S[3 * i] * S[j] + S[3 * i + 1] * S[3 + j] + S[3 * i + 2] * S[6 + j];
+    float D[12];  // Exp(xi) - I, 3x4
+    const float rx = (float)xi[3], ry = (float)xi[4], rz = (float)xi[5];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) D[4 * i + j] = a * S[3 * i + j] + b * S2[3 * i + j];
+      const float jx = (i == 0 ? 1.f : 0.f) + b * S[3 * i] + c * S2[3 * i];
+      const float jy = (i == 1 ? 1.f : 0.f) + b * S[3 * i + 1] + c * S2[3 * i + 1];
+      const float jz = (i == 2 ? 1.f : 0.f) + b * S[3 * i + 2] + c * S2[3 * i + 2];
+      D[4 * i + 3] = jx * rx + jy * ry + jz * rz;
+    }
+    df Rd[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Rd[3 * i + j] = df_from_double(T0[4 * i + j]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        // (T D)(i, j) = sum_k R(i, k) D(k, j)  (D's last row is zero)
+        const df td = Rd[3 * i] * D[j] + Rd[3 * i + 1] * D[4 + j] + Rd[3 * i + 2] * D[8 + j];
+        const df v = df_from_double(T0[4 * i + j]) + td;
+        Tn[4 * i + j] = (double)v.h + (double)v.l;
+      }
+    }
+  } else {
+    double E[12];
+    exp_se3(xi, E);
+    compose34(T0, E, Tn);
+  }
 #pragma unroll
   for (int q = 0; q < 12; ++q) out[12 * (size_t)p + q] = Tn[q];
   const double lam = wv.lm[b].lam;
