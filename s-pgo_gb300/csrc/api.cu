@@ -783,11 +783,8 @@ constexpr int kF64 = std::is_same<T, double>::value ? 1 : 0;
 
 template <typename T>
 static int enqueue_linearize(spgo_solver *s, cudaStream_t st, bool stats, bool ctrl) {
-  // frame tables of the state: computed here at the first linearisation after a reset;
-  // later the accepted candidate's tables (its cost pass read them) are the state's
-  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_FIRST, kF64<T>, st)); }
-  // the cost at the first linearisation point (later ones come from the cost pass that accepted them)
-  { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 1, GATE_FIRST, st)); }
+  // (the frame tables and the cost of the state come from enqueue_reset for the first
+  // linearisation, and from the accepted candidate's chain and cost pass after that)
   { PROF(K_LINEARIZE); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 0, GATE_RELIN, st)); }
   { PROF(K_SYSTEM); CUDA_TRY(launch_system<T>(s->pv, s->wv, GATE_RELIN, st)); }
   {
@@ -797,6 +794,21 @@ static int enqueue_linearize(spgo_solver *s, cudaStream_t st, bool stats, bool c
     if (ctrl) CUDA_TRY(launch_controller(s->pv, s->wv, s->wv.ctrl, st));
   }
   return SPGO_OK;
+}
+
+// reset every problem's LM state, then the frame tables and the cost of the state for
+// the first linearisation (outside the per-iteration sequence, so the iterations a
+// CUDA graph replays carry no launches that only the first one needs)
+template <typename T>
+static int enqueue_reset_t(spgo_solver *s, cudaStream_t st, double lam) {
+  { PROF(K_BOOKKEEP); CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, lam, st)); }
+  { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_FIRST, kF64<T>, st)); }
+  { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 1, GATE_FIRST, st)); }
+  return SPGO_OK;
+}
+static int enqueue_reset(spgo_solver *s, cudaStream_t st, double lam) {
+  return s->plan->precision == SPGO_PREC_FP64 ? enqueue_reset_t<double>(s, st, lam)
+                                               : enqueue_reset_t<float>(s, st, lam);
 }
 
 template <typename T>
@@ -839,8 +851,8 @@ static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
 template <typename T>
 static int enqueue_gn(spgo_solver *s, int iters, float step_size, cudaStream_t st) {
   for (int it = 0; it < iters; ++it) {
-    { PROF(K_BOOKKEEP); CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, 0.0, st)); }
     int rc;
+    if ((rc = enqueue_reset_t<T>(s, st, 0.0)) != SPGO_OK) return rc;
     if ((rc = enqueue_linearize<T>(s, st, false, false)) != SPGO_OK) return rc;
     if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
     { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->alpha, 1, st)); }
@@ -1078,8 +1090,7 @@ int spgo_gn_step(spgo_solver *s, int32_t iterations, float step_size, void *stre
 
 int spgo_lm_reset(spgo_solver *s, void *stream) {
   if (!s) return fail(SPGO_ERR_INVALID_ARG, "null solver");
-  CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, stream));
-  return SPGO_OK;
+  return enqueue_reset(s, (cudaStream_t)stream, s->prm.lambda0);
 }
 
 static int enqueue_iterations(spgo_solver *s, int32_t n_iters, cudaStream_t st) {
@@ -1225,7 +1236,7 @@ int spgo_autotune(spgo_solver *s, spgo_params *chosen, void *stream) {
     s->prm.cost_block = cands[ci].cost_block;
     s->prm.lin_block = cands[ci].lin_block;
     s->prm.use_tc = cands[ci].use_tc;
-    rc = launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, st);
+    rc = enqueue_reset(s, st, s->prm.lambda0);
     for (int it = 0; rc == SPGO_OK && it < 2; ++it)
       rc = f64 ? enqueue_lm_iteration<double>(s, st) : enqueue_lm_iteration<float>(s, st);
     double ms[K_NKINDS];
@@ -1254,7 +1265,7 @@ int spgo_autotune(spgo_solver *s, spgo_params *chosen, void *stream) {
   drop_graphs(s);
   cudaStreamSynchronize(st);
   cudaFree(save);
-  if (rc == SPGO_OK) rc = launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, st) == 0 ? SPGO_OK : SPGO_ERR_CUDA;
+  if (rc == SPGO_OK) rc = enqueue_reset(s, st, s->prm.lambda0);
   if (rc == SPGO_OK && chosen) std::memcpy(chosen, &s->prm, sizeof(Params));
   return rc;
 }
@@ -1265,8 +1276,9 @@ int spgo_export_system(spgo_solver *s, int32_t problem, double *A, double *g, do
   cudaStream_t st = (cudaStream_t)stream;
   const spgo_plan *p = s->plan;
   // linearise every problem at its current state (lambda untouched: reset sets lambda0)
-  CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, s->prm.lambda0, st));
-  int rc = p->precision == SPGO_PREC_FP64 ? enqueue_linearize<double>(s, st, false, false) : enqueue_linearize<float>(s, st, false, false);
+  int rc = enqueue_reset(s, st, s->prm.lambda0);
+  if (rc != SPGO_OK) return rc;
+  rc = p->precision == SPGO_PREC_FP64 ? enqueue_linearize<double>(s, st, false, false) : enqueue_linearize<float>(s, st, false, false);
   if (rc != SPGO_OK) return rc;
   const int N = p->p_npose[problem], P = 6 * N, L = p->p_lm_cnt[problem];
   const bool f64 = p->precision == SPGO_PREC_FP64;
@@ -1291,8 +1303,9 @@ int spgo_export_reduced(spgo_solver *s, int32_t problem, double lambda, double *
   cudaStream_t st = (cudaStream_t)stream;
   const spgo_plan *p = s->plan;
   const bool f64 = p->precision == SPGO_PREC_FP64;
-  CUDA_TRY(launch_reset(s->pv, s->wv, s->prm, lambda, st));
-  int rc = f64 ? enqueue_linearize<double>(s, st, false, false) : enqueue_linearize<float>(s, st, false, false);
+  int rc = enqueue_reset(s, st, lambda);
+  if (rc != SPGO_OK) return rc;
+  rc = f64 ? enqueue_linearize<double>(s, st, false, false) : enqueue_linearize<float>(s, st, false, false);
   if (rc != SPGO_OK) return rc;
   if (!f64 && s->prm.use_tc) {
     CUDA_TRY(launch_schur_tc(s->pv, s->wv, s->prm, st));
