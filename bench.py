@@ -170,8 +170,8 @@ def roofline_numerator(kind: str, sizes, slab_floats: int, ts: int, probs):
 # DRAM bytes (read + write) per launch of the profiled kernels on this workload
 # (256-problem batch, mixed precision): one ncu capture, dram__bytes_read.sum +
 # dram__bytes_write.sum, profiles/ncu_kernels_config3_batch.md
-NCU_TRAFFIC = {"cost": 119.79e6, "linearize": 251.66e6, "schur": 224.36e6, "factor_solve": 24.00e6,
-               "backsub": 206.44e6}
+NCU_TRAFFIC = {"cost": 119.56e6, "linearize": 251.76e6, "schur": 224.89e6, "factor_solve": 24.00e6,
+               "backsub": 206.67e6}
 NCU_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/ncu_kernels_config3_batch.md"
 
 
