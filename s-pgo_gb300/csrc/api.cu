@@ -1218,8 +1218,12 @@ int spgo_autotune(spgo_solver *s, spgo_params *chosen, void *stream) {
   const size_t np = (size_t)p->NP * 12, nl = (size_t)p->L;
   double *save = nullptr;
   CUDA_TRY(cudaMalloc(&save, sizeof(double) * (np + nl + 1)));
-  CUDA_TRY(cudaMemcpyAsync(save, s->poses, sizeof(double) * np, cudaMemcpyDeviceToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(save + np, s->alpha, sizeof(double) * nl, cudaMemcpyDeviceToDevice, st));
+  cudaError_t ce = cudaMemcpyAsync(save, s->poses, sizeof(double) * np, cudaMemcpyDeviceToDevice, st);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(save + np, s->alpha, sizeof(double) * nl, cudaMemcpyDeviceToDevice, st);
+  if (ce != cudaSuccess) {
+    cudaFree(save);
+    return fail(SPGO_ERR_CUDA, std::string("autotune: state copy: ") + cudaGetErrorString(ce));
+  }
   const Params base = s->prm;
   struct Cand {
     int cost_block, lin_block, use_tc;
