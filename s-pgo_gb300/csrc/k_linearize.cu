@@ -110,21 +110,20 @@ constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [
 // Dynamic shared memory after LinSmem, sized by the batch's widest chunk window
 // (W = max_nb + 1 frames) and the CTA's warps:
 //   dc    [W][6] float x 2   FP32 path: c_host - c_(f0 + f, cam), hi and lo
-//   pair  [W][27] T          (host, target) pair terms of the chunk, by target - f0
 //   stage [warps][27][33] T  per-warp staging of the pair terms
 //   slab  [6 (W - 1)][32] T  the chunk's slab
-// (the cost pass uses dc only)
+// (the cost pass uses dc only).  At W = 33 and four warps the FP32 Jacobian pass
+// takes 42.3 KB: five CTAs per SM.
 template <typename T>
 struct LinLayout {
-  size_t dc, pair, stage, slab, total;
+  size_t dc, stage, slab, total;
   __host__ __device__ LinLayout(int max_nb, int warps, bool cost) {
     const size_t W = (size_t)max_nb + 1;
     auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
     dc = up(sizeof(LinSmem<T>));
-    pair = dc + up(W * 12 * sizeof(float));
-    stage = pair + up(W * 27 * sizeof(T));
+    stage = dc + up(W * 12 * sizeof(float));
     slab = stage + up((size_t)warps * 27 * kStagePitch * sizeof(T));
-    total = cost ? pair : slab + (size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(T);
+    total = cost ? stage : slab + (size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(T);
   }
 };
 
@@ -135,7 +134,8 @@ struct LinLayout {
 // observation's s K^T j_alpha written into the slab row of its frame.  The pair
 // terms of a warp are staged in shared memory and summed over runs of equal
 // target frame (observations are sorted by frame, and every landmark of the
-// chunk has the same host) by 27 lanes, one value each.  Phase C: per landmark,
+// chunk has the same host) by 27 lanes, one value each, and each run's sum is
+// added to the global pair accumulator.  Phase C: per landmark,
 // the suffix (frames after the anchor) and prefix (frames before it) sums that
 // turn those rows into b_l(i), then B_l(i) = Ad_i^T b_l(i).
 // COST = true is the cost pass: residuals only, in double-float on the FP32 path
@@ -166,7 +166,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
   const LinLayout<T> lay(pv.max_nb, blockDim.x >> 5, COST);
   float *dch = reinterpret_cast<float *>(smem_raw + lay.dc);  // [W][6] hi, then [W][6] lo
   float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
-  T(*pair)[27] = reinterpret_cast<T(*)[27]>(smem_raw + lay.pair);
   T *stage = reinterpret_cast<T *>(smem_raw + lay.stage);
   T *slab_s = reinterpret_cast<T *>(smem_raw + lay.slab);
   const int rows = 6 * nb;
@@ -216,18 +215,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
       dcl[idx] = d.l;
     }
   }
-  if (!COST) {
+  if (!COST)
     for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_s[i] = T(0);
-    for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) (&pair[0][0])[i] = T(0);
-  }
   __syncthreads();
 
   // phase B: observations are sorted by target frame inside the chunk and every
   // landmark of the chunk has the same host, so a warp's pair terms (host, target)
-  // form contiguous runs: reduce each run with shuffles, add it to the chunk's
-  // shared pair slot, and flush the slots to the global accumulators once.
+  // form contiguous runs: each run's sum goes straight into the global pair
+  // accumulator (lo, hi) = (min, max)(host, target), one reduction per value and run
+  // (about as many as a per-chunk shared copy would flush, without its shared
+  // memory, its zeroing and its flush pass)
   const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
   const int D = pv.p_pair_D[b];
+  auto pair_add = [&](int n, int comp, T v) {  // (operands re-read here: few registers stay live)
+    const int host_a = sm.a[0];
+    const int lo = min(host_a, n), hi = max(host_a, n);
+    red_add(reinterpret_cast<T *>(wv.pair_acc) + ((size_t)pv.p_pair_off[b] + (size_t)lo * D + (hi - lo - 1)) * 27 + comp,
+            v);
+  };
   const int lane = tid & 31;
   const T lscale = (T)prm.loss_scale;
   T cost_t = T(0);  // a thread sums a handful of terms; the FP64 reduction starts at the warp
@@ -377,7 +382,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
     }
     if (!COST) {
       // stage the 27 pair values, then lanes 0..26 each sum one value over the
-      // runs of equal target frame and add each run into the chunk's pair slot
+      // runs of equal target frame and add each run to its global pair accumulator
       T *st = stage + (size_t)(tid >> 5) * 27 * kStagePitch;
       int *keys = sm.key[tid >> 5];
 #pragma unroll
@@ -393,13 +398,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
         for (int i = 0; i < 32; ++i) {
           const int k = keys[i];
           if (k != cur) {
-            if (cur >= 0 && acc != T(0)) atomicAdd(&pair[cur - f0][lane], acc);
+            if (cur >= 0 && acc != T(0)) pair_add(cur, lane, acc);
             acc = T(0);
             cur = k;
           }
           acc += col[i];
         }
-        if (cur >= 0 && acc != T(0)) atomicAdd(&pair[cur - f0][lane], acc);
+        if (cur >= 0 && acc != T(0)) pair_add(cur, lane, acc);
       }
       __syncwarp();
     }
@@ -417,20 +422,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
     return;
   }
   __syncthreads();
-
-  // pair slots -> global accumulators: (lo, hi) = (min, max)(host, target)
-  {
-    const int a = sm.a[0];
-    T *pair_acc = reinterpret_cast<T *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
-    for (int i = tid; i < (nb + 1) * 27; i += blockDim.x) {
-      const int sl = i / 27, comp = i % 27;
-      const int n = f0 + sl;
-      const T v = pair[sl][comp];
-      if (n == a || v == T(0)) continue;
-      const int lo = min(a, n), hi = max(a, n);
-      red_add(pair_acc + ((size_t)lo * D + (hi - lo - 1)) * 27 + comp, v);
-    }
-  }
 
   // phase C.1: per (landmark, component) suffix / prefix sums along the window
   for (int idx = tid; idx < cnt * 6; idx += blockDim.x) {

@@ -331,7 +331,12 @@ def test_large_system_path_matches_oracle(built_lib, cuda_device, prec, tol):
     assert abs(st["cost"] - res.cost) / res.cost < 1e-6
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 2e-4)])
+# Mixed: three undamped steps from the identity start amplify the FP32 Hessian and
+# gradient sums, whose atomic order changes from run to run.  Over 36 runs (seeds 11,
+# 12, 13, six each, with the pair sums accumulated per chunk in shared memory and
+# with them added per run straight to the global accumulators) the largest errors
+# were 4.1e-4 (inverse depth, relative to the largest) and 1.2e-4 (pose entries).
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-8), ("mixed", 8e-4)])
 def test_gn_step_on_reference_scene(built_lib, cuda_device, prec, tol):
     """A window of the reference's own scene distribution (identity start, inverse
     depth 1, noise-free pixels, (0, 0) anchor pixels where the anchor observation was
