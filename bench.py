@@ -112,12 +112,24 @@ class ClockSampler:
         self.path = os.path.join("/tmp", f"spgo_clocks_{os.getpid()}.csv")
 
     def start(self):
+        """Start sampling every 100 ms and return once the first sample is written
+        (nvidia-smi takes a few hundred ms to start; without the wait a short timed
+        region would see none of its samples)."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        t_end = time.time() + 5.0
+        while time.time() < t_end and self.proc.poll() is None:
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:

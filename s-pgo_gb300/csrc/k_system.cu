@@ -70,43 +70,63 @@ __device__ __forceinline__ void shift_record(T *v, const Vec3<T> &z) {
   for (int i = 0; i < 3; ++i) v[21 + i] += Z[3 * i] * mv0 + Z[3 * i + 1] * mv1 + Z[3 * i + 2] * mv2;
 }
 
-// component `comp` (0..26) of the record v moved by E_z (see shift_record),
-// reading the whole 27-vector from shared memory
-template <typename T>
-__device__ __forceinline__ T shifted_component(const T *v, int comp, const Vec3<T> &z) {
-  const T Z[9] = {T(0), -z.z, z.y, z.z, T(0), -z.x, -z.y, z.x, T(0)};
-  auto Pm = [&](int i, int j) { return v[t6(i, j)]; };
-  auto Qm = [&](int i, int j) { return v[t6(i, 3 + j)]; };
-  auto Rm = [&](int i, int j) { return v[t6(3 + i, 3 + j)]; };
-  if (comp >= 21) {
-    const int r = comp - 21;
-    if (r >= 3) return v[comp];
-    return v[comp] + Z[3 * r] * v[24] + Z[3 * r + 1] * v[25] + Z[3 * r + 2] * v[26];
-  }
-  // (i, j), i <= j, of the upper-triangle index
-  int i = 0, rem = comp;
+// (i, j), i <= j, of upper-triangle index comp < 21 of a symmetric 6x6
+__device__ __forceinline__ void upper_ij(int comp, int &i, int &j) {
+  int rem = comp;
+  i = 0;
   while (rem >= 6 - i) {
     rem -= 6 - i;
     ++i;
   }
-  const int j = i + rem;
-  if (i >= 3) return v[comp];
+  j = i + rem;
+}
+
+// row i and column j of Z = [z]x = [[0, -z3, z2], [z3, 0, -z1], [-z2, z1, 0]],
+// selected (a runtime index into a local Z array would live in local memory)
+template <typename T>
+__device__ __forceinline__ void skew_row(const Vec3<T> &z, int i, T (&r)[3]) {
+  r[0] = i == 0 ? T(0) : (i == 1 ? z.z : -z.y);
+  r[1] = i == 0 ? -z.z : (i == 1 ? T(0) : z.x);
+  r[2] = i == 0 ? z.y : (i == 1 ? -z.x : T(0));
+}
+template <typename T>
+__device__ __forceinline__ void skew_col(const Vec3<T> &z, int j, T (&c)[3]) {
+  c[0] = j == 0 ? T(0) : (j == 1 ? -z.z : z.y);
+  c[1] = j == 0 ? z.z : (j == 1 ? T(0) : -z.x);
+  c[2] = j == 0 ? -z.y : (j == 1 ? z.x : T(0));
+}
+
+// component `comp` (0..26) of the record v moved by E_z (see shift_record),
+// reading the whole 27-vector from shared memory.  The caller decodes the lane's
+// component once: (i, j) = upper_ij(comp) for comp < 21, i = comp - 21 for the
+// three rotational gradient components 21..23 (unused for the rest).
+template <typename T>
+__device__ __forceinline__ T shifted_component(const T *v, int comp, int i, int j, const Vec3<T> &z) {
+  auto Pm = [&](int a, int c) { return v[t6(a, c)]; };
+  auto Qm = [&](int a, int c) { return v[t6(a, 3 + c)]; };
+  auto Rm = [&](int a, int c) { return v[t6(3 + a, 3 + c)]; };
+  if (comp >= 24 || (comp < 21 && i >= 3)) return v[comp];
+  T zi[3];  // row i of Z
+  skew_row(z, i, zi);
+  if (comp >= 21) return v[comp] + zi[0] * v[24] + zi[1] * v[25] + zi[2] * v[26];
   if (j >= 3) {  // Q' = Q + Z R
     T acc = Qm(i, j - 3);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) acc += Z[3 * i + k] * Rm(k, j - 3);
+    for (int k = 0; k < 3; ++k) acc += zi[k] * Rm(k, j - 3);
     return acc;
   }
   // P' = P - Q Z + Z Q^T - Z R Z
+  T zj[3];  // column j of Z
+  skew_col(z, j, zj);
   T acc = Pm(i, j);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    acc -= Qm(i, k) * Z[3 * k + j];
-    acc += Z[3 * i + k] * Qm(j, k);
+    acc -= Qm(i, k) * zj[k];
+    acc += zi[k] * Qm(j, k);
     T zr = T(0);
 #pragma unroll
-    for (int l = 0; l < 3; ++l) zr += Rm(k, l) * Z[3 * l + j];
-    acc -= Z[3 * i + k] * zr;
+    for (int l = 0; l < 3; ++l) zr += Rm(k, l) * zj[l];
+    acc -= zi[k] * zr;
   }
   return acc;
 }
@@ -116,32 +136,65 @@ __device__ __forceinline__ T shifted_component(const T *v, int comp, const Vec3<
 // running sum is re-centred from c_{lo-1} to c_lo before adding M(lo, hi), so
 // every partial sum sits at the origin of its row i and only relative centres
 // enter the arithmetic.  Reads and clears the accumulators.
+// Each lane first copies its component of the next stage_len<T>() records into
+// shared memory with asynchronous copies (all in flight at once, no registers
+// held), so the step chain waits on no global load: one memory round trip per
+// stage instead of one per step.
+constexpr int kPrefixWarps = 4;
 template <typename T>
-__global__ void __launch_bounds__(256) k_pair_prefix(PlanView pv, WorkView wv) {
-  __shared__ T acc_s[8][28];
+__host__ __device__ constexpr int prefix_stage_len() { return sizeof(T) == 4 ? 32 : 16; }
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst_smem)),
+               "l"(src), "n"((int)sizeof(T))
+               : "memory");
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPrefixWarps * 32) k_pair_prefix(PlanView pv, WorkView wv) {
+  constexpr int kStage = prefix_stage_len<T>();
+  __shared__ T acc_s[kPrefixWarps][28];
+  __shared__ T rec_s[kPrefixWarps][kStage * 27];  // [step][component], a lane reads only its own
   const int b = blockIdx.y;
   if (!problem_active(wv.lm, b, GATE_RELIN)) return;
   const int N = pv.p_npose[b], D = pv.p_pair_D[b];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int hi = 1 + blockIdx.x * (blockDim.x >> 5) + w;
+  const int hi = 1 + blockIdx.x * kPrefixWarps + w;
   if (hi > N) return;
   const int fo = pv.p_frame_off[b];
   T *acc_base = reinterpret_cast<T *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
   T *out_base = reinterpret_cast<T *>(wv.pairF) + (size_t)pv.p_pair_off[b] * 27;
   T *acc = acc_s[w];
+  T *stage = rec_s[w];
   if (lane < 27) acc[lane] = T(0);
   __syncwarp();
   const int lo0 = max(0, hi - D);
-  const int cl = lane < 27 ? lane : 0;
-  T next = acc_base[((size_t)lo0 * D + (hi - lo0 - 1)) * 27 + cl];  // prefetched one record ahead
+  int ci = 0, cj = 0;
+  if (lane < 21) upper_ij(lane, ci, cj);
+  else ci = lane - 21;
+  // record (lo, hi) sits at (lo D + hi - lo - 1) 27: consecutive lo are (D - 1) 27 apart
+  const ptrdiff_t rec_step = (ptrdiff_t)(D - 1) * 27;
   // the re-centring offsets z(lo) = c(lo - 1) - c(lo) of the next 32 steps, one per
   // lane, handed out by shuffles: the step chain does not wait on their loads
   Vec3<T> zb = v3<T>(T(0), T(0), T(0));
   if (lo0 + 1 + lane < hi) zb = FramesT<T>::rel(wv, fo + lo0 + lane, 0, fo + lo0 + 1 + lane, 0);
   for (int lo = lo0; lo < hi; ++lo) {
     const size_t rec = (size_t)lo * D + (hi - lo - 1);
-    const T cur = next;
-    if (lo + 1 < hi) next = acc_base[((size_t)(lo + 1) * D + (hi - lo - 2)) * 27 + cl];
+    const int q = (lo - lo0) % kStage;
+    if (q == 0 && lane < 27) {
+      // this lane's component of the records lo .. lo + cnt - 1, then (once the
+      // copies have landed) their accumulators cleared for the next linearisation
+      const int cnt = min(kStage, hi - lo);
+      T *src = acc_base + rec * 27 + lane;
+#pragma unroll 8
+      for (int s = 0; s < cnt; ++s) cp_async_elem(stage + s * 27 + lane, src + s * rec_step);
+      asm volatile("cp.async.wait_all;" ::: "memory");
+#pragma unroll 8
+      for (int s = 0; s < cnt; ++s) src[s * rec_step] = T(0);
+    }
+    const T cur = lane < 27 ? stage[q * 27 + lane] : T(0);
     if (lo > lo0) {
       const int s = (lo - lo0 - 1) & 31;
       const Vec3<T> z = v3<T>(__shfl_sync(0xffffffffu, zb.x, s), __shfl_sync(0xffffffffu, zb.y, s),
@@ -150,14 +203,13 @@ __global__ void __launch_bounds__(256) k_pair_prefix(PlanView pv, WorkView wv) {
         const int ll = lo + 1 + lane;
         zb = ll < hi ? FramesT<T>::rel(wv, fo + ll - 1, 0, fo + ll, 0) : v3<T>(T(0), T(0), T(0));
       }
-      const T v = lane < 27 ? shifted_component(acc, lane, z) : T(0);
+      const T v = lane < 27 ? shifted_component(acc, lane, ci, cj, z) : T(0);
       __syncwarp();
       if (lane < 27) acc[lane] = v;
       __syncwarp();
     }
     if (lane < 27) {
       const T nv = acc[lane] + cur;
-      acc_base[rec * 27 + lane] = T(0);
       acc[lane] = nv;
       out_base[rec * 27 + lane] = nv;
     }
@@ -178,12 +230,12 @@ __global__ void k_pair_suffix(PlanView pv, WorkView wv) {
   T *base = reinterpret_cast<T *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + (size_t)i * D) * 27 + comp;
   T acc = T(0);
   int dp = min(D, N - i);
-  for (; dp >= 4; dp -= 4) {  // four records loaded before any is summed
-    T v[4];
+  for (; dp >= 8; dp -= 8) {  // eight records loaded before any is summed
+    T v[8];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = base[(size_t)(dp - 1 - q) * 27];
+    for (int q = 0; q < 8; ++q) v[q] = base[(size_t)(dp - 1 - q) * 27];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 8; ++q) {
       acc += v[q];
       base[(size_t)(dp - 1 - q) * 27] = acc;
     }
@@ -194,6 +246,16 @@ __global__ void k_pair_suffix(PlanView pv, WorkView wv) {
     *p = acc;
   }
 }
+
+template <typename T> struct Pair2;
+template <> struct Pair2<float> {
+  using type = float2;
+  __device__ static float2 make(float a, float b) { return make_float2(a, b); }
+};
+template <> struct Pair2<double> {
+  using type = double2;
+  __device__ static double2 make(double a, double b) { return make_double2(a, b); }
+};
 
 // A(i, j) = Ad_i^T F(i, j) Ad_j about origin c_i: Ad_i = diag(R_i, R_i),
 // Ad_j = [[R_j, 0], [[c_j - c_i]x R_j, R_j]];  g(i) = [R_i^T f_w ; R_i^T f_v]
@@ -233,7 +295,8 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
       for (int c = 0; c < 3; ++c)
         CRj[3 * r + c] = X[3 * r] * Rj[c] + X[3 * r + 1] * Rj[3 + c] + X[3 * r + 2] * Rj[6 + c];
   }
-  T *A = reinterpret_cast<T *>(wv.A) + pv.p_S_off[b];
+  // the whole 6x6 block first: out[r][c] = A(6i + r, 6j + c)
+  T out[6][6];
 #pragma unroll
   for (int col = 0; col < 6; ++col) {
     T adj[6];
@@ -250,17 +313,28 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
       for (int k = 0; k < 6; ++k) a += F[t6(r, k)] * adj[k];
       w[r] = a;
     }
-    T out[6];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      out[r] = Ri[r] * w[0] + Ri[3 + r] * w[1] + Ri[6 + r] * w[2];
-      out[3 + r] = Ri[r] * w[3] + Ri[3 + r] * w[4] + Ri[6 + r] * w[5];
+      out[r][col] = Ri[r] * w[0] + Ri[3 + r] * w[1] + Ri[6 + r] * w[2];
+      out[3 + r][col] = Ri[r] * w[3] + Ri[3 + r] * w[4] + Ri[6 + r] * w[5];
     }
+  }
+  // both copies as pairs of adjacent elements (every offset below is even and the
+  // workspace segment 256-byte aligned): the block (i, j) row by row, and for
+  // i != j its transpose (j, i), whose rows are 6 elements at 6i of rows 6j + c
+  using V2 = typename Pair2<T>::type;
+  T *A = reinterpret_cast<T *>(wv.A) + pv.p_S_off[b];
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-      A[(size_t)(6 * i + r) * P + 6 * j + col] = out[r];
-      if (i != j) A[(size_t)(6 * j + col) * P + 6 * i + r] = out[r];
-    }
+  for (int r = 0; r < 6; ++r)
+#pragma unroll
+    for (int c = 0; c < 6; c += 2)
+      *reinterpret_cast<V2 *>(A + (size_t)(6 * i + r) * P + 6 * j + c) = Pair2<T>::make(out[r][c], out[r][c + 1]);
+  if (i != j) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+#pragma unroll
+      for (int r = 0; r < 6; r += 2)
+        *reinterpret_cast<V2 *>(A + (size_t)(6 * j + c) * P + 6 * i + r) = Pair2<T>::make(out[r][c], out[r + 1][c]);
   }
   if (e == 0) {
     const T *f = F + 21;
@@ -279,7 +353,7 @@ int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream
   cudaStream_t st = (cudaStream_t)stream;
   const int nmax = pv.max_P / 6;
   const int nd = pv.max_D > 0 ? pv.max_D : 1;
-  k_pair_prefix<T><<<dim3(grid_for(nmax, 8), pv.B), 256, 0, st>>>(pv, wv);
+  k_pair_prefix<T><<<dim3(grid_for(nmax, kPrefixWarps), pv.B), kPrefixWarps * 32, 0, st>>>(pv, wv);
   k_pair_suffix<T><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);
   k_pairs_to_A<T><<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
   g_launches += 3;
