@@ -159,6 +159,8 @@ struct spgo_plan {
   std::vector<int32_t> wk_prob, wk_ti, wk_tj, wk_cbeg, wk_cend, wk_chunks;
   // tensor-core Schur work: (problem, 128-row tile, column range <= 256, chunks)
   std::vector<int32_t> tc_prob, tc_row0, tc_col0, tc_ncols, tc_cbeg, tc_cend, tc_chunks;
+  // batched factorisation: CTA k factors problem fs_prob[k], widest first
+  std::vector<int32_t> fs_prob;
   std::vector<Seg> segs;
   size_t static_bytes = 0, ws_bytes = 0;
   // host staging: [0, big_bytes) of the device buffer, then the small arrays
@@ -257,6 +259,7 @@ static void build_layout(spgo_plan *p) {
   big(p->off_obs_slot, (size_t)Ot);
   small(p->tc_prob); small(p->tc_row0); small(p->tc_col0); small(p->tc_ncols);
   small(p->tc_cbeg); small(p->tc_cend); small(p->tc_chunks);
+  small(p->fs_prob);
   p->small = arena_get(p->static_bytes - p->big_bytes);
   for (size_t i = 0; i < p->segs.size(); ++i)
     if (small_src[i] && p->segs[i].bytes)
@@ -622,6 +625,12 @@ static int plan_build(const spgo_host_problem *probs, int nprob, int precision, 
       else
         p->large.push_back(b);
     }
+    // widest first: the CTAs of the widest systems (the longest) start first and
+    // the narrow ones fill in beside and behind them
+    p->fs_prob.resize(nprob);
+    std::iota(p->fs_prob.begin(), p->fs_prob.end(), 0);
+    std::stable_sort(p->fs_prob.begin(), p->fs_prob.end(),
+                     [&](int32_t x, int32_t y) { return p->p_npose[x] > p->p_npose[y]; });
   }
   build_layout(p);
   return SPGO_OK;
@@ -731,6 +740,7 @@ static void make_views(spgo_solver *s) {
   v.tc_col0 = seg_ptr<int32_t>(p, st, i++); v.tc_ncols = seg_ptr<int32_t>(p, st, i++);
   v.tc_cbeg = seg_ptr<int32_t>(p, st, i++); v.tc_cend = seg_ptr<int32_t>(p, st, i++);
   v.tc_chunks = seg_ptr<int32_t>(p, st, i++);
+  v.fs_prob = seg_ptr<int32_t>(p, st, i++);
   v.n_tc_items = (int32_t)p->tc_prob.size();
   v.max_P_small = p->max_P_small;
   unsigned char *w = s->d_ws;

@@ -169,6 +169,20 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
   T *stage = reinterpret_cast<T *>(smem_raw + lay.stage);
   T *slab_s = reinterpret_cast<T *>(smem_raw + lay.slab);
   const int rows = 6 * nb;
+  const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
+  // cost pass: each thread's observation record is loaded one loop pass ahead (the
+  // first one here, so its DRAM latency overlaps phase A), so a pass does not open
+  // with a round trip to DRAM; the Jacobian pass has no registers to spare for it
+  int nx_slot = 0, nx_n = 0;
+  float4 nx_z = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto load_obs = [&](int64_t o) {
+    if (o < oe) {
+      nx_slot = pv.obs_slot[o];
+      nx_n = pv.obs_frame[o];
+      nx_z = reinterpret_cast<const float4 *>(pv.obs_uv)[o];
+    }
+  };
+  if (COST) load_obs(ob + tid);
 
   // phase A
   if (tid < cnt) {
@@ -225,7 +239,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
   // accumulator (lo, hi) = (min, max)(host, target), one reduction per value and run
   // (about as many as a per-chunk shared copy would flush, without its shared
   // memory, its zeroing and its flush pass)
-  const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
   const int D = pv.p_pair_D[b];
   auto pair_add = [&](int n, int comp, T v) {  // (operands re-read here: few registers stay live)
     const int host_a = sm.a[0];
@@ -246,10 +259,19 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
 #pragma unroll
       for (int k = 0; k < 6; ++k) m[k] = T(0);
     }
+    int cur_slot = nx_slot, cur_n = nx_n;
+    float4 cur_z = nx_z;
+    if (COST) {
+      load_obs(o + blockDim.x);  // the next pass's record, in flight during this one
+    } else if (o < oe) {
+      cur_slot = pv.obs_slot[o];
+      cur_n = pv.obs_frame[o];
+      cur_z = reinterpret_cast<const float4 *>(pv.obs_uv)[o];
+    }
     if (o < oe) {
-      const int slot = pv.obs_slot[o];
-      const int n = pv.obs_frame[o];
-      const float4 z = reinterpret_cast<const float4 *>(pv.obs_uv)[o];
+      const int slot = cur_slot;
+      const int n = cur_n;
+      const float4 z = cur_z;
       float4 rstore = make_float4(0.f, 0.f, 0.f, 0.f);  // cost pass: residuals to keep
       float4 rlast = make_float4(0.f, 0.f, 0.f, 0.f);   // linearisation (FP32): residuals kept
       if constexpr (!COST && std::is_same<T, float>::value) rlast = reinterpret_cast<const float4 *>(wv.res)[o];

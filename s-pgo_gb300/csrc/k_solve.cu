@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int fail_s;
   __shared__ T tmp_s[kPanel];
-  const int b = blockIdx.x;
+  const int b = pv.fs_prob[blockIdx.x];
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   const int N = pv.p_npose[b], P = 6 * N;
   if (P > pv.max_P_small) return;  // a large system: k_chol_large.cu

@@ -60,6 +60,8 @@ struct PlanView {                 // device pointers into the static buffer
   const int32_t *pose_prob;
   // tensor-core Schur work items
   const int32_t *tc_prob, *tc_row0, *tc_col0, *tc_ncols, *tc_cbeg, *tc_cend, *tc_chunks;
+  // batched factorisation order: CTA k factors problem fs_prob[k] (widest first)
+  const int32_t *fs_prob;
   int32_t n_tc_items;
   int32_t max_P_small;    // widest problem the batched (shared-memory) factorisation takes
 };
