@@ -21,55 +21,6 @@ __device__ __forceinline__ constexpr int t6(int i, int j) {  // symmetric 6x6 up
   return i <= j ? i * 6 - (i * (i - 1)) / 2 + (j - i) : j * 6 - (j * (j - 1)) / 2 + (i - j);
 }
 
-// E_z^T M E_z and E_z^T m for E_z = [[I, 0], [-[z]x, I]]: moves a pair record
-// from origin x to origin y = x - z (K^y = K^x E_{x - y}).  With Z = [z]x:
-//   P' = P - Q Z + Z Q^T - Z R Z,  Q' = Q + Z R,  R' = R,  m' = [m_w + Z m_v ; m_v]
-template <typename T>
-__device__ __forceinline__ void shift_record(T *v, const Vec3<T> &z) {
-  const T Z[9] = {T(0), -z.z, z.y, z.z, T(0), -z.x, -z.y, z.x, T(0)};
-  T P[9], Q[9], R[9];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      P[3 * i + j] = v[t6(i, j)];
-      Q[3 * i + j] = v[t6(i, 3 + j)];
-      R[3 * i + j] = v[t6(3 + i, 3 + j)];
-    }
-  T QZ[9], ZQt[9], ZR[9];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      T a = T(0), bq = T(0), c = T(0);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        a += Q[3 * i + k] * Z[3 * k + j];
-        bq += Z[3 * i + k] * Q[3 * j + k];
-        c += Z[3 * i + k] * R[3 * k + j];
-      }
-      QZ[3 * i + j] = a;
-      ZQt[3 * i + j] = bq;
-      ZR[3 * i + j] = c;
-    }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = i; j < 3; ++j) {
-      T zrz = T(0);
-#pragma unroll
-      for (int k = 0; k < 3; ++k) zrz += ZR[3 * i + k] * Z[3 * k + j];
-      v[t6(i, j)] = P[3 * i + j] - QZ[3 * i + j] + ZQt[3 * i + j] - zrz;
-    }
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) v[t6(i, 3 + j)] = Q[3 * i + j] + ZR[3 * i + j];
-  const T mv0 = v[24], mv1 = v[25], mv2 = v[26];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) v[21 + i] += Z[3 * i] * mv0 + Z[3 * i + 1] * mv1 + Z[3 * i + 2] * mv2;
-}
-
 // (i, j), i <= j, of upper-triangle index comp < 21 of a symmetric 6x6
 __device__ __forceinline__ void upper_ij(int comp, int &i, int &j) {
   int rem = comp;
@@ -96,7 +47,12 @@ __device__ __forceinline__ void skew_col(const Vec3<T> &z, int j, T (&c)[3]) {
   c[2] = j == 0 ? -z.y : (j == 1 ? z.x : T(0));
 }
 
-// component `comp` (0..26) of the record v moved by E_z (see shift_record),
+// Re-centring a pair record: E_z^T M E_z and E_z^T m for E_z = [[I, 0], [-[z]x, I]]
+// move a record from origin x to origin y = x - z (K^y = K^x E_{x - y}).  With the
+// 6x6 block M = [[P, Q], [Q^T, R]] (upper triangle, 21 values), m = [m_w; m_v] and
+// Z = [z]x:  P' = P - Q Z + Z Q^T - Z R Z,  Q' = Q + Z R,  R' = R,
+//            m' = [m_w + Z m_v ; m_v].
+// shifted_component returns component `comp` (0..26) of the moved record,
 // reading the whole 27-vector from shared memory.  The caller decodes the lane's
 // component once: (i, j) = upper_ij(comp) for comp < 21, i = comp - 21 for the
 // three rotational gradient components 21..23 (unused for the rest).
