@@ -124,6 +124,15 @@ typedef struct spgo_params {
                                     0: FP32 SIMT */
     int32_t cost_block;          /* threads per CTA of the cost pass (0: 64; else 32..256, x32) */
     int32_t lin_block;           /* threads per CTA of the Jacobian pass (0: 256; else 32..256, x32) */
+    int32_t outer_steps;         /* mixed path: steps of iterative refinement of the whole damped
+                                    normal equations (poses and inverse depths) against a
+                                    residual J^T (r - J x) - Lambda x formed from the FP32
+                                    Jacobian with exact products and FP64-grade sums; the FP32
+                                    system (pose Hessian, tensor-core Schur complement, FP32
+                                    Cholesky) only preconditions.  0: the FP32 step as solved */
+    int32_t wait_us;             /* limit of every bounded device-side wait, microseconds
+                                    (0: 2 s).  Shortening it only makes waits give up sooner:
+                                    the problem is flagged and its step rejected */
 } spgo_params;
 
 typedef struct spgo_problem_status {
@@ -266,10 +275,11 @@ int64_t spgo_launch_count(const spgo_solver *s);
  * enable: create `capacity` event pairs (0 disables); each profiled launch
  * uses one pair until they run out.  read: synchronise `stream`, return the
  * summed milliseconds and launch counts per kind, and recycle the events.
- * Kinds (n_kinds >= 10): 0 pose chain, 1 linearisation, 2 cost pass,
+ * Kinds (n_kinds >= 11): 0 pose chain, 1 linearisation, 2 cost pass,
  * 3 pair reduction, 4 Schur complement, 5 assembly, 6 factor + solve,
- * 7 inverse-depth back-substitution, 8 pose update, 9 LM bookkeeping. */
-#define SPGO_PROFILE_KINDS 10
+ * 7 inverse-depth back-substitution, 8 pose update, 9 LM bookkeeping,
+ * 10 step refinement (mixed path). */
+#define SPGO_PROFILE_KINDS 11
 int spgo_profile_enable(spgo_solver *s, int32_t capacity);
 int spgo_profile_read(spgo_solver *s, double *ms, int64_t *count, int32_t n_kinds, void *stream);
 
@@ -285,13 +295,22 @@ int spgo_profile_read(spgo_solver *s, double *ms, int64_t *count, int32_t n_kind
  * incremental poses) and d_alpha [n_landmarks], and writes it to d_cost[0].
  * Only params->loss, loss_scale and near_boost are read.
  *
+ * Preconditions the host cannot check (the arrays are in device memory):
+ * d_poses holds n_poses * 12 doubles and d_alpha n_landmarks doubles; host[l]
+ * and obs_frame[o] lie in [0, n_poses]; obs_ptr is non-decreasing with
+ * obs_ptr[0] >= 0 and obs_ptr[n_landmarks] <= n_obs.  The kernel checks the
+ * indices it dereferences: a landmark or observation that breaks them is skipped
+ * and the returned cost is NaN.
+ *
  * It calls no cudaMalloc/cudaFree or allocating library routine: its scratch
  * is a file-scope device array of about 0.9 MB that every GPU loading this
  * library keeps until the process exits, so problems are limited to
  * n_poses + 1 <= SPGO_NOALLOC_MAX_FRAMES and n_landmarks <=
  * SPGO_NOALLOC_MAX_LANDMARKS (larger ones return SPGO_ERR_UNSUPPORTED).
  * The first call on a device looks up that array's device address (no
- * allocation); make that first call before any stream capture.  All calls
+ * allocation); make that first call before any stream capture.  The address is
+ * kept for the process: a device reset (cudaDeviceReset) after the first call
+ * is not supported (a failed launch makes the next call look it up again).  All calls
  * share the array: calls whose kernels overlap on the GPU race, so order them
  * (one stream, or events).  Enqueue only; d_cost is valid once `stream`
  * reaches the end of the call. */

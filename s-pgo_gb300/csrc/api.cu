@@ -171,6 +171,8 @@ struct spgo_plan {
   size_t w_Sx = 0, w_lg = 0, w_lgflag = 0;
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl, w_trace;
+  // refinement of the mixed path's step (k_refine.cu)
+  size_t w_facs = 0, w_twist = 0, w_pdual = 0, w_dal = 0, w_tl = 0, w_gaacc = 0, w_gacc = 0, w_rhsB = 0, w_ddelta = 0;
 
   ~spgo_plan() {
     for (cudaEvent_t e : uploads) {  // the blocks go back to the cache only once no copy reads them
@@ -280,7 +282,7 @@ static void build_layout(spgo_plan *p) {
   p->w_frcl = take((size_t)p->F * 6 * 4);
   p->w_pcand = take((size_t)p->NP * 12 * 8);
   p->w_acand = take((size_t)p->L * 8);
-  p->w_res = take((size_t)p->O * 16);
+  p->w_res = take((size_t)p->O * 16 * 2);  // the state's and the candidate's residuals
   p->w_pacc = take((size_t)p->total_pairs * 27 * ts);
   p->w_pF = take((size_t)p->total_pairs * 27 * ts);
   p->w_A = take((size_t)p->total_S * ts);
@@ -304,6 +306,17 @@ static void build_layout(spgo_plan *p) {
   p->w_probe = take((size_t)p->B * 32 * 8);
   p->w_ctrl = take(mlp_deployed_bytes());
   p->w_trace = take((size_t)p->B * SPGO_TRACE_MAX * 3 * 8);
+  if (p->precision == SPGO_PREC_MIXED) {
+    p->w_facs = take((size_t)p->total_S * 4);
+    p->w_twist = take((size_t)p->total_pairs * 6 * 4);
+    p->w_pdual = take((size_t)p->total_pairs * 12 * 8);
+    p->w_dal = take((size_t)p->L * 8);
+    p->w_tl = take((size_t)p->L * 4);
+    p->w_gaacc = take((size_t)p->L * 8);
+    p->w_gacc = take((size_t)p->total_params * 8);
+    p->w_rhsB = take((size_t)p->total_params * 4);
+    p->w_ddelta = take((size_t)p->total_params * 8);
+  }
   p->ws_bytes = o;
 }
 
@@ -677,7 +690,8 @@ static void drop_graphs(spgo_solver *s) {
 
 // profiled kernel kinds (spgo_profile_read order)
 enum { K_CHAIN, K_LINEARIZE, K_COST, K_SYSTEM, K_SCHUR, K_ASSEMBLE, K_FACTOR, K_BACKSUB, K_UPDATE,
-       K_BOOKKEEP, K_NKINDS };
+       K_BOOKKEEP, K_REFINE, K_NKINDS };
+static_assert(K_NKINDS == SPGO_PROFILE_KINDS, "profile kinds");
 
 struct ProfScope {
   spgo_solver *s;
@@ -783,6 +797,17 @@ static void make_views(spgo_solver *s) {
   x.probe_costs = reinterpret_cast<double *>(w + p->w_probe);
   x.trace = reinterpret_cast<double *>(w + p->w_trace);
   x.ctrl = w + p->w_ctrl;
+  if (p->precision == SPGO_PREC_MIXED) {
+    x.facs = reinterpret_cast<float *>(w + p->w_facs);
+    x.twist = reinterpret_cast<float *>(w + p->w_twist);
+    x.pdual = reinterpret_cast<double *>(w + p->w_pdual);
+    x.dal = reinterpret_cast<double *>(w + p->w_dal);
+    x.tl = reinterpret_cast<float *>(w + p->w_tl);
+    x.gaacc = reinterpret_cast<double *>(w + p->w_gaacc);
+    x.gacc = reinterpret_cast<double *>(w + p->w_gacc);
+    x.rhsB = reinterpret_cast<float *>(w + p->w_rhsB);
+    x.ddelta = reinterpret_cast<double *>(w + p->w_ddelta);
+  }
 }
 
 // one linearisation + reduced system (+ damping from the device-side lambda)
@@ -841,13 +866,44 @@ static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
   return SPGO_OK;
 }
 
+// the candidate state of the damped step: solve, then (mixed path, outer_steps > 0)
+// iterative refinement against the accurately summed residual of the whole system,
+// then the inverse-depth back-substitution and the pose update (each adding its share
+// of the predicted decrease)
+template <typename T>
+static int enqueue_candidate(spgo_solver *s, cudaStream_t st) {
+  int rc;
+  if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
+  const int outer = std::is_same<T, float>::value && s->wv.facs ? s->prm.outer_steps : 0;
+  if (outer <= 0) {
+    { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st)); }
+    { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
+    return SPGO_OK;
+  }
+  {
+    PROF(K_REFINE);
+    CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
+    for (int k = 0; k < outer; ++k) {
+      CUDA_TRY(launch_resid_pass(s->pv, s->wv, s->prm, s->alpha, k == 0, st));
+      CUDA_TRY(launch_resid_solve(s->pv, s->wv, k == 0, st));
+      for (const int b : s->plan->large)
+        CUDA_TRY(launch_refine_large(s->pv, s->wv, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b], st));
+      if (k + 1 < outer) CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
+    }
+  }
+  { PROF(K_BACKSUB); CUDA_TRY(launch_backsub_refined(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, st)); }
+  {
+    PROF(K_UPDATE);
+    CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st, s->wv.gacc));
+  }
+  return SPGO_OK;
+}
+
 template <typename T>
 static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
   int rc;
   if ((rc = enqueue_linearize<T>(s, st, s->controller, s->controller)) != SPGO_OK) return rc;
-  if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
-  { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st)); }
-  { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
+  if ((rc = enqueue_candidate<T>(s, st)) != SPGO_OK) return rc;
   { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, kF64<T>, st)); }
   { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st)); }
   {
@@ -855,6 +911,12 @@ static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
     CUDA_TRY(launch_decide(s->pv, s->wv, s->prm, st));
   }
   { PROF(K_BOOKKEEP); CUDA_TRY(launch_commit(s->pv, s->wv, s->poses, s->alpha, st)); }
+  if (std::is_same<T, float>::value && s->wv.facs && s->prm.outer_steps > 0) {
+    // the refinement recomputes the Jacobian at the state from the frame tables, which
+    // a rejected candidate's chain has overwritten: back to the state's
+    PROF(K_CHAIN);
+    CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_REJECTED, kF64<T>, st));
+  }
   return SPGO_OK;
 }
 
@@ -879,12 +941,13 @@ static int enqueue_probe(spgo_solver *s, int nf, const double *factors, cudaStre
   CUDA_TRY(cudaMemcpyAsync(s->wv.lm_backup, s->wv.lm, sizeof(LMState) * s->plan->B, cudaMemcpyDeviceToDevice, st));
   for (int j = 0; j < nf; ++j) {
     CUDA_TRY(launch_scale_lambda(s->pv, s->wv, factors[j], st));
-    if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
-    CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st));
-    CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st));
+    if ((rc = enqueue_candidate<T>(s, st)) != SPGO_OK) return rc;
     CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, kF64<T>, st));
     CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st));
     CUDA_TRY(launch_take_probe(s->pv, s->wv, j, st));
+    // (the next probe's refinement reads the state's frame tables)
+    if (std::is_same<T, float>::value && s->wv.facs && s->prm.outer_steps > 0 && j + 1 < nf)
+      CUDA_TRY(launch_chain(s->pv, s->wv, s->poses, GATE_RUNNING, kF64<T>, st));
   }
   CUDA_TRY(cudaMemcpyAsync(s->wv.lm, s->wv.lm_backup, sizeof(LMState) * s->plan->B, cudaMemcpyDeviceToDevice, st));
   // the probes overwrote the frame tables: back to the state's
@@ -914,6 +977,8 @@ void spgo_default_params(spgo_params *p) {
   p->refine_steps = 1;
   p->use_graph = 1;
   p->use_tc = 1;
+  p->outer_steps = 2;
+  p->wait_us = 0;
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
@@ -1080,7 +1145,7 @@ int spgo_set_params(spgo_solver *s, const spgo_params *p) {
   if (!s || !p) return fail(SPGO_ERR_INVALID_ARG, "null argument");
   if (p->loss < 0 || p->loss > 2) return fail(SPGO_ERR_INVALID_ARG, "unknown loss");
   if (!(p->loss_scale > 0) || !(p->eps >= 0) || !(p->alpha_min < p->alpha_max) || p->max_iters < 0 ||
-      p->refine_steps < 0 || !(p->lambda0 >= 0))
+      p->refine_steps < 0 || !(p->lambda0 >= 0) || p->outer_steps < 0 || p->outer_steps > 8 || p->wait_us < 0)
     return fail(SPGO_ERR_INVALID_ARG, "parameter out of range");
   for (const int32_t blk : {p->cost_block, p->lin_block})
     if (blk != 0 && (blk < 32 || blk > 256 || blk % 32 != 0))

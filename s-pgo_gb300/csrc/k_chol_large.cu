@@ -368,9 +368,10 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
 }
 
 // backward L^T x = z (z in place in lg_y); then x is added to the solution so far
-// (first: x itself) and written to delta (last) or to lg_x and its split
+// (first: x itself) and written to delta (last) or to lg_x and its split; accum
+// (a refinement correction of the mixed path): delta += x and ddelta = x
 template <typename T>
-__global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b, int first, int last) {
+__global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b, int first, int last, int accum) {
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   __shared__ T part[4][kLgNB];
   __shared__ T zs[kLgNB];
@@ -451,7 +452,11 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
     lg_set_flag(flag + k);
     if (timed_out) wv.lm[b].fail = 1;
   }
-  if (tid < nb) {
+  if (tid < nb && accum) {
+    const int i = kb + tid;
+    wv.delta[po + i] += (double)zs[tid];
+    wv.ddelta[po + i] = (double)zs[tid];
+  } else if (tid < nb) {
     const int i = kb + tid;
     const double xi = (first ? 0.0 : wv.lg_x[po + i]) + (double)zs[tid];
     if (last) {
@@ -532,12 +537,28 @@ int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, in
     k_lg_fwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0);
     e = cudaMemsetAsync(fb, 0, sizeof(int) * (size_t)nblk, st);
     if (e != cudaSuccess) return (int)e;
-    k_lg_bwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0, it == refine);
+    k_lg_bwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0, it == refine, 0);
     n += 2;
   }
   k_lg_zero_failed<<<grid_for(P, 256), 256, 0, st>>>(pv, wv, b);
   ++n;
   g_launches += n;
+  return (int)cudaGetLastError();
+}
+
+// one refinement correction of the mixed path: the right-hand side is in lg_y
+// (k_resid_solve); delta += S^-1 lg_y with the factor of this iteration
+int launch_refine_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, void *stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nblk = (P + kLgNB - 1) / kLgNB;
+  int *ff = wv.lg_flag + param_off, *fb = wv.lg_flag + pv.total_params + param_off;
+  cudaError_t e = cudaMemsetAsync(ff, 0, sizeof(int) * (size_t)nblk, st);
+  if (e != cudaSuccess) return (int)e;
+  k_lg_fwd<float><<<nblk, 256, 0, st>>>(pv, wv, b, 0);
+  e = cudaMemsetAsync(fb, 0, sizeof(int) * (size_t)nblk, st);
+  if (e != cudaSuccess) return (int)e;
+  k_lg_bwd<float><<<nblk, 256, 0, st>>>(pv, wv, b, 0, 0, 1);
+  g_launches += 2;
   return (int)cudaGetLastError();
 }
 

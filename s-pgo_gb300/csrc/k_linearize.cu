@@ -170,6 +170,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
   T *slab_s = reinterpret_cast<T *>(smem_raw + lay.slab);
   const int rows = 6 * nb;
   const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
+  // residual store: the Jacobian pass reads the state's half; the cost pass of the
+  // state after a reset writes the state's half, a candidate's the other half
+  const int sel = wv.lm[b].res_sel;
+  float *res_buf = wv.res + (size_t)(COST && gate != GATE_FIRST ? 1 - sel : sel) * (size_t)pv.O * 4;
   // cost pass: each thread's observation record is loaded one loop pass ahead (the
   // first one here, so its DRAM latency overlaps phase A), so a pass does not open
   // with a round trip to DRAM; the Jacobian pass has no registers to spare for it
@@ -274,7 +278,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
       const float4 z = cur_z;
       float4 rstore = make_float4(0.f, 0.f, 0.f, 0.f);  // cost pass: residuals to keep
       float4 rlast = make_float4(0.f, 0.f, 0.f, 0.f);   // linearisation (FP32): residuals kept
-      if constexpr (!COST && std::is_same<T, float>::value) rlast = reinterpret_cast<const float4 *>(wv.res)[o];
+      if constexpr (!COST && std::is_same<T, float>::value) rlast = reinterpret_cast<const float4 *>(res_buf)[o];
       const int a = sm.a[slot];
       const Vec3<T> X = v3<T>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
       const int fa = fo + a, fn = fo + n;
@@ -387,7 +391,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
           q[5] += u0.z * sj0 + u1.z * sj1;
         }
       }
-      if constexpr (COST && std::is_same<T, float>::value) reinterpret_cast<float4 *>(wv.res)[o] = rstore;
+      if constexpr (COST && std::is_same<T, float>::value) reinterpret_cast<float4 *>(res_buf)[o] = rstore;
       if (!COST) {
         atomicAdd(&sm.C[slot], accC);
         atomicAdd(&sm.ga[slot], accG);

@@ -1,0 +1,652 @@
+// Iterative refinement of the mixed path's LM step.
+//
+// The FP32 reduced system (pose Hessian from FP32 pair sums, tensor-core Schur
+// complement, FP32 Cholesky) gives a step whose error, on the ill-conditioned
+// systems of the circle scenes, reaches 1e-3 relative.  Such steps do not change
+// where LM converges, but they change where it is after a fixed iteration budget,
+// and the accepted cost then differs from the FP64 solver's by far more than the
+// 1e-6 the solvers are compared at.  The cause is the accumulation of the normal
+// equations (the sums over observations and landmarks, which cancel in S = A -
+// W D^-1 W^T and in the gradient), not the FP32 Jacobian itself.
+//
+// So the FP32 system only preconditions.  Each refinement step forms the
+// residual of the whole damped system
+//   r_p = J_p^T W (r - J x) - lam diag(A) x_p,   r_a = J_a^T W (r - J x) - (lam C + eps) x_a
+// from the FP32 Jacobian, recomputed per observation, with every product J e
+// exact (two-product) and every sum in double-float / FP64, then applies the FP32
+// system's inverse: x_p += S^-1 (r_p - W D^-1 r_a), x_a += D^-1 (r_a - W^T dx_p).
+// The first residual pass also sums the accurate gradient J^T W r, which the
+// predicted decrease of the gain ratio uses.
+//
+//   k_pair_twists     per problem: the world twist of every pose pair's poses,
+//                     W(lo, hi) = sum_{i in [lo, hi)} Ad_i x_i about c_lo (FP64 sums,
+//                     stored FP32), so J_o x_p = s_o K_o W(lo, hi) per observation
+//   k_resid_pass      per landmark chunk: the inverse-depth step of the chunk's
+//                     landmarks, then one thread per observation: e = r - J x and its
+//                     dual s K^T W e (pair records, FP64 atomics per run of equal
+//                     target frame) and j_a^T W e (per landmark, FP64); then
+//                     t = D^-1 r_a and W t into the pose right-hand side
+//   k_resid_solve     per problem: the pair records reduced to per-pose vectors
+//                     (FP64), the right-hand side, and the solve with the stored FP32
+//                     factor (or, for systems too wide for one CTA, the multi-CTA
+//                     substitutions of k_chol_large.cu)
+//   k_backsub_refined per chunk: the last inverse-depth correction, the candidate
+//                     inverse depths and their share of the predicted decrease
+//
+// Replaces nothing in the reference, whose GPU step is an FP32 Gauss-Newton step
+// solved once (src/Optimization/Solver_cuda.cu:594-782, linear_solvers.cu:195-218).
+#include "kernels.cuh"
+#include "frames.cuh"
+#include "dfloat.cuh"
+#include "chol_subst.cuh"
+
+namespace spgo {
+
+__device__ __forceinline__ double df_to_double(const df &a) { return (double)a.h + (double)a.l; }
+
+// a b + c d exactly rounded to a double-float
+__device__ __forceinline__ df prod2(float a, float b, float c, float d) {
+  const df p = two_prod(a, b), q = two_prod(c, d);
+  df s = two_sum(p.h, q.h);
+  s.l += p.l + q.l;
+  return fast_two_sum(s.h, s.l);
+}
+
+// left camera of frame f: rotation (cam -> world) and centre, FP64 from the
+// double-float frame tables of the mixed path
+__device__ __forceinline__ void frame_Rc(const WorkView &wv, int f, double *R, double *c) {
+  const float *Rh = wv.fr_Rf + (size_t)f * 18, *Rl = wv.fr_Rl + (size_t)f * 18;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) R[k] = (double)Rh[k] + (double)Rl[k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) c[k] = (double)wv.fr_ch[(size_t)f * 6 + k] + (double)wv.fr_cl[(size_t)f * 6 + k];
+}
+
+__device__ __forceinline__ bool refine_active(const WorkView &wv, int b) {
+  return problem_active(wv.lm, b, GATE_RUNNING) && !wv.lm[b].fail;
+}
+
+// ---- pose-pair twists -------------------------------------------------------
+// Ad_i x_i = [R_i psi_i ; (c_i - o) x R_i psi_i + R_i rho_i] about origin o (the
+// convention of the pose blocks, k_system.cu).  With the prefix sums
+// Om(k) = sum_{i<k} R_i psi_i and V(k) = sum_{i<k} c_i x R_i psi_i + R_i rho_i,
+// W(lo, hi) = [Om(hi) - Om(lo) ; V(hi) - V(lo) - c_lo x (Om(hi) - Om(lo))].
+constexpr int kTwThreads = 128;
+
+__global__ void __launch_bounds__(kTwThreads) k_pair_twists(PlanView pv, WorkView wv) {
+  extern __shared__ double tw_s[];  // [(N + 1) * 6]
+  const int b = blockIdx.x;
+  if (!refine_active(wv, b)) return;
+  const int N = pv.p_npose[b], D = pv.p_pair_D[b], fo = pv.p_frame_off[b], po = pv.p_param_off[b];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    double R[9], c[3];
+    frame_Rc(wv, fo + i, R, c);
+    const double *x = wv.delta + po + 6 * i;
+    double w[3], v[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      w[r] = R[3 * r] * x[0] + R[3 * r + 1] * x[1] + R[3 * r + 2] * x[2];
+      v[r] = R[3 * r] * x[3] + R[3 * r + 1] * x[4] + R[3 * r + 2] * x[5];
+    }
+    double *o = tw_s + (size_t)(i + 1) * 6;
+    o[0] = w[0];
+    o[1] = w[1];
+    o[2] = w[2];
+    o[3] = v[0] + (c[1] * w[2] - c[2] * w[1]);
+    o[4] = v[1] + (c[2] * w[0] - c[0] * w[2]);
+    o[5] = v[2] + (c[0] * w[1] - c[1] * w[0]);
+  }
+  if (threadIdx.x < 6) tw_s[threadIdx.x] = 0.0;
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double acc = 0.0;
+    for (int i = 1; i <= N; ++i) {
+      acc += tw_s[i * 6 + threadIdx.x];
+      tw_s[i * 6 + threadIdx.x] = acc;
+    }
+  }
+  __syncthreads();
+  float *out = wv.twist + (size_t)pv.p_pair_off[b] * 6;
+  for (int t = threadIdx.x; t < N * D; t += blockDim.x) {
+    const int lo = t / D, hi = lo + t % D + 1;
+    if (hi > N) continue;
+    double R[9], c[3];
+    frame_Rc(wv, fo + lo, R, c);
+    double dw[3], dv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      dw[k] = tw_s[hi * 6 + k] - tw_s[lo * 6 + k];
+      dv[k] = tw_s[hi * 6 + 3 + k] - tw_s[lo * 6 + 3 + k];
+    }
+    float *o = out + (size_t)t * 6;
+    o[0] = (float)dw[0];
+    o[1] = (float)dw[1];
+    o[2] = (float)dw[2];
+    o[3] = (float)(dv[0] - (c[1] * dw[2] - c[2] * dw[1]));
+    o[4] = (float)(dv[1] - (c[2] * dw[0] - c[0] * dw[2]));
+    o[5] = (float)(dv[2] - (c[0] * dw[1] - c[1] * dw[0]));
+  }
+}
+
+int launch_pair_twists(const PlanView &pv, const WorkView &wv, void *stream) {
+  const size_t sm = (size_t)(pv.max_P / 6 + 1) * 6 * sizeof(double);
+  k_pair_twists<<<pv.B, kTwThreads, sm, (cudaStream_t)stream>>>(pv, wv);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---- residual pass ------------------------------------------------------------
+constexpr int kRpThreads = 128;
+constexpr int kRpWarps = kRpThreads / 32;
+constexpr int kRpPitch = 33;
+
+struct RefSmem {
+  float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre (hi)
+  float Xl[SPGO_CHUNK][3];  // its low words
+  float dX[SPGO_CHUNK][3];  // dX / d alpha
+  float da[SPGO_CHUNK];     // inverse-depth step (FP32 copy for the residuals)
+  float t[SPGO_CHUNK];      // D^-1 r_a
+  int a[SPGO_CHUNK];
+  double dl[kRpWarps][SPGO_CHUNK];  // j_a^T W e, per warp
+  double gl[kRpWarps][SPGO_CHUNK];  // j_a^T W r (first pass), per warp
+  int key[kRpWarps][32];
+};
+
+// dynamic shared memory: dc [W][6] float x 2 (hi, lo), then the per-warp staging
+// [warps][2 ncomp][33] float of the pair duals (ncomp = 12 on the first pass, else 6)
+__host__ __device__ inline size_t rp_smem(int max_nb, bool first) {
+  const size_t W = (size_t)max_nb + 1;
+  const size_t dc = ((W * 12 * sizeof(float)) + 15) & ~(size_t)15;
+  return dc + (size_t)kRpWarps * 2 * (first ? 12 : 6) * kRpPitch * sizeof(float);
+}
+
+template <bool FIRST>
+__global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView wv, Params prm,
+                                                           const double *__restrict__ alpha_state) {
+  constexpr int NC = FIRST ? 12 : 6;  // double-float dual components staged per observation
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ RefSmem sm;
+  const int c = blockIdx.x;
+  const int b = pv.ch_prob[c];
+  if (!refine_active(wv, b)) return;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int f0 = pv.ch_f0[c], nb = pv.ch_nb[c], lm0 = pv.ch_lm0[c], cnt = pv.ch_cnt[c];
+  const int fo = pv.p_frame_off[b], po = pv.p_param_off[b];
+  const float *intr = pv.p_intr + 8 * b;
+  const float fxs[2] = {intr[0], intr[4]}, fys[2] = {intr[1], intr[5]};
+  const double lam = wv.lm[b].lam;
+  const float eps = prm.eps;
+  const size_t dcb = (((size_t)(pv.max_nb + 1) * 12 * sizeof(float)) + 15) & ~(size_t)15;
+  float *dch = reinterpret_cast<float *>(smem_raw);
+  float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
+  float *stage = reinterpret_cast<float *>(smem_raw + dcb);
+  const float *slab = reinterpret_cast<const float *>(wv.slab) + pv.ch_slab[c];
+  const float *Cv = reinterpret_cast<const float *>(wv.C);
+  const int rows = 6 * nb;
+
+  if (warp == 0) {
+    // the chunk's anchor points (as in the linearisation: double-float, then split)
+    if (lane < cnt) {
+      const int li = lm0 + lane;
+      const int a = pv.lm_host[li];
+      const double al = alpha_state[pv.lm_user[li]];
+      const df ald = df_from_double(al);
+      const df t3[3] = {df_sub(pv.lm_uv[2 * li], intr[2]) / df_make(intr[0]) / ald,
+                        df_sub(pv.lm_uv[2 * li + 1], intr[3]) / df_make(intr[1]) / ald, df_make(1.f) / ald};
+      const float *Rh = wv.fr_Rf + (size_t)(fo + a) * 18, *Rl = wv.fr_Rl + (size_t)(fo + a) * 18;
+      const float alf = (float)al;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const df v = df{Rh[3 * k], Rl[3 * k]} * t3[0] + df{Rh[3 * k + 1], Rl[3 * k + 1]} * t3[1] +
+                     df{Rh[3 * k + 2], Rl[3 * k + 2]} * t3[2];
+        sm.X[lane][k] = v.h;
+        sm.Xl[lane][k] = v.l;
+        sm.dX[lane][k] = -v.h / alf;
+      }
+      sm.a[lane] = a;
+    }
+#pragma unroll
+    for (int w = 0; w < kRpWarps; ++w) {
+      sm.dl[w][lane] = 0.0;
+      sm.gl[w][lane] = 0.0;
+    }
+  } else if (warp == 1) {
+    // inverse-depth step: first pass x_a = D^-1 (g_a - W^T x_p) from the FP32 system,
+    // later x_a += t - D^-1 W^T dx_p (the previous pass's t and pose correction)
+    const double *v = (FIRST ? wv.delta : wv.ddelta) + po + 6 * f0;
+    float s0 = 0.f, s1 = 0.f;
+    for (int rb = 0; rb < rows; rb += 32) {
+      const float dv = rb + lane < rows ? (float)v[rb + lane] : 0.f;
+      const float *sr = slab + (size_t)rb * SPGO_CHUNK + lane;
+      const int nr = min(32, rows - rb);
+      float q[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) q[k] = k < nr ? sr[(size_t)k * SPGO_CHUNK] : 0.f;
+#pragma unroll
+      for (int k = 0; k < 32; k += 2) {
+        s0 += q[k] * __shfl_sync(0xffffffffu, dv, k);
+        s1 += q[k + 1] * __shfl_sync(0xffffffffu, dv, k + 1);
+      }
+    }
+    if (lane < cnt) {
+      const int li = lm0 + lane;
+      const float C = Cv[li];
+      const float Dd = C * (float)(1.0 + lam) + eps;
+      const float s = s0 + s1;
+      double da;
+      if (FIRST)
+        da = (double)((reinterpret_cast<const float *>(wv.ga)[li] - s) / Dd);
+      else
+        da = wv.dal[li] + (double)(wv.tl[li] - s / Dd);
+      wv.dal[li] = da;
+      sm.da[lane] = (float)da;
+    }
+  } else {
+    // the host's left centre minus every window frame's camera centres (double-float)
+    const int fh = fo + pv.lm_host[lm0];
+    for (int idx = tid - 64; idx < (nb + 1) * 6; idx += blockDim.x - 64) {
+      const int f = idx / 6, cam = (idx / 3) & 1, k = idx % 3;
+      const size_t fn = (size_t)(fo + f0 + f);
+      df d = df_sub(wv.fr_ch[(size_t)fh * 6 + k], wv.fr_ch[fn * 6 + cam * 3 + k]);
+      d = d + df_make(wv.fr_cl[(size_t)fh * 6 + k] - wv.fr_cl[fn * 6 + cam * 3 + k]);
+      dch[idx] = d.h;
+      dcl[idx] = d.l;
+    }
+  }
+  __syncthreads();
+
+  const int D = pv.p_pair_D[b];
+  const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
+  const float lscale = prm.loss_scale;
+  // residuals at the linearisation point: the state's half of the residual store
+  const float *res_buf = wv.res + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 4;
+  for (int64_t base = ob + (tid & ~31); base < oe; base += blockDim.x) {
+    const int64_t o = base + lane;
+    df pe[6], pg[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) pe[k] = pg[k] = df_make(0.f);
+    int key = -1, slot = -1;
+    double vle = 0.0, vlg = 0.0;  // this observation's landmark duals
+    if (o < oe) {
+      slot = pv.obs_slot[o];
+      const int n = pv.obs_frame[o];
+      const float4 rl = reinterpret_cast<const float4 *>(res_buf)[o];
+      const int a = sm.a[slot];
+      const int fn = fo + n;
+      const bool has_pose = n != a;
+      const int lo = min(a, n), hi = max(a, n);
+      const float sgn = n > a ? 1.f : -1.f;
+      const float boost = (prm.near_boost && abs(n - a) < 2) ? 16.f : 1.f;
+      const float da = sm.da[slot];
+      const Vec3<float> X = v3<float>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
+      const Vec3<float> dXda = v3<float>(sm.dX[slot][0], sm.dX[slot][1], sm.dX[slot][2]);
+      Vec3<float> Xp = X;
+      float W[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (has_pose) {
+        if (lo != a) {  // point relative to the pair origin: left centre of frame lo
+          const Vec3<float> d = FramesT<float>::rel(wv, fo + a, 0, fo + lo, 0);
+          Xp = v3<float>(X.x + d.x, X.y + d.y, X.z + d.z);
+        }
+        const float *tw = wv.twist + ((size_t)pv.p_pair_off[b] + (size_t)lo * D + (hi - lo - 1)) * 6;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) W[k] = tw[k];
+      }
+      df dle = df_make(0.f), dlg = df_make(0.f);
+#pragma unroll
+      for (int cam = 0; cam < 2; ++cam) {
+        // camera-frame point as the linearisation forms it (double-float, rounded once)
+        const float *Rn = FramesT<float>::R(wv, fn, cam);
+        const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
+        const int fw = n - f0;
+        df Xc[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{dch[fw * 6 + cam * 3 + k], dcl[fw * 6 + cam * 3 + k]};
+        df tt[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          tt[k] = df_dot3(Rn[k], Rl[k], Rn[3 + k], Rl[3 + k], Rn[6 + k], Rl[6 + k], Xc[0], Xc[1], Xc[2]);
+        const Vec3<float> t = v3<float>(tt[0].h, tt[1].h, tt[2].h);
+        const float r0 = cam ? rl.z : rl.x, r1 = cam ? rl.w : rl.y;
+        float rho;
+        const float w2 = boost * robust<float>(prm.loss, lscale, r0 * r0 + r1 * r1, rho);
+        const float fx = fxs[cam], fy = fys[cam], iz = 1.f / t.z;
+        const float j00 = fx * iz, j02 = -fx * t.x * iz * iz, j11 = fy * iz, j12 = -fy * t.y * iz * iz;
+        const Vec3<float> u0 = v3<float>(j00 * Rn[0] + j02 * Rn[2], j00 * Rn[3] + j02 * Rn[5], j00 * Rn[6] + j02 * Rn[8]);
+        const Vec3<float> u1 = v3<float>(j11 * Rn[1] + j12 * Rn[2], j11 * Rn[4] + j12 * Rn[5], j11 * Rn[7] + j12 * Rn[8]);
+        const float ja0 = dot(u0, dXda), ja1 = dot(u1, dXda);
+        float e0 = r0 - ja0 * da, e1 = r1 - ja1 * da;
+        float K0[6], K1[6];
+        if (has_pose) {
+          const Vec3<float> k0 = cross(Xp, u0), k1 = cross(Xp, u1);
+          K0[0] = sgn * k0.x; K0[1] = sgn * k0.y; K0[2] = sgn * k0.z;
+          K0[3] = sgn * u0.x; K0[4] = sgn * u0.y; K0[5] = sgn * u0.z;
+          K1[0] = sgn * k1.x; K1[1] = sgn * k1.y; K1[2] = sgn * k1.z;
+          K1[3] = sgn * u1.x; K1[4] = sgn * u1.y; K1[5] = sgn * u1.z;
+          float jw0 = 0.f, jw1 = 0.f;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            jw0 += K0[k] * W[k];
+            jw1 += K1[k] * W[k];
+          }
+          e0 -= jw0;
+          e1 -= jw1;
+        }
+        const float ew0 = w2 * e0, ew1 = w2 * e1;
+        dle = dle + prod2(ja0, ew0, ja1, ew1);
+        const float gw0 = w2 * r0, gw1 = w2 * r1;
+        if (FIRST) dlg = dlg + prod2(ja0, gw0, ja1, gw1);
+        if (has_pose) {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            pe[k] = pe[k] + prod2(K0[k], ew0, K1[k], ew1);
+            if (FIRST) pg[k] = pg[k] + prod2(K0[k], gw0, K1[k], gw1);
+          }
+        }
+      }
+      vle = df_to_double(dle);
+      if (FIRST) vlg = df_to_double(dlg);
+      if (has_pose) key = n;
+    }
+    {
+      // the warp's own landmark accumulators: lanes sharing a landmark (different
+      // frames) add in rounds of their rank among those peers, no atomics
+      const unsigned peers = __match_any_sync(0xffffffffu, slot);
+      const int rank = __popc(peers & ((1u << lane) - 1u));
+      for (int r = 0; __any_sync(0xffffffffu, slot >= 0 && rank >= r); ++r) {
+        if (slot >= 0 && rank == r) {
+          sm.dl[warp][slot] += vle;
+          if (FIRST) sm.gl[warp][slot] += vlg;
+        }
+        __syncwarp();
+      }
+    }
+    // stage the pair duals, then lanes 0..NC-1 each sum one over the runs of equal
+    // target frame (double-float) and add each run to its pair record (FP64)
+    float *st = stage + (size_t)warp * 2 * NC * kRpPitch;
+    int *keys = sm.key[warp];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      st[(2 * k) * kRpPitch + lane] = pe[k].h;
+      st[(2 * k + 1) * kRpPitch + lane] = pe[k].l;
+      if (FIRST) {
+        st[(2 * (6 + k)) * kRpPitch + lane] = pg[k].h;
+        st[(2 * (6 + k) + 1) * kRpPitch + lane] = pg[k].l;
+      }
+    }
+    keys[lane] = key;
+    __syncwarp();
+    if (__any_sync(0xffffffffu, key >= 0) && lane < NC) {
+      const int host_a = sm.a[0];
+      const float *ch = st + (2 * lane) * kRpPitch, *cl = st + (2 * lane + 1) * kRpPitch;
+      double *rec0 = wv.pdual + (size_t)pv.p_pair_off[b] * 12 + lane;
+      auto emit = [&](int n, const df &v) {
+        const int lo = min(host_a, n), hi = max(host_a, n);
+        atomicAdd(rec0 + ((size_t)lo * D + (hi - lo - 1)) * 12, df_to_double(v));
+      };
+      df acc = df_make(0.f);
+      int cur = keys[0];
+      for (int i = 0; i < 32; ++i) {
+        const int k = keys[i];
+        if (k != cur) {
+          if (cur >= 0) emit(cur, acc);
+          acc = df_make(0.f);
+          cur = k;
+        }
+        acc = acc + df{ch[i], cl[i]};
+      }
+      if (cur >= 0) emit(cur, acc);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // landmark residuals r_a = j_a^T W e - (lam C + eps) x_a, t = D^-1 r_a
+  if (tid < cnt) {
+    const int li = lm0 + tid;
+    const float C = Cv[li];
+    const float Dd = C * (float)(1.0 + lam) + eps;
+    double dsum = 0.0, gsum = 0.0;
+#pragma unroll
+    for (int w = 0; w < kRpWarps; ++w) {
+      dsum += sm.dl[w][tid];
+      gsum += sm.gl[w][tid];
+    }
+    const double ra = dsum - (lam * (double)C + (double)eps) * wv.dal[li];
+    const float t = (float)(ra / (double)Dd);
+    sm.t[tid] = t;
+    wv.tl[li] = t;
+    if (FIRST) wv.gaacc[li] = gsum;
+  } else if (tid < SPGO_CHUNK) {
+    sm.t[tid] = 0.f;
+  }
+  __syncthreads();
+  // W t into the pose right-hand side: warp per slab row, lane = landmark slot
+  const float tv = sm.t[lane];
+  for (int r = warp; r < rows; r += kRpWarps) {
+    const float v = warp_sum(slab[(size_t)r * SPGO_CHUNK + lane] * tv);
+    if (lane == 0 && v != 0.f) atomicAdd(wv.rhsB + po + 6 * f0 + r, v);
+  }
+}
+
+int launch_resid_pass(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha, int first,
+                      void *stream) {
+  if (pv.n_chunks == 0) return 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t sm = rp_smem(pv.max_nb, first != 0);
+  if (first)
+    k_resid_pass<true><<<pv.n_chunks, kRpThreads, sm, st>>>(pv, wv, prm, alpha);
+  else
+    k_resid_pass<false><<<pv.n_chunks, kRpThreads, sm, st>>>(pv, wv, prm, alpha);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---- pair records -> per-pose right-hand side, and the solve ---------------------
+// A record (lo, hi) holds m = [m_w ; m_v] about c_lo; about the world origin it is
+// n = [m_w + c_lo x m_v ; m_v].  Pose i collects every record with lo <= i < hi,
+// moved to c_i: sum n_w - c_i x sum m_v.  With diff(k) = sum_{lo = k} n - sum_{hi = k} n
+// that sum is the prefix sum of diff up to i.  Then r(i) = [R_i^T (.)_w ; R_i^T (.)_v].
+constexpr int kRsThreads = 256;
+
+__host__ __device__ inline size_t rs_layout(int max_Ps, int max_N, size_t *off_cb, size_t *off_y, size_t *off_dinv,
+                                            size_t *off_tmp, size_t *off_L) {
+  auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  size_t o = up((size_t)(max_N + 1) * 12 * sizeof(double));
+  *off_cb = o;
+  o = up(o + (size_t)max_Ps * sizeof(int));
+  *off_y = o;
+  o = up(o + (size_t)max_Ps * sizeof(float));
+  *off_dinv = o;
+  o = up(o + (size_t)max_Ps * sizeof(float));
+  *off_tmp = o;
+  o = up(o + (size_t)kPanel * sizeof(float));
+  *off_L = o;
+  o = up(o + (size_t)max_Ps * (max_Ps + 1) / 2 * sizeof(float));
+  return o;
+}
+
+size_t resid_solve_smem(int max_P_small, int max_N) {
+  size_t a, b, c, d, e;
+  return rs_layout(max_P_small, max_N, &a, &b, &c, &d, &e);
+}
+
+template <bool FIRST>
+__global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkView wv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int b = pv.fs_prob[blockIdx.x];
+  if (!refine_active(wv, b)) return;
+  constexpr int NC = FIRST ? 12 : 6;
+  const int N = pv.p_npose[b], D = pv.p_pair_D[b], P = 6 * N;
+  const int fo = pv.p_frame_off[b], po = pv.p_param_off[b];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  size_t o_cb, o_y, o_dinv, o_tmp, o_L;
+  rs_layout(pv.max_P_small, pv.max_P / 6, &o_cb, &o_y, &o_dinv, &o_tmp, &o_L);
+  double *diff = reinterpret_cast<double *>(smem_raw);  // [(N + 1)][12]
+  for (int k = tid; k < (N + 1) * 12; k += nt) diff[k] = 0.0;
+  __syncthreads();
+  double *recs = wv.pdual + (size_t)pv.p_pair_off[b] * 12;
+  // thread per lo: its records' row sum in registers, each record's column share by
+  // an atomic on diff(hi) (threads of a warp have distinct lo, hence distinct hi)
+  for (int lo = tid; lo < N; lo += nt) {
+    double Rlo[9], clo[3];
+    frame_Rc(wv, fo + lo, Rlo, clo);
+    double row[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) row[k] = 0.0;
+    for (int d = 1; d <= D && lo + d <= N; ++d) {
+      double *rec = recs + ((size_t)lo * D + d - 1) * 12;
+      const int hi = lo + d;
+#pragma unroll
+      for (int s = 0; s < NC; s += 6) {
+        double m[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          m[k] = rec[s + k];
+          rec[s + k] = 0.0;  // cleared for the next pass
+        }
+        const double n[6] = {m[0] + (clo[1] * m[5] - clo[2] * m[4]), m[1] + (clo[2] * m[3] - clo[0] * m[5]),
+                             m[2] + (clo[0] * m[4] - clo[1] * m[3]), m[3], m[4], m[5]};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          row[s + k] += n[k];
+          if (n[k] != 0.0) atomicAdd(&diff[hi * 12 + s + k], -n[k]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k) atomicAdd(&diff[lo * 12 + k], row[k]);
+  }
+  __syncthreads();
+  if (tid < NC) {  // prefix sums: diff(i) becomes the sum over the records covering pose i
+    double acc = 0.0;
+    for (int i = 0; i < N; ++i) {
+      acc += diff[i * 12 + tid];
+      diff[i * 12 + tid] = acc;
+    }
+  }
+  __syncthreads();
+  const bool small = P <= pv.max_P_small;
+  float *y = reinterpret_cast<float *>(smem_raw + o_y);
+  const double lam = wv.lm[b].lam;
+  const float *A = reinterpret_cast<const float *>(wv.A) + pv.p_S_off[b];
+  for (int i = tid; i < N; i += nt) {
+    double R[9], ci[3];
+    frame_Rc(wv, fo + i, R, ci);
+#pragma unroll
+    for (int s = 0; s < NC; s += 6) {
+      const double *S = diff + i * 12 + s;
+      const double w[3] = {S[0] - (ci[1] * S[5] - ci[2] * S[4]), S[1] - (ci[2] * S[3] - ci[0] * S[5]),
+                           S[2] - (ci[0] * S[4] - ci[1] * S[3])};
+      double out[6];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        out[r] = R[r] * w[0] + R[3 + r] * w[1] + R[6 + r] * w[2];
+        out[3 + r] = R[r] * S[3] + R[3 + r] * S[4] + R[6 + r] * S[5];
+      }
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const int p = 6 * i + k;
+        if (s == 0) {
+          const double x = wv.delta[po + p];
+          const double rhs = out[k] - lam * (double)A[(size_t)p * P + p] * x - (double)wv.rhsB[po + p];
+          wv.rhsB[po + p] = 0.f;
+          if (small)
+            y[p] = (float)rhs;
+          else
+            reinterpret_cast<float *>(wv.lg_y)[po + p] = (float)rhs;
+        } else {
+          wv.gacc[po + p] = out[k];
+        }
+      }
+    }
+  }
+  if (!small) return;  // the multi-CTA substitutions (k_chol_large.cu) follow
+  int *cb = reinterpret_cast<int *>(smem_raw + o_cb);
+  float *dinv = reinterpret_cast<float *>(smem_raw + o_dinv);
+  float *tmp = reinterpret_cast<float *>(smem_raw + o_tmp);
+  float *Lm = reinterpret_cast<float *>(smem_raw + o_L);
+  const size_t npk = (size_t)P * (P + 1) / 2;
+  const float *fac = wv.facs + pv.p_S_off[b];
+  for (size_t k = tid; k < npk; k += nt) Lm[k] = fac[k];
+  for (int k = tid; k < P; k += nt) {
+    dinv[k] = fac[npk + k];
+    cb[k] = k * P - (k * (k + 1)) / 2;
+  }
+  __syncthreads();
+  chol_substitute<float>(Lm, cb, y, dinv, tmp, P);
+  for (int k = tid; k < P; k += nt) {
+    const double dx = (double)y[k];
+    wv.delta[po + k] += dx;
+    wv.ddelta[po + k] = dx;
+  }
+}
+
+int launch_resid_solve(const PlanView &pv, const WorkView &wv, int first, void *stream) {
+  const size_t sm = resid_solve_smem(pv.max_P_small, pv.max_P / 6);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (first) {
+    cudaFuncSetAttribute(k_resid_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_resid_solve<true><<<pv.B, kRsThreads, sm, st>>>(pv, wv);
+  } else {
+    cudaFuncSetAttribute(k_resid_solve<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_resid_solve<false><<<pv.B, kRsThreads, sm, st>>>(pv, wv);
+  }
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// ---- the last inverse-depth correction, candidate and predicted decrease -------------
+// one warp per chunk, lane = landmark slot: x_a += t - D^-1 W^T dx_p, alpha' =
+// clamp(alpha + x_a), pred += x_a (g_a + (lam C + eps) x_a) with the accurate g_a
+__global__ void k_backsub_refined(PlanView pv, WorkView wv, Params prm, const double *alpha, double *alpha_out) {
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int slot = threadIdx.x & 31;
+  if (c >= pv.n_chunks) return;
+  const int b = pv.ch_prob[c];
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  const bool failed = wv.lm[b].fail != 0;
+  const int f0 = pv.ch_f0[c], nb = pv.ch_nb[c], lm0 = pv.ch_lm0[c], cnt = pv.ch_cnt[c];
+  const int po = pv.p_param_off[b];
+  const float *slab = reinterpret_cast<const float *>(wv.slab) + pv.ch_slab[c];
+  const double *dl = wv.ddelta + po + 6 * f0;
+  const int rows = 6 * nb;
+  float s0 = 0.f, s1 = 0.f;
+  if (!failed) {
+    for (int rb = 0; rb < rows; rb += 32) {
+      const float dv = rb + slot < rows ? (float)dl[rb + slot] : 0.f;
+      const float *sr = slab + (size_t)rb * SPGO_CHUNK + slot;
+      const int nr = min(32, rows - rb);
+      float v[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) v[k] = k < nr ? sr[(size_t)k * SPGO_CHUNK] : 0.f;
+#pragma unroll
+      for (int k = 0; k < 32; k += 2) {
+        s0 += v[k] * __shfl_sync(0xffffffffu, dv, k);
+        s1 += v[k + 1] * __shfl_sync(0xffffffffu, dv, k + 1);
+      }
+    }
+  }
+  double pred = 0.0;
+  if (slot < cnt && !failed) {
+    const int li = lm0 + slot;
+    const double lam = wv.lm[b].lam;
+    const float C = reinterpret_cast<const float *>(wv.C)[li];
+    const float Dd = C * (float)(1.0 + lam) + prm.eps;
+    const double da = wv.dal[li] + (double)(wv.tl[li] - (s0 + s1) / Dd);
+    pred = da * (wv.gaacc[li] + (lam * (double)C + (double)prm.eps) * da);
+    const int u = pv.lm_user[li];
+    alpha_out[u] = fmin(fmax(alpha[u] + da, (double)prm.alpha_min), (double)prm.alpha_max);
+  }
+  pred = warp_sum(pred);
+  if (slot == 0 && pred != 0.0) atomicAdd(wv.pred_acc + b, pred);
+}
+
+int launch_backsub_refined(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
+                           double *alpha_out, void *stream) {
+  if (pv.n_chunks == 0) return 0;
+  k_backsub_refined<<<grid_for(pv.n_chunks, 4), 128, 0, (cudaStream_t)stream>>>(pv, wv, prm, alpha, alpha_out);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+}  // namespace spgo

@@ -7,6 +7,7 @@
 // (Solver_cuda.cu:497-553).
 #include "kernels.cuh"
 #include "dfloat.cuh"
+#include "chol_subst.cuh"
 
 #include <type_traits>
 
@@ -14,9 +15,8 @@ namespace spgo {
 
 // Storage of the factor: element (i, j), i >= j, at Lm[cb[j] + i] with per-column
 // base offsets cb in shared memory: packed lower triangle, column-major (column j
-// holds rows j..P-1; cb[j] = j P - j (j + 1) / 2) when it fits in shared memory,
-// else the full column-major matrix in global scratch (cb[j] = j P).
-constexpr int kPanel = 16;  // block width of the factorisation and the substitutions
+// holds rows j..P-1; cb[j] = j P - j (j + 1) / 2).  The block width kPanel and the
+// substitutions are in chol_subst.cuh.
 constexpr int kRowRegs = 8; // row entries per lane held in registers by the assembly and residual (P <= 256)
 
 // S(r, c) of the damped reduced system for r >= c, from A (pose blocks), S_L
@@ -169,66 +169,7 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
     __syncthreads();
   }
   for (int it = 0; it <= refine; ++it) {
-    // forward L z = y, block by block; warp 0 solves the 16x16 diagonal block with
-    // lane c owning unknown c (one shuffle per unknown)
-    for (int kb = 0; kb < P; kb += kPanel) {
-      const int ke = min(kb + kPanel, P), w = ke - kb;
-      if (warp == 0) {
-        // lane = unknown; its row of the diagonal block and the pivots are loaded
-        // first, so the serial chain is multiply, shuffle, FMA per unknown
-        T lr[kPanel], di[kPanel];
-#pragma unroll
-        for (int c = 0; c < kPanel; ++c) {
-          lr[c] = (lane < w && c < lane) ? Lm[ix(kb + lane, kb + c)] : T(0);
-          di[c] = c < w ? dinv[kb + c] : T(0);
-        }
-        T v = lane < w ? y[kb + lane] : T(0);
-#pragma unroll
-        for (int c = 0; c < kPanel; ++c) {
-          T yc = v * di[c];
-          yc = __shfl_sync(0xffffffffu, yc, c);
-          if (lane == c) v = yc;
-          v -= lr[c] * yc;
-        }
-        if (lane < w) y[kb + lane] = v;
-      }
-      __syncthreads();
-      for (int i = ke + tid; i < P; i += nt) {
-        T v = y[i];
-        for (int c = 0; c < w; ++c) v -= Lm[ix(i, kb + c)] * y[kb + c];
-        y[i] = v;
-      }
-      __syncthreads();
-    }
-    // backward L^T w = z, blocks from the bottom
-    for (int kb = ((P - 1) / kPanel) * kPanel; kb >= 0; kb -= kPanel) {
-      const int ke = min(kb + kPanel, P), w = ke - kb;
-      for (int c = warp; c < w; c += nw) {
-        T acc = T(0);
-        for (int i = ke + lane; i < P; i += 32) acc += Lm[ix(i, kb + c)] * y[i];
-        acc = warp_sum(acc);
-        if (lane == 0) tmp[c] = acc;
-      }
-      __syncthreads();
-      if (warp == 0) {
-        T lc[kPanel], di[kPanel];  // column `lane` of the diagonal block, pivots
-#pragma unroll
-        for (int c = 0; c < kPanel; ++c) {
-          lc[c] = (c < w && lane < c) ? Lm[ix(kb + c, kb + lane)] : T(0);
-          di[c] = c < w ? dinv[kb + c] : T(0);
-        }
-        T v = lane < w ? y[kb + lane] - tmp[lane] : T(0);
-#pragma unroll
-        for (int c = kPanel - 1; c >= 0; --c) {
-          T xc = v * di[c];
-          xc = __shfl_sync(0xffffffffu, xc, c);
-          if (lane == c) v = xc;
-          v -= lc[c] * xc;
-        }
-        if (lane < w) y[kb + lane] = v;
-      }
-      __syncthreads();
-    }
+    chol_substitute<T>(Lm, cb, y, dinv, tmp, P);
     for (int i = tid; i < P; i += nt) x[i] += (double)y[i];
     __syncthreads();
     if (it == refine) break;
@@ -340,8 +281,9 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
 
 #undef ix
 
+// store: keep the packed factor and the pivots in wv.facs for the refinement solves
 template <typename T>
-__global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, int refine) {
+__global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, int refine, int store) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int fail_s;
   __shared__ T tmp_s[kPanel];
@@ -375,6 +317,13 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
   const bool failed = fail_s != 0;
   for (int i = threadIdx.x; i < P; i += blockDim.x) wv.delta[po + i] = failed ? 0.0 : x[i];
   if (threadIdx.x == 0 && failed) wv.lm[b].fail = 1;
+  if constexpr (std::is_same<T, float>::value) {
+    if (store && !failed) {  // packed factor, then the pivots' reciprocals
+      float *dst = wv.facs + off;
+      for (size_t k = threadIdx.x; k < npk; k += blockDim.x) dst[k] = Lm[k];
+      for (int k = threadIdx.x; k < P; k += blockDim.x) dst[npk + k] = dinv[k];
+    }
+  }
   // clear the consumed S_L tiles (every element whose row tile >= column tile) and g_L
   constexpr int TR = 6 * SPGO_TILE_BLOCKS;
   for (int r = threadIdx.x >> 5; r < P; r += blockDim.x >> 5) {
@@ -397,8 +346,9 @@ int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &pr
   if (pv.max_P_small <= 0) return 0;
   const size_t sm = factor_packed_bytes(pv.max_P_small, sizeof(T));
   const int refine = mixed ? prm.refine_steps : 0;
+  const int store = (mixed && prm.outer_steps > 0 && wv.facs) ? 1 : 0;
   cudaFuncSetAttribute(k_factor_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_factor_solve<T><<<pv.B, 256, sm, (cudaStream_t)stream>>>(pv, wv, refine);
+  k_factor_solve<T><<<pv.B, 256, sm, (cudaStream_t)stream>>>(pv, wv, refine, store);
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -466,9 +416,10 @@ int launch_backsub(const PlanView &pv, const WorkView &wv, const Params &prm, co
 }
 
 // ---- T_k <- T_k Exp(scale * delta_k) in FP64; pred += delta^T (g + lam diag(A) delta) ----
+// gacc: the accurate pose gradient of the refined step (else g of the linearisation)
 template <typename T>
 __global__ void k_update_poses(PlanView pv, WorkView wv, const double *poses, double *out, double scale,
-                               int gate) {
+                               int gate, const double *gacc) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= pv.NP) return;
   const int b = pv.pose_prob[p];
@@ -550,16 +501,16 @@ __global__ void k_update_poses(PlanView pv, WorkView wv, const double *poses, do
   for (int q = 0; q < 6; ++q) {
     const double d = wv.delta[po + q];
     const double akk = (double)A[(size_t)(6 * k + q) * P + 6 * k + q];
-    pred += d * ((double)g[po + q] + lam * akk * d);
+    pred += d * ((gacc ? gacc[po + q] : (double)g[po + q]) + lam * akk * d);
   }
   atomicAdd(wv.pred_acc + b, pred);
 }
 
 template <typename T>
 int launch_update_poses(const PlanView &pv, const WorkView &wv, const double *poses, double *poses_out,
-                        double scale, int direct, void *stream) {
+                        double scale, int direct, void *stream, const double *gacc) {
   k_update_poses<T><<<grid_for(pv.NP, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, poses, poses_out, scale,
-                                                                       direct ? GATE_ALL : GATE_RUNNING);
+                                                                       direct ? GATE_ALL : GATE_RUNNING, gacc);
   ++g_launches;
   return (int)cudaGetLastError();
 }
@@ -574,7 +525,7 @@ __global__ void k_reset(PlanView pv, WorkView wv, double lam) {
   s.cost = s.cost_cand = s.pred = s.cost0 = s.cost_lin = 0.0;
   s.iters = s.accepted = s.status = 0;
   s.relin = 1;
-  s.fail = s.flag = s.factor_failures = s.pad = 0;
+  s.fail = s.flag = s.factor_failures = s.res_sel = 0;
   s.rho1 = s.rho2 = s.rho3 = s.last_rel = s.last_predrel = 0.0;
   s.gnorm = s.dmean = s.dmax = s.dmin = s.cmean = 0.0;
   s.last_acc = s.rej_streak = 0;
@@ -651,6 +602,7 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
     s.lam *= fmax(1.0 / 3.0, 1.0 - t * t * t);
     s.nu = 2.0;
     s.relin = 1;
+    s.res_sel ^= 1;  // the candidate's residuals are now the state's
     if (rel < prm.tol) s.status = SPGO_STATUS_CONVERGED;
   } else {
     if (s.fail) s.factor_failures += 1;
@@ -813,8 +765,10 @@ int launch_to_double(const void *src, int f64, double *dst, int64_t n, void *str
 
 template int launch_factor_solve<float>(const PlanView &, const WorkView &, const Params &, int, void *);
 template int launch_factor_solve<double>(const PlanView &, const WorkView &, const Params &, int, void *);
-template int launch_update_poses<float>(const PlanView &, const WorkView &, const double *, double *, double, int, void *);
-template int launch_update_poses<double>(const PlanView &, const WorkView &, const double *, double *, double, int, void *);
+template int launch_update_poses<float>(const PlanView &, const WorkView &, const double *, double *, double, int, void *,
+                                        const double *);
+template int launch_update_poses<double>(const PlanView &, const WorkView &, const double *, double *, double, int, void *,
+                                         const double *);
 template int launch_backsub<float>(const PlanView &, const WorkView &, const Params &, const double *, double *, int, void *);
 template int launch_backsub<double>(const PlanView &, const WorkView &, const Params &, const double *, double *, int, void *);
 template int launch_export_B_n<float>(const PlanView &, const WorkView &, int, int, double *, double *, double *, void *);

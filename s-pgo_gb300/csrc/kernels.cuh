@@ -12,6 +12,7 @@ __device__ __forceinline__ bool problem_active(const LMState *lm, int b, int gat
   if (s.status != 0) return false;
   if (gate == GATE_RELIN) return s.relin != 0;
   if (gate == GATE_FIRST) return s.relin != 0 && s.iters == 0;
+  if (gate == GATE_REJECTED) return s.relin == 0;
   return true;
 }
 

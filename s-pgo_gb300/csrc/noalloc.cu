@@ -14,6 +14,13 @@
 // clearing between calls.  Calls whose kernels overlap on the GPU (different
 // streams, or different host threads, without ordering between them) race on
 // the array: the caller must order them.
+//
+// The problem's arrays are in the caller's device memory, so the host cannot
+// check them: the cost kernel checks every index it dereferences (host and
+// observation frames in [0, n_poses], obs_ptr non-decreasing inside [0, n_obs]),
+// skips an access that would leave the arrays and marks its block's partial sum
+// NaN, so the returned cost is NaN instead of a value read from a previous call's
+// frames or from outside the scratch array.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -66,11 +73,16 @@ __global__ void k_noalloc_chain(int N, const double *__restrict__ poses, const d
 }
 
 // cost of 32 landmarks per block (warp per landmark, lanes over observations),
-// FP64 throughout; one partial sum per block
+// FP64 throughout; one partial sum per block (NaN when an index was out of range)
 __global__ void __launch_bounds__(256) k_noalloc_cost(spgo_device_problem pr, const double *__restrict__ alpha,
                                                       spgo_params prm, const double *__restrict__ frames,
                                                       double *__restrict__ partial) {
   __shared__ double warp_sum_s[8];
+  __shared__ int bad_s;
+  if (threadIdx.x == 0) bad_s = 0;
+  __syncthreads();
+  const int N = pr.n_poses;
+  bool bad = false;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double fx[2] = {pr.intrinsics[0], pr.intrinsics[4]}, fy[2] = {pr.intrinsics[1], pr.intrinsics[5]};
   const double cx[2] = {pr.intrinsics[2], pr.intrinsics[6]}, cy[2] = {pr.intrinsics[3], pr.intrinsics[7]};
@@ -79,6 +91,11 @@ __global__ void __launch_bounds__(256) k_noalloc_cost(spgo_device_problem pr, co
     const int l = blockIdx.x * kLmPerBlock + s;
     if (l >= pr.n_landmarks) break;
     const int a = pr.host[l];
+    const int64_t ob = pr.obs_ptr[l], oe = pr.obs_ptr[l + 1];
+    if (a < 0 || a > N || ob < 0 || oe < ob || oe > pr.n_obs) {
+      bad = true;
+      continue;
+    }
     const double al = alpha[l];
     const double *fa = frames + (size_t)a * kFrameRec;
     const double tx = ((double)pr.anchor_uv[2 * l] - cx[0]) / fx[0] / al;
@@ -86,8 +103,12 @@ __global__ void __launch_bounds__(256) k_noalloc_cost(spgo_device_problem pr, co
     const double tz = 1.0 / al;
     const double X[3] = {fa[0] * tx + fa[1] * ty + fa[2] * tz, fa[3] * tx + fa[4] * ty + fa[5] * tz,
                          fa[6] * tx + fa[7] * ty + fa[8] * tz};
-    for (int64_t o = pr.obs_ptr[l] + lane; o < pr.obs_ptr[l + 1]; o += 32) {
+    for (int64_t o = ob + lane; o < oe; o += 32) {
       const int n = pr.obs_frame[o];
+      if (n < 0 || n > N) {
+        bad = true;
+        continue;
+      }
       const double *fn = frames + (size_t)n * kFrameRec;
       const double boost = (prm.near_boost && abs(n - a) < 2) ? 16.0 : 1.0;
       for (int cam = 0; cam < 2; ++cam) {
@@ -107,11 +128,12 @@ __global__ void __launch_bounds__(256) k_noalloc_cost(spgo_device_problem pr, co
   }
   acc = spgo::warp_sum(acc);
   if (lane == 0) warp_sum_s[warp] = acc;
+  if (bad) bad_s = 1;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
     for (int w = 0; w < 8; ++w) t += warp_sum_s[w];
-    partial[blockIdx.x] = t;
+    partial[blockIdx.x] = bad_s ? __longlong_as_double(0x7ff8000000000000LL) : t;
   }
 }
 
@@ -173,6 +195,11 @@ extern "C" int spgo_cost_noalloc(const spgo_device_problem *prob, const double *
   k_noalloc_chain<<<1, 1, 0, st>>>(N, d_poses, prob->T_r_to_l, frames);
   if (nblk > 0) k_noalloc_cost<<<nblk, 256, 0, st>>>(*prob, d_alpha, *params, frames, partial);
   k_noalloc_reduce<<<1, 256, 0, st>>>(nblk, partial, d_cost);
-  if (cudaGetLastError() != cudaSuccess) return fail_na(SPGO_ERR_CUDA, "spgo_cost_noalloc: kernel launch failed");
+  if (cudaGetLastError() != cudaSuccess) {
+    // (e.g. the context was reset after the address was resolved: resolve it again next time)
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_addr[dev] = nullptr;
+    return fail_na(SPGO_ERR_CUDA, "spgo_cost_noalloc: kernel launch failed");
+  }
   return SPGO_OK;
 }

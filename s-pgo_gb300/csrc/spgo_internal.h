@@ -26,8 +26,9 @@
 namespace spgo {
 
 // which problems a kernel works on: all, those needing a relinearisation, those still
-// running, those about to be linearised for the first time since the reset
-enum Gate { GATE_ALL = 0, GATE_RELIN = 1, GATE_RUNNING = 2, GATE_FIRST = 3 };
+// running, those about to be linearised for the first time since the reset, those
+// still running whose last step was rejected (after the decision)
+enum Gate { GATE_ALL = 0, GATE_RELIN = 1, GATE_RUNNING = 2, GATE_FIRST = 3, GATE_REJECTED = 4 };
 
 struct PlanView {                 // device pointers into the static buffer
   int32_t B, F, NP, L;
@@ -68,7 +69,8 @@ struct PlanView {                 // device pointers into the static buffer
 
 struct LMState {
   double lam, nu, cost, cost_cand, pred, cost0, cost_lin;
-  int32_t iters, accepted, status, relin, fail, flag, factor_failures, pad;
+  int32_t iters, accepted, status, relin, fail, flag, factor_failures;
+  int32_t res_sel;  // which half of WorkView::res holds the residuals of the state (the other: the candidate's)
   // history and statistics the learned damping controller reads
   double rho1, rho2, rho3, last_rel, last_predrel;
   double gnorm, dmean, dmax, dmin, cmean;
@@ -86,7 +88,8 @@ struct WorkView {
   float *fr_cl;     // [F][2][3] float(c - float(c))
   double *poses_cand;   // [NP][12]
   double *alpha_cand;   // [L] (caller order)
-  float *res;           // [O][4] residuals of the last cost pass (FP32 path): u_l, v_l, u_r, v_r
+  float *res;           // [2][O][4] residuals of the cost passes (FP32 path): u_l, v_l, u_r, v_r; half
+                        // LMState::res_sel holds the state's, the other the last candidate's
   void *pair_acc;       // [total_pairs][27] T  (accumulated by the linearisation)
   void *pairF;          // [total_pairs][27] T  (prefix / suffix sums)
   void *A;              // [total_S] T      pose-pose blocks
@@ -111,6 +114,16 @@ struct WorkView {
   int *lg_flag;         // [2 total_params]: block-done flags of the multi-CTA substitutions
   double *cost_acc;     // [B]
   double *pred_acc;     // [B]
+  // iterative refinement of the mixed path's step (k_refine.cu); null on the FP64 path
+  float *facs;          // [total_S] per problem: packed FP32 Cholesky factor, then 1 / L_kk
+  float *twist;         // [total_pairs][6] sum over the pair's poses of Ad_i delta_i (about c_lo)
+  double *pdual;        // [total_pairs][12] J^T e (0..5) and J^T r (6..11) per pose pair
+  double *dal;          // [L] internal order: the inverse-depth step so far
+  float *tl;            // [L] internal order: D^-1 r_a of the last residual pass
+  double *gaacc;        // [L] internal order: accurate inverse-depth gradient
+  double *gacc;         // [total_params] accurate pose gradient
+  float *rhsB;          // [total_params] B D^-1 r_a of the last residual pass
+  double *ddelta;       // [total_params] the last pose correction
 };
 
 struct Params {
@@ -120,7 +133,13 @@ struct Params {
   int32_t max_iters, refine_steps;
   int32_t use_graph, use_tc;
   int32_t cost_block, lin_block;
+  int32_t outer_steps, wait_us;
 };
+
+// bounded device-side waits: the limit in nanoseconds (wait_us = 0: 2 s)
+__host__ __device__ inline unsigned long long wait_limit_ns(const Params &p) {
+  return p.wait_us > 0 ? 1000ull * (unsigned long long)p.wait_us : 2000000000ull;
+}
 
 // launch wrappers (defined in the .cu files); all return cudaError_t as int
 int launch_chain(const PlanView &pv, const WorkView &wv, const double *poses, int gate, int f64, void *stream);
@@ -138,12 +157,21 @@ int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, in
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed,
                         void *stream);
+// iterative refinement of the mixed path's step (k_refine.cu)
+int launch_pair_twists(const PlanView &pv, const WorkView &wv, void *stream);
+int launch_resid_pass(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha, int first,
+                      void *stream);
+int launch_resid_solve(const PlanView &pv, const WorkView &wv, int first, void *stream);
+int launch_refine_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, void *stream);
+int launch_backsub_refined(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
+                           double *alpha_out, void *stream);
+size_t resid_solve_smem(int max_P_small, int max_N);
 template <typename T>
 int launch_backsub(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
                    double *alpha_out, int direct, void *stream);
 template <typename T>
 int launch_update_poses(const PlanView &pv, const WorkView &wv, const double *poses, double *poses_out,
-                        double scale, int direct, void *stream);
+                        double scale, int direct, void *stream, const double *gacc = nullptr);
 int launch_decide(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
 int launch_commit(const PlanView &pv, const WorkView &wv, double *poses, double *alpha, void *stream);
 int launch_post_linearize(const PlanView &pv, const WorkView &wv, void *stream);

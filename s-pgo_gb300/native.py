@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libspgo.so")
 
 SPGO_OK = 0
+SPGO_ERR_INVALID_ARG, SPGO_ERR_UNSUPPORTED, SPGO_ERR_BUFFER_SMALL, SPGO_ERR_CUDA, SPGO_ERR_NOT_SPD = -1, -2, -3, -4, -5
 PREC_MIXED, PREC_FP64 = 0, 1
 LOSS_L2, LOSS_CAUCHY, LOSS_HUBER = 0, 1, 2
 STATUS_RUNNING, STATUS_CONVERGED, STATUS_MAX_ITERS, STATUS_STALLED = 0, 1, 2, 3
@@ -30,7 +31,7 @@ EXPORTED = [
 TRACE_MAX = 128
 MLP_PARAMS, MLP_INPUTS, MLP_CACHE_PER_SAMPLE = 5378, 16, 386
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
-                 "update", "bookkeeping"]
+                 "update", "bookkeeping", "refine"]
 
 
 class HostProblem(C.Structure):
@@ -58,7 +59,8 @@ class Params(C.Structure):
                 ("alpha_min", C.c_float), ("alpha_max", C.c_float), ("lambda0", C.c_double),
                 ("lambda_max", C.c_double), ("tol", C.c_double), ("max_iters", C.c_int32),
                 ("refine_steps", C.c_int32), ("use_graph", C.c_int32), ("use_tc", C.c_int32),
-                ("cost_block", C.c_int32), ("lin_block", C.c_int32)]
+                ("cost_block", C.c_int32), ("lin_block", C.c_int32), ("outer_steps", C.c_int32),
+                ("wait_us", C.c_int32)]
 
 
 class ProblemStatus(C.Structure):

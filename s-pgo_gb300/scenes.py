@@ -222,14 +222,27 @@ def config2(seed: int = 2) -> Problem:
     return corridor_scene(seed, 500, 200000, window=20, outlier_frac=0.05, name="config2")
 
 
-def config3(seed: int = 3, n_problems: int = 256):
-    """256 circle problems, N ~ U[8, 32], L ~ U[200, 3000], per-problem seeds."""
+def config3_specs(seed: int = 3, n_problems: int = 256):
+    """(problem seed, N, L) of each config-3 problem: N ~ U[8, 32], L ~ U[200, 3000]."""
     rng = np.random.Generator(np.random.PCG64(seed))
     Ns = rng.integers(8, 33, n_problems)
     Ls = rng.integers(200, 3001, n_problems)
     seeds = rng.integers(0, 2**31 - 1, n_problems)
-    return [circle_scene(int(s), int(n), int(l), name=f"config3[{i}]")
-            for i, (n, l, s) in enumerate(zip(Ns, Ls, seeds))]
+    return [(int(s), int(n), int(l)) for s, n, l in zip(seeds, Ns, Ls)]
+
+
+def config3(seed: int = 3, n_problems: int = 256):
+    """256 circle problems, N ~ U[8, 32], L ~ U[200, 3000], per-problem seeds."""
+    return [circle_scene(s, n, l, name=f"config3[{i}]")
+            for i, (s, n, l) in enumerate(config3_specs(seed, n_problems))]
+
+
+def round_pixels_f32(p: Problem) -> Problem:
+    """The problem with its pixels rounded to float32, the precision the solver's plan
+    stores them in: the FP64 oracle and the GPU solvers then see the same data."""
+    p.obs_uv = np.asarray(p.obs_uv, dtype=np.float32).astype(np.float64)
+    p.anchor_uv = np.asarray(p.anchor_uv, dtype=np.float32).astype(np.float64)
+    return p
 
 
 # ---------------------------------------------------------------------------

@@ -74,5 +74,24 @@ def test_noalloc_rejects_oversize(built_lib, cuda_device):
     d.intrinsics = d.T_r_to_l = d.host = d.anchor_uv = d.obs_ptr = d.obs_frame = d.obs_uv = buf.data_ptr()
     rc = built_lib.spgo_cost_noalloc(C.byref(d), C.c_void_p(buf.data_ptr()), C.c_void_p(buf.data_ptr()),
                                      C.byref(nat.default_params()), C.c_void_p(buf.data_ptr()), None)
-    assert rc == nat.SPGO_OK - 2
+    assert rc == nat.SPGO_ERR_UNSUPPORTED
     assert b"allocation-free limits" in built_lib.spgo_last_error()
+
+
+def test_noalloc_bad_frame_index_gives_nan(built_lib, cuda_device):
+    """An observation frame outside [0, n_poses] in the caller's device arrays is
+    skipped by the kernel's own checks and turns the cost into NaN (the call itself
+    succeeds: the host cannot see device memory)."""
+    dev = cuda_device
+    p = scenes.circle_scene(77, 9, 300)
+    bs = BatchSolver([p], precision="fp64", device=dev)
+    keep = []
+    good = device_problem(p, dev, keep)
+    assert np.isfinite(noalloc_cost(built_lib, good, bs.poses, bs.alpha, bs.params, dev))
+    q = p.copy()
+    q.obs_frame = np.array(p.obs_frame, copy=True)
+    q.obs_frame[5] = 1000  # no such frame
+    bad = device_problem(q, dev, keep)
+    assert np.isnan(noalloc_cost(built_lib, bad, bs.poses, bs.alpha, bs.params, dev))
+    # the next call with valid arrays is unaffected
+    assert np.isfinite(noalloc_cost(built_lib, good, bs.poses, bs.alpha, bs.params, dev))
