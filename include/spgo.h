@@ -102,6 +102,9 @@ typedef struct spgo_plan_sizes {
                                     sum over chunks of 2 (6 nb)^2 x 32 (W D^-1 W^T blocks) */
     int32_t n_tc_items;          /* tensor-core Schur work items (128x128 tiles x chunk lists) */
     int32_t tc_chunk_tiles;      /* (chunk, 128x128 tile) products per tensor-core pass */
+    int64_t schur_flops_landmark; /* algorithmic FLOPs of the landmark Schur complement:
+                                    sum over landmarks of 2 (6 k)^2, k = pose blocks its
+                                    Jacobian spans (no chunk padding, no split products) */
 } spgo_plan_sizes;
 
 /* solver parameters */
@@ -142,7 +145,10 @@ typedef struct spgo_problem_status {
     int32_t iterations;          /* LM solves (accepted + rejected)  */
     int32_t accepted;
     int32_t status;              /* SPGO_STATUS_*                    */
-    int32_t factor_failures;
+    int32_t factor_failures;     /* steps rejected for a non-positive pivot  */
+    int32_t wait_timeouts;       /* steps rejected because a bounded device wait ran out
+                                    (spgo_params.wait_us)               */
+    int32_t pad;
 } spgo_problem_status;
 
 typedef struct spgo_plan   spgo_plan;

@@ -283,8 +283,10 @@ static void build_layout(spgo_plan *p) {
   p->w_pcand = take((size_t)p->NP * 12 * 8);
   p->w_acand = take((size_t)p->L * 8);
   p->w_res = take((size_t)p->O * 16 * 2);  // the state's and the candidate's residuals
-  p->w_pacc = take((size_t)p->total_pairs * 27 * ts);
-  p->w_pF = take((size_t)p->total_pairs * 27 * ts);
+  // pose-pair records and their prefix / suffix sums: FP64 on both paths (the mixed
+  // path's Jacobian pass sums them exactly, its pair reduction runs in FP64)
+  p->w_pacc = take((size_t)p->total_pairs * 27 * 8);
+  p->w_pF = take((size_t)p->total_pairs * 27 * 8);
   p->w_A = take((size_t)p->total_S * ts);
   p->w_g = take((size_t)p->total_params * ts);
   p->w_SL = take((size_t)p->total_S * ts);
@@ -860,7 +862,7 @@ static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
     PROF(K_FACTOR);
     CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st));
     for (const int b : s->plan->large)
-      CUDA_TRY(launch_factor_large<T>(s->pv, s->wv, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b],
+      CUDA_TRY(launch_factor_large<T>(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b],
                                       mixed ? s->prm.refine_steps : 0, st));
   }
   return SPGO_OK;
@@ -887,7 +889,7 @@ static int enqueue_candidate(spgo_solver *s, cudaStream_t st) {
       CUDA_TRY(launch_resid_pass(s->pv, s->wv, s->prm, s->alpha, k == 0, st));
       CUDA_TRY(launch_resid_solve(s->pv, s->wv, k == 0, st));
       for (const int b : s->plan->large)
-        CUDA_TRY(launch_refine_large(s->pv, s->wv, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b], st));
+        CUDA_TRY(launch_refine_large(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b], st));
       if (k + 1 < outer) CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
     }
   }
@@ -1013,6 +1015,11 @@ int spgo_plan_sizes_get(const spgo_plan *p, spgo_plan_sizes *o) {
   o->schur_chunk_tiles = (int32_t)p->wk_chunks.size();
   o->schur_flops = 0;
   for (size_t c = 0; c < p->ch_nb.size(); ++c) o->schur_flops += 2LL * (6LL * p->ch_nb[c]) * (6LL * p->ch_nb[c]) * 32;
+  o->schur_flops_landmark = 0;
+  for (int32_t l = 0; l < p->L; ++l) {
+    const int64_t k = p->lm_hi[l] - p->lm_lo[l];
+    o->schur_flops_landmark += 2 * (6 * k) * (6 * k);
+  }
   o->n_tc_items = (int32_t)p->tc_prob.size();
   o->tc_chunk_tiles = (int32_t)p->tc_chunks.size();
   o->static_bytes = p->static_bytes;
@@ -1234,6 +1241,7 @@ int spgo_lm_status(spgo_solver *s, spgo_problem_status *out, void *stream) {
     out[b].accepted = h[b].accepted;
     out[b].status = h[b].status;
     out[b].factor_failures = h[b].factor_failures;
+    out[b].wait_timeouts = h[b].wait_timeouts;
   }
   return SPGO_OK;
 }

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256) k_lg_potrf(PlanView pv, WorkView wv, int 
     }
     __syncthreads();
   }
-  if (tid == 0 && bad) wv.lm[b].fail = 1;
+  if (tid == 0 && bad) atomicOr(&wv.lm[b].fail, FAIL_PIVOT);
   for (int k = tid; k < nb; k += blockDim.x) dinv[kb + k] = di[k];
   for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
     const int i = idx % nb, j = idx / nb;
@@ -258,9 +258,9 @@ __global__ void __launch_bounds__(256) k_lg_syrk(PlanView pv, WorkView wv, int b
 // own flag; backward L^T x = z the same from the bottom (the CTA of block k waits
 // only for blocks finished by lower-numbered CTAs, so the chain never waits on a CTA
 // that has not started).  Thread (r, q) handles unknown r of the block and a 16-wide
-// quarter q of each other block.  Every wait is bounded (2 s); a timeout marks the
-// problem failed (the step is rejected) and the CTA carries on.
-constexpr uint64_t kLgWaitNs = 2000000000ull;
+// quarter q of each other block.  Every wait is bounded (the parameter's limit,
+// 2 s by default); a timeout marks the problem failed (the step is rejected and
+// counted as a timeout, not as a factorisation failure) and the CTA carries on.
 
 __device__ __forceinline__ uint64_t lg_clock_ns() {
   uint64_t t;
@@ -283,7 +283,7 @@ __device__ __forceinline__ void lg_set_flag(int *flag) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b, int first) {
+__global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b, int first, uint64_t wait_ns) {
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   __shared__ T part[4][kLgNB];
   __shared__ T zs[kLgNB];
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
   const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + po;
   T *z = reinterpret_cast<T *>(wv.lg_y) + po;  // in place: this block's right-hand side in, z out
   int *flag = wv.lg_flag + po;
-  const uint64_t deadline = lg_clock_ns() + kLgWaitNs;
+  const uint64_t deadline = lg_clock_ns() + wait_ns;
   if (tid == 0) timed_out = 0;
   __syncthreads();
   T acc = T(0);
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
   if (tid == 0) {
     __threadfence();
     lg_set_flag(flag + k);
-    if (timed_out) wv.lm[b].fail = 1;
+    if (timed_out) atomicOr(&wv.lm[b].fail, FAIL_TIMEOUT);
   }
 }
 
@@ -371,7 +371,8 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
 // (first: x itself) and written to delta (last) or to lg_x and its split; accum
 // (a refinement correction of the mixed path): delta += x and ddelta = x
 template <typename T>
-__global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b, int first, int last, int accum) {
+__global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b, int first, int last, int accum,
+                                                 uint64_t wait_ns) {
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   __shared__ T part[4][kLgNB];
   __shared__ T zs[kLgNB];
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
   const T *dinv = reinterpret_cast<const T *>(wv.lg_dinv) + po;
   T *x = reinterpret_cast<T *>(wv.lg_y) + po;
   int *flag = wv.lg_flag + pv.total_params + po;
-  const uint64_t deadline = lg_clock_ns() + kLgWaitNs;
+  const uint64_t deadline = lg_clock_ns() + wait_ns;
   if (tid == 0) timed_out = 0;
   __syncthreads();
   T acc = T(0);
@@ -450,7 +451,7 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
   if (tid == 0) {
     __threadfence();
     lg_set_flag(flag + k);
-    if (timed_out) wv.lm[b].fail = 1;
+    if (timed_out) atomicOr(&wv.lm[b].fail, FAIL_TIMEOUT);
   }
   if (tid < nb && accum) {
     const int i = kb + tid;
@@ -509,9 +510,10 @@ __global__ void __launch_bounds__(256) k_lg_resid(PlanView pv, WorkView wv, int 
 }
 
 template <typename T>
-int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, int refine,
-                        void *stream) {
+int launch_factor_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
+                        int refine, void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
+  const uint64_t wait_ns = wait_limit_ns(prm);
   k_lg_assemble<T><<<P, 256, 0, st>>>(pv, wv, b);
   int n = 1;
   for (int kb = 0; kb < P; kb += kLgNB) {
@@ -534,10 +536,10 @@ int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, in
     }
     cudaError_t e = cudaMemsetAsync(ff, 0, sizeof(int) * (size_t)nblk, st);
     if (e != cudaSuccess) return (int)e;
-    k_lg_fwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0);
+    k_lg_fwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0, wait_ns);
     e = cudaMemsetAsync(fb, 0, sizeof(int) * (size_t)nblk, st);
     if (e != cudaSuccess) return (int)e;
-    k_lg_bwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0, it == refine, 0);
+    k_lg_bwd<T><<<nblk, 256, 0, st>>>(pv, wv, b, it == 0, it == refine, 0, wait_ns);
     n += 2;
   }
   k_lg_zero_failed<<<grid_for(P, 256), 256, 0, st>>>(pv, wv, b);
@@ -548,21 +550,25 @@ int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, in
 
 // one refinement correction of the mixed path: the right-hand side is in lg_y
 // (k_resid_solve); delta += S^-1 lg_y with the factor of this iteration
-int launch_refine_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, void *stream) {
+int launch_refine_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
+                        void *stream) {
   cudaStream_t st = (cudaStream_t)stream;
+  const uint64_t wait_ns = wait_limit_ns(prm);
   const int nblk = (P + kLgNB - 1) / kLgNB;
   int *ff = wv.lg_flag + param_off, *fb = wv.lg_flag + pv.total_params + param_off;
   cudaError_t e = cudaMemsetAsync(ff, 0, sizeof(int) * (size_t)nblk, st);
   if (e != cudaSuccess) return (int)e;
-  k_lg_fwd<float><<<nblk, 256, 0, st>>>(pv, wv, b, 0);
+  k_lg_fwd<float><<<nblk, 256, 0, st>>>(pv, wv, b, 0, wait_ns);
   e = cudaMemsetAsync(fb, 0, sizeof(int) * (size_t)nblk, st);
   if (e != cudaSuccess) return (int)e;
-  k_lg_bwd<float><<<nblk, 256, 0, st>>>(pv, wv, b, 0, 0, 1);
+  k_lg_bwd<float><<<nblk, 256, 0, st>>>(pv, wv, b, 0, 0, 1, wait_ns);
   g_launches += 2;
   return (int)cudaGetLastError();
 }
 
-template int launch_factor_large<float>(const PlanView &, const WorkView &, int, int, int, int, void *);
-template int launch_factor_large<double>(const PlanView &, const WorkView &, int, int, int, int, void *);
+template int launch_factor_large<float>(const PlanView &, const WorkView &, const Params &, int, int, int, int,
+                                        void *);
+template int launch_factor_large<double>(const PlanView &, const WorkView &, const Params &, int, int, int, int,
+                                         void *);
 
 }  // namespace spgo

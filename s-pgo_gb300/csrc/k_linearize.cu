@@ -112,8 +112,7 @@ constexpr int kStagePitch = 33;     // per-warp staging of the 27 pair values, [
 //   dc    [W][6] float x 2   FP32 path: c_host - c_(f0 + f, cam), hi and lo
 //   stage [warps][27][33] T  per-warp staging of the pair terms
 //   slab  [6 (W - 1)][32] T  the chunk's slab
-// (the cost pass uses dc only).  At W = 33 and four warps the FP32 Jacobian pass
-// takes 42.3 KB: five CTAs per SM.
+// (the cost pass uses dc only).
 template <typename T>
 struct LinLayout {
   size_t dc, stage, slab, total;
@@ -140,18 +139,20 @@ struct LinLayout {
 // turn those rows into b_l(i), then B_l(i) = Ad_i^T b_l(i).
 // COST = true is the cost pass: residuals only, in double-float on the FP32 path
 // (FP64-accurate cost for the gain ratio), which it also stores as FP32 per
-// observation.  The linearisation (COST = false) always follows a cost pass at
-// the same state (the first one after a reset, or the accepted candidate's), so
-// on the FP32 path it reads those residuals instead of forming them from
-// pixel-sized FP32 quantities (whose ~3e-5 px rounding would move the optimum
-// by ~1e-5 m), and it takes the cost from that pass too; only the camera-frame
-// point for the Jacobian is formed there (double-float, without the projection).
-// Register caps (FP32 path): 64 for the cost pass, a latency-bound stream over the
-// observations that runs in small CTAs and gains from the extra resident warps
-// (16 instead of 12 64-thread CTAs per SM); 85 for the Jacobian pass.
+// observation.  The linearisation always follows a cost pass at the same state
+// (the first one after a reset, or the accepted candidate's) and takes the cost
+// from it.  COST = false here is the FP64 path's Jacobian pass; the FP32 path's is
+// k_jacobian_acc below, which reads those stored residuals instead of forming them
+// from pixel-sized FP32 quantities (whose ~3e-5 px rounding would move the optimum
+// by ~1e-5 m).
+// Register cap (FP32 cost pass): 64, a latency-bound stream over the observations
+// that runs in small CTAs and gains from the extra resident warps (16 instead of
+// 12 64-thread CTAs per SM).
 template <typename T, bool COST>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_linearize(PlanView pv, WorkView wv, Params prm,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanView pv, WorkView wv, Params prm,
                                                    const double *__restrict__ alpha_state, int gate) {
+  // (the FP32 path's Jacobian pass is k_jacobian_acc)
+  static_assert(COST || std::is_same<T, double>::value, "FP32 linearisation: k_jacobian_acc");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
   const int b = pv.ch_prob[c];
@@ -277,8 +278,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
       const int n = cur_n;
       const float4 z = cur_z;
       float4 rstore = make_float4(0.f, 0.f, 0.f, 0.f);  // cost pass: residuals to keep
-      float4 rlast = make_float4(0.f, 0.f, 0.f, 0.f);   // linearisation (FP32): residuals kept
-      if constexpr (!COST && std::is_same<T, float>::value) rlast = reinterpret_cast<const float4 *>(res_buf)[o];
       const int a = sm.a[slot];
       const Vec3<T> X = v3<T>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
       const int fa = fo + a, fn = fo + n;
@@ -330,24 +329,6 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
             rstore.x = r0;
             rstore.y = r1;
           }
-        } else if constexpr (std::is_same<T, float>::value) {
-          // the camera-frame point for the Jacobian: X + (c_a - c_n) and the
-          // rotation in double-float, rounded once (an FP32 rotation of the
-          // rounded point measured 1e-5 relative error in the Hessian blocks
-          // on a 45-pose circle scene; this keeps them at the 1e-7 level)
-          const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
-          const int fw = n - f0;
-          df Xc[3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k)
-            Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{dch[fw * 6 + cam * 3 + k], dcl[fw * 6 + cam * 3 + k]};
-          df tt[3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k)
-            tt[k] = df_dot3(Rn[k], Rl[k], Rn[3 + k], Rl[3 + k], Rn[6 + k], Rl[6 + k], Xc[0], Xc[1], Xc[2]);
-          t = v3<T>(tt[0].h, tt[1].h, tt[2].h);
-          r0 = cam ? rlast.z : rlast.x;
-          r1 = cam ? rlast.w : rlast.y;
         } else {
           const Vec3<T> d = FramesT<T>::rel(wv, fa, 0, fn, cam);
           t = mulT(Rn, v3<T>(X.x + d.x, X.y + d.y, X.z + d.z));
@@ -498,6 +479,311 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (COST ? 4 : 3) : 1) k_li
   }
 }
 
+// ---- the mixed path's Jacobian pass: exactly summed normal equations --------------
+// The same FP32 Jacobian as k_linearize (the camera-frame point formed in
+// double-float from the frame tables and rounded once; the residuals of the cost
+// pass at the same state), but the sums that build the normal equations are not
+// left to FP32: the reduced camera system S = A + damping - W D^-1 W^T cancels most
+// of A, and FP32 sums over thousands of observations put errors into A and W that,
+// measured against S, reach its smallest eigenvalues (an FP32-assembled S of a
+// badly initialised circle problem came out indefinite where the FP64 one has
+// scaled smallest eigenvalue 4e-4).  So, with the weighted rows w K (w^2 the robust
+// weight) and the weighted residuals w r rounded once:
+//   * every product of the pair records (21 Hessian and 6 gradient values per
+//     observation) is formed exactly (two-product) and summed in double-float;
+//     each run of equal target frame goes to the FP64 pair record by an FP64 atomic
+//     (the pair reduction then runs in FP64, k_system.cu);
+//   * the slab terms s (w h)(w j_alpha) likewise, and the per-landmark suffix /
+//     prefix sums along the window and the move to each pose frame run in
+//     double-float; the slab is rounded to FP32 once, at the end.
+// C and g_a (positive sums and the preconditioner's own right-hand side) stay FP32.
+struct JacSmem {
+  float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre (hi)
+  float Xl[SPGO_CHUNK][3];  // its low words
+  float dX[SPGO_CHUNK][3];  // dX / d alpha
+  float C[SPGO_CHUNK], ga[SPGO_CHUNK];
+  int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
+  int key[8][32];           // per warp: target frame of each lane's observation (-1: none)
+};
+constexpr int kJacVals = 27;          // 21 Hessian + 6 gradient values per pair record
+constexpr int kJacPitch = 33;
+
+// dynamic shared memory: dc [W][6] float x 2 (hi, lo) | stage [warps][2 * 27][33]
+// float (double-float pair terms) | slab hi and lo [6 (W - 1)][32] float each
+struct JacLayout {
+  size_t dc, stage, slab_h, slab_l, total;
+  __host__ __device__ JacLayout(int max_nb, int warps) {
+    const size_t W = (size_t)max_nb + 1;
+    auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    dc = up(sizeof(JacSmem));
+    stage = dc + up(W * 12 * sizeof(float));
+    slab_h = stage + up((size_t)warps * 2 * kJacVals * kJacPitch * sizeof(float));
+    slab_l = slab_h + up((size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(float));
+    total = slab_l + (size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(float);
+  }
+};
+
+// a b + c d, exactly rounded to a double-float
+__device__ __forceinline__ df prod2_df(float a, float b, float c, float d) {
+  const df p = two_prod(a, b), q = two_prod(c, d);
+  df t = two_sum(p.h, q.h);
+  t.l += p.l + q.l;
+  return fast_two_sum(t.h, t.l);
+}
+
+__global__ void __launch_bounds__(256, 2) k_jacobian_acc(PlanView pv, WorkView wv, Params prm,
+                                                         const double *__restrict__ alpha_state, int gate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int c = blockIdx.x;
+  const int b = pv.ch_prob[c];
+  if (!problem_active(wv.lm, b, gate)) return;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int f0 = pv.ch_f0[c], nb = pv.ch_nb[c], lm0 = pv.ch_lm0[c], cnt = pv.ch_cnt[c];
+  const int fo = pv.p_frame_off[b];
+  const float *intr = pv.p_intr + 8 * b;
+  const float fxs[2] = {intr[0], intr[4]}, fys[2] = {intr[1], intr[5]};
+  JacSmem &sm = *reinterpret_cast<JacSmem *>(smem_raw);
+  const JacLayout lay(pv.max_nb, blockDim.x >> 5);
+  float *dch = reinterpret_cast<float *>(smem_raw + lay.dc);
+  float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
+  float *stage = reinterpret_cast<float *>(smem_raw + lay.stage);
+  float *slab_h = reinterpret_cast<float *>(smem_raw + lay.slab_h);
+  float *slab_l = reinterpret_cast<float *>(smem_raw + lay.slab_l);
+  const int rows = 6 * nb;
+  const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
+  const float *res_buf = wv.res + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 4;  // the state's residuals
+
+  // phase A: the chunk's anchor points (double-float, then split)
+  if (tid < cnt) {
+    const int li = lm0 + tid;
+    const int a = pv.lm_host[li];
+    const double al = alpha_state[pv.lm_user[li]];
+    const df ald = df_from_double(al);
+    const df t3[3] = {df_sub(pv.lm_uv[2 * li], intr[2]) / df_make(intr[0]) / ald,
+                      df_sub(pv.lm_uv[2 * li + 1], intr[3]) / df_make(intr[1]) / ald, df_make(1.f) / ald};
+    const float *Rh = wv.fr_Rf + (size_t)(fo + a) * 18, *Rl = wv.fr_Rl + (size_t)(fo + a) * 18;
+    const float alf = (float)al;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const df v = df{Rh[3 * k], Rl[3 * k]} * t3[0] + df{Rh[3 * k + 1], Rl[3 * k + 1]} * t3[1] +
+                   df{Rh[3 * k + 2], Rl[3 * k + 2]} * t3[2];
+      sm.X[tid][k] = v.h;
+      sm.Xl[tid][k] = v.l;
+      sm.dX[tid][k] = -v.h / alf;
+    }
+    sm.C[tid] = 0.f;
+    sm.ga[tid] = 0.f;
+    sm.a[tid] = a;
+    sm.lo[tid] = pv.lm_lo[li];
+    sm.hi[tid] = pv.lm_hi[li];
+  }
+  {  // the host's left centre minus every window frame's camera centres (double-float)
+    const int fh = fo + pv.lm_host[lm0];
+    for (int idx = tid; idx < (nb + 1) * 6; idx += blockDim.x) {
+      const int f = idx / 6, cam = (idx / 3) & 1, k = idx % 3;
+      const size_t fn = (size_t)(fo + f0 + f);
+      df d = df_sub(wv.fr_ch[(size_t)fh * 6 + k], wv.fr_ch[fn * 6 + cam * 3 + k]);
+      d = d + df_make(wv.fr_cl[(size_t)fh * 6 + k] - wv.fr_cl[fn * 6 + cam * 3 + k]);
+      dch[idx] = d.h;
+      dcl[idx] = d.l;
+    }
+  }
+  for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_h[i] = slab_l[i] = 0.f;
+  __syncthreads();
+
+  // phase B: thread per observation; runs of equal target frame inside a warp go to
+  // the FP64 pair record (host, target)
+  const int D = pv.p_pair_D[b];
+  double *pair_base = reinterpret_cast<double *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * kJacVals;
+  const float lscale = prm.loss_scale;
+  for (int64_t base = ob + (tid & ~31); base < oe; base += blockDim.x) {
+    const int64_t o = base + lane;
+    df M[21], m[6];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) M[k] = df_make(0.f);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) m[k] = df_make(0.f);
+    int key = -1;
+    if (o < oe) {
+      const int slot = pv.obs_slot[o];
+      const int n = pv.obs_frame[o];
+      const float4 rl = reinterpret_cast<const float4 *>(res_buf)[o];
+      const int a = sm.a[slot];
+      const Vec3<float> X = v3<float>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
+      const Vec3<float> dXda = v3<float>(sm.dX[slot][0], sm.dX[slot][1], sm.dX[slot][2]);
+      const int fn = fo + n;
+      const bool has_pose = (n != a);
+      const int lo = min(a, n);
+      const float sgn = n > a ? 1.f : -1.f;
+      const float boost = (prm.near_boost && abs(n - a) < 2) ? 16.f : 1.f;
+      Vec3<float> Xp = X;
+      if (has_pose && lo != a) {  // point relative to the pair origin: left centre of frame lo
+        const Vec3<float> d = FramesT<float>::rel(wv, fo + a, 0, fo + lo, 0);
+        Xp = v3<float>(X.x + d.x, X.y + d.y, X.z + d.z);
+      }
+      df q[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) q[k] = df_make(0.f);
+      float accC = 0.f, accG = 0.f;
+#pragma unroll
+      for (int cam = 0; cam < 2; ++cam) {
+        const float *Rn = FramesT<float>::R(wv, fn, cam);
+        const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
+        const int fw = n - f0;
+        df Xc[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{dch[fw * 6 + cam * 3 + k], dcl[fw * 6 + cam * 3 + k]};
+        df tt[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          tt[k] = df_dot3(Rn[k], Rl[k], Rn[3 + k], Rl[3 + k], Rn[6 + k], Rl[6 + k], Xc[0], Xc[1], Xc[2]);
+        const Vec3<float> t = v3<float>(tt[0].h, tt[1].h, tt[2].h);
+        const float r0 = cam ? rl.z : rl.x, r1 = cam ? rl.w : rl.y;
+        float rho;
+        const float w2 = boost * robust<float>(prm.loss, lscale, r0 * r0 + r1 * r1, rho);
+        const float w = sqrtf(w2);
+        const float fx = fxs[cam], fy = fys[cam], iz = 1.f / t.z;
+        const float j00 = fx * iz, j02 = -fx * t.x * iz * iz, j11 = fy * iz, j12 = -fy * t.y * iz * iz;
+        const Vec3<float> u0 = v3<float>(j00 * Rn[0] + j02 * Rn[2], j00 * Rn[3] + j02 * Rn[5], j00 * Rn[6] + j02 * Rn[8]);
+        const Vec3<float> u1 = v3<float>(j11 * Rn[1] + j12 * Rn[2], j11 * Rn[4] + j12 * Rn[5], j11 * Rn[7] + j12 * Rn[8]);
+        const float ja0 = dot(u0, dXda), ja1 = dot(u1, dXda);
+        accC += w2 * (ja0 * ja0 + ja1 * ja1);
+        accG += w2 * (ja0 * r0 + ja1 * r1);
+        if (has_pose) {
+          const Vec3<float> k0 = cross(Xp, u0), k1 = cross(Xp, u1);
+          const float K0[6] = {w * k0.x, w * k0.y, w * k0.z, w * u0.x, w * u0.y, w * u0.z};
+          const float K1[6] = {w * k1.x, w * k1.y, w * k1.z, w * u1.x, w * u1.y, w * u1.z};
+          const float rw0 = sgn * (w * r0), rw1 = sgn * (w * r1);
+#pragma unroll
+          for (int i = 0; i < 6; ++i) {
+#pragma unroll
+            for (int j = i; j < 6; ++j) M[tri6(i, j)] = M[tri6(i, j)] + prod2_df(K0[i], K0[j], K1[i], K1[j]);
+            m[i] = m[i] + prod2_df(K0[i], rw0, K1[i], rw1);
+          }
+          const Vec3<float> h0 = cross(X, u0), h1 = cross(X, u1);
+          const float jw0 = sgn * (w * ja0), jw1 = sgn * (w * ja1);
+          const float H0[6] = {w * h0.x, w * h0.y, w * h0.z, w * u0.x, w * u0.y, w * u0.z};
+          const float H1[6] = {w * h1.x, w * h1.y, w * h1.z, w * u1.x, w * u1.y, w * u1.z};
+#pragma unroll
+          for (int k = 0; k < 6; ++k) q[k] = q[k] + prod2_df(H0[k], jw0, H1[k], jw1);
+        }
+      }
+      atomicAdd(&sm.C[slot], accC);
+      atomicAdd(&sm.ga[slot], accG);
+      if (has_pose) {
+        key = n;
+        // frames after the anchor cover blocks [a, n): row n - 1 feeds a suffix sum;
+        // frames before it cover [n, a): row n feeds a prefix sum.  Rows are distinct.
+        const int row = (n > a ? n - 1 : n) - f0;
+        const size_t at = (size_t)(6 * row) * SPGO_CHUNK + slot;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+          slab_h[at + k * SPGO_CHUNK] = q[k].h;
+          slab_l[at + k * SPGO_CHUNK] = q[k].l;
+        }
+      }
+    }
+    // stage the 27 double-float pair values, then lanes 0..26 each sum one value
+    // over the runs of equal target frame and add each run to its FP64 pair record
+    float *st = stage + (size_t)(tid >> 5) * 2 * kJacVals * kJacPitch;
+    int *keys = sm.key[tid >> 5];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) {
+      st[(2 * k) * kJacPitch + lane] = M[k].h;
+      st[(2 * k + 1) * kJacPitch + lane] = M[k].l;
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      st[(2 * (21 + k)) * kJacPitch + lane] = m[k].h;
+      st[(2 * (21 + k) + 1) * kJacPitch + lane] = m[k].l;
+    }
+    keys[lane] = key;
+    __syncwarp();
+    if (__any_sync(0xffffffffu, key >= 0) && lane < kJacVals) {
+      const float *ch = st + (2 * lane) * kJacPitch, *cl = st + (2 * lane + 1) * kJacPitch;
+      const int host_a = sm.a[0];
+      auto emit = [&](int n, const df &v) {
+        const int lo = min(host_a, n), hi = max(host_a, n);
+        atomicAdd(pair_base + ((size_t)lo * D + (hi - lo - 1)) * kJacVals + lane, (double)v.h + (double)v.l);
+      };
+      df acc = df_make(0.f);
+      int cur = keys[0];
+      for (int i = 0; i < 32; ++i) {
+        const int k = keys[i];
+        if (k != cur) {
+          if (cur >= 0) emit(cur, acc);
+          acc = df_make(0.f);
+          cur = k;
+        }
+        acc = acc + df{ch[i], cl[i]};
+      }
+      if (cur >= 0) emit(cur, acc);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // phase C.1: per (landmark, component) suffix / prefix sums along the window (double-float)
+  for (int idx = tid; idx < cnt * 6; idx += blockDim.x) {
+    const int slot = idx % cnt, k = idx / cnt;
+    const int a = sm.a[slot], lo_l = sm.lo[slot], hi_l = sm.hi[slot];
+    df acc = df_make(0.f);
+    for (int i = hi_l - 1; i >= a; --i) {
+      const size_t at = (size_t)(6 * (i - f0) + k) * SPGO_CHUNK + slot;
+      acc = acc + df{slab_h[at], slab_l[at]};
+      slab_h[at] = acc.h;
+      slab_l[at] = acc.l;
+    }
+    acc = df_make(0.f);
+    for (int i = lo_l; i < a; ++i) {
+      const size_t at = (size_t)(6 * (i - f0) + k) * SPGO_CHUNK + slot;
+      acc = acc + df{slab_h[at], slab_l[at]};
+      slab_h[at] = acc.h;
+      slab_l[at] = acc.l;
+    }
+  }
+  __syncthreads();
+  // phase C.2: B_l(i) = Ad_i^T b_l(i) about the anchor centre,
+  //   [R_i^T (b_w - (c_i - c_a) x b_v) ; R_i^T b_v], in double-float, rounded once
+  float *gslab = reinterpret_cast<float *>(wv.slab) + pv.ch_slab[c];
+  for (int idx = tid; idx < cnt * nb; idx += blockDim.x) {
+    const int slot = idx % cnt, i = f0 + idx / cnt;
+    const size_t at = (size_t)(6 * (i - f0)) * SPGO_CHUNK + slot;
+    if (i < sm.lo[slot] || i >= sm.hi[slot]) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) gslab[at + k * SPGO_CHUNK] = 0.f;
+      continue;
+    }
+    const int fi = fo + i, fa = fo + sm.a[slot];
+    const float *Rh = wv.fr_Rf + (size_t)fi * 18, *Rl = wv.fr_Rl + (size_t)fi * 18;
+    df d[3], bw[3], bv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      d[k] = df_sub(wv.fr_ch[(size_t)fi * 6 + k], wv.fr_ch[(size_t)fa * 6 + k]) +
+             df_make(wv.fr_cl[(size_t)fi * 6 + k] - wv.fr_cl[(size_t)fa * 6 + k]);
+      bw[k] = df{slab_h[at + k * SPGO_CHUNK], slab_l[at + k * SPGO_CHUNK]};
+      bv[k] = df{slab_h[at + (3 + k) * SPGO_CHUNK], slab_l[at + (3 + k) * SPGO_CHUNK]};
+    }
+    const df tw[3] = {bw[0] - (d[1] * bv[2] - d[2] * bv[1]), bw[1] - (d[2] * bv[0] - d[0] * bv[2]),
+                      bw[2] - (d[0] * bv[1] - d[1] * bv[0])};
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      // (R^T v)_r = sum_k R(k, r) v_k
+      const df Bw = df_dot3(Rh[r], Rl[r], Rh[3 + r], Rl[3 + r], Rh[6 + r], Rl[6 + r], tw[0], tw[1], tw[2]);
+      const df Bv = df_dot3(Rh[r], Rl[r], Rh[3 + r], Rl[3 + r], Rh[6 + r], Rl[6 + r], bv[0], bv[1], bv[2]);
+      gslab[at + r * SPGO_CHUNK] = Bw.h + Bw.l;
+      gslab[at + (3 + r) * SPGO_CHUNK] = Bv.h + Bv.l;
+    }
+  }
+  for (int idx = tid; idx < rows * SPGO_CHUNK; idx += blockDim.x)  // empty columns: the Schur pass reads all 32
+    if (idx % SPGO_CHUNK >= cnt) gslab[idx] = 0.f;
+  if (tid < cnt) {
+    reinterpret_cast<float *>(wv.C)[lm0 + tid] = sm.C[tid];
+    reinterpret_cast<float *>(wv.ga)[lm0 + tid] = sm.ga[tid];
+  }
+}
+
 // ---- the FP32 path's pose chain in double-float ----
 // The same scan with 3x4 products in double-float (~48 significant bits, the
 // precision of the FP32 path's frame tables: fr_Rf + fr_Rl, fr_ch + fr_cl), on the
@@ -516,6 +802,7 @@ __device__ __forceinline__ void compose34_df(const df *A, const df *B, df *C) {
   }
 }
 
+// (also the FP64 copies, h + l, which the FP64 reduction of the pose-pair records reads)
 __device__ __forceinline__ void write_frame_df(const WorkView &wv, size_t f, const df *G, const df *Trl) {
   df Gr[12];
   compose34_df(G, Trl, Gr);
@@ -527,11 +814,15 @@ __device__ __forceinline__ void write_frame_df(const WorkView &wv, size_t f, con
       wv.fr_Rf[f * 18 + 9 + 3 * i + j] = Gr[4 * i + j].h;
       wv.fr_Rl[f * 18 + 3 * i + j] = G[4 * i + j].l;
       wv.fr_Rl[f * 18 + 9 + 3 * i + j] = Gr[4 * i + j].l;
+      wv.fr_Rd[f * 18 + 3 * i + j] = (double)G[4 * i + j].h + (double)G[4 * i + j].l;
+      wv.fr_Rd[f * 18 + 9 + 3 * i + j] = (double)Gr[4 * i + j].h + (double)Gr[4 * i + j].l;
     }
     wv.fr_ch[f * 6 + i] = G[4 * i + 3].h;
     wv.fr_ch[f * 6 + 3 + i] = Gr[4 * i + 3].h;
     wv.fr_cl[f * 6 + i] = G[4 * i + 3].l;
     wv.fr_cl[f * 6 + 3 + i] = Gr[4 * i + 3].l;
+    wv.fr_c[f * 6 + i] = (double)G[4 * i + 3].h + (double)G[4 * i + 3].l;
+    wv.fr_c[f * 6 + 3 + i] = (double)Gr[4 * i + 3].h + (double)Gr[4 * i + 3].l;
   }
 }
 
@@ -609,6 +900,11 @@ int launch_linearize(const PlanView &pv, const WorkView &wv, const Params &prm, 
     const int nt = prm.cost_block > 0 ? prm.cost_block : kCostThreads;
     const size_t sm = LinLayout<T>(pv.max_nb, nt / 32, true).total;
     k_linearize<T, true><<<pv.n_chunks, nt, sm, st>>>(pv, wv, prm, alpha, gate);
+  } else if constexpr (std::is_same<T, float>::value) {
+    const int nt = prm.lin_block > 0 ? prm.lin_block : kLinThreads;
+    const size_t sm = JacLayout(pv.max_nb, nt / 32).total;
+    cudaFuncSetAttribute(k_jacobian_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_jacobian_acc<<<pv.n_chunks, nt, sm, st>>>(pv, wv, prm, alpha, gate);
   } else {
     const int nt = prm.lin_block > 0 ? prm.lin_block : kLinThreads;
     const size_t sm = LinLayout<T>(pv.max_nb, nt / 32, false).total;

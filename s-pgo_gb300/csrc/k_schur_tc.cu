@@ -150,7 +150,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = sm.tmem_slot;
-  const uint64_t deadline = tc::globaltimer_ns() + kTimeoutNs;
+  // the waits of the pipeline give up at `deadline` (the parameter's limit); the drains
+  // of copies and MMAs already issued keep their own 2 s beyond it, so a CTA that gave
+  // up never exits with asynchronous work in flight
+  const uint64_t deadline = tc::globaltimer_ns() + wait_limit_ns(prm);
   float acc[kTcTile];  // warps 4-7: one tile row per thread
 
   if (warp == 9) {
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkVie
       }
     }
   }
-  if (failed && tid == 0) wv.lm[b].fail = 1;
+  if (failed && tid == 0) atomicOr(&wv.lm[b].fail, FAIL_TIMEOUT);
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 8) tc::tmem_dealloc(tmem, 256);

@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
   __syncthreads();
   const bool failed = fail_s != 0;
   for (int i = threadIdx.x; i < P; i += blockDim.x) wv.delta[po + i] = failed ? 0.0 : x[i];
-  if (threadIdx.x == 0 && failed) wv.lm[b].fail = 1;
+  if (threadIdx.x == 0 && failed) atomicOr(&wv.lm[b].fail, FAIL_PIVOT);
   if constexpr (std::is_same<T, float>::value) {
     if (store && !failed) {  // packed factor, then the pivots' reciprocals
       float *dst = wv.facs + off;
@@ -529,6 +529,7 @@ __global__ void k_reset(PlanView pv, WorkView wv, double lam) {
   s.rho1 = s.rho2 = s.rho3 = s.last_rel = s.last_predrel = 0.0;
   s.gnorm = s.dmean = s.dmax = s.dmin = s.cmean = 0.0;
   s.last_acc = s.rej_streak = 0;
+  s.wait_timeouts = s.pad2 = 0;
   wv.lm[b] = s;
   wv.cost_acc[b] = 0.0;
   wv.pred_acc[b] = 0.0;
@@ -605,7 +606,10 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
     s.res_sel ^= 1;  // the candidate's residuals are now the state's
     if (rel < prm.tol) s.status = SPGO_STATUS_CONVERGED;
   } else {
-    if (s.fail) s.factor_failures += 1;
+    if (s.fail & FAIL_TIMEOUT)
+      s.wait_timeouts += 1;
+    else if (s.fail)
+      s.factor_failures += 1;
     s.flag = 0;
     s.relin = 0;
     s.lam *= s.nu;

@@ -21,155 +21,103 @@ __device__ __forceinline__ constexpr int t6(int i, int j) {  // symmetric 6x6 up
   return i <= j ? i * 6 - (i * (i - 1)) / 2 + (j - i) : j * 6 - (j * (j - 1)) / 2 + (i - j);
 }
 
-// (i, j), i <= j, of upper-triangle index comp < 21 of a symmetric 6x6
-__device__ __forceinline__ void upper_ij(int comp, int &i, int &j) {
-  int rem = comp;
-  i = 0;
-  while (rem >= 6 - i) {
-    rem -= 6 - i;
-    ++i;
-  }
-  j = i + rem;
-}
-
-// row i and column j of Z = [z]x = [[0, -z3, z2], [z3, 0, -z1], [-z2, z1, 0]],
-// selected (a runtime index into a local Z array would live in local memory)
-template <typename T>
-__device__ __forceinline__ void skew_row(const Vec3<T> &z, int i, T (&r)[3]) {
-  r[0] = i == 0 ? T(0) : (i == 1 ? z.z : -z.y);
-  r[1] = i == 0 ? -z.z : (i == 1 ? T(0) : z.x);
-  r[2] = i == 0 ? z.y : (i == 1 ? -z.x : T(0));
-}
-template <typename T>
-__device__ __forceinline__ void skew_col(const Vec3<T> &z, int j, T (&c)[3]) {
-  c[0] = j == 0 ? T(0) : (j == 1 ? -z.z : z.y);
-  c[1] = j == 0 ? z.z : (j == 1 ? T(0) : -z.x);
-  c[2] = j == 0 ? -z.y : (j == 1 ? z.x : T(0));
-}
-
-// Re-centring a pair record: E_z^T M E_z and E_z^T m for E_z = [[I, 0], [-[z]x, I]]
-// move a record from origin x to origin y = x - z (K^y = K^x E_{x - y}).  With the
-// 6x6 block M = [[P, Q], [Q^T, R]] (upper triangle, 21 values), m = [m_w; m_v] and
-// Z = [z]x:  P' = P - Q Z + Z Q^T - Z R Z,  Q' = Q + Z R,  R' = R,
-//            m' = [m_w + Z m_v ; m_v].
-// shifted_component returns component `comp` (0..26) of the moved record,
-// reading the whole 27-vector from shared memory.  The caller decodes the lane's
-// component once: (i, j) = upper_ij(comp) for comp < 21, i = comp - 21 for the
-// three rotational gradient components 21..23 (unused for the rest).
-template <typename T>
-__device__ __forceinline__ T shifted_component(const T *v, int comp, int i, int j, const Vec3<T> &z) {
-  auto Pm = [&](int a, int c) { return v[t6(a, c)]; };
-  auto Qm = [&](int a, int c) { return v[t6(a, 3 + c)]; };
-  auto Rm = [&](int a, int c) { return v[t6(3 + a, 3 + c)]; };
-  if (comp >= 24 || (comp < 21 && i >= 3)) return v[comp];
-  T zi[3];  // row i of Z
-  skew_row(z, i, zi);
-  if (comp >= 21) return v[comp] + zi[0] * v[24] + zi[1] * v[25] + zi[2] * v[26];
-  if (j >= 3) {  // Q' = Q + Z R
-    T acc = Qm(i, j - 3);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) acc += zi[k] * Rm(k, j - 3);
-    return acc;
-  }
-  // P' = P - Q Z + Z Q^T - Z R Z
-  T zj[3];  // column j of Z
-  skew_col(z, j, zj);
-  T acc = Pm(i, j);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    acc -= Qm(i, k) * zj[k];
-    acc += zi[k] * Qm(j, k);
-    T zr = T(0);
-#pragma unroll
-    for (int l = 0; l < 3; ++l) zr += Rm(k, l) * zj[l];
-    acc -= zi[k] * zr;
-  }
-  return acc;
-}
-
-// pass A, one warp per (problem, hi), lane = component:
+// pass A, one thread per (problem, hi):
 // P(i, hi) = sum_{lo <= i} M(lo, hi), each term about its own origin c_lo; the
 // running sum is re-centred from c_{lo-1} to c_lo before adding M(lo, hi), so
 // every partial sum sits at the origin of its row i and only relative centres
-// enter the arithmetic.  Reads and clears the accumulators.
-// Each lane first copies its component of the next stage_len<T>() records into
-// shared memory with asynchronous copies (all in flight at once, no registers
-// held), so the step chain waits on no global load: one memory round trip per
-// stage instead of one per step.
-constexpr int kPrefixWarps = 4;
-template <typename T>
-__host__ __device__ constexpr int prefix_stage_len() { return sizeof(T) == 4 ? 32 : 16; }
-
-template <typename T>
-__device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src) {
-  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst_smem)),
-               "l"(src), "n"((int)sizeof(T))
-               : "memory");
+// enter the arithmetic.  Re-centring a record: E_z^T M E_z and E_z^T m for
+// E_z = [[I, 0], [-[z]x, I]] move a record from origin x to origin y = x - z
+// (K^y = K^x E_{x - y}).  With the 6x6 block M = [[P, Q], [Q^T, R]] (upper triangle,
+// 21 values), m = [m_w; m_v] and Z = [z]x:  P' = P - Q Z + Z Q^T - Z R Z,
+// Q' = Q + Z R,  R' = R,  m' = [m_w + Z m_v ; m_v].  Reads and clears the records.
+// The thread holds the whole 27-value running sum, so the shift's shared products
+// are formed once per step (about a sixth of the arithmetic of one lane per
+// component, which matters in FP64):
+//   (Z R)[:, j] = z x R[:, j],  (Q Z)[i, :] = -(z x Q[i, :]),  ((Z R) Z)[i, :] = -(z x (Z R)[i, :]),
+//   P' = P - Q Z - (Q Z)^T - (Z R) Z,  Q' = Q + Z R,  m_w' = m_w + z x m_v.
+__device__ __forceinline__ void cross3(const double *a, const double *b, double *o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kPrefixWarps * 32) k_pair_prefix(PlanView pv, WorkView wv) {
-  constexpr int kStage = prefix_stage_len<T>();
-  __shared__ T acc_s[kPrefixWarps][28];
-  __shared__ T rec_s[kPrefixWarps][kStage * 27];  // [step][component], a lane reads only its own
+__device__ __forceinline__ void shift_record(double *v, const double *z) {
+  double P[3][3], Q[3][3], R[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      P[a][c] = v[t6(a, c)];
+      Q[a][c] = v[t6(a, 3 + c)];
+      R[a][c] = v[t6(3 + a, 3 + c)];
+    }
+  double ZR[3][3], QZ[3][3], ZRZ[3][3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {  // columns of Z R
+    const double rc[3] = {R[0][j], R[1][j], R[2][j]};
+    double o[3];
+    cross3(z, rc, o);
+    ZR[0][j] = o[0];
+    ZR[1][j] = o[1];
+    ZR[2][j] = o[2];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {  // rows of Q Z and (Z R) Z
+    double o[3];
+    cross3(z, Q[i], o);
+    QZ[i][0] = -o[0];
+    QZ[i][1] = -o[1];
+    QZ[i][2] = -o[2];
+    cross3(z, ZR[i], o);
+    ZRZ[i][0] = -o[0];
+    ZRZ[i][1] = -o[1];
+    ZRZ[i][2] = -o[2];
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+#pragma unroll
+    for (int c = a; c < 3; ++c) v[t6(a, c)] = P[a][c] - QZ[a][c] - QZ[c][a] - ZRZ[a][c];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[t6(a, 3 + c)] = Q[a][c] + ZR[a][c];
+  }
+  const double mv[3] = {v[24], v[25], v[26]};
+  double o[3];
+  cross3(z, mv, o);
+  v[21] += o[0];
+  v[22] += o[1];
+  v[23] += o[2];
+}
+
+__global__ void __launch_bounds__(64) k_pair_prefix_rec(PlanView pv, WorkView wv) {
   const int b = blockIdx.y;
   if (!problem_active(wv.lm, b, GATE_RELIN)) return;
   const int N = pv.p_npose[b], D = pv.p_pair_D[b];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int hi = 1 + blockIdx.x * kPrefixWarps + w;
+  const int hi = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   if (hi > N) return;
   const int fo = pv.p_frame_off[b];
-  T *acc_base = reinterpret_cast<T *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
-  T *out_base = reinterpret_cast<T *>(wv.pairF) + (size_t)pv.p_pair_off[b] * 27;
-  T *acc = acc_s[w];
-  T *stage = rec_s[w];
-  if (lane < 27) acc[lane] = T(0);
-  __syncwarp();
+  double *acc_base = reinterpret_cast<double *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
+  double *out_base = reinterpret_cast<double *>(wv.pairF) + (size_t)pv.p_pair_off[b] * 27;
   const int lo0 = max(0, hi - D);
-  int ci = 0, cj = 0;
-  if (lane < 21) upper_ij(lane, ci, cj);
-  else ci = lane - 21;
-  // record (lo, hi) sits at (lo D + hi - lo - 1) 27: consecutive lo are (D - 1) 27 apart
-  const ptrdiff_t rec_step = (ptrdiff_t)(D - 1) * 27;
-  // the re-centring offsets z(lo) = c(lo - 1) - c(lo) of the next 32 steps, one per
-  // lane, handed out by shuffles: the step chain does not wait on their loads
-  Vec3<T> zb = v3<T>(T(0), T(0), T(0));
-  if (lo0 + 1 + lane < hi) zb = FramesT<T>::rel(wv, fo + lo0 + lane, 0, fo + lo0 + 1 + lane, 0);
+  double v[27];
+#pragma unroll
+  for (int k = 0; k < 27; ++k) v[k] = 0.0;
   for (int lo = lo0; lo < hi; ++lo) {
-    const size_t rec = (size_t)lo * D + (hi - lo - 1);
-    const int q = (lo - lo0) % kStage;
-    if (q == 0 && lane < 27) {
-      // this lane's component of the records lo .. lo + cnt - 1, then (once the
-      // copies have landed) their accumulators cleared for the next linearisation
-      const int cnt = min(kStage, hi - lo);
-      T *src = acc_base + rec * 27 + lane;
-#pragma unroll 8
-      for (int s = 0; s < cnt; ++s) cp_async_elem(stage + s * 27 + lane, src + s * rec_step);
-      asm volatile("cp.async.wait_all;" ::: "memory");
-#pragma unroll 8
-      for (int s = 0; s < cnt; ++s) src[s * rec_step] = T(0);
-    }
-    const T cur = lane < 27 ? stage[q * 27 + lane] : T(0);
     if (lo > lo0) {
-      const int s = (lo - lo0 - 1) & 31;
-      const Vec3<T> z = v3<T>(__shfl_sync(0xffffffffu, zb.x, s), __shfl_sync(0xffffffffu, zb.y, s),
-                              __shfl_sync(0xffffffffu, zb.z, s));
-      if (s == 31) {  // the next batch
-        const int ll = lo + 1 + lane;
-        zb = ll < hi ? FramesT<T>::rel(wv, fo + ll - 1, 0, fo + ll, 0) : v3<T>(T(0), T(0), T(0));
-      }
-      const T v = lane < 27 ? shifted_component(acc, lane, ci, cj, z) : T(0);
-      __syncwarp();
-      if (lane < 27) acc[lane] = v;
-      __syncwarp();
+      const Vec3<double> zz = FramesT<double>::rel(wv, fo + lo - 1, 0, fo + lo, 0);
+      const double z[3] = {zz.x, zz.y, zz.z};
+      shift_record(v, z);
     }
-    if (lane < 27) {
-      const T nv = acc[lane] + cur;
-      acc[lane] = nv;
-      out_base[rec * 27 + lane] = nv;
+    double *rec = acc_base + ((size_t)lo * D + (hi - lo - 1)) * 27;
+    double *out = out_base + ((size_t)lo * D + (hi - lo - 1)) * 27;
+    double r[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) r[k] = rec[k];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+      rec[k] = 0.0;  // cleared for the next linearisation
+      v[k] += r[k];
+      out[k] = v[k];
     }
-    __syncwarp();
   }
 }
 
@@ -214,8 +162,10 @@ template <> struct Pair2<double> {
 };
 
 // A(i, j) = Ad_i^T F(i, j) Ad_j about origin c_i: Ad_i = diag(R_i, R_i),
-// Ad_j = [[R_j, 0], [[c_j - c_i]x R_j, R_j]];  g(i) = [R_i^T f_w ; R_i^T f_v]
-template <typename T>
+// Ad_j = [[R_j, 0], [[c_j - c_i]x R_j, R_j]];  g(i) = [R_i^T f_w ; R_i^T f_v].
+// Computed in T, stored as TO (the mixed path reduces in FP64 and stores FP32: one
+// rounding of the exact sums)
+template <typename T, typename TO = T>
 __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
   const int b = blockIdx.y;
   if (!problem_active(wv.lm, b, GATE_RELIN)) return;
@@ -278,40 +228,44 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
   // both copies as pairs of adjacent elements (every offset below is even and the
   // workspace segment 256-byte aligned): the block (i, j) row by row, and for
   // i != j its transpose (j, i), whose rows are 6 elements at 6i of rows 6j + c
-  using V2 = typename Pair2<T>::type;
-  T *A = reinterpret_cast<T *>(wv.A) + pv.p_S_off[b];
+  using V2 = typename Pair2<TO>::type;
+  TO *A = reinterpret_cast<TO *>(wv.A) + pv.p_S_off[b];
 #pragma unroll
   for (int r = 0; r < 6; ++r)
 #pragma unroll
     for (int c = 0; c < 6; c += 2)
-      *reinterpret_cast<V2 *>(A + (size_t)(6 * i + r) * P + 6 * j + c) = Pair2<T>::make(out[r][c], out[r][c + 1]);
+      *reinterpret_cast<V2 *>(A + (size_t)(6 * i + r) * P + 6 * j + c) =
+          Pair2<TO>::make((TO)out[r][c], (TO)out[r][c + 1]);
   if (i != j) {
 #pragma unroll
     for (int c = 0; c < 6; ++c)
 #pragma unroll
       for (int r = 0; r < 6; r += 2)
-        *reinterpret_cast<V2 *>(A + (size_t)(6 * j + c) * P + 6 * i + r) = Pair2<T>::make(out[r][c], out[r + 1][c]);
+        *reinterpret_cast<V2 *>(A + (size_t)(6 * j + c) * P + 6 * i + r) =
+            Pair2<TO>::make((TO)out[r][c], (TO)out[r + 1][c]);
   }
   if (e == 0) {
     const T *f = F + 21;
-    T *g = reinterpret_cast<T *>(wv.g) + pv.p_param_off[b] + 6 * i;
+    TO *g = reinterpret_cast<TO *>(wv.g) + pv.p_param_off[b] + 6 * i;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      g[r] = Ri[r] * f[0] + Ri[3 + r] * f[1] + Ri[6 + r] * f[2];
-      g[3 + r] = Ri[r] * f[3] + Ri[3 + r] * f[4] + Ri[6 + r] * f[5];
+      g[r] = (TO)(Ri[r] * f[0] + Ri[3 + r] * f[1] + Ri[6 + r] * f[2]);
+      g[3 + r] = (TO)(Ri[r] * f[3] + Ri[3 + r] * f[4] + Ri[6 + r] * f[5]);
     }
   }
 }
 
+// The pose-pair records are FP64 on both paths; the reduction runs in FP64 and the
+// mixed path (T = float) stores A and g as FP32.
 template <typename T>
 int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream) {
   (void)gate;
   cudaStream_t st = (cudaStream_t)stream;
   const int nmax = pv.max_P / 6;
   const int nd = pv.max_D > 0 ? pv.max_D : 1;
-  k_pair_prefix<T><<<dim3(grid_for(nmax, kPrefixWarps), pv.B), kPrefixWarps * 32, 0, st>>>(pv, wv);
-  k_pair_suffix<T><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);
-  k_pairs_to_A<T><<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
+  k_pair_prefix_rec<<<dim3(grid_for(nmax, 64), pv.B), 64, 0, st>>>(pv, wv);
+  k_pair_suffix<double><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);
+  k_pairs_to_A<double, T><<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
   g_launches += 3;
   return (int)cudaGetLastError();
 }

@@ -69,13 +69,18 @@ struct PlanView {                 // device pointers into the static buffer
 
 struct LMState {
   double lam, nu, cost, cost_cand, pred, cost0, cost_lin;
-  int32_t iters, accepted, status, relin, fail, flag, factor_failures;
+  int32_t iters, accepted, status, relin;
+  int32_t fail;  // this iteration's step failed: bit 0 a non-positive pivot, bit 1 a bounded wait ran out
+  int32_t flag, factor_failures;
   int32_t res_sel;  // which half of WorkView::res holds the residuals of the state (the other: the candidate's)
   // history and statistics the learned damping controller reads
   double rho1, rho2, rho3, last_rel, last_predrel;
   double gnorm, dmean, dmax, dmin, cmean;
   int32_t last_acc, rej_streak;
+  int32_t wait_timeouts, pad2;  // steps rejected because a bounded device wait ran out
 };
+
+constexpr int32_t FAIL_PIVOT = 1, FAIL_TIMEOUT = 2;
 
 // per-iteration scratch (precision-dependent arrays typed at the kernel)
 struct WorkView {
@@ -152,8 +157,8 @@ template <typename T>
 int launch_schur(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
 size_t factor_packed_bytes(int P, size_t ts);  // shared memory of the batched factorisation
 template <typename T>
-int launch_factor_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, int refine,
-                        void *stream);
+int launch_factor_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
+                        int refine, void *stream);
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed,
                         void *stream);
@@ -162,7 +167,8 @@ int launch_pair_twists(const PlanView &pv, const WorkView &wv, void *stream);
 int launch_resid_pass(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha, int first,
                       void *stream);
 int launch_resid_solve(const PlanView &pv, const WorkView &wv, int first, void *stream);
-int launch_refine_large(const PlanView &pv, const WorkView &wv, int b, int P, int param_off, void *stream);
+int launch_refine_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
+                        void *stream);
 int launch_backsub_refined(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
                            double *alpha_out, void *stream);
 size_t resid_solve_smem(int max_P_small, int max_N);

@@ -51,7 +51,8 @@ class PlanSizes(C.Structure):
                 ("total_obs", C.c_int64), ("n_chunks", C.c_int32), ("n_schur_items", C.c_int32),
                 ("max_params", C.c_int32), ("schur_chunk_tiles", C.c_int32), ("static_bytes", C.c_size_t),
                 ("workspace_bytes", C.c_size_t), ("slab_elems", C.c_int64), ("pair_records", C.c_int64),
-                ("schur_flops", C.c_int64), ("n_tc_items", C.c_int32), ("tc_chunk_tiles", C.c_int32)]
+                ("schur_flops", C.c_int64), ("n_tc_items", C.c_int32), ("tc_chunk_tiles", C.c_int32),
+                ("schur_flops_landmark", C.c_int64)]
 
 
 class Params(C.Structure):
@@ -65,7 +66,8 @@ class Params(C.Structure):
 
 class ProblemStatus(C.Structure):
     _fields_ = [("cost0", C.c_double), ("cost", C.c_double), ("lambda_", C.c_double), ("iterations", C.c_int32),
-                ("accepted", C.c_int32), ("status", C.c_int32), ("factor_failures", C.c_int32)]
+                ("accepted", C.c_int32), ("status", C.c_int32), ("factor_failures", C.c_int32),
+                ("wait_timeouts", C.c_int32), ("pad", C.c_int32)]
 
 
 class DeviceProblem(C.Structure):

@@ -205,7 +205,8 @@ class BatchSolver:
     # -- parameters ---------------------------------------------------------------
     def set_params(self, loss: Optional[str] = None, loss_scale=None, near_boost=None, eps=None,
                    alpha_min=None, alpha_max=None, lambda0=None, lambda_max=None, tol=None, max_iters=None,
-                   refine_steps=None, use_graph=None, use_tc=None, cost_block=None, lin_block=None):
+                   refine_steps=None, use_graph=None, use_tc=None, cost_block=None, lin_block=None,
+                   outer_steps=None, wait_us=None):
         p = self.params
         if loss is not None:
             p.loss = _LOSS[loss]
@@ -228,6 +229,10 @@ class BatchSolver:
             p.cost_block = int(cost_block)
         if lin_block is not None:
             p.lin_block = int(lin_block)
+        if outer_steps is not None:
+            p.outer_steps = int(outer_steps)
+        if wait_us is not None:
+            p.wait_us = int(wait_us)
         self._apply_params()
 
     def _apply_params(self):
@@ -245,7 +250,8 @@ class BatchSolver:
         out = (nat.ProblemStatus * B)()
         nat.check(self.L.spgo_lm_status(self._solver, out, self._sp()), "lm_status")
         return [dict(cost0=s.cost0, cost=s.cost, lam=s.lambda_, iterations=s.iterations, accepted=s.accepted,
-                     status=s.status, factor_failures=s.factor_failures) for s in out]
+                     status=s.status, factor_failures=s.factor_failures, wait_timeouts=s.wait_timeouts)
+                for s in out]
 
     def trace(self) -> List[dict]:
         """Per problem, the LM iterations since the last reset (up to ``native.TRACE_MAX``):
