@@ -7,15 +7,28 @@ landmarks each (circle generator, 1 px noise), every problem run to a
 relative cost decrease below 1e-6 or 30 LM iterations.  One step = one solve
 of the whole batch from its initial state.
 
-* ``value``: solves/s of the chosen form (mixed precision, batched) with the
-  inputs resident in HBM; L2 is flushed (256 MB write) between timed steps.
-* ``e2e``: the same metric through the public API per step: marshal and plan
-  the host problems, upload, solve, read back poses and inverse depths.  The
-  headline runs batches through ``solver.solve_stream`` (batches planned on a
-  worker thread ahead of their solve, ``--inflight`` batches solving at once on
-  their own CUDA streams); ``serial_value`` is one ``BatchSolver`` after another.
-* ``plain_fp64``: the plain FP64 GPU solver (problems one at a time), its
-  solves/s and how many chosen-form costs reach its converged cost (rel 1e-6).
+The chosen form is the mixed path (FP32 Jacobian and Hessian blocks summed
+exactly, tensor-core Schur complement, FP32 Cholesky, the step refined against
+the accurately summed residual of the whole system), batched, with the learned
+damping controller unless ``--controller 0``.  Its reference point is the plain
+FP64 GPU solver (Nielsen LM, no controller, 30 iterations):
+
+* ``value``: solves per second that reach the plain FP64 solver's final cost
+  (relative 1e-6): the chosen form's batch solves/s times the fraction of its
+  problems that end at or below the plain cost.  Inputs resident in HBM; L2
+  flushed (256 MB write) between timed steps.  ``raw_solves_per_s`` is the batch
+  rate without that filter.
+* ``plain_fp64``: the plain FP64 solver batched (the comparison point) and one
+  problem at a time, the fraction of chosen-form problems that reach its cost,
+  the iterations they need to, and the effects of batching, precision and the
+  learned controller taken one at a time.
+* ``e2e``: the same metric through the public API per step: marshal and plan the
+  host problems, upload, solve, read back poses and inverse depths
+  (``solver.solve_stream``: batches planned on a worker thread ahead of their
+  solve, ``--inflight`` batches solving at once on their own CUDA streams).
+* ``roofline``: the dominant kernel's algorithmic work per launch (HBM bytes or
+  FLOPs) over its CUDA-event duration, against the measured peaks; also the
+  whole LM iteration's algorithmic bytes against HBM.
 * ``cpu_baseline``: the FP64 CPU oracle on a bounded sample of the batch.
 * ``--impl reference``: the CPU oracle alone on host cores (process pool),
   same metric.
@@ -39,6 +52,7 @@ METRIC = "time-to-converged cost (rel 1e-6) & batched solves/s: chosen vs plain 
 WORKLOAD = ("config3: 256 independent problems, N~U[8,32] poses, L~U[200,3000] landmarks, "
             "run to rel cost change < 1e-6 or 30 LM iterations")
 N_PROBLEMS = 256
+REACH_TOL = 1e-6
 
 
 def _env_rank():
@@ -79,21 +93,25 @@ def _oracle_solve(args):
 
 
 def _config3_specs(seed: int, n: int = N_PROBLEMS):
-    import numpy as np
-    rng = np.random.Generator(np.random.PCG64(seed))
-    Ns = rng.integers(8, 33, n)
-    Ls = rng.integers(200, 3001, n)
-    seeds = rng.integers(0, 2**31 - 1, n)
-    return [(int(s), int(a), int(b)) for s, a, b in zip(seeds, Ns, Ls)]
+    """(problem seed, N, L) of the batch's problems (the scene generator's own draw)."""
+    import __graft_entry__
+    __graft_entry__.load_package()
+    import spgo_gb300.scenes as scenes
+    return scenes.config3_specs(seed, n)
 
 
-def cpu_oracle_sample(specs, n_sample: int, workers: int):
-    """Solve ``n_sample`` problems with the FP64 oracle in a spawned pool; solves/s."""
+def _make_pool(workers: int):
     import multiprocessing as mp
-    ctx = mp.get_context("spawn")
+    return mp.get_context("spawn").Pool(workers)
+
+
+def cpu_oracle_sample(pool, specs, n_sample: int):
+    """Solve ``n_sample`` problems with the FP64 oracle on an existing pool: solves/s.
+    Problems go out one at a time, largest first, so the wall time is not set by one
+    large problem left for last."""
+    sample = sorted(specs[:n_sample], key=lambda s: -(s[1] * s[2]))
     t0 = time.perf_counter()
-    with ctx.Pool(workers) as pool:
-        out = pool.map(_oracle_solve, specs[:n_sample], chunksize=1)
+    out = pool.map(_oracle_solve, sample, chunksize=1)
     wall = time.perf_counter() - t0
     return n_sample / wall, wall, out
 
@@ -159,35 +177,27 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# algorithmic bytes per launch (roofline numerators)
+# algorithmic work per launch (roofline numerators)
 # ---------------------------------------------------------------------------
-def roofline_numerator(kind: str, sizes, slab_floats: int, ts: int, probs):
-    """(bound, unit, algorithmic amount per launch) for a profiled kernel kind.
+def roofline_numerator(kind: str, sizes, probs):
+    """(bound, unit, algorithmic amount per launch) of a profiled kernel kind.
 
-    linearisation / cost: HBM bytes (observations 20 B, landmark record 40 B, C/g_a,
-    slab written); Schur: FLOPs of the W D^-1 W^T chunk blocks, sum 2 (6 nb)^2 32;
-    factor_solve: dense Cholesky + two solve pairs per problem (P^3/3 + 4 P^2)."""
+    Jacobian pass 24 B per stereo observation + 24 B per landmark; cost pass
+    24 O + 16 L; refinement (two residual passes per LM iteration) 2 (24 O + 24 L);
+    landmark Schur complement sum over landmarks of 2 (6 k)^2 FLOPs (k = pose blocks
+    of the landmark's window); factor + solve P^3 / 3 + 4 P^2 per problem (FP32)."""
     O, L = sizes.total_obs, sizes.total_landmarks
     if kind == "linearize":
-        return "hbm", "GB/s", 20.0 * O + 40.0 * L + 2.0 * ts * L + ts * slab_floats
+        return "hbm", "GB/s", 24.0 * O + 24.0 * L
     if kind == "cost":
-        return "hbm", "GB/s", 20.0 * O + 40.0 * L
+        return "hbm", "GB/s", 24.0 * O + 16.0 * L
+    if kind == "refine":
+        return "hbm", "GB/s", 2 * (24.0 * O + 24.0 * L)
     if kind == "schur":
-        return "tensor", "TFLOP/s", float(sizes.schur_flops)
+        return "tensor", "TFLOP/s", float(sizes.schur_flops_landmark)
     if kind == "factor_solve":
         return "fp32", "TFLOP/s", float(sum((6 * p.n_poses) ** 3 / 3.0 + 4 * (6 * p.n_poses) ** 2 for p in probs))
     return None, None, 0.0
-
-
-# DRAM bytes (read + write) per launch of the profiled kernels on this workload
-# (256-problem batch, mixed precision), dram__bytes_read.sum + dram__bytes_write.sum:
-# the cost and Jacobian passes at the tuned CTA sizes (64, 128) from
-# profiles/ncu_linearize_config3_tuned.md, the rest from
-# profiles/ncu_kernels_config3_batch.md
-NCU_TRAFFIC = {"cost": 119.64e6, "linearize": 251.50e6, "schur": 224.89e6, "factor_solve": 24.00e6,
-               "backsub": 206.67e6}
-NCU_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/ncu_linearize_config3_tuned.md "
-                      "(cost, linearize) and profiles/ncu_kernels_config3_batch.md (the rest)")
 
 
 def roofline_peaks(peaks: dict, tc: bool):
@@ -203,6 +213,47 @@ def roofline_peaks(peaks: dict, tc: bool):
             "fp32": (152 * 128 * 2 * mhz * 1e6 / 1e12, "nominal FP32 SIMT at sm_max_mhz")}
 
 
+def measured_traffic(kind: str, sizes):
+    """DRAM bytes per launch of a profiled kernel kind from the committed ncu capture
+    record (profiles/dram_traffic.json), scaled from the captured case to this batch
+    by the unit it is quoted per; None when the kind was not captured or its kernel
+    sources changed since the capture (their SHA-256 is in the record)."""
+    import hashlib
+    try:
+        rec = json.load(open(os.path.join(REPO, "profiles", "dram_traffic.json")))
+    except Exception:
+        return None, "no capture record"
+    k = rec.get("kernels", {}).get(kind)
+    if not k:
+        return None, "kind not captured"
+    h = hashlib.sha256()
+    for f in k["sources"]:
+        with open(os.path.join(REPO, f), "rb") as fh:
+            h.update(fh.read())
+    if h.hexdigest() != k["source_sha256"]:
+        return None, "stale: the kernel's sources changed since the capture"
+    units = {"obs": sizes.total_obs, "schur_flops": sizes.schur_flops_landmark}[k["per"]]
+    return k["bytes_per_unit"] * units, f"ncu capture of {k['case']}, scaled per {k['per']}"
+
+
+def _reached(costs, plain):
+    import numpy as np
+    return np.asarray(costs) <= np.asarray(plain) * (1.0 + REACH_TOL)
+
+
+def _iters_to_plain(traces, plain, cost0):
+    """Per problem, the LM iterations after which its trace first reaches the plain
+    cost (None if it never does)."""
+    out = []
+    for t, pc, c0 in zip(traces, plain, cost0):
+        if c0 <= pc * (1.0 + REACH_TOL):
+            out.append(0)
+            continue
+        hit = [k + 1 for k, c in enumerate(t) if c <= pc * (1.0 + REACH_TOL)]
+        out.append(hit[0] if hit else None)
+    return out
+
+
 def run_reference(args):
     rank, world, _ = _env_rank()
     if rank != 0:
@@ -211,11 +262,12 @@ def run_reference(args):
     specs = _config3_specs(_batch_seed(0))
     per_step = max(workers, 16)
     times = []
-    for it in range(args.warmup + args.steps):
-        sample = [specs[(it * per_step + k) % len(specs)] for k in range(per_step)]
-        _, wall, _ = cpu_oracle_sample(sample, per_step, workers)
-        if it >= args.warmup:
-            times.append(wall)
+    with _make_pool(workers) as pool:
+        for it in range(args.warmup + args.steps):
+            sample = [specs[(it * per_step + k) % len(specs)] for k in range(per_step)]
+            _, wall, _ = cpu_oracle_sample(pool, sample, per_step)
+            if it >= args.warmup:
+                times.append(wall)
     total = sum(times)
     value = per_step * len(times) / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
@@ -224,7 +276,7 @@ def run_reference(args):
             "data": "synthetic", "config": {"workload": WORKLOAD, "sample_per_step": per_step},
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": workers, "kind": "port",
                              "sample": f"{per_step} config-3 problems per step, FP64 numpy oracle LM, "
-                                       f"one process per core"},
+                                       f"one process per core (one pool for the run)"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -238,6 +290,18 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    # CPU baseline first, on a spawned pool made before this process touches the GPU
+    specs = _config3_specs(_batch_seed(rank))
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        workers = max(1, os.cpu_count() or 1)
+        n_s = max(workers, 16)
+        with _make_pool(workers) as pool:
+            rate, wall, _ = cpu_oracle_sample(pool, specs, n_s)
+        cpu = {"value": rate, "unit": "solves/s", "cores": workers, "kind": "port",
+               "sample": f"first {n_s} problems of the batch, FP64 numpy oracle LM "
+                         f"(same stopping rule), one process per core, {wall:.1f} s"}
+
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     import __graft_entry__
@@ -246,18 +310,6 @@ def run_ours(args):
     importlib.import_module("spgo_gb300.build").build()
     scenes = importlib.import_module("spgo_gb300.scenes")
     sv = importlib.import_module("spgo_gb300.solver")
-    nat = importlib.import_module("spgo_gb300.native")
-
-    specs = _config3_specs(_batch_seed(rank))
-    # CPU baseline first (spawned pool, before the solver does any GPU work)
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        workers = max(1, os.cpu_count() or 1)
-        n_s = max(workers, 16)
-        rate, wall, _ = cpu_oracle_sample(specs, n_s, workers)
-        cpu = {"value": rate, "unit": "solves/s", "cores": workers, "kind": "port",
-               "sample": f"first {n_s} problems of the batch, FP64 numpy oracle LM "
-                         f"(same stopping rule), one process per core, {wall:.1f} s"}
 
     probs = scenes.config3(seed=_batch_seed(rank))
     n_obs = sum(p.n_obs for p in probs)
@@ -273,14 +325,21 @@ def run_ours(args):
         if os.path.exists(learned.DEFAULT_WEIGHTS):
             ctl_params = learned.Controller.load(device=dev).deployed()
 
+    plain_params = dict(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4)
+    base_params = dict(plain_params, max_iters=args.max_iters, use_tc=args.tc)
+    if args.outer >= 0:
+        base_params["outer_steps"] = args.outer
     tuned = None
 
-    def make(precision):
+    def make(precision, controller=True):
         s = sv.BatchSolver(probs, precision=precision, device=dev, stream=stream)
-        s.set_params(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4, use_tc=args.tc)
-        if tuned is not None:  # later solvers of the same batch reuse the tuned shapes
-            s.set_params(**tuned)
-        if ctl_params is not None:
+        if precision == "mixed":
+            s.set_params(**base_params)
+            if tuned is not None:  # later solvers of the same batch reuse the tuned shapes
+                s.set_params(**tuned)
+        else:
+            s.set_params(**plain_params)
+        if controller and ctl_params is not None:
             s.set_controller(ctl_params)
         return s
 
@@ -295,6 +354,25 @@ def run_ours(args):
         tuned = dict(cost_block=bs.params.cost_block, lin_block=bs.params.lin_block, use_tc=bs.params.use_tc)
     p0, a0 = bs.poses.clone(), bs.alpha.clone()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed_solves(solver, n, warm):
+        """(per-solve ms, last statuses) of n solves of `solver` from its initial state
+        after `warm` untimed ones (L2 flushed before each)."""
+        q0, b0 = solver.poses.clone(), solver.alpha.clone()
+        out, st = [], None
+        for k in range(warm + n):
+            solver.poses.copy_(q0)
+            solver.alpha.copy_(b0)
+            flush.fill_(k & 0xFF)
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = solver.solve(check_every=args.check_every)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            if k >= warm:
+                out.append(e0.elapsed_time(e1))
+        return out, st
 
     def one_step():
         bs.poses.copy_(p0)
@@ -327,6 +405,7 @@ def run_ours(args):
         torch.distributed.barrier()
     clk = clocks.stop()
     launches = bs.launch_count() - launches0
+    chosen_trace = bs.trace()
     # per-kernel CUDA-event timing (graphs off while the events are recorded): one more
     # step of the same work, after the timed region
     bs.profile(200000)
@@ -338,9 +417,11 @@ def run_ours(args):
     bs.profile(0)
     total_ms = float(sum(ms))
     total_ms = max_over_ranks(total_ms, world, dev)
-    value = N_PROBLEMS * world * args.steps / (total_ms / 1e3)
+    raw_value = N_PROBLEMS * world * args.steps / (total_ms / 1e3)
     iters = [s["iterations"] for s in status]
     chosen_costs = np.array([s["cost"] for s in status])
+    cost0 = np.array([s["cost0"] for s in status])
+    ms_per_iter = (total_ms / args.steps) / max(1, max(iters))
 
     # kernel shares and roofline of the dominant kernel
     peaks = {}
@@ -351,49 +432,96 @@ def run_ours(args):
     pk = roofline_peaks(peaks, bool(args.tc))
     tot = sum(v[0] for v in prof.values()) or 1.0
     kernels = {k: {"ms": round(v[0], 4), "launches": v[1], "share": round(v[0] / tot, 4)} for k, v in prof.items()}
-    slab_floats = int(bs.slab_floats())
     for k, v in prof.items():
-        b_, u_, amt = roofline_numerator(k, bs.sizes, slab_floats, 4, probs)
+        b_, u_, amt = roofline_numerator(k, bs.sizes, probs)
         if b_ and v[1]:
             ms_ = v[0] / v[1]
             ach = amt / (ms_ / 1e3) / (1e9 if b_ == "hbm" else 1e12)
             kernels[k].update(bound=b_, achieved=round(ach, 3), unit=u_, frac=round(ach / pk[b_][0], 4))
-    dom = max(prof, key=lambda k: prof[k][0])
+    dom = max((k for k in prof if roofline_numerator(k, bs.sizes, probs)[0] and prof[k][1]),
+              key=lambda k: prof[k][0])
     avg_ms = prof[dom][0] / max(1, prof[dom][1])
-    bound, unit, amount = roofline_numerator(dom, bs.sizes, slab_floats, 4, probs)
-    if bound:
-        achieved = amount / (avg_ms / 1e3) / (1e9 if bound == "hbm" else 1e12)
-        peak, peak_src = pk[bound]
-    else:
-        achieved, peak, peak_src = None, None, None
+    bound, unit, amount = roofline_numerator(dom, bs.sizes, probs)
+    achieved = amount / (avg_ms / 1e3) / (1e9 if bound == "hbm" else 1e12)
+    peak, peak_src = pk[bound]
+    traffic, traffic_src = measured_traffic(dom, bs.sizes)
     roof = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": (achieved / peak) if achieved else None,
-            "traffic": NCU_TRAFFIC.get(dom),
-            "traffic_source": NCU_TRAFFIC_SOURCE, "algorithmic_per_launch": amount,
-            "avg_launch_ms": avg_ms, "peak_source": peak_src,
-            "note": "algorithmic bytes per launch / CUDA-event launch duration (profiled step after the "
+            "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+            "algorithmic_per_launch": amount, "avg_launch_ms": avg_ms, "peak_source": peak_src,
+            "note": "algorithmic work per launch / CUDA-event launch duration (profiled step after the "
                     "timed region, CUDA graphs off)"}
+    if "schur" in prof and prof["schur"][1] and bs.sizes.tc_chunk_tiles:
+        # the tensor-core kernel executes more than the algorithmic count: 128 x 128 tiles
+        # padded to the chunk windows, and three TF32 products per split value pair
+        sms = prof["schur"][0] / prof["schur"][1]
+        executed = 3.0 * 2.0 * 128 * 128 * 32 * bs.sizes.tc_chunk_tiles
+        kernels["schur"]["executed_tflops"] = round(executed / (sms / 1e3) / 1e12, 3)
+    # the whole LM iteration against HBM: the passes over observations and landmarks and
+    # the dense per-problem systems (A, S_L, factor: 3 x 4 P^2 bytes)
+    iter_bytes = (24.0 * n_obs + 24.0 * n_lm) + (24.0 * n_obs + 16.0 * n_lm) + \
+        (2 * (24.0 * n_obs + 24.0 * n_lm) if prof.get("refine", (0, 0))[1] else 0.0) + \
+        sum(3 * 4.0 * (6 * p.n_poses) ** 2 for p in probs)
+    roof["iteration_hbm"] = {"bytes": iter_bytes, "ms": ms_per_iter,
+                             "gbs": iter_bytes / (ms_per_iter / 1e3) / 1e9,
+                             "frac": iter_bytes / (ms_per_iter / 1e3) / 1e9 / pk["hbm"][0]}
 
-    # plain FP64 GPU solver, one problem at a time (untimed for the headline)
+    # the plain FP64 GPU solver (the comparison point): batched, and problem at a time;
+    # the mixed path without the controller (precision alone)
     plain = None
+    reached_frac = None
+    plain_costs = None
     if not args.no_plain:
-        plain_costs, t_plain = [], 0.0
-        for p in probs:
-            s1 = sv.BatchSolver([p], precision="fp64", device=dev, stream=stream)
-            s1.set_params(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4)
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            st1 = s1.solve(check_every=args.check_every)[0]
-            torch.cuda.synchronize(dev)
-            t_plain += time.perf_counter() - t0
-            plain_costs.append(st1["cost"])
-            s1.close()
-        plain_costs = np.array(plain_costs)
-        reached = chosen_costs <= plain_costs * (1.0 + 1e-6)
-        plain = {"solves_per_s": N_PROBLEMS / t_plain, "ms_per_batch": 1e3 * t_plain,
-                 "chosen_speedup": (t_plain * 1e3) / (total_ms / args.steps),
-                 "reached_plain_cost_frac": float(reached.mean()),
-                 "median_rel_cost_diff": float(np.median(np.abs(chosen_costs - plain_costs) / plain_costs))}
+        s64 = make("fp64", controller=False)
+        ms64, st64 = timed_solves(s64, 1, 1)
+        s64.close()
+        plain_costs = np.array([s["cost"] for s in st64])
+        plain_iters = [s["iterations"] for s in st64]
+        sm_ = make("mixed", controller=False)
+        msm, stm = timed_solves(sm_, 1, 1)
+        sm_.close()
+        mixed_costs = np.array([s["cost"] for s in stm])
+        mixed_iters = [s["iterations"] for s in stm]
+        reached = _reached(chosen_costs, plain_costs)
+        reached_frac = float(reached.mean())
+        to_plain = _iters_to_plain([t["cost"] for t in chosen_trace], plain_costs, cost0)
+        hit = [k for k in to_plain if k is not None]
+        t_serial = None
+        if args.plain_serial:
+            t_serial = 0.0
+            for p in probs:
+                s1 = sv.BatchSolver([p], precision="fp64", device=dev, stream=stream)
+                s1.set_params(**plain_params)
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                s1.solve(check_every=args.check_every)
+                torch.cuda.synchronize(dev)
+                t_serial += time.perf_counter() - t0
+                s1.close()
+        chosen_ms = total_ms / args.steps
+        plain = {
+            "batched_ms": min(ms64), "batched_solves_per_s": N_PROBLEMS / (min(ms64) / 1e3),
+            "mean_iterations": float(np.mean(plain_iters)),
+            "chosen_speedup_vs_batched": min(ms64) / chosen_ms,
+            "reached_plain_cost_frac": reached_frac,
+            "median_rel_cost_diff": float(np.median((chosen_costs - plain_costs) / plain_costs)),
+            "chosen_iterations_to_plain_cost_mean": float(np.mean(hit)) if hit else None,
+            "chosen_iterations_to_plain_cost_max": int(max(hit)) if hit else None,
+            "effects": {
+                "precision (mixed vs FP64, both batched, no controller)": {
+                    "speedup": min(ms64) / min(msm),
+                    "reached_plain_cost_frac": float(_reached(mixed_costs, plain_costs).mean()),
+                    "mixed_ms": min(msm), "mean_iterations": float(np.mean(mixed_iters))},
+                "controller (learned vs Nielsen, mixed, batched)": {
+                    "speedup": min(msm) / chosen_ms,
+                    "iteration_ratio": float(np.mean(mixed_iters)) / max(1e-9, float(np.mean(iters)))},
+            },
+        }
+        if t_serial is not None:
+            plain["serial_ms"] = 1e3 * t_serial
+            plain["serial_solves_per_s"] = N_PROBLEMS / t_serial
+            plain["chosen_speedup_vs_serial"] = (t_serial * 1e3) / chosen_ms
+            plain["effects"]["batching (FP64, 256 at once vs one at a time)"] = {"speedup": 1e3 * t_serial / min(ms64)}
+    value = raw_value * reached_frac if reached_frac is not None else raw_value
 
     # end-to-end through the public API with host buffers: every batch is marshalled,
     # planned, uploaded, solved and read back.  Serially (one BatchSolver after
@@ -414,34 +542,44 @@ def run_ours(args):
         del poses, alphas
     serial_val = N_PROBLEMS * world / (float(np.mean(e2e_ms)) / 1e3)
     n_stream = max(12, args.steps)
-    stream_params = {**dict(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4, use_tc=args.tc), **(tuned or {})}
+    stream_params = {**base_params, **(tuned or {})}
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
+    stream_reached = []
     for _st, _poses, _alphas in sv.solve_stream([probs] * n_stream, "mixed", stream_params, ctl_params, device=dev,
                                                 inflight=args.inflight, check_every=args.check_every):
-        pass
+        if plain_costs is not None:
+            stream_reached.append(float(_reached([s["cost"] for s in _st], plain_costs).mean()))
     torch.cuda.synchronize(dev)
     stream_ms = 1e3 * (time.perf_counter() - t0) / n_stream
-    e2e_val = N_PROBLEMS * world / (stream_ms / 1e3)
+    stream_frac = float(np.mean(stream_reached)) if stream_reached else 1.0
+    e2e_val = N_PROBLEMS * world / (stream_ms / 1e3) * stream_frac
 
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)",
             "data": "synthetic (seeded config-3 generator)",
+            "raw_solves_per_s": raw_value, "solves_to_plain_cost_per_s": value,
             "config": {"workload": WORKLOAD, "problems_per_gpu": N_PROBLEMS, "landmarks": n_lm, "obs": n_obs,
-                       "precision": "mixed", "schur": "tcgen05 split TF32" if tuned["use_tc"] else "SIMT FP32",
+                       "precision": "mixed", "outer_refinement_steps": int(bs.params.outer_steps),
+                       "chosen_max_iters": int(args.max_iters),
+                       "schur": "tcgen05 split TF32" if tuned["use_tc"] else "SIMT FP32",
                        "damping": "learned MLP + Nielsen fallback" if ctl_params is not None else "Nielsen",
                        "autotuned": tuned,
                        "l2": "256 MB flush written between timed steps",
                        "parallelism": f"replicas x{world} (independent batches)",
-                       "iterations_max": int(max(iters)), "iterations_mean": float(np.mean(iters))},
+                       "iterations_max": int(max(iters)), "iterations_mean": float(np.mean(iters)),
+                       "value_definition": "batch solves/s x fraction of problems ending at or below the plain "
+                                           "FP64 GPU solver's cost (rel 1e-6, plain: 30 LM iterations)"},
             "roofline": roof, "kernels": kernels, "gpu_launches": int(launches), "clocks": clk,
             "cpu_baseline": cpu, "plain_fp64": plain,
             "e2e": {"value": e2e_val, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": stream_ms, "steps": n_stream, "inflight": args.inflight,
+                    "reached_plain_cost_frac": stream_frac,
                     "api": "solver.solve_stream: batches planned on a worker thread ahead of their solve, "
-                           f"{args.inflight} batches solving at once on their own CUDA streams",
-                    "serial_value": serial_val,
+                           f"{args.inflight} batches solving at once on their own CUDA streams; solves that "
+                           "reach the plain FP64 cost per second",
+                    "serial_value": serial_val * stream_frac,
                     "serial_ms_per_step": float(np.mean(e2e_ms))}}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -459,8 +597,11 @@ def main():
     ap.add_argument("--check-every", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-serial", type=int, default=1, help="1: also time the FP64 solver one problem at a time")
     ap.add_argument("--tc", type=int, default=1, help="1: tensor-core Schur complement in the mixed path, 0: SIMT")
     ap.add_argument("--controller", type=int, default=1, help="1: learned damping (shipped weights), 0: Nielsen")
+    ap.add_argument("--outer", type=int, default=-1, help="refinement steps of the mixed step (-1: library default)")
+    ap.add_argument("--max-iters", type=int, default=30, help="LM iteration cap of the chosen form")
     ap.add_argument("--autotune", type=int, default=1, help="1: time the run-time launch shapes first")
     ap.add_argument("--inflight", type=int, default=4, help="e2e: batches solving at once in solve_stream")
     ap.add_argument("--shapes", default="", help="COST,LIN: cost-pass and Jacobian-pass CTA sizes instead of "
