@@ -136,6 +136,9 @@ typedef struct spgo_params {
     int32_t wait_us;             /* limit of every bounded device-side wait, microseconds
                                     (0: 2 s).  Shortening it only makes waits give up sooner:
                                     the problem is flagged and its step rejected */
+    float   ctl_min_log10;       /* learned damping: the largest decrease of lambda one proposal
+                                    may make, as log10 of the factor (default -1: at most 10x) */
+    int32_t pad_;
 } spgo_params;
 
 typedef struct spgo_problem_status {

@@ -828,7 +828,7 @@ static int enqueue_linearize(spgo_solver *s, cudaStream_t st, bool stats, bool c
     PROF(K_BOOKKEEP);
     if (stats || ctrl) CUDA_TRY(launch_lm_stats(s->pv, s->wv, std::is_same<T, double>::value, st));
     CUDA_TRY(launch_post_linearize(s->pv, s->wv, st));
-    if (ctrl) CUDA_TRY(launch_controller(s->pv, s->wv, s->wv.ctrl, st));
+    if (ctrl) CUDA_TRY(launch_controller(s->pv, s->wv, s->prm, s->wv.ctrl, st));
   }
   return SPGO_OK;
 }
@@ -981,6 +981,7 @@ void spgo_default_params(spgo_params *p) {
   p->use_tc = 1;
   p->outer_steps = 2;
   p->wait_us = 0;
+  p->ctl_min_log10 = -1.0f;
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
@@ -1152,7 +1153,8 @@ int spgo_set_params(spgo_solver *s, const spgo_params *p) {
   if (!s || !p) return fail(SPGO_ERR_INVALID_ARG, "null argument");
   if (p->loss < 0 || p->loss > 2) return fail(SPGO_ERR_INVALID_ARG, "unknown loss");
   if (!(p->loss_scale > 0) || !(p->eps >= 0) || !(p->alpha_min < p->alpha_max) || p->max_iters < 0 ||
-      p->refine_steps < 0 || !(p->lambda0 >= 0) || p->outer_steps < 0 || p->outer_steps > 8 || p->wait_us < 0)
+      p->refine_steps < 0 || !(p->lambda0 >= 0) || p->outer_steps < 0 || p->outer_steps > 8 || p->wait_us < 0 ||
+      !(p->ctl_min_log10 <= 0.f && p->ctl_min_log10 >= -6.f))
     return fail(SPGO_ERR_INVALID_ARG, "parameter out of range");
   for (const int32_t blk : {p->cost_block, p->lin_block})
     if (blk != 0 && (blk < 32 || blk > 256 || blk % 32 != 0))

@@ -89,6 +89,32 @@ __device__ __forceinline__ df df_dot3(float a0h, float a0l, float a1h, float a1l
   return fast_two_sum(s.h, lo);
 }
 
+// a0 b0 + a1 b1 + a2 b2 + a3 b3 as a double-float: the four products exactly
+// (two-product), their high parts by a cascade of error-free sums, every low part
+// and error term in one float (~2^-44 relative to the terms' magnitudes)
+__device__ __forceinline__ df sum4_prod(float a0, float b0, float a1, float b1, float a2, float b2, float a3,
+                                        float b3) {
+  const df p0 = two_prod(a0, b0), p1 = two_prod(a1, b1), p2 = two_prod(a2, b2), p3 = two_prod(a3, b3);
+  const df s = two_sum(p0.h, p1.h), t = two_sum(p2.h, p3.h);
+  const df u = two_sum(s.h, t.h);
+  const float lo = ((p0.l + p1.l) + (p2.l + p3.l)) + ((s.l + t.l) + u.l);
+  return fast_two_sum(u.h, lo);
+}
+
+// Running sum kept unnormalised (h plus an accumulated error term): the next add
+// depends on the previous one through a single float addition.  Read with
+// df_acc_value.
+struct df_acc {
+  float h = 0.f, l = 0.f;
+  __device__ __forceinline__ void add(float xh, float xl) {
+    const float sh = h + xh;
+    const float bb = sh - h;
+    l += ((h - (sh - bb)) + (xh - bb)) + xl;
+    h = sh;
+  }
+};
+__device__ __forceinline__ double df_acc_value(const df_acc &a) { return (double)a.h + (double)a.l; }
+
 // a - b for plain floats, exactly, as a double-float
 __device__ __forceinline__ df df_sub(float a, float b) { return two_sum(a, -b); }
 

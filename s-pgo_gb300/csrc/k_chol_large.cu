@@ -273,7 +273,7 @@ __device__ __forceinline__ bool lg_wait_flag(const int *flag, uint64_t deadline)
     int v;
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
     if (v) return true;
-    if ((it & 63) == 63 && lg_clock_ns() > deadline) return false;
+    if ((it & 7) == 7 && lg_clock_ns() > deadline) return false;  // (~1 us between looks at the clock)
     __nanosleep(100);
   }
 }

@@ -531,7 +531,7 @@ __device__ __forceinline__ df prod2_df(float a, float b, float c, float d) {
   return fast_two_sum(t.h, t.l);
 }
 
-__global__ void __launch_bounds__(256, 2) k_jacobian_acc(PlanView pv, WorkView wv, Params prm,
+__global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView wv, Params prm,
                                                          const double *__restrict__ alpha_state, int gate) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
@@ -592,17 +592,24 @@ __global__ void __launch_bounds__(256, 2) k_jacobian_acc(PlanView pv, WorkView w
   __syncthreads();
 
   // phase B: thread per observation; runs of equal target frame inside a warp go to
-  // the FP64 pair record (host, target)
+  // the FP64 pair record (host, target).  A lane keeps its observation's weighted
+  // pose rows of both cameras (zero without a pose term) and forms each of the 27
+  // pair values once, as the exact sum of its four products, straight into the staging.
   const int D = pv.p_pair_D[b];
   double *pair_base = reinterpret_cast<double *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * kJacVals;
   const float lscale = prm.loss_scale;
   for (int64_t base = ob + (tid & ~31); base < oe; base += blockDim.x) {
     const int64_t o = base + lane;
-    df M[21], m[6];
+    float K[2][2][6];  // [camera][row][parameter]: w K, about the pair origin
+    float RW[2][2];    // s w r
 #pragma unroll
-    for (int k = 0; k < 21; ++k) M[k] = df_make(0.f);
+    for (int c2 = 0; c2 < 2; ++c2)
 #pragma unroll
-    for (int k = 0; k < 6; ++k) m[k] = df_make(0.f);
+      for (int r2 = 0; r2 < 2; ++r2) {
+        RW[c2][r2] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) K[c2][r2][k] = 0.f;
+      }
     int key = -1;
     if (o < oe) {
       const int slot = pv.obs_slot[o];
@@ -652,15 +659,12 @@ __global__ void __launch_bounds__(256, 2) k_jacobian_acc(PlanView pv, WorkView w
         accG += w2 * (ja0 * r0 + ja1 * r1);
         if (has_pose) {
           const Vec3<float> k0 = cross(Xp, u0), k1 = cross(Xp, u1);
-          const float K0[6] = {w * k0.x, w * k0.y, w * k0.z, w * u0.x, w * u0.y, w * u0.z};
-          const float K1[6] = {w * k1.x, w * k1.y, w * k1.z, w * u1.x, w * u1.y, w * u1.z};
-          const float rw0 = sgn * (w * r0), rw1 = sgn * (w * r1);
-#pragma unroll
-          for (int i = 0; i < 6; ++i) {
-#pragma unroll
-            for (int j = i; j < 6; ++j) M[tri6(i, j)] = M[tri6(i, j)] + prod2_df(K0[i], K0[j], K1[i], K1[j]);
-            m[i] = m[i] + prod2_df(K0[i], rw0, K1[i], rw1);
-          }
+          K[cam][0][0] = w * k0.x; K[cam][0][1] = w * k0.y; K[cam][0][2] = w * k0.z;
+          K[cam][0][3] = w * u0.x; K[cam][0][4] = w * u0.y; K[cam][0][5] = w * u0.z;
+          K[cam][1][0] = w * k1.x; K[cam][1][1] = w * k1.y; K[cam][1][2] = w * k1.z;
+          K[cam][1][3] = w * u1.x; K[cam][1][4] = w * u1.y; K[cam][1][5] = w * u1.z;
+          RW[cam][0] = sgn * (w * r0);
+          RW[cam][1] = sgn * (w * r1);
           const Vec3<float> h0 = cross(X, u0), h1 = cross(X, u1);
           const float jw0 = sgn * (w * ja0), jw1 = sgn * (w * ja1);
           const float H0[6] = {w * h0.x, w * h0.y, w * h0.z, w * u0.x, w * u0.y, w * u0.z};
@@ -689,34 +693,37 @@ __global__ void __launch_bounds__(256, 2) k_jacobian_acc(PlanView pv, WorkView w
     float *st = stage + (size_t)(tid >> 5) * 2 * kJacVals * kJacPitch;
     int *keys = sm.key[tid >> 5];
 #pragma unroll
-    for (int k = 0; k < 21; ++k) {
-      st[(2 * k) * kJacPitch + lane] = M[k].h;
-      st[(2 * k + 1) * kJacPitch + lane] = M[k].l;
-    }
+    for (int i = 0; i < 6; ++i) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      st[(2 * (21 + k)) * kJacPitch + lane] = m[k].h;
-      st[(2 * (21 + k) + 1) * kJacPitch + lane] = m[k].l;
+      for (int j = i; j < 6; ++j) {
+        const df v = sum4_prod(K[0][0][i], K[0][0][j], K[0][1][i], K[0][1][j], K[1][0][i], K[1][0][j], K[1][1][i],
+                               K[1][1][j]);
+        st[(2 * tri6(i, j)) * kJacPitch + lane] = v.h;
+        st[(2 * tri6(i, j) + 1) * kJacPitch + lane] = v.l;
+      }
+      const df v = sum4_prod(K[0][0][i], RW[0][0], K[0][1][i], RW[0][1], K[1][0][i], RW[1][0], K[1][1][i], RW[1][1]);
+      st[(2 * (21 + i)) * kJacPitch + lane] = v.h;
+      st[(2 * (21 + i) + 1) * kJacPitch + lane] = v.l;
     }
     keys[lane] = key;
     __syncwarp();
     if (__any_sync(0xffffffffu, key >= 0) && lane < kJacVals) {
       const float *ch = st + (2 * lane) * kJacPitch, *cl = st + (2 * lane + 1) * kJacPitch;
       const int host_a = sm.a[0];
-      auto emit = [&](int n, const df &v) {
+      auto emit = [&](int n, const df_acc &v) {
         const int lo = min(host_a, n), hi = max(host_a, n);
-        atomicAdd(pair_base + ((size_t)lo * D + (hi - lo - 1)) * kJacVals + lane, (double)v.h + (double)v.l);
+        atomicAdd(pair_base + ((size_t)lo * D + (hi - lo - 1)) * kJacVals + lane, df_acc_value(v));
       };
-      df acc = df_make(0.f);
+      df_acc acc;
       int cur = keys[0];
       for (int i = 0; i < 32; ++i) {
         const int k = keys[i];
         if (k != cur) {
           if (cur >= 0) emit(cur, acc);
-          acc = df_make(0.f);
+          acc = df_acc();
           cur = k;
         }
-        acc = acc + df{ch[i], cl[i]};
+        acc.add(ch[i], cl[i]);
       }
       if (cur >= 0) emit(cur, acc);
     }

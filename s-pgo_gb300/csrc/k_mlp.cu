@@ -295,8 +295,11 @@ __device__ void lm_features_warp(const PlanView &pv, const LMState &s, int b, fl
 // proposal lambda * 10^out0 replaces the schedule's lambda when its logit out1 > 0
 // (it predicts that deviating from the schedule gives the lower cost).  After a
 // rejected step no relinearisation happens and the Nielsen increase stands: the
-// fallback whenever a step fails the gain-ratio test.
-__global__ void k_controller(PlanView pv, WorkView wv, const MlpSmem *Wd) {
+// fallback whenever a step fails the gain-ratio test.  A proposal lowers lambda by at
+// most 10^-min_dl (prm.ctl_min_log10): the one-step-greedy choices the network is
+// trained on include cuts of up to 10^6, which on these L2 problems send some
+// trajectories into worse minima than the schedule's.
+__global__ void k_controller(PlanView pv, WorkView wv, const MlpSmem *Wd, float min_dl) {
   __shared__ MlpSmem m;
   stage_mlp(Wd, m);
   __syncthreads();
@@ -309,7 +312,7 @@ __global__ void k_controller(PlanView pv, WorkView wv, const MlpSmem *Wd) {
   float o0, o1;
   mlp_infer_warp(m, x, o0, o1);
   if ((threadIdx.x & 31) == 0 && o1 > 0.f) {
-    const double dl = fmin(3.0, fmax(-6.0, (double)o0));
+    const double dl = fmin(3.0, fmax((double)min_dl, (double)o0));
     s.lam = fmin(1e12, fmax(1e-14, s.lam * exp10(dl)));
   }
 }
@@ -444,8 +447,9 @@ int launch_lm_stats(const PlanView &pv, const WorkView &wv, int f64, void *strea
   return (int)cudaGetLastError();
 }
 
-int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wd, void *stream) {
-  k_controller<<<grid_for(pv.B, 8), 256, 0, (cudaStream_t)stream>>>(pv, wv, reinterpret_cast<const MlpSmem *>(Wd));
+int launch_controller(const PlanView &pv, const WorkView &wv, const Params &prm, const void *Wd, void *stream) {
+  k_controller<<<grid_for(pv.B, 8), 256, 0, (cudaStream_t)stream>>>(pv, wv, reinterpret_cast<const MlpSmem *>(Wd),
+                                                                    prm.ctl_min_log10);
   ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -262,11 +262,19 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
   const float *res_buf = wv.res + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 4;
   for (int64_t base = ob + (tid & ~31); base < oe; base += blockDim.x) {
     const int64_t o = base + lane;
-    df pe[6], pg[6];
+    // this observation's pose rows s K of both cameras (zero without a pose term), its
+    // inverse-depth rows, and the weighted linearised residuals w^2 e and w^2 r; each
+    // dual is then formed once as the exact sum of its four products
+    float K[2][2][6], JA[2][2], EW[2][2], GW[2][2];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) pe[k] = pg[k] = df_make(0.f);
+    for (int c2 = 0; c2 < 2; ++c2)
+#pragma unroll
+      for (int r2 = 0; r2 < 2; ++r2) {
+        JA[c2][r2] = EW[c2][r2] = GW[c2][r2] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) K[c2][r2][k] = 0.f;
+      }
     int key = -1, slot = -1;
-    double vle = 0.0, vlg = 0.0;  // this observation's landmark duals
     if (o < oe) {
       slot = pv.obs_slot[o];
       const int n = pv.obs_frame[o];
@@ -291,7 +299,6 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
 #pragma unroll
         for (int k = 0; k < 6; ++k) W[k] = tw[k];
       }
-      df dle = df_make(0.f), dlg = df_make(0.f);
 #pragma unroll
       for (int cam = 0; cam < 2; ++cam) {
         // camera-frame point as the linearisation forms it (double-float, rounded once)
@@ -316,37 +323,35 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
         const Vec3<float> u1 = v3<float>(j11 * Rn[1] + j12 * Rn[2], j11 * Rn[4] + j12 * Rn[5], j11 * Rn[7] + j12 * Rn[8]);
         const float ja0 = dot(u0, dXda), ja1 = dot(u1, dXda);
         float e0 = r0 - ja0 * da, e1 = r1 - ja1 * da;
-        float K0[6], K1[6];
         if (has_pose) {
           const Vec3<float> k0 = cross(Xp, u0), k1 = cross(Xp, u1);
-          K0[0] = sgn * k0.x; K0[1] = sgn * k0.y; K0[2] = sgn * k0.z;
-          K0[3] = sgn * u0.x; K0[4] = sgn * u0.y; K0[5] = sgn * u0.z;
-          K1[0] = sgn * k1.x; K1[1] = sgn * k1.y; K1[2] = sgn * k1.z;
-          K1[3] = sgn * u1.x; K1[4] = sgn * u1.y; K1[5] = sgn * u1.z;
+          K[cam][0][0] = sgn * k0.x; K[cam][0][1] = sgn * k0.y; K[cam][0][2] = sgn * k0.z;
+          K[cam][0][3] = sgn * u0.x; K[cam][0][4] = sgn * u0.y; K[cam][0][5] = sgn * u0.z;
+          K[cam][1][0] = sgn * k1.x; K[cam][1][1] = sgn * k1.y; K[cam][1][2] = sgn * k1.z;
+          K[cam][1][3] = sgn * u1.x; K[cam][1][4] = sgn * u1.y; K[cam][1][5] = sgn * u1.z;
           float jw0 = 0.f, jw1 = 0.f;
 #pragma unroll
           for (int k = 0; k < 6; ++k) {
-            jw0 += K0[k] * W[k];
-            jw1 += K1[k] * W[k];
+            jw0 += K[cam][0][k] * W[k];
+            jw1 += K[cam][1][k] * W[k];
           }
           e0 -= jw0;
           e1 -= jw1;
         }
-        const float ew0 = w2 * e0, ew1 = w2 * e1;
-        dle = dle + prod2(ja0, ew0, ja1, ew1);
-        const float gw0 = w2 * r0, gw1 = w2 * r1;
-        if (FIRST) dlg = dlg + prod2(ja0, gw0, ja1, gw1);
-        if (has_pose) {
-#pragma unroll
-          for (int k = 0; k < 6; ++k) {
-            pe[k] = pe[k] + prod2(K0[k], ew0, K1[k], ew1);
-            if (FIRST) pg[k] = pg[k] + prod2(K0[k], gw0, K1[k], gw1);
-          }
-        }
+        JA[cam][0] = ja0;
+        JA[cam][1] = ja1;
+        EW[cam][0] = w2 * e0;
+        EW[cam][1] = w2 * e1;
+        GW[cam][0] = w2 * r0;
+        GW[cam][1] = w2 * r1;
       }
-      vle = df_to_double(dle);
-      if (FIRST) vlg = df_to_double(dlg);
       if (has_pose) key = n;
+    }
+    double vle = 0.0, vlg = 0.0;  // this observation's landmark duals
+    if (slot >= 0) {
+      vle = df_to_double(sum4_prod(JA[0][0], EW[0][0], JA[0][1], EW[0][1], JA[1][0], EW[1][0], JA[1][1], EW[1][1]));
+      if (FIRST)
+        vlg = df_to_double(sum4_prod(JA[0][0], GW[0][0], JA[0][1], GW[0][1], JA[1][0], GW[1][0], JA[1][1], GW[1][1]));
     }
     {
       // the warp's own landmark accumulators: lanes sharing a landmark (different
@@ -362,16 +367,18 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
       }
     }
     // stage the pair duals, then lanes 0..NC-1 each sum one over the runs of equal
-    // target frame (double-float) and add each run to its pair record (FP64)
+    // target frame and add each run to its pair record (FP64)
     float *st = stage + (size_t)warp * 2 * NC * kRpPitch;
     int *keys = sm.key[warp];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      st[(2 * k) * kRpPitch + lane] = pe[k].h;
-      st[(2 * k + 1) * kRpPitch + lane] = pe[k].l;
+      const df v = sum4_prod(K[0][0][k], EW[0][0], K[0][1][k], EW[0][1], K[1][0][k], EW[1][0], K[1][1][k], EW[1][1]);
+      st[(2 * k) * kRpPitch + lane] = v.h;
+      st[(2 * k + 1) * kRpPitch + lane] = v.l;
       if (FIRST) {
-        st[(2 * (6 + k)) * kRpPitch + lane] = pg[k].h;
-        st[(2 * (6 + k) + 1) * kRpPitch + lane] = pg[k].l;
+        const df u = sum4_prod(K[0][0][k], GW[0][0], K[0][1][k], GW[0][1], K[1][0][k], GW[1][0], K[1][1][k], GW[1][1]);
+        st[(2 * (6 + k)) * kRpPitch + lane] = u.h;
+        st[(2 * (6 + k) + 1) * kRpPitch + lane] = u.l;
       }
     }
     keys[lane] = key;
@@ -380,20 +387,20 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
       const int host_a = sm.a[0];
       const float *ch = st + (2 * lane) * kRpPitch, *cl = st + (2 * lane + 1) * kRpPitch;
       double *rec0 = wv.pdual + (size_t)pv.p_pair_off[b] * 12 + lane;
-      auto emit = [&](int n, const df &v) {
+      auto emit = [&](int n, const df_acc &v) {
         const int lo = min(host_a, n), hi = max(host_a, n);
-        atomicAdd(rec0 + ((size_t)lo * D + (hi - lo - 1)) * 12, df_to_double(v));
+        atomicAdd(rec0 + ((size_t)lo * D + (hi - lo - 1)) * 12, df_acc_value(v));
       };
-      df acc = df_make(0.f);
+      df_acc acc;
       int cur = keys[0];
       for (int i = 0; i < 32; ++i) {
         const int k = keys[i];
         if (k != cur) {
           if (cur >= 0) emit(cur, acc);
-          acc = df_make(0.f);
+          acc = df_acc();
           cur = k;
         }
-        acc = acc + df{ch[i], cl[i]};
+        acc.add(ch[i], cl[i]);
       }
       if (cur >= 0) emit(cur, acc);
     }

@@ -139,6 +139,8 @@ struct Params {
   int32_t use_graph, use_tc;
   int32_t cost_block, lin_block;
   int32_t outer_steps, wait_us;
+  float ctl_min_log10;
+  int32_t pad_;
 };
 
 // bounded device-side waits: the limit in nanoseconds (wait_us = 0: 2 s)
@@ -187,7 +189,7 @@ int launch_export_B_n(const PlanView &pv, const WorkView &wv, int problem, int n
                       double *C, double *ga, void *stream);
 
 int launch_lm_stats(const PlanView &pv, const WorkView &wv, int f64, void *stream);
-int launch_controller(const PlanView &pv, const WorkView &wv, const void *Wb, void *stream);
+int launch_controller(const PlanView &pv, const WorkView &wv, const Params &prm, const void *Wb, void *stream);
 int launch_features(const PlanView &pv, const WorkView &wv, float *feat, void *stream);
 int launch_mlp_deploy(const float *theta, void *dst, void *stream);
 size_t mlp_deployed_bytes();

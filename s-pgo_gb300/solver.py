@@ -206,7 +206,7 @@ class BatchSolver:
     def set_params(self, loss: Optional[str] = None, loss_scale=None, near_boost=None, eps=None,
                    alpha_min=None, alpha_max=None, lambda0=None, lambda_max=None, tol=None, max_iters=None,
                    refine_steps=None, use_graph=None, use_tc=None, cost_block=None, lin_block=None,
-                   outer_steps=None, wait_us=None):
+                   outer_steps=None, wait_us=None, ctl_min_log10=None):
         p = self.params
         if loss is not None:
             p.loss = _LOSS[loss]
@@ -233,6 +233,8 @@ class BatchSolver:
             p.outer_steps = int(outer_steps)
         if wait_us is not None:
             p.wait_us = int(wait_us)
+        if ctl_min_log10 is not None:
+            p.ctl_min_log10 = float(ctl_min_log10)
         self._apply_params()
 
     def _apply_params(self):
