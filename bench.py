@@ -4,14 +4,16 @@
 Workload (synthetic, seeded): 256 independent stereo pose-graph / bundle-
 adjustment problems, N ~ U[8, 32] incremental poses and L ~ U[200, 3000]
 landmarks each (circle generator, 1 px noise), every problem run to a
-relative cost decrease below 1e-6 or 30 LM iterations.  One step = one solve
-of the whole batch from its initial state.
+relative cost decrease below 1e-6 or an iteration cap (the plain FP64 solver:
+30).  One step = one solve of the whole batch from its initial state.
 
 The chosen form is the mixed path (FP32 Jacobian and Hessian blocks summed
 exactly, tensor-core Schur complement, FP32 Cholesky, the step refined against
-the accurately summed residual of the whole system), batched, with the learned
-damping controller unless ``--controller 0``.  Its reference point is the plain
-FP64 GPU solver (Nielsen LM, no controller, 30 iterations):
+the accurately summed residual of the whole system), batched, with Nielsen
+damping and at most 40 LM iterations (``--max-iters``); ``--controller 1``
+puts the learned damping controller in the chosen form instead, and the
+controller arm of ``plain_fp64.effects`` always times it.  Its reference point
+is the plain FP64 GPU solver (Nielsen LM, no controller, 30 iterations):
 
 * ``value``: solves per second that reach the plain FP64 solver's final cost
   (relative 1e-6): the chosen form's batch solves/s times the fraction of its
@@ -28,7 +30,7 @@ FP64 GPU solver (Nielsen LM, no controller, 30 iterations):
   solve, ``--inflight`` batches solving at once on their own CUDA streams).
 * ``roofline``: the dominant kernel's algorithmic work per launch (HBM bytes or
   FLOPs) over its CUDA-event duration, against the measured peaks; also the
-  whole LM iteration's algorithmic bytes against HBM.
+  whole solve's algorithmic bytes against HBM.
 * ``cpu_baseline``: the FP64 CPU oracle on a bounded sample of the batch.
 * ``--impl reference``: the CPU oracle alone on host cores (process pool),
   same metric.
@@ -183,7 +185,7 @@ def roofline_numerator(kind: str, sizes, probs):
     """(bound, unit, algorithmic amount per launch) of a profiled kernel kind.
 
     Jacobian pass 24 B per stereo observation + 24 B per landmark; cost pass
-    24 O + 16 L; refinement (two residual passes per LM iteration) 2 (24 O + 24 L);
+    24 O + 16 L; residual pass of the step refinement 24 O + 24 L;
     landmark Schur complement sum over landmarks of 2 (6 k)^2 FLOPs (k = pose blocks
     of the landmark's window); factor + solve P^3 / 3 + 4 P^2 per problem (FP32)."""
     O, L = sizes.total_obs, sizes.total_landmarks
@@ -191,8 +193,8 @@ def roofline_numerator(kind: str, sizes, probs):
         return "hbm", "GB/s", 24.0 * O + 24.0 * L
     if kind == "cost":
         return "hbm", "GB/s", 24.0 * O + 16.0 * L
-    if kind == "refine":
-        return "hbm", "GB/s", 2 * (24.0 * O + 24.0 * L)
+    if kind == "resid_pass":
+        return "hbm", "GB/s", 24.0 * O + 24.0 * L
     if kind == "schur":
         return "tensor", "TFLOP/s", float(sizes.schur_flops_landmark)
     if kind == "factor_solve":
@@ -318,12 +320,13 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
 
-    # learned damping: the shipped network (trained by train_controller.py), if present
-    ctl_params = None
-    if args.controller:
-        learned = importlib.import_module("spgo_gb300.learned")
-        if os.path.exists(learned.DEFAULT_WEIGHTS):
-            ctl_params = learned.Controller.load(device=dev).deployed()
+    # learned damping: the shipped network (trained by train_controller.py), if present;
+    # the chosen form uses it with --controller 1, the controller arm of the effects always
+    net_params = None
+    learned = importlib.import_module("spgo_gb300.learned")
+    if os.path.exists(learned.DEFAULT_WEIGHTS):
+        net_params = learned.Controller.load(device=dev).deployed()
+    ctl_params = net_params if args.controller else None
 
     plain_params = dict(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4)
     base_params = dict(plain_params, max_iters=args.max_iters, use_tc=args.tc)
@@ -331,7 +334,8 @@ def run_ours(args):
         base_params["outer_steps"] = args.outer
     tuned = None
 
-    def make(precision, controller=True):
+    def make(precision, controller=None):
+        """A solver of the batch; controller: deployed network weights or None (Nielsen)."""
         s = sv.BatchSolver(probs, precision=precision, device=dev, stream=stream)
         if precision == "mixed":
             s.set_params(**base_params)
@@ -339,11 +343,11 @@ def run_ours(args):
                 s.set_params(**tuned)
         else:
             s.set_params(**plain_params)
-        if controller and ctl_params is not None:
-            s.set_controller(ctl_params)
+        if controller is not None:
+            s.set_controller(controller)
         return s
 
-    bs = make("mixed")
+    bs = make("mixed", ctl_params)
     if args.shapes:
         cb, lb = (int(x) for x in args.shapes.split(","))
         tuned = dict(cost_block=cb, lin_block=lb, use_tc=bs.params.use_tc)
@@ -421,7 +425,6 @@ def run_ours(args):
     iters = [s["iterations"] for s in status]
     chosen_costs = np.array([s["cost"] for s in status])
     cost0 = np.array([s["cost0"] for s in status])
-    ms_per_iter = (total_ms / args.steps) / max(1, max(iters))
 
     # kernel shares and roofline of the dominant kernel
     peaks = {}
@@ -456,14 +459,17 @@ def run_ours(args):
         sms = prof["schur"][0] / prof["schur"][1]
         executed = 3.0 * 2.0 * 128 * 128 * 32 * bs.sizes.tc_chunk_tiles
         kernels["schur"]["executed_tflops"] = round(executed / (sms / 1e3) / 1e12, 3)
-    # the whole LM iteration against HBM: the passes over observations and landmarks and
-    # the dense per-problem systems (A, S_L, factor: 3 x 4 P^2 bytes)
-    iter_bytes = (24.0 * n_obs + 24.0 * n_lm) + (24.0 * n_obs + 16.0 * n_lm) + \
-        (2 * (24.0 * n_obs + 24.0 * n_lm) if prof.get("refine", (0, 0))[1] else 0.0) + \
-        sum(3 * 4.0 * (6 * p.n_poses) ** 2 for p in probs)
-    roof["iteration_hbm"] = {"bytes": iter_bytes, "ms": ms_per_iter,
-                             "gbs": iter_bytes / (ms_per_iter / 1e3) / 1e9,
-                             "frac": iter_bytes / (ms_per_iter / 1e3) / 1e9 / pk["hbm"][0]}
+    # the whole solve against HBM: the algorithmic bytes of every pass over observations
+    # and landmarks the profiled solve launched, plus the dense per-problem systems each
+    # factorisation reads and writes (A, S_L, factor: 3 x 4 P^2 bytes), over the timed
+    # solve's duration (the profiled solve repeats its work with graphs off)
+    dense = sum(3 * 4.0 * (6 * p.n_poses) ** 2 for p in probs)
+    step_bytes = sum(v[1] * roofline_numerator(k, bs.sizes, probs)[2]
+                     for k, v in prof.items() if roofline_numerator(k, bs.sizes, probs)[0] == "hbm")
+    step_bytes += prof.get("factor_solve", (0, 0))[1] * dense
+    step_ms = total_ms / args.steps
+    roof["solve_hbm"] = {"bytes": step_bytes, "ms": step_ms, "gbs": step_bytes / (step_ms / 1e3) / 1e9,
+                         "frac": step_bytes / (step_ms / 1e3) / 1e9 / pk["hbm"][0]}
 
     # the plain FP64 GPU solver (the comparison point): batched, and problem at a time;
     # the mixed path without the controller (precision alone)
@@ -471,13 +477,14 @@ def run_ours(args):
     reached_frac = None
     plain_costs = None
     if not args.no_plain:
-        s64 = make("fp64", controller=False)
+        s64 = make("fp64")
         ms64, st64 = timed_solves(s64, 1, 1)
         s64.close()
         plain_costs = np.array([s["cost"] for s in st64])
         plain_iters = [s["iterations"] for s in st64]
-        sm_ = make("mixed", controller=False)
+        sm_ = make("mixed")
         msm, stm = timed_solves(sm_, 1, 1)
+        mix_trace = sm_.trace()
         sm_.close()
         mixed_costs = np.array([s["cost"] for s in stm])
         mixed_iters = [s["iterations"] for s in stm]
@@ -485,6 +492,28 @@ def run_ours(args):
         reached_frac = float(reached.mean())
         to_plain = _iters_to_plain([t["cost"] for t in chosen_trace], plain_costs, cost0)
         hit = [k for k in to_plain if k is not None]
+        ctl_effect = None
+        if net_params is not None:
+            # the learned controller on the mixed path against Nielsen on the same path:
+            # wall time, problems reaching the plain cost, LM iterations to reach it
+            sc_ = make("mixed", net_params)
+            msc, stc = timed_solves(sc_, 1, 1)
+            ctl_trace = sc_.trace()
+            sc_.close()
+            ctl_costs = np.array([s["cost"] for s in stc])
+            ctl_iters = [s["iterations"] for s in stc]
+            ctl_hit = [k for k in _iters_to_plain([t["cost"] for t in ctl_trace], plain_costs, cost0)
+                       if k is not None]
+            mix_hit = [k for k in _iters_to_plain([t["cost"] for t in mix_trace], plain_costs, cost0)
+                       if k is not None]
+            ctl_effect = {
+                "speedup": min(msm) / min(msc),
+                "reached_plain_cost_frac": float(_reached(ctl_costs, plain_costs).mean()),
+                "learned_ms": min(msc), "mean_iterations": float(np.mean(ctl_iters)),
+                "iteration_ratio": float(np.mean(mixed_iters)) / max(1e-9, float(np.mean(ctl_iters))),
+                "iterations_to_plain_cost_mean": float(np.mean(ctl_hit)) if ctl_hit else None,
+                "nielsen_iterations_to_plain_cost_mean":
+                    float(np.mean(mix_hit)) if mix_hit else None}
         t_serial = None
         if args.plain_serial:
             t_serial = 0.0
@@ -511,9 +540,7 @@ def run_ours(args):
                     "speedup": min(ms64) / min(msm),
                     "reached_plain_cost_frac": float(_reached(mixed_costs, plain_costs).mean()),
                     "mixed_ms": min(msm), "mean_iterations": float(np.mean(mixed_iters))},
-                "controller (learned vs Nielsen, mixed, batched)": {
-                    "speedup": min(msm) / chosen_ms,
-                    "iteration_ratio": float(np.mean(mixed_iters)) / max(1e-9, float(np.mean(iters)))},
+                "controller (learned vs Nielsen, mixed, batched)": ctl_effect,
             },
         }
         if t_serial is not None:
@@ -531,7 +558,7 @@ def run_ours(args):
     for k in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        s2 = make("mixed")
+        s2 = make("mixed", ctl_params)
         s2.solve(check_every=args.check_every)
         poses, alphas = s2.get_state()
         torch.cuda.synchronize(dev)
@@ -599,9 +626,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--plain-serial", type=int, default=1, help="1: also time the FP64 solver one problem at a time")
     ap.add_argument("--tc", type=int, default=1, help="1: tensor-core Schur complement in the mixed path, 0: SIMT")
-    ap.add_argument("--controller", type=int, default=1, help="1: learned damping (shipped weights), 0: Nielsen")
+    ap.add_argument("--controller", type=int, default=0, help="chosen form's damping: 1 learned (shipped weights), "
+                    "0 Nielsen")
     ap.add_argument("--outer", type=int, default=-1, help="refinement steps of the mixed step (-1: library default)")
-    ap.add_argument("--max-iters", type=int, default=30, help="LM iteration cap of the chosen form")
+    ap.add_argument("--max-iters", type=int, default=40, help="LM iteration cap of the chosen form")
     ap.add_argument("--autotune", type=int, default=1, help="1: time the run-time launch shapes first")
     ap.add_argument("--inflight", type=int, default=4, help="e2e: batches solving at once in solve_stream")
     ap.add_argument("--shapes", default="", help="COST,LIN: cost-pass and Jacobian-pass CTA sizes instead of "

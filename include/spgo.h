@@ -137,7 +137,8 @@ typedef struct spgo_params {
                                     (0: 2 s).  Shortening it only makes waits give up sooner:
                                     the problem is flagged and its step rejected */
     float   ctl_min_log10;       /* learned damping: the largest decrease of lambda one proposal
-                                    may make, as log10 of the factor (default -1: at most 10x) */
+                                    may make, as log10 of the factor, in [-6, 0] (default -6:
+                                    the network's own range) */
     int32_t pad_;
 } spgo_params;
 
@@ -284,11 +285,12 @@ int64_t spgo_launch_count(const spgo_solver *s);
  * enable: create `capacity` event pairs (0 disables); each profiled launch
  * uses one pair until they run out.  read: synchronise `stream`, return the
  * summed milliseconds and launch counts per kind, and recycle the events.
- * Kinds (n_kinds >= 11): 0 pose chain, 1 linearisation, 2 cost pass,
+ * Kinds (n_kinds >= 12): 0 pose chain, 1 linearisation, 2 cost pass,
  * 3 pair reduction, 4 Schur complement, 5 assembly, 6 factor + solve,
  * 7 inverse-depth back-substitution, 8 pose update, 9 LM bookkeeping,
- * 10 step refinement (mixed path). */
-#define SPGO_PROFILE_KINDS 11
+ * 10 step refinement: its reduced solves and pair twists (mixed path),
+ * 11 step refinement: one residual pass over the observations (mixed path). */
+#define SPGO_PROFILE_KINDS 12
 int spgo_profile_enable(spgo_solver *s, int32_t capacity);
 int spgo_profile_read(spgo_solver *s, double *ms, int64_t *count, int32_t n_kinds, void *stream);
 

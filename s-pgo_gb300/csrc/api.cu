@@ -692,7 +692,7 @@ static void drop_graphs(spgo_solver *s) {
 
 // profiled kernel kinds (spgo_profile_read order)
 enum { K_CHAIN, K_LINEARIZE, K_COST, K_SYSTEM, K_SCHUR, K_ASSEMBLE, K_FACTOR, K_BACKSUB, K_UPDATE,
-       K_BOOKKEEP, K_REFINE, K_NKINDS };
+       K_BOOKKEEP, K_REFINE, K_RESID, K_NKINDS };
 static_assert(K_NKINDS == SPGO_PROFILE_KINDS, "profile kinds");
 
 struct ProfScope {
@@ -882,16 +882,14 @@ static int enqueue_candidate(spgo_solver *s, cudaStream_t st) {
     { PROF(K_UPDATE); CUDA_TRY(launch_update_poses<T>(s->pv, s->wv, s->poses, s->wv.poses_cand, 1.0, 0, st)); }
     return SPGO_OK;
   }
-  {
+  { PROF(K_REFINE); CUDA_TRY(launch_pair_twists(s->pv, s->wv, st)); }
+  for (int k = 0; k < outer; ++k) {
+    { PROF(K_RESID); CUDA_TRY(launch_resid_pass(s->pv, s->wv, s->prm, s->alpha, k == 0, st)); }
     PROF(K_REFINE);
-    CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
-    for (int k = 0; k < outer; ++k) {
-      CUDA_TRY(launch_resid_pass(s->pv, s->wv, s->prm, s->alpha, k == 0, st));
-      CUDA_TRY(launch_resid_solve(s->pv, s->wv, k == 0, st));
-      for (const int b : s->plan->large)
-        CUDA_TRY(launch_refine_large(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b], st));
-      if (k + 1 < outer) CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
-    }
+    CUDA_TRY(launch_resid_solve(s->pv, s->wv, k == 0, st));
+    for (const int b : s->plan->large)
+      CUDA_TRY(launch_refine_large(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b], st));
+    if (k + 1 < outer) CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
   }
   { PROF(K_BACKSUB); CUDA_TRY(launch_backsub_refined(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, st)); }
   {
@@ -981,7 +979,7 @@ void spgo_default_params(spgo_params *p) {
   p->use_tc = 1;
   p->outer_steps = 2;
   p->wait_us = 0;
-  p->ctl_min_log10 = -1.0f;
+  p->ctl_min_log10 = -6.0f;
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {

@@ -296,9 +296,10 @@ __device__ void lm_features_warp(const PlanView &pv, const LMState &s, int b, fl
 // (it predicts that deviating from the schedule gives the lower cost).  After a
 // rejected step no relinearisation happens and the Nielsen increase stands: the
 // fallback whenever a step fails the gain-ratio test.  A proposal lowers lambda by at
-// most 10^-min_dl (prm.ctl_min_log10): the one-step-greedy choices the network is
-// trained on include cuts of up to 10^6, which on these L2 problems send some
-// trajectories into worse minima than the schedule's.
+// most a factor 10^-min_dl (prm.ctl_min_log10, default -6: the network's own range).
+// Tightening the bound does not make the network's choices safer: its proposals were
+// learned with the full range, and cutting them short leaves lambda neither where the
+// schedule nor where the network would put it.
 __global__ void k_controller(PlanView pv, WorkView wv, const MlpSmem *Wd, float min_dl) {
   __shared__ MlpSmem m;
   stage_mlp(Wd, m);

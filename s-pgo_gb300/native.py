@@ -31,7 +31,7 @@ EXPORTED = [
 TRACE_MAX = 128
 MLP_PARAMS, MLP_INPUTS, MLP_CACHE_PER_SAMPLE = 5378, 16, 386
 PROFILE_KINDS = ["chain", "linearize", "cost", "pair_reduce", "schur", "assemble", "factor_solve", "backsub",
-                 "update", "bookkeeping", "refine"]
+                 "update", "bookkeeping", "refine", "resid_pass"]
 
 
 class HostProblem(C.Structure):
