@@ -311,7 +311,7 @@ static void build_layout(spgo_plan *p) {
   if (p->precision == SPGO_PREC_MIXED) {
     p->w_facs = take((size_t)p->total_S * 4);
     p->w_twist = take((size_t)p->total_pairs * 6 * 4);
-    p->w_pdual = take((size_t)p->total_pairs * 12 * 8);
+    p->w_pdual = take((size_t)p->total_pairs * 6 * 8);
     p->w_dal = take((size_t)p->L * 8);
     p->w_tl = take((size_t)p->L * 4);
     p->w_gaacc = take((size_t)p->L * 8);

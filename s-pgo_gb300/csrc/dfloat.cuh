@@ -115,9 +115,37 @@ struct df_acc {
 };
 __device__ __forceinline__ double df_acc_value(const df_acc &a) { return (double)a.h + (double)a.l; }
 
+__device__ __forceinline__ df &operator+=(df &a, const df &b) {
+  a = a + b;
+  return a;
+}
+
+// A double split into a double-float with integer operations only (FP64 runs at a
+// small fraction of the FP32 rate on this GPU, conversions included): h = x with its
+// mantissa truncated to 24 bits, l = the remaining 29 bits rounded to 24.  Below 2^-126
+// it becomes 0; beyond the float range, infinity (NaN stays NaN).
+__device__ __forceinline__ df df_split_double(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi32 = (unsigned)(u >> 32), lo32 = (unsigned)u;
+  const int e = (int)((hi32 >> 20) & 0x7ffu) - 1023;  // unbiased exponent
+  const unsigned sign = hi32 & 0x80000000u;
+  if (e < -126) return df{0.f, 0.f};
+  if (e > 127) {  // beyond the float range: infinity, or NaN for a NaN
+    const bool nan = e == 1024 && ((hi32 & 0xfffffu) | lo32) != 0u;
+    return df{__uint_as_float(sign | (nan ? 0x7fc00000u : 0x7f800000u)), 0.f};
+  }
+  const float h = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | ((hi32 & 0xfffffu) << 3) | (lo32 >> 29));
+  // the low 29 mantissa bits carry weight 2^(e - 52)
+  const int el = e - 52;
+  const float scale = el >= -126 ? __uint_as_float((unsigned)(el + 127) << 23) : 0.f;
+  const float l = __uint_as_float(__float_as_uint(__uint2float_rn(lo32 & 0x1fffffffu) * scale) | sign);
+  return df{h, l};
+}
+
 // a - b for plain floats, exactly, as a double-float
 __device__ __forceinline__ df df_sub(float a, float b) { return two_sum(a, -b); }
 
 __device__ __forceinline__ float df_to_float(const df &a) { return a.h + a.l; }
+__device__ __forceinline__ double df_to_double(const df &a) { return (double)a.h + (double)a.l; }
 
 }  // namespace spgo

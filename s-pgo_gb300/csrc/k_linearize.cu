@@ -493,10 +493,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
 //     observation) is formed exactly (two-product) and summed in double-float;
 //     each run of equal target frame goes to the FP64 pair record by an FP64 atomic
 //     (the pair reduction then runs in FP64, k_system.cu);
-//   * the slab terms s (w h)(w j_alpha) likewise, and the per-landmark suffix /
-//     prefix sums along the window and the move to each pose frame run in
-//     double-float; the slab is rounded to FP32 once, at the end.
-// C and g_a (positive sums and the preconditioner's own right-hand side) stay FP32.
+//   * the slab terms s (w h)(w j_alpha) likewise, from the same rounded rows (moved
+//     from the pair origin to the anchor centre in double-float), and the
+//     per-landmark suffix / prefix sums along the window and the move to each pose
+//     frame run in double-float; the slab is rounded to FP32 once, at the end.
+// C and g_a (positive sums and the preconditioner's own right-hand side) stay FP32;
+// g_a is also summed exactly (per observation an exact four-product sum, per landmark
+// FP64) for the refined step's predicted decrease, which near the optimum is a small
+// difference of large terms.
 struct JacSmem {
   float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre (hi)
   float Xl[SPGO_CHUNK][3];  // its low words
@@ -504,6 +508,7 @@ struct JacSmem {
   float C[SPGO_CHUNK], ga[SPGO_CHUNK];
   int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
   int key[8][32];           // per warp: target frame of each lane's observation (-1: none)
+  double gl[8][SPGO_CHUNK]; // per warp: exactly summed g_a
 };
 constexpr int kJacVals = 27;          // 21 Hessian + 6 gradient values per pair record
 constexpr int kJacPitch = 33;
@@ -522,14 +527,6 @@ struct JacLayout {
     total = slab_l + (size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(float);
   }
 };
-
-// a b + c d, exactly rounded to a double-float
-__device__ __forceinline__ df prod2_df(float a, float b, float c, float d) {
-  const df p = two_prod(a, b), q = two_prod(c, d);
-  df t = two_sum(p.h, q.h);
-  t.l += p.l + q.l;
-  return fast_two_sum(t.h, t.l);
-}
 
 __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView wv, Params prm,
                                                          const double *__restrict__ alpha_state, int gate) {
@@ -589,6 +586,7 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
     }
   }
   for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_h[i] = slab_l[i] = 0.f;
+  for (int i = tid; i < 8 * SPGO_CHUNK; i += blockDim.x) (&sm.gl[0][0])[i] = 0.0;
   __syncthreads();
 
   // phase B: thread per observation; runs of equal target frame inside a warp go to
@@ -602,17 +600,18 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
     const int64_t o = base + lane;
     float K[2][2][6];  // [camera][row][parameter]: w K, about the pair origin
     float RW[2][2];    // s w r
+    float JW[2][2];    // s w j_alpha
 #pragma unroll
     for (int c2 = 0; c2 < 2; ++c2)
 #pragma unroll
       for (int r2 = 0; r2 < 2; ++r2) {
-        RW[c2][r2] = 0.f;
+        RW[c2][r2] = JW[c2][r2] = 0.f;
 #pragma unroll
         for (int k = 0; k < 6; ++k) K[c2][r2][k] = 0.f;
       }
-    int key = -1;
+    int key = -1, slot = -1;
     if (o < oe) {
-      const int slot = pv.obs_slot[o];
+      slot = pv.obs_slot[o];
       const int n = pv.obs_frame[o];
       const float4 rl = reinterpret_cast<const float4 *>(res_buf)[o];
       const int a = sm.a[slot];
@@ -623,14 +622,10 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
       const int lo = min(a, n);
       const float sgn = n > a ? 1.f : -1.f;
       const float boost = (prm.near_boost && abs(n - a) < 2) ? 16.f : 1.f;
-      Vec3<float> Xp = X;
-      if (has_pose && lo != a) {  // point relative to the pair origin: left centre of frame lo
-        const Vec3<float> d = FramesT<float>::rel(wv, fo + a, 0, fo + lo, 0);
-        Xp = v3<float>(X.x + d.x, X.y + d.y, X.z + d.z);
-      }
-      df q[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) q[k] = df_make(0.f);
+      // point relative to the pair origin (the left centre of frame lo): X + d
+      Vec3<float> d = v3<float>(0.f, 0.f, 0.f);
+      if (has_pose && lo != a) d = FramesT<float>::rel(wv, fo + a, 0, fo + lo, 0);
+      const Vec3<float> Xp = v3<float>(X.x + d.x, X.y + d.y, X.z + d.z);
       float accC = 0.f, accG = 0.f;
 #pragma unroll
       for (int cam = 0; cam < 2; ++cam) {
@@ -657,26 +652,37 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
         const float ja0 = dot(u0, dXda), ja1 = dot(u1, dXda);
         accC += w2 * (ja0 * ja0 + ja1 * ja1);
         accG += w2 * (ja0 * r0 + ja1 * r1);
+        RW[cam][0] = sgn * (w * r0);
+        RW[cam][1] = sgn * (w * r1);
+        const float jw0 = sgn * (w * ja0), jw1 = sgn * (w * ja1);
+        JW[cam][0] = jw0;
+        JW[cam][1] = jw1;
         if (has_pose) {
           const Vec3<float> k0 = cross(Xp, u0), k1 = cross(Xp, u1);
           K[cam][0][0] = w * k0.x; K[cam][0][1] = w * k0.y; K[cam][0][2] = w * k0.z;
           K[cam][0][3] = w * u0.x; K[cam][0][4] = w * u0.y; K[cam][0][5] = w * u0.z;
           K[cam][1][0] = w * k1.x; K[cam][1][1] = w * k1.y; K[cam][1][2] = w * k1.z;
           K[cam][1][3] = w * u1.x; K[cam][1][4] = w * u1.y; K[cam][1][5] = w * u1.z;
-          RW[cam][0] = sgn * (w * r0);
-          RW[cam][1] = sgn * (w * r1);
-          const Vec3<float> h0 = cross(X, u0), h1 = cross(X, u1);
-          const float jw0 = sgn * (w * ja0), jw1 = sgn * (w * ja1);
-          const float H0[6] = {w * h0.x, w * h0.y, w * h0.z, w * u0.x, w * u0.y, w * u0.z};
-          const float H1[6] = {w * h1.x, w * h1.y, w * h1.z, w * u1.x, w * u1.y, w * u1.z};
-#pragma unroll
-          for (int k = 0; k < 6; ++k) q[k] = q[k] + prod2_df(H0[k], jw0, H1[k], jw1);
         }
       }
       atomicAdd(&sm.C[slot], accC);
       atomicAdd(&sm.ga[slot], accG);
       if (has_pose) {
         key = n;
+        // the observation's slab term q = sum over its rows of (w h)(s w j_alpha), h the
+        // pose row about the anchor centre: from the same rounded rows w K (about the
+        // pair origin, X + d) as the pair records, each value an exact four-product sum,
+        // then moved to the anchor centre in double-float: q_w -= d x q_v
+        df q[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+          q[k] = sum4_prod(K[0][0][k], JW[0][0], K[0][1][k], JW[0][1], K[1][0][k], JW[1][0], K[1][1][k], JW[1][1]);
+        if (lo != a) {
+          const df c0 = q[5] * d.y - q[4] * d.z, c1 = q[3] * d.z - q[5] * d.x, c2 = q[4] * d.x - q[3] * d.y;  // d x q_v
+          q[0] = q[0] - c0;
+          q[1] = q[1] - c1;
+          q[2] = q[2] - c2;
+        }
         // frames after the anchor cover blocks [a, n): row n - 1 feeds a suffix sum;
         // frames before it cover [n, a): row n feeds a prefix sum.  Rows are distinct.
         const int row = (n > a ? n - 1 : n) - f0;
@@ -686,6 +692,19 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
           slab_h[at + k * SPGO_CHUNK] = q[k].h;
           slab_l[at + k * SPGO_CHUNK] = q[k].l;
         }
+      }
+    }
+    {
+      // exactly summed g_a: the observation's j_a^T W r (the signs of JW and RW cancel),
+      // added by the lanes sharing a landmark in rounds of their rank among those peers
+      const double vg = slot >= 0 ? df_to_double(sum4_prod(JW[0][0], RW[0][0], JW[0][1], RW[0][1], JW[1][0],
+                                                           RW[1][0], JW[1][1], RW[1][1]))
+                                  : 0.0;
+      const unsigned peers = __match_any_sync(0xffffffffu, slot);
+      const int rank = __popc(peers & ((1u << lane) - 1u));
+      for (int r = 0; __any_sync(0xffffffffu, slot >= 0 && rank >= r); ++r) {
+        if (slot >= 0 && rank == r) sm.gl[tid >> 5][slot] += vg;
+        __syncwarp();
       }
     }
     // stage the 27 double-float pair values, then lanes 0..26 each sum one value
@@ -788,6 +807,12 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
   if (tid < cnt) {
     reinterpret_cast<float *>(wv.C)[lm0 + tid] = sm.C[tid];
     reinterpret_cast<float *>(wv.ga)[lm0 + tid] = sm.ga[tid];
+    if (wv.gaacc) {
+      double g = 0.0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) g += sm.gl[w][tid];
+      wv.gaacc[lm0 + tid] = g;
+    }
   }
 }
 

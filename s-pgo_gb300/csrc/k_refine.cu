@@ -42,8 +42,6 @@
 
 namespace spgo {
 
-__device__ __forceinline__ double df_to_double(const df &a) { return (double)a.h + (double)a.l; }
-
 // a b + c d exactly rounded to a double-float
 __device__ __forceinline__ df prod2(float a, float b, float c, float d) {
   const df p = two_prod(a, b), q = two_prod(c, d);
@@ -148,22 +146,33 @@ struct RefSmem {
   float t[SPGO_CHUNK];      // D^-1 r_a
   int a[SPGO_CHUNK];
   double dl[kRpWarps][SPGO_CHUNK];  // j_a^T W e, per warp
-  double gl[kRpWarps][SPGO_CHUNK];  // j_a^T W r (first pass), per warp
   int key[kRpWarps][32];
 };
 
-// dynamic shared memory: dc [W][6] float x 2 (hi, lo), then the per-warp staging
-// [warps][2 ncomp][33] float of the pair duals (ncomp = 12 on the first pass, else 6)
-__host__ __device__ inline size_t rp_smem(int max_nb, bool first) {
-  const size_t W = (size_t)max_nb + 1;
-  const size_t dc = ((W * 12 * sizeof(float)) + 15) & ~(size_t)15;
-  return dc + (size_t)kRpWarps * 2 * (first ? 12 : 6) * kRpPitch * sizeof(float);
-}
+// dynamic shared memory (W = window frames): dc [W][6] float x 2 (hi, lo) | the
+// window's frame tables [W][36] (rotations of both cameras, hi then lo words) | the
+// pair origins' offsets [W][4] | the pair twists [W][6] | the per-warp staging
+// [warps][2 x 6][33] float of the pair duals
+struct RpLayout {
+  size_t dc, rw, xpo, tws, stage, total;
+  __host__ __device__ explicit RpLayout(int max_nb) {
+    const size_t W = (size_t)max_nb + 1;
+    auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
+    dc = 0;
+    rw = up(W * 12 * sizeof(float));
+    xpo = rw + up(W * 36 * sizeof(float));
+    tws = xpo + up(W * 4 * sizeof(float));
+    stage = tws + up(W * 6 * sizeof(float));
+    total = stage + (size_t)kRpWarps * 2 * 6 * kRpPitch * sizeof(float);
+  }
+};
 
+// The accurate gradient itself (J^T W r, pose and inverse-depth parts) comes from the
+// linearisation, which sums it exactly (k_linearize.cu, k_system.cu); each pass here
+// forms only the duals of e.
 template <bool FIRST>
-__global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView wv, Params prm,
+__global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkView wv, Params prm,
                                                            const double *__restrict__ alpha_state) {
-  constexpr int NC = FIRST ? 12 : 6;  // double-float dual components staged per observation
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ RefSmem sm;
   const int c = blockIdx.x;
@@ -176,10 +185,14 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
   const float fxs[2] = {intr[0], intr[4]}, fys[2] = {intr[1], intr[5]};
   const double lam = wv.lm[b].lam;
   const float eps = prm.eps;
-  const size_t dcb = (((size_t)(pv.max_nb + 1) * 12 * sizeof(float)) + 15) & ~(size_t)15;
-  float *dch = reinterpret_cast<float *>(smem_raw);
+  const RpLayout lay(pv.max_nb);
+  float *dch = reinterpret_cast<float *>(smem_raw + lay.dc);
   float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
-  float *stage = reinterpret_cast<float *>(smem_raw + dcb);
+  float *Rw = reinterpret_cast<float *>(smem_raw + lay.rw);
+  float *xpo = reinterpret_cast<float *>(smem_raw + lay.xpo);
+  float *tws = reinterpret_cast<float *>(smem_raw + lay.tws);
+  float *stage = reinterpret_cast<float *>(smem_raw + lay.stage);
+  const int D = pv.p_pair_D[b];
   const float *slab = reinterpret_cast<const float *>(wv.slab) + pv.ch_slab[c];
   const float *Cv = reinterpret_cast<const float *>(wv.C);
   const int rows = 6 * nb;
@@ -206,10 +219,7 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
       sm.a[lane] = a;
     }
 #pragma unroll
-    for (int w = 0; w < kRpWarps; ++w) {
-      sm.dl[w][lane] = 0.0;
-      sm.gl[w][lane] = 0.0;
-    }
+    for (int w = 0; w < kRpWarps; ++w) sm.dl[w][lane] = 0.0;
   } else if (warp == 1) {
     // inverse-depth step: first pass x_a = D^-1 (g_a - W^T x_p) from the FP32 system,
     // later x_a += t - D^-1 W^T dx_p (the previous pass's t and pose correction)
@@ -242,8 +252,10 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
       sm.da[lane] = (float)da;
     }
   } else {
-    // the host's left centre minus every window frame's camera centres (double-float)
-    const int fh = fo + pv.lm_host[lm0];
+    // the host's left centre minus every window frame's camera centres (double-float),
+    // the window's frame tables, and per window frame n the offset c_a - c_n of the
+    // pair origin (n < a) and the twist of the pair (a, n)
+    const int ah = pv.lm_host[lm0], fh = fo + ah;
     for (int idx = tid - 64; idx < (nb + 1) * 6; idx += blockDim.x - 64) {
       const int f = idx / 6, cam = (idx / 3) & 1, k = idx % 3;
       const size_t fn = (size_t)(fo + f0 + f);
@@ -252,10 +264,31 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
       dch[idx] = d.h;
       dcl[idx] = d.l;
     }
+    for (int idx = tid - 64; idx < (nb + 1) * 36; idx += blockDim.x - 64) {
+      const int f = idx / 36, r = idx % 36;
+      const size_t fn = (size_t)(fo + f0 + f);
+      Rw[idx] = r < 18 ? wv.fr_Rf[fn * 18 + r] : wv.fr_Rl[fn * 18 + r - 18];
+    }
+    for (int f = tid - 64; f < nb + 1; f += blockDim.x - 64) {
+      const int n = f0 + f;
+      Vec3<float> d = v3<float>(0.f, 0.f, 0.f);
+      if (n < ah) d = FramesT<float>::rel(wv, fh, 0, fo + n, 0);
+      xpo[4 * f] = d.x;
+      xpo[4 * f + 1] = d.y;
+      xpo[4 * f + 2] = d.z;
+      const int lo = min(ah, n), hi = max(ah, n);
+      float t6v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      if (hi > lo && hi - lo <= D) {  // a pair that observations of this chunk can form
+        const float *tw = wv.twist + ((size_t)pv.p_pair_off[b] + (size_t)lo * D + (hi - lo - 1)) * 6;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) t6v[k] = tw[k];
+      }
+#pragma unroll
+      for (int k = 0; k < 6; ++k) tws[6 * f + k] = t6v[k];
+    }
   }
   __syncthreads();
 
-  const int D = pv.p_pair_D[b];
   const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
   const float lscale = prm.loss_scale;
   // residuals at the linearisation point: the state's half of the residual store
@@ -263,14 +296,14 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
   for (int64_t base = ob + (tid & ~31); base < oe; base += blockDim.x) {
     const int64_t o = base + lane;
     // this observation's pose rows s K of both cameras (zero without a pose term), its
-    // inverse-depth rows, and the weighted linearised residuals w^2 e and w^2 r; each
-    // dual is then formed once as the exact sum of its four products
-    float K[2][2][6], JA[2][2], EW[2][2], GW[2][2];
+    // inverse-depth rows, and the weighted linearised residuals w^2 e; each dual is
+    // then formed once as the exact sum of its four products
+    float K[2][2][6], JA[2][2], EW[2][2];
 #pragma unroll
     for (int c2 = 0; c2 < 2; ++c2)
 #pragma unroll
       for (int r2 = 0; r2 < 2; ++r2) {
-        JA[c2][r2] = EW[c2][r2] = GW[c2][r2] = 0.f;
+        JA[c2][r2] = EW[c2][r2] = 0.f;
 #pragma unroll
         for (int k = 0; k < 6; ++k) K[c2][r2][k] = 0.f;
       }
@@ -280,31 +313,24 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
       const int n = pv.obs_frame[o];
       const float4 rl = reinterpret_cast<const float4 *>(res_buf)[o];
       const int a = sm.a[slot];
-      const int fn = fo + n;
+      const int fw = n - f0;
       const bool has_pose = n != a;
-      const int lo = min(a, n), hi = max(a, n);
       const float sgn = n > a ? 1.f : -1.f;
       const float boost = (prm.near_boost && abs(n - a) < 2) ? 16.f : 1.f;
       const float da = sm.da[slot];
       const Vec3<float> X = v3<float>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
       const Vec3<float> dXda = v3<float>(sm.dX[slot][0], sm.dX[slot][1], sm.dX[slot][2]);
-      Vec3<float> Xp = X;
-      float W[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      if (has_pose) {
-        if (lo != a) {  // point relative to the pair origin: left centre of frame lo
-          const Vec3<float> d = FramesT<float>::rel(wv, fo + a, 0, fo + lo, 0);
-          Xp = v3<float>(X.x + d.x, X.y + d.y, X.z + d.z);
-        }
-        const float *tw = wv.twist + ((size_t)pv.p_pair_off[b] + (size_t)lo * D + (hi - lo - 1)) * 6;
+      // point relative to the pair origin (the left centre of frame min(a, n)), the
+      // pair's twist (zero without a pose term)
+      const Vec3<float> Xp = v3<float>(X.x + xpo[4 * fw], X.y + xpo[4 * fw + 1], X.z + xpo[4 * fw + 2]);
+      float W[6];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) W[k] = tw[k];
-      }
+      for (int k = 0; k < 6; ++k) W[k] = tws[6 * fw + k];
 #pragma unroll
       for (int cam = 0; cam < 2; ++cam) {
         // camera-frame point as the linearisation forms it (double-float, rounded once)
-        const float *Rn = FramesT<float>::R(wv, fn, cam);
-        const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
-        const int fw = n - f0;
+        const float *Rn = Rw + fw * 36 + cam * 9;
+        const float *Rl = Rw + fw * 36 + 18 + cam * 9;
         df Xc[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
@@ -342,58 +368,49 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
         JA[cam][1] = ja1;
         EW[cam][0] = w2 * e0;
         EW[cam][1] = w2 * e1;
-        GW[cam][0] = w2 * r0;
-        GW[cam][1] = w2 * r1;
       }
       if (has_pose) key = n;
     }
-    double vle = 0.0, vlg = 0.0;  // this observation's landmark duals
-    if (slot >= 0) {
-      vle = df_to_double(sum4_prod(JA[0][0], EW[0][0], JA[0][1], EW[0][1], JA[1][0], EW[1][0], JA[1][1], EW[1][1]));
-      if (FIRST)
-        vlg = df_to_double(sum4_prod(JA[0][0], GW[0][0], JA[0][1], GW[0][1], JA[1][0], GW[1][0], JA[1][1], GW[1][1]));
-    }
+    const double vle =  // this observation's landmark dual
+        slot >= 0 ? df_to_double(sum4_prod(JA[0][0], EW[0][0], JA[0][1], EW[0][1], JA[1][0], EW[1][0], JA[1][1],
+                                           EW[1][1]))
+                  : 0.0;
     {
       // the warp's own landmark accumulators: lanes sharing a landmark (different
       // frames) add in rounds of their rank among those peers, no atomics
       const unsigned peers = __match_any_sync(0xffffffffu, slot);
       const int rank = __popc(peers & ((1u << lane) - 1u));
       for (int r = 0; __any_sync(0xffffffffu, slot >= 0 && rank >= r); ++r) {
-        if (slot >= 0 && rank == r) {
-          sm.dl[warp][slot] += vle;
-          if (FIRST) sm.gl[warp][slot] += vlg;
-        }
+        if (slot >= 0 && rank == r) sm.dl[warp][slot] += vle;
         __syncwarp();
       }
     }
-    // stage the pair duals, then lanes 0..NC-1 each sum one over the runs of equal
-    // target frame and add each run to its pair record (FP64)
-    float *st = stage + (size_t)warp * 2 * NC * kRpPitch;
+    // stage the six pair duals; then 24 lanes, one per (dual, 8-observation segment),
+    // each sum their segment's runs of equal target frame and add every run to its
+    // pair record (FP64; a run crossing a segment boundary arrives in two parts)
+    float *st = stage + (size_t)warp * 2 * 6 * kRpPitch;
     int *keys = sm.key[warp];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       const df v = sum4_prod(K[0][0][k], EW[0][0], K[0][1][k], EW[0][1], K[1][0][k], EW[1][0], K[1][1][k], EW[1][1]);
       st[(2 * k) * kRpPitch + lane] = v.h;
       st[(2 * k + 1) * kRpPitch + lane] = v.l;
-      if (FIRST) {
-        const df u = sum4_prod(K[0][0][k], GW[0][0], K[0][1][k], GW[0][1], K[1][0][k], GW[1][0], K[1][1][k], GW[1][1]);
-        st[(2 * (6 + k)) * kRpPitch + lane] = u.h;
-        st[(2 * (6 + k) + 1) * kRpPitch + lane] = u.l;
-      }
     }
     keys[lane] = key;
     __syncwarp();
-    if (__any_sync(0xffffffffu, key >= 0) && lane < NC) {
+    if (__any_sync(0xffffffffu, key >= 0) && lane < 24) {
       const int host_a = sm.a[0];
-      const float *ch = st + (2 * lane) * kRpPitch, *cl = st + (2 * lane + 1) * kRpPitch;
-      double *rec0 = wv.pdual + (size_t)pv.p_pair_off[b] * 12 + lane;
-      auto emit = [&](int n, const df_acc &v) {
+      const int v = lane % 6, i0 = (lane / 6) * 8;
+      const float *ch = st + (2 * v) * kRpPitch, *cl = st + (2 * v + 1) * kRpPitch;
+      double *rec0 = wv.pdual + (size_t)pv.p_pair_off[b] * 6 + v;
+      auto emit = [&](int n, const df_acc &a) {
         const int lo = min(host_a, n), hi = max(host_a, n);
-        atomicAdd(rec0 + ((size_t)lo * D + (hi - lo - 1)) * 12, df_acc_value(v));
+        atomicAdd(rec0 + ((size_t)lo * D + (hi - lo - 1)) * 6, df_acc_value(a));
       };
       df_acc acc;
-      int cur = keys[0];
-      for (int i = 0; i < 32; ++i) {
+      int cur = keys[i0];
+#pragma unroll
+      for (int i = i0; i < i0 + 8; ++i) {
         const int k = keys[i];
         if (k != cur) {
           if (cur >= 0) emit(cur, acc);
@@ -412,17 +429,13 @@ __global__ void __launch_bounds__(kRpThreads) k_resid_pass(PlanView pv, WorkView
     const int li = lm0 + tid;
     const float C = Cv[li];
     const float Dd = C * (float)(1.0 + lam) + eps;
-    double dsum = 0.0, gsum = 0.0;
+    double dsum = 0.0;
 #pragma unroll
-    for (int w = 0; w < kRpWarps; ++w) {
-      dsum += sm.dl[w][tid];
-      gsum += sm.gl[w][tid];
-    }
+    for (int w = 0; w < kRpWarps; ++w) dsum += sm.dl[w][tid];
     const double ra = dsum - (lam * (double)C + (double)eps) * wv.dal[li];
     const float t = (float)(ra / (double)Dd);
     sm.t[tid] = t;
     wv.tl[li] = t;
-    if (FIRST) wv.gaacc[li] = gsum;
   } else if (tid < SPGO_CHUNK) {
     sm.t[tid] = 0.f;
   }
@@ -439,7 +452,7 @@ int launch_resid_pass(const PlanView &pv, const WorkView &wv, const Params &prm,
                       void *stream) {
   if (pv.n_chunks == 0) return 0;
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t sm = rp_smem(pv.max_nb, first != 0);
+  const size_t sm = RpLayout(pv.max_nb).total;
   if (first)
     k_resid_pass<true><<<pv.n_chunks, kRpThreads, sm, st>>>(pv, wv, prm, alpha);
   else
@@ -453,132 +466,145 @@ int launch_resid_pass(const PlanView &pv, const WorkView &wv, const Params &prm,
 // n = [m_w + c_lo x m_v ; m_v].  Pose i collects every record with lo <= i < hi,
 // moved to c_i: sum n_w - c_i x sum m_v.  With diff(k) = sum_{lo = k} n - sum_{hi = k} n
 // that sum is the prefix sum of diff up to i.  Then r(i) = [R_i^T (.)_w ; R_i^T (.)_v].
+// The row sums (fixed lo) re-centre linearly: sum_hi n = sum_hi m_w + c_lo x sum_hi m_v;
+// the column sums (fixed hi) take c_lo x m_v per record.  One thread per (row or column,
+// component), no atomics.
 constexpr int kRsThreads = 256;
 
-__host__ __device__ inline size_t rs_layout(int max_Ps, int max_N, size_t *off_cb, size_t *off_y, size_t *off_dinv,
-                                            size_t *off_tmp, size_t *off_L) {
+// shared memory: centres, row and column sums | cb | y | tmp | the packed factor
+// followed by its pivots' reciprocals (as stored by the factorisation)
+__host__ __device__ inline size_t rs_layout(int max_Ps, int max_N, size_t *off_cb, size_t *off_y, size_t *off_tmp,
+                                            size_t *off_L) {
   auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
-  size_t o = up((size_t)(max_N + 1) * 12 * sizeof(double));
+  size_t o = up((size_t)(max_N + 1) * 15 * sizeof(double));  // centres [N+1][3], rows, columns [N+1][6]
   *off_cb = o;
   o = up(o + (size_t)max_Ps * sizeof(int));
   *off_y = o;
   o = up(o + (size_t)max_Ps * sizeof(float));
-  *off_dinv = o;
-  o = up(o + (size_t)max_Ps * sizeof(float));
   *off_tmp = o;
   o = up(o + (size_t)kPanel * sizeof(float));
   *off_L = o;
-  o = up(o + (size_t)max_Ps * (max_Ps + 1) / 2 * sizeof(float));
+  o = up(o + ((size_t)max_Ps * (max_Ps + 1) / 2 + max_Ps) * sizeof(float));
   return o;
 }
 
 size_t resid_solve_smem(int max_P_small, int max_N) {
-  size_t a, b, c, d, e;
-  return rs_layout(max_P_small, max_N, &a, &b, &c, &d, &e);
+  size_t a, b, c, d;
+  return rs_layout(max_P_small, max_N, &a, &b, &c, &d);
 }
 
-template <bool FIRST>
+// 16-byte asynchronous global -> shared copies (no registers held while in flight)
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkView wv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int b = pv.fs_prob[blockIdx.x];
   if (!refine_active(wv, b)) return;
-  constexpr int NC = FIRST ? 12 : 6;
   const int N = pv.p_npose[b], D = pv.p_pair_D[b], P = 6 * N;
   const int fo = pv.p_frame_off[b], po = pv.p_param_off[b];
   const int tid = threadIdx.x, nt = blockDim.x;
-  size_t o_cb, o_y, o_dinv, o_tmp, o_L;
-  rs_layout(pv.max_P_small, pv.max_P / 6, &o_cb, &o_y, &o_dinv, &o_tmp, &o_L);
-  double *diff = reinterpret_cast<double *>(smem_raw);  // [(N + 1)][12]
-  for (int k = tid; k < (N + 1) * 12; k += nt) diff[k] = 0.0;
-  __syncthreads();
-  double *recs = wv.pdual + (size_t)pv.p_pair_off[b] * 12;
-  // thread per lo: its records' row sum in registers, each record's column share by
-  // an atomic on diff(hi) (threads of a warp have distinct lo, hence distinct hi)
-  for (int lo = tid; lo < N; lo += nt) {
-    double Rlo[9], clo[3];
-    frame_Rc(wv, fo + lo, Rlo, clo);
-    double row[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) row[k] = 0.0;
-    for (int d = 1; d <= D && lo + d <= N; ++d) {
-      double *rec = recs + ((size_t)lo * D + d - 1) * 12;
-      const int hi = lo + d;
-#pragma unroll
-      for (int s = 0; s < NC; s += 6) {
-        double m[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          m[k] = rec[s + k];
-          rec[s + k] = 0.0;  // cleared for the next pass
-        }
-        const double n[6] = {m[0] + (clo[1] * m[5] - clo[2] * m[4]), m[1] + (clo[2] * m[3] - clo[0] * m[5]),
-                             m[2] + (clo[0] * m[4] - clo[1] * m[3]), m[3], m[4], m[5]};
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          row[s + k] += n[k];
-          if (n[k] != 0.0) atomicAdd(&diff[hi * 12 + s + k], -n[k]);
-        }
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < NC; ++k) atomicAdd(&diff[lo * 12 + k], row[k]);
+  size_t o_cb, o_y, o_tmp, o_L;
+  rs_layout(pv.max_P_small, pv.max_P / 6, &o_cb, &o_y, &o_tmp, &o_L);
+  const bool small = P <= pv.max_P_small;
+  const size_t npk = (size_t)P * (P + 1) / 2;
+  float *Lm = reinterpret_cast<float *>(smem_raw + o_L);
+  if (small) {
+    // the stored factor and pivots (contiguous, 16-byte aligned: S offsets are multiples
+    // of 36 floats) start copying now and land while the pair duals are reduced
+    const float *fac = wv.facs + pv.p_S_off[b];
+    const size_t n = npk + P, n4 = n / 4;
+    for (size_t k = tid; k < n4; k += nt) cp_async16(Lm + 4 * k, fac + 4 * k);
+    for (size_t k = 4 * n4 + tid; k < n; k += nt) Lm[k] = fac[k];
   }
+  double *cs = reinterpret_cast<double *>(smem_raw);  // [N + 1][3] left camera centres
+  double *rowm = cs + (size_t)(N + 1) * 3;            // [N + 1][6]: sum over hi of m(lo, hi)
+  double *colm = rowm + (size_t)(N + 1) * 6;          // [N + 1][6]: sum over lo of n(lo, hi)
+  for (int k = tid; k < N * 3; k += nt)
+    cs[k] = (double)wv.fr_ch[(size_t)(fo + k / 3) * 6 + k % 3] + (double)wv.fr_cl[(size_t)(fo + k / 3) * 6 + k % 3];
   __syncthreads();
-  if (tid < NC) {  // prefix sums: diff(i) becomes the sum over the records covering pose i
+  double *recs = wv.pdual + (size_t)pv.p_pair_off[b] * 6;
+  for (int t = tid; t < 12 * N; t += nt) {
+    const int k = t % 6;
+    if (t < 6 * N) {  // row lo = t / 6
+      const int lo = t / 6;
+      const double *r = recs + (size_t)lo * D * 6 + k;
+      const int nd = min(D, N - lo);
+      double acc = 0.0;
+#pragma unroll 4
+      for (int d = 0; d < nd; ++d) acc += r[(size_t)d * 6];
+      rowm[lo * 6 + k] = acc;
+    } else {  // column hi = (t - 6 N) / 6 + 1
+      const int hi = (t - 6 * N) / 6 + 1;
+      double acc = 0.0;
+      if (k < 3) {
+        const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+#pragma unroll 4
+        for (int lo = max(0, hi - D); lo < hi; ++lo) {
+          const double *r = recs + ((size_t)lo * D + (hi - lo - 1)) * 6;
+          acc += r[k] + (cs[lo * 3 + k1] * r[3 + k2] - cs[lo * 3 + k2] * r[3 + k1]);
+        }
+      } else {
+#pragma unroll 4
+        for (int lo = max(0, hi - D); lo < hi; ++lo) acc += recs[((size_t)lo * D + (hi - lo - 1)) * 6 + k];
+      }
+      colm[hi * 6 + k] = acc;
+    }
+  }
+  if (tid < 6) colm[tid] = 0.0;  // no record ends at pose 0
+  __syncthreads();
+  for (size_t k = tid; k < (size_t)N * D * 6; k += nt) recs[k] = 0.0;  // cleared for the next pass
+  if (tid < 6) {  // prefix sums over the poses; rowm(i) becomes the sum of the records covering pose i
+    const int k = tid, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
     double acc = 0.0;
     for (int i = 0; i < N; ++i) {
-      acc += diff[i * 12 + tid];
-      diff[i * 12 + tid] = acc;
+      const double *c = cs + i * 3;
+      const double *m = rowm + i * 6;
+      const double nrow = k < 3 ? m[k] + (c[k1] * m[3 + k2] - c[k2] * m[3 + k1]) : m[k];
+      acc += nrow - colm[i * 6 + k];
+      __syncwarp(0x3fu);
+      rowm[i * 6 + k] = acc;  // every lane has read row i's m_v above
     }
   }
   __syncthreads();
-  const bool small = P <= pv.max_P_small;
   float *y = reinterpret_cast<float *>(smem_raw + o_y);
   const double lam = wv.lm[b].lam;
   const float *A = reinterpret_cast<const float *>(wv.A) + pv.p_S_off[b];
   for (int i = tid; i < N; i += nt) {
     double R[9], ci[3];
     frame_Rc(wv, fo + i, R, ci);
+    const double *S = rowm + i * 6;
+    const double w[3] = {S[0] - (ci[1] * S[5] - ci[2] * S[4]), S[1] - (ci[2] * S[3] - ci[0] * S[5]),
+                         S[2] - (ci[0] * S[4] - ci[1] * S[3])};
+    double out[6];
 #pragma unroll
-    for (int s = 0; s < NC; s += 6) {
-      const double *S = diff + i * 12 + s;
-      const double w[3] = {S[0] - (ci[1] * S[5] - ci[2] * S[4]), S[1] - (ci[2] * S[3] - ci[0] * S[5]),
-                           S[2] - (ci[0] * S[4] - ci[1] * S[3])};
-      double out[6];
+    for (int r = 0; r < 3; ++r) {
+      out[r] = R[r] * w[0] + R[3 + r] * w[1] + R[6 + r] * w[2];
+      out[3 + r] = R[r] * S[3] + R[3 + r] * S[4] + R[6 + r] * S[5];
+    }
 #pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        out[r] = R[r] * w[0] + R[3 + r] * w[1] + R[6 + r] * w[2];
-        out[3 + r] = R[r] * S[3] + R[3 + r] * S[4] + R[6 + r] * S[5];
-      }
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        const int p = 6 * i + k;
-        if (s == 0) {
-          const double x = wv.delta[po + p];
-          const double rhs = out[k] - lam * (double)A[(size_t)p * P + p] * x - (double)wv.rhsB[po + p];
-          wv.rhsB[po + p] = 0.f;
-          if (small)
-            y[p] = (float)rhs;
-          else
-            reinterpret_cast<float *>(wv.lg_y)[po + p] = (float)rhs;
-        } else {
-          wv.gacc[po + p] = out[k];
-        }
-      }
+    for (int k = 0; k < 6; ++k) {
+      const int p = 6 * i + k;
+      const double x = wv.delta[po + p];
+      const double rhs = out[k] - lam * (double)A[(size_t)p * P + p] * x - (double)wv.rhsB[po + p];
+      wv.rhsB[po + p] = 0.f;
+      if (small)
+        y[p] = (float)rhs;
+      else
+        reinterpret_cast<float *>(wv.lg_y)[po + p] = (float)rhs;
     }
   }
   if (!small) return;  // the multi-CTA substitutions (k_chol_large.cu) follow
   int *cb = reinterpret_cast<int *>(smem_raw + o_cb);
-  float *dinv = reinterpret_cast<float *>(smem_raw + o_dinv);
   float *tmp = reinterpret_cast<float *>(smem_raw + o_tmp);
-  float *Lm = reinterpret_cast<float *>(smem_raw + o_L);
-  const size_t npk = (size_t)P * (P + 1) / 2;
-  const float *fac = wv.facs + pv.p_S_off[b];
-  for (size_t k = tid; k < npk; k += nt) Lm[k] = fac[k];
-  for (int k = tid; k < P; k += nt) {
-    dinv[k] = fac[npk + k];
-    cb[k] = k * P - (k * (k + 1)) / 2;
-  }
+  const float *dinv = Lm + npk;
+  for (int k = tid; k < P; k += nt) cb[k] = k * P - (k * (k + 1)) / 2;
+  cp_async_wait_all();
   __syncthreads();
   chol_substitute<float>(Lm, cb, y, dinv, tmp, P);
   for (int k = tid; k < P; k += nt) {
@@ -589,15 +615,11 @@ __global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkVie
 }
 
 int launch_resid_solve(const PlanView &pv, const WorkView &wv, int first, void *stream) {
+  (void)first;  // every pass reduces the same duals of e
   const size_t sm = resid_solve_smem(pv.max_P_small, pv.max_P / 6);
   cudaStream_t st = (cudaStream_t)stream;
-  if (first) {
-    cudaFuncSetAttribute(k_resid_solve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_resid_solve<true><<<pv.B, kRsThreads, sm, st>>>(pv, wv);
-  } else {
-    cudaFuncSetAttribute(k_resid_solve<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_resid_solve<false><<<pv.B, kRsThreads, sm, st>>>(pv, wv);
-  }
+  cudaFuncSetAttribute(k_resid_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_resid_solve<<<pv.B, kRsThreads, sm, st>>>(pv, wv);
   ++g_launches;
   return (int)cudaGetLastError();
 }

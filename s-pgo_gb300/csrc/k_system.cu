@@ -12,8 +12,10 @@
 // kept about a nearby camera centre, so the working precision (FP32 in the
 // mixed path) never sees world-sized lever arms.
 // g(i) = Ad_i^T sum_{lo <= i < hi} m_{lo,hi} is the e = 0 diagonal of the same sums.
+#include <type_traits>
 #include "kernels.cuh"
 #include "frames.cuh"
+#include "dfloat.cuh"
 
 namespace spgo {
 
@@ -35,14 +37,17 @@ __device__ __forceinline__ constexpr int t6(int i, int j) {  // symmetric 6x6 up
 // component, which matters in FP64):
 //   (Z R)[:, j] = z x R[:, j],  (Q Z)[i, :] = -(z x Q[i, :]),  ((Z R) Z)[i, :] = -(z x (Z R)[i, :]),
 //   P' = P - Q Z - (Q Z)^T - (Z R) Z,  Q' = Q + Z R,  m_w' = m_w + z x m_v.
-__device__ __forceinline__ void cross3(const double *a, const double *b, double *o) {
+template <typename V>
+__device__ __forceinline__ void cross3(const V *a, const V *b, V *o) {
   o[0] = a[1] * b[2] - a[2] * b[1];
   o[1] = a[2] * b[0] - a[0] * b[2];
   o[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-__device__ __forceinline__ void shift_record(double *v, const double *z) {
-  double P[3][3], Q[3][3], R[3][3];
+// V = double, or df (the mixed path's reduction, on the FP32 pipes)
+template <typename V>
+__device__ __forceinline__ void shift_record(V *v, const V *z) {
+  V P[3][3], Q[3][3], R[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -51,11 +56,11 @@ __device__ __forceinline__ void shift_record(double *v, const double *z) {
       Q[a][c] = v[t6(a, 3 + c)];
       R[a][c] = v[t6(3 + a, 3 + c)];
     }
-  double ZR[3][3], QZ[3][3], ZRZ[3][3];
+  V ZR[3][3], QZ[3][3], ZRZ[3][3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) {  // columns of Z R
-    const double rc[3] = {R[0][j], R[1][j], R[2][j]};
-    double o[3];
+    const V rc[3] = {R[0][j], R[1][j], R[2][j]};
+    V o[3];
     cross3(z, rc, o);
     ZR[0][j] = o[0];
     ZR[1][j] = o[1];
@@ -63,7 +68,7 @@ __device__ __forceinline__ void shift_record(double *v, const double *z) {
   }
 #pragma unroll
   for (int i = 0; i < 3; ++i) {  // rows of Q Z and (Z R) Z
-    double o[3];
+    V o[3];
     cross3(z, Q[i], o);
     QZ[i][0] = -o[0];
     QZ[i][1] = -o[1];
@@ -80,8 +85,8 @@ __device__ __forceinline__ void shift_record(double *v, const double *z) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) v[t6(a, 3 + c)] = Q[a][c] + ZR[a][c];
   }
-  const double mv[3] = {v[24], v[25], v[26]};
-  double o[3];
+  const V mv[3] = {v[24], v[25], v[26]};
+  V o[3];
   cross3(z, mv, o);
   v[21] += o[0];
   v[22] += o[1];
@@ -247,26 +252,203 @@ __global__ void k_pairs_to_A(PlanView pv, WorkView wv) {
   if (e == 0) {
     const T *f = F + 21;
     TO *g = reinterpret_cast<TO *>(wv.g) + pv.p_param_off[b] + 6 * i;
+    T gi[6];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-      g[r] = (TO)(Ri[r] * f[0] + Ri[3 + r] * f[1] + Ri[6 + r] * f[2]);
-      g[3 + r] = (TO)(Ri[r] * f[3] + Ri[3 + r] * f[4] + Ri[6 + r] * f[5]);
+      gi[r] = Ri[r] * f[0] + Ri[3 + r] * f[1] + Ri[6 + r] * f[2];
+      gi[3 + r] = Ri[r] * f[3] + Ri[3 + r] * f[4] + Ri[6 + r] * f[5];
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) g[r] = (TO)gi[r];
+    if (wv.gacc) {  // the mixed path's refined step: the gradient unrounded, for its predicted decrease
+      double *ga = wv.gacc + pv.p_param_off[b] + 6 * i;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) ga[r] = (double)gi[r];
     }
   }
 }
 
-// The pose-pair records are FP64 on both paths; the reduction runs in FP64 and the
-// mixed path (T = float) stores A and g as FP32.
+// ---- the mixed path's pair reduction, in double-float ----------------------------
+// The records arrive as FP64 sums (the linearisation's atomics).  FP64 arithmetic runs at
+// a small fraction of the FP32 rate on this GPU, so the reduction runs in double-float
+// (~48 bits on the FP32 pipes, far more than the FP32 blocks it produces keep).  Instead
+// of re-centring a running sum along each chain (a serial chain of shifts), every record
+// is moved once to the problem's own origin o = c_0 (its lever arms are at most the
+// window's extent, tens of metres, which costs a few of the 48 bits), the prefix and
+// suffix sums run about o, and each block moves its sum from o to c_i on the way to A.
+__device__ __forceinline__ void df_rel_c(const WorkView &wv, int fx, int fy, df *z) {  // c_x - c_y, left cameras
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    z[k] = df_sub(wv.fr_ch[(size_t)fx * 6 + k], wv.fr_ch[(size_t)fy * 6 + k]) +
+           df_make(wv.fr_cl[(size_t)fx * 6 + k] - wv.fr_cl[(size_t)fy * 6 + k]);
+}
+
+constexpr int kPrThreads = 256;
+
+// one CTA per problem: 0. records read, cleared, split and moved from c_lo to o;
+// 1. thread per (hi, component): prefix over lo, P(i, hi) = sum_{lo <= i} M(lo, hi);
+// 2. thread per (i, component): suffix over hi, F(i, i + e) = sum_{d > e} P(i, i + d)
+__global__ void __launch_bounds__(kPrThreads) k_pair_reduce_df(PlanView pv, WorkView wv) {
+  const int b = blockIdx.x;
+  if (!problem_active(wv.lm, b, GATE_RELIN)) return;
+  const int N = pv.p_npose[b], D = pv.p_pair_D[b];
+  const int fo = pv.p_frame_off[b];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double *acc = reinterpret_cast<double *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
+  df *F = reinterpret_cast<df *>(wv.pairF) + (size_t)pv.p_pair_off[b] * 27;
+  for (int r = tid; r < N * D; r += nt) {
+    const int lo = r / D, hi = lo + r % D + 1;
+    if (hi > N) continue;
+    double *rec = acc + (size_t)r * 27;
+    df v[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) v[k] = df_split_double(rec[k]);
+#pragma unroll
+    for (int k = 0; k < 27; ++k) rec[k] = 0.0;  // cleared for the next linearisation
+    if (lo > 0) {
+      df z[3];
+      df_rel_c(wv, fo + lo, fo, z);  // from c_lo to o = c_0
+      shift_record(v, z);
+    }
+    df *out = F + (size_t)r * 27;
+#pragma unroll
+    for (int k = 0; k < 27; ++k) out[k] = v[k];
+  }
+  __syncthreads();
+  for (int t = tid; t < N * 27; t += nt) {
+    const int hi = t / 27 + 1, comp = t % 27;
+    df s = df_make(0.f);
+#pragma unroll 4
+    for (int lo = max(0, hi - D); lo < hi; ++lo) {
+      df *x = F + ((size_t)lo * D + (hi - lo - 1)) * 27 + comp;
+      s = s + *x;
+      *x = s;
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < N * 27; t += nt) {
+    const int i = t / 27, comp = t % 27;
+    df s = df_make(0.f);
+#pragma unroll 4
+    for (int dp = min(D, N - i); dp >= 1; --dp) {
+      df *x = F + ((size_t)i * D + dp - 1) * 27 + comp;
+      s = s + *x;
+      *x = s;
+    }
+  }
+}
+
+// A(i, j) = Ad_i^T F(i, j) Ad_j about c_i (F moved there from o first) and g(i), in
+// double-float, rounded once to FP32; the unrounded g also to gacc (the refined step's
+// predicted decrease)
+__global__ void __launch_bounds__(128) k_pairs_to_A_df(PlanView pv, WorkView wv) {
+  const int b = blockIdx.y;
+  if (!problem_active(wv.lm, b, GATE_RELIN)) return;
+  const int N = pv.p_npose[b], D = pv.p_pair_D[b];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= N * D) return;
+  const int i = t / D, e = t % D;
+  if (e >= min(D, N - i)) return;
+  const int j = i + e;
+  const int P = 6 * N;
+  const int fo = pv.p_frame_off[b];
+  const df *Fg = reinterpret_cast<const df *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + (size_t)i * D + e) * 27;
+  df F[27], Ri[9], Rj[9];
+#pragma unroll
+  for (int k = 0; k < 27; ++k) F[k] = Fg[k];
+  {
+    const float *h = wv.fr_Rf + (size_t)(fo + i) * 18, *l = wv.fr_Rl + (size_t)(fo + i) * 18;
+    const float *hj = wv.fr_Rf + (size_t)(fo + j) * 18, *lj = wv.fr_Rl + (size_t)(fo + j) * 18;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      Ri[k] = df{h[k], l[k]};
+      Rj[k] = df{hj[k], lj[k]};
+    }
+  }
+  if (i > 0) {
+    df z[3];
+    df_rel_c(wv, fo, fo + i, z);  // from o = c_0 to c_i
+    shift_record(F, z);
+  }
+  df cji[3];
+  df_rel_c(wv, fo + j, fo + i, cji);
+  // C R_j with C = [c_j - c_i]x
+  df CRj[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    CRj[c] = cji[1] * Rj[6 + c] - cji[2] * Rj[3 + c];
+    CRj[3 + c] = cji[2] * Rj[c] - cji[0] * Rj[6 + c];
+    CRj[6 + c] = cji[0] * Rj[3 + c] - cji[1] * Rj[c];
+  }
+  float out[6][6];
+#pragma unroll
+  for (int col = 0; col < 6; ++col) {
+    // column col of Ad_j: [R_j e_col ; C R_j e_col] (col < 3), [0 ; R_j e_(col-3)]
+    df w[6];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      df a = col < 3 ? F[t6(r, 0)] * Rj[col] + F[t6(r, 1)] * Rj[3 + col] + F[t6(r, 2)] * Rj[6 + col]
+                     : df_make(0.f);
+      const int cc = col < 3 ? col : col - 3;
+      const df *ad = col < 3 ? CRj : Rj;
+      a = a + F[t6(r, 3)] * ad[cc] + F[t6(r, 4)] * ad[3 + cc] + F[t6(r, 5)] * ad[6 + cc];
+      w[r] = a;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      out[r][col] = df_to_float(Ri[r] * w[0] + Ri[3 + r] * w[1] + Ri[6 + r] * w[2]);
+      out[3 + r][col] = df_to_float(Ri[r] * w[3] + Ri[3 + r] * w[4] + Ri[6 + r] * w[5]);
+    }
+  }
+  float *A = reinterpret_cast<float *>(wv.A) + pv.p_S_off[b];
+#pragma unroll
+  for (int r = 0; r < 6; ++r)
+#pragma unroll
+    for (int c = 0; c < 6; c += 2)
+      *reinterpret_cast<float2 *>(A + (size_t)(6 * i + r) * P + 6 * j + c) = make_float2(out[r][c], out[r][c + 1]);
+  if (i != j) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+#pragma unroll
+      for (int r = 0; r < 6; r += 2)
+        *reinterpret_cast<float2 *>(A + (size_t)(6 * j + c) * P + 6 * i + r) = make_float2(out[r][c], out[r + 1][c]);
+  }
+  if (e == 0) {
+    const df *f = F + 21;
+    float *g = reinterpret_cast<float *>(wv.g) + pv.p_param_off[b] + 6 * i;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const df gw = Ri[r] * f[0] + Ri[3 + r] * f[1] + Ri[6 + r] * f[2];
+      const df gv = Ri[r] * f[3] + Ri[3 + r] * f[4] + Ri[6 + r] * f[5];
+      g[r] = df_to_float(gw);
+      g[3 + r] = df_to_float(gv);
+      if (wv.gacc) {
+        wv.gacc[pv.p_param_off[b] + 6 * i + r] = df_to_double(gw);
+        wv.gacc[pv.p_param_off[b] + 6 * i + 3 + r] = df_to_double(gv);
+      }
+    }
+  }
+}
+
+// The pose-pair records are FP64 sums on both paths.  The FP64 path reduces them in
+// FP64 along each chain; the mixed path (T = float) in double-float about one origin
+// per problem, storing A and g as FP32.
 template <typename T>
 int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream) {
   (void)gate;
   cudaStream_t st = (cudaStream_t)stream;
   const int nmax = pv.max_P / 6;
   const int nd = pv.max_D > 0 ? pv.max_D : 1;
-  k_pair_prefix_rec<<<dim3(grid_for(nmax, 64), pv.B), 64, 0, st>>>(pv, wv);
-  k_pair_suffix<double><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);
-  k_pairs_to_A<double, T><<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
-  g_launches += 3;
+  if constexpr (std::is_same<T, float>::value) {
+    k_pair_reduce_df<<<pv.B, kPrThreads, 0, st>>>(pv, wv);
+    k_pairs_to_A_df<<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
+    g_launches += 2;
+  } else {
+    k_pair_prefix_rec<<<dim3(grid_for(nmax, 64), pv.B), 64, 0, st>>>(pv, wv);
+    k_pair_suffix<double><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);
+    k_pairs_to_A<double, T><<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
+    g_launches += 3;
+  }
   return (int)cudaGetLastError();
 }
 

@@ -122,11 +122,11 @@ struct WorkView {
   // iterative refinement of the mixed path's step (k_refine.cu); null on the FP64 path
   float *facs;          // [total_S] per problem: packed FP32 Cholesky factor, then 1 / L_kk
   float *twist;         // [total_pairs][6] sum over the pair's poses of Ad_i delta_i (about c_lo)
-  double *pdual;        // [total_pairs][12] J^T e (0..5) and J^T r (6..11) per pose pair
+  double *pdual;        // [total_pairs][6] J^T W e per pose pair, about c_lo
   double *dal;          // [L] internal order: the inverse-depth step so far
   float *tl;            // [L] internal order: D^-1 r_a of the last residual pass
-  double *gaacc;        // [L] internal order: accurate inverse-depth gradient
-  double *gacc;         // [total_params] accurate pose gradient
+  double *gaacc;        // [L] internal order: exactly summed inverse-depth gradient (linearisation)
+  double *gacc;         // [total_params] exactly summed pose gradient (linearisation)
   float *rhsB;          // [total_params] B D^-1 r_a of the last residual pass
   double *ddelta;       // [total_params] the last pose correction
 };

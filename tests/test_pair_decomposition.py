@@ -16,8 +16,9 @@ per-(lo, hi) records M = sum w^2 K^T K over lo <= i, hi > j, each moved to a com
 origin by E_z = [[I, 0], [-[z]x, I]] (M -> E_z^T M E_z).  This file restates that
 assembly as the kernels run it (csrc/k_linearize.cu: records about the left centre
 of frame lo; csrc/k_system.cu: prefix over lo re-centred step by step onto row i's
-centre, suffix over hi, then Ad_i^T F Ad_j about c_i) and checks A, g and the
-pose-depth blocks B against the oracle's dense products.
+centre, suffix over hi, then Ad_i^T F Ad_j about c_i; the mixed path's variant with
+one origin per problem) and checks A, g and the pose-depth blocks B against the
+oracle's dense products.
 """
 import numpy as np
 import pytest
@@ -46,8 +47,12 @@ def Ad(R, c, x):
     return a
 
 
-def pair_assembly(prob, loss):
-    """A, g_T, B of the problem assembled the way the kernels do (FP64)."""
+def pair_assembly(prob, loss, one_origin=False):
+    """A, g_T, B of the problem assembled the way the kernels do (FP64).  one_origin:
+    the mixed path's order (csrc/k_system.cu k_pair_reduce_df, k_pairs_to_A_df; the slab
+    terms of csrc/k_linearize.cu k_jacobian_acc): every record moved once from c_lo to
+    c_0, prefix and suffix sums about c_0, each block moved from c_0 to c_i; the slab
+    terms formed from the rows about the pair origin and moved to the anchor centre."""
     N = int(prob.n_poses)
     P = 6 * N
     G = S.global_poses(prob.poses)
@@ -73,9 +78,14 @@ def pair_assembly(prob, loss):
             K = np.concatenate([np.cross(Xw[o] - cw[lo[o]], u[o]), u[o]], -1)   # about c_lo
             M[lo[o], hi[o]] += w2[o] * K.T @ K
             m[lo[o], hi[o]] += sgn[o] * w2[o] * K.T @ res[o]
-            Ka = np.concatenate([np.cross(Xw[o] - cw[a[o]], u[o]), u[o]], -1)   # about c_a
+            if one_origin:
+                q = sgn[o] * w2[o] * K.T @ ja[o]                                  # about c_lo
+                q[:3] -= np.cross(cw[a[o]] - cw[lo[o]], q[3:])                    # to c_a
+            else:
+                Ka = np.concatenate([np.cross(Xw[o] - cw[a[o]], u[o]), u[o]], -1)   # about c_a
+                q = sgn[o] * w2[o] * Ka.T @ ja[o]
             for i in range(lo[o], hi[o]):
-                b[lm[o], i] += sgn[o] * w2[o] * Ka.T @ ja[o]
+                b[lm[o], i] += q
 
     # pass A: P(i, hi) = sum_{lo <= i} M(lo, hi), the running sum moved from c_{lo-1}
     # to c_lo before each record is added (every partial sum about its row's centre)
@@ -84,11 +94,20 @@ def pair_assembly(prob, loss):
     for h in range(1, N + 1):
         acc, gacc = np.zeros((6, 6)), np.zeros(6)
         for lo_ in range(h):
-            if lo_ > 0:
-                e = E(cw[lo_ - 1] - cw[lo_])
-                acc, gacc = e.T @ acc @ e, e.T @ gacc
-            acc, gacc = acc + M[lo_, h], gacc + m[lo_, h]
+            if one_origin:   # each record moved from c_lo to c_0, plain sums
+                e = E(cw[lo_] - cw[0])
+                acc, gacc = acc + e.T @ M[lo_, h] @ e, gacc + e.T @ m[lo_, h]
+            else:
+                if lo_ > 0:
+                    e = E(cw[lo_ - 1] - cw[lo_])
+                    acc, gacc = e.T @ acc @ e, e.T @ gacc
+                acc, gacc = acc + M[lo_, h], gacc + m[lo_, h]
             Pf[lo_, h], pf[lo_, h] = acc, gacc
+    if one_origin:   # each row's sums moved from c_0 to c_i
+        for i in range(N):
+            e = E(cw[0] - cw[i])
+            for h in range(i + 1, N + 1):
+                Pf[i, h], pf[i, h] = e.T @ Pf[i, h] @ e, e.T @ pf[i, h]
     # pass B: F(i, j) = sum_{hi > j} P(i, hi), all about c_i;  A(i, j) = Ad_i^T F Ad_j
     A = np.zeros((P, P))
     g = np.zeros(P)
@@ -108,24 +127,26 @@ def pair_assembly(prob, loss):
     return A, g, B
 
 
+@pytest.mark.parametrize("one_origin", [False, True], ids=["chain", "one_origin"])
 @pytest.mark.parametrize("loss", [S.Loss(), S.REFERENCE_GPU_LOSS, S.Loss(S.LOSS_HUBER, 2.0)],
                          ids=["l2", "cauchy_near_boost", "huber"])
-def test_pair_assembly_matches_dense_products(loss):
+def test_pair_assembly_matches_dense_products(loss, one_origin):
     p = scenes.circle_scene(5, 6, 60)
     lin = S.linearize(p, loss)
-    A, g, B = pair_assembly(p, loss)
+    A, g, B = pair_assembly(p, loss, one_origin)
     scale = lambda x: max(np.abs(x).max(), 1e-300)
     assert np.abs(A - lin.A).max() / scale(lin.A) < 1e-11
     assert np.abs(g - lin.g_T).max() / scale(lin.g_T) < 1e-11
     assert np.abs(B - lin.B).max() / scale(lin.B) < 1e-11
 
 
-def test_pair_assembly_covisibility_window():
+@pytest.mark.parametrize("one_origin", [False, True], ids=["chain", "one_origin"])
+def test_pair_assembly_covisibility_window(one_origin):
     """A corridor with a 4-frame covisibility window: the records only span
     hi - lo <= window, and the prefix / suffix sums still give the dense blocks."""
     p = scenes.corridor_scene(3, 9, 120, window=4)
     lin = S.linearize(p, S.REFERENCE_GPU_LOSS)
-    A, g, B = pair_assembly(p, S.REFERENCE_GPU_LOSS)
+    A, g, B = pair_assembly(p, S.REFERENCE_GPU_LOSS, one_origin)
     assert np.abs(A - lin.A).max() / np.abs(lin.A).max() < 1e-11
     assert np.abs(g - lin.g_T).max() / np.abs(lin.g_T).max() < 1e-11
     assert np.abs(B - lin.B).max() / np.abs(lin.B).max() < 1e-11
