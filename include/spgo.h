@@ -132,7 +132,8 @@ typedef struct spgo_params {
                                     residual J^T (r - J x) - Lambda x formed from the FP32
                                     Jacobian with exact products and FP64-grade sums; the FP32
                                     system (pose Hessian, tensor-core Schur complement, FP32
-                                    Cholesky) only preconditions.  0: the FP32 step as solved */
+                                    Cholesky) only preconditions.  Default 1; 0: the FP32 step
+                                    as solved */
     int32_t wait_us;             /* limit of every bounded device-side wait, microseconds
                                     (0: 2 s).  Shortening it only makes waits give up sooner:
                                     the problem is flagged and its step rejected */

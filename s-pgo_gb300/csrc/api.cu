@@ -977,7 +977,7 @@ void spgo_default_params(spgo_params *p) {
   p->refine_steps = 1;
   p->use_graph = 1;
   p->use_tc = 1;
-  p->outer_steps = 2;
+  p->outer_steps = 1;
   p->wait_us = 0;
   p->ctl_min_log10 = -6.0f;
 }

@@ -283,7 +283,7 @@ __device__ __forceinline__ void df_rel_c(const WorkView &wv, int fx, int fy, df 
            df_make(wv.fr_cl[(size_t)fx * 6 + k] - wv.fr_cl[(size_t)fy * 6 + k]);
 }
 
-constexpr int kPrThreads = 256;
+constexpr int kPrThreads = 512;
 
 // one CTA per problem: 0. records read, cleared, split and moved from c_lo to o;
 // 1. thread per (hi, component): prefix over lo, P(i, hi) = sum_{lo <= i} M(lo, hi);
@@ -315,25 +315,40 @@ __global__ void __launch_bounds__(kPrThreads) k_pair_reduce_df(PlanView pv, Work
     for (int k = 0; k < 27; ++k) out[k] = v[k];
   }
   __syncthreads();
+  // the running sums: eight records loaded before any is summed and stored back (the
+  // stores could alias later loads, so without that each step is a round trip)
   for (int t = tid; t < N * 27; t += nt) {
     const int hi = t / 27 + 1, comp = t % 27;
     df s = df_make(0.f);
-#pragma unroll 4
-    for (int lo = max(0, hi - D); lo < hi; ++lo) {
-      df *x = F + ((size_t)lo * D + (hi - lo - 1)) * 27 + comp;
-      s = s + *x;
-      *x = s;
+    for (int lo0 = max(0, hi - D); lo0 < hi; lo0 += 8) {
+      df v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (lo0 + q < hi) v[q] = F[((size_t)(lo0 + q) * D + (hi - lo0 - q - 1)) * 27 + comp];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (lo0 + q < hi) {
+          s = s + v[q];
+          F[((size_t)(lo0 + q) * D + (hi - lo0 - q - 1)) * 27 + comp] = s;
+        }
     }
   }
   __syncthreads();
   for (int t = tid; t < N * 27; t += nt) {
     const int i = t / 27, comp = t % 27;
+    df *base = F + (size_t)i * D * 27 + comp;
     df s = df_make(0.f);
-#pragma unroll 4
-    for (int dp = min(D, N - i); dp >= 1; --dp) {
-      df *x = F + ((size_t)i * D + dp - 1) * 27 + comp;
-      s = s + *x;
-      *x = s;
+    for (int dp0 = min(D, N - i); dp0 >= 1; dp0 -= 8) {
+      df v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (dp0 - q >= 1) v[q] = base[(size_t)(dp0 - q - 1) * 27];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (dp0 - q >= 1) {
+          s = s + v[q];
+          base[(size_t)(dp0 - q - 1) * 27] = s;
+        }
     }
   }
 }

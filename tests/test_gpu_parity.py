@@ -417,3 +417,27 @@ def test_lm_trace_matches_status(built_lib, cuda_device):
         assert np.allclose(t["cost"], ref_cost, rtol=1e-9, atol=0)
         assert np.allclose(t["lam"], [x["lam"] for x in res.trace], rtol=1e-9, atol=0)
     bs.close()
+
+
+@pytest.mark.parametrize("config", ["config1", "config2"])
+def test_large_path_step_matches_fp64_step(built_lib, cuda_device, config):
+    """Configs 1 and 2 at full size (P = 600 and 3000: the multi-CTA factorisation and
+    substitutions): the mixed path's first damped step (FP32 Cholesky preconditioning a
+    step refined against the accurately summed residual of the whole system) against the
+    FP64 path's step from the same state, relative to the step's size: poses and inverse
+    depths within 1e-5 (the mixed step's own floor is the FP32 Jacobian, ~1e-7)."""
+    p = getattr(scenes, config)()
+    loss = dict(loss="huber", loss_scale=2.0) if config == "config2" else dict(loss="l2")
+    out = {}
+    for prec in ("fp64", "mixed"):
+        bs = BatchSolver([f32_obs(p)], precision=prec)
+        bs.set_params(max_iters=1, tol=0.0, lambda0=1e-2, **loss)
+        st = bs.solve()[0]
+        assert st["accepted"] == 1 and st["factor_failures"] == 0 and st["wait_timeouts"] == 0, st
+        out[prec] = (bs.get_poses(0) - p.poses, bs.get_alpha(0) - p.alpha, st["cost"])
+        bs.close()
+    dp = np.abs(out["mixed"][0] - out["fp64"][0]).max() / np.abs(out["fp64"][0]).max()
+    da = np.abs(out["mixed"][1] - out["fp64"][1]).max() / np.abs(out["fp64"][1]).max()
+    dc = abs(out["mixed"][2] - out["fp64"][2]) / out["fp64"][2]
+    print(f"{config}: pose step {dp:.2e}, inverse-depth step {da:.2e}, cost after the step {dc:.2e}")
+    assert dp < 1e-5 and da < 1e-5 and dc < 1e-7
