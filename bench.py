@@ -334,9 +334,12 @@ def run_ours(args):
         base_params["outer_steps"] = args.outer
     tuned = None
 
+    plan_opts, plan_tune = None, None
+
     def make(precision, controller=None):
         """A solver of the batch; controller: deployed network weights or None (Nielsen)."""
-        s = sv.BatchSolver(probs, precision=precision, device=dev, stream=stream)
+        s = sv.BatchSolver(probs, precision=precision, device=dev, stream=stream,
+                           plan_options=plan_opts if precision == "mixed" else None)
         if precision == "mixed":
             s.set_params(**base_params)
             if tuned is not None:  # later solvers of the same batch reuse the tuned shapes
@@ -354,6 +357,12 @@ def run_ours(args):
         bs.set_params(**tuned)
     elif args.autotune:
         tuned = bs.autotune()  # launch shapes timed on this batch (untimed, before the warm-up)
+        # plan-time Schur work shapes, timed on this batch with the tuned launch shapes; the
+        # chosen form is re-planned with the fastest
+        plan_tune = bs.autotune_plan_shapes()
+        plan_opts = plan_tune["best"]
+        bs.close()
+        bs = make("mixed", ctl_params)
     else:
         tuned = dict(cost_block=bs.params.cost_block, lin_block=bs.params.lin_block, use_tc=bs.params.use_tc)
     p0, a0 = bs.poses.clone(), bs.alpha.clone()
@@ -574,7 +583,8 @@ def run_ours(args):
     t0 = time.perf_counter()
     stream_reached = []
     for _st, _poses, _alphas in sv.solve_stream([probs] * n_stream, "mixed", stream_params, ctl_params, device=dev,
-                                                inflight=args.inflight, check_every=args.check_every):
+                                                inflight=args.inflight, check_every=args.check_every,
+                                                plan_options=plan_opts):
         if plain_costs is not None:
             stream_reached.append(float(_reached([s["cost"] for s in _st], plain_costs).mean()))
     torch.cuda.synchronize(dev)
@@ -592,7 +602,7 @@ def run_ours(args):
                        "chosen_max_iters": int(args.max_iters),
                        "schur": "tcgen05 split TF32" if tuned["use_tc"] else "SIMT FP32",
                        "damping": "learned MLP + Nielsen fallback" if ctl_params is not None else "Nielsen",
-                       "autotuned": tuned,
+                       "autotuned": tuned, "autotuned_plan": plan_tune,
                        "l2": "256 MB flush written between timed steps",
                        "parallelism": f"replicas x{world} (independent batches)",
                        "iterations_max": int(max(iters)), "iterations_mean": float(np.mean(iters)),

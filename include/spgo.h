@@ -105,7 +105,20 @@ typedef struct spgo_plan_sizes {
     int64_t schur_flops_landmark; /* algorithmic FLOPs of the landmark Schur complement:
                                     sum over landmarks of 2 (6 k)^2, k = pose blocks its
                                     Jacobian spans (no chunk padding, no split products) */
+    int32_t tc_split;            /* the plan's Schur work shapes (spgo_plan_options) */
+    int32_t simt_split;
 } spgo_plan_sizes;
+
+/* Plan-time shapes of the Schur complement's work lists (spgo_plan_create_opts; a
+ * zero field takes its default).  tc_split: landmark chunks per tensor-core work item
+ * (one 128x128 output tile), 1..64, default 64; simt_split: chunks per SIMT work item
+ * (one 48x48 tile), 1..64, default 16.  Fewer chunks per item: more CTAs, more partial
+ * tiles added into S_L.  BatchSolver.autotune_plan times them on the caller's batch. */
+typedef struct spgo_plan_options {
+    int32_t tc_split;
+    int32_t simt_split;
+    int32_t reserved[6];         /* zero */
+} spgo_plan_options;
 
 /* solver parameters */
 typedef struct spgo_params {
@@ -119,7 +132,10 @@ typedef struct spgo_params {
     double  lambda_max;
     double  tol;                 /* relative cost decrease that counts as converged */
     int32_t max_iters;           /* per-problem LM iteration cap                 */
-    int32_t refine_steps;        /* FP64 iterative-refinement steps (mixed precision) */
+    int32_t refine_steps;        /* mixed path with outer_steps = 0: refinement steps of the
+                                    reduced solve against the exactly assembled S (default 1);
+                                    with outer_steps > 0 the refinement of the whole step
+                                    replaces them */
     int32_t use_graph;           /* 1: spgo_lm_iterate replays a captured CUDA graph
                                     (not on the legacy default stream, not while profiling) */
     int32_t use_tc;              /* 1 (default): mixed path forms the landmark Schur complement
@@ -172,6 +188,9 @@ void        spgo_default_params(spgo_params *p);
  * current one solves.  Thread-safe. */
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems,
                      int32_t precision, spgo_plan **out);
+/* The same with the work shapes of `opts` (NULL: the defaults). */
+int spgo_plan_create_opts(const spgo_host_problem *problems, int32_t n_problems,
+                          int32_t precision, const spgo_plan_options *opts, spgo_plan **out);
 int spgo_plan_sizes_get(const spgo_plan *plan, spgo_plan_sizes *out);
 int spgo_plan_destroy(spgo_plan *plan);
 /* Landmark permutation: internal slot -> (problem-local) landmark order is

@@ -132,6 +132,7 @@ static void arena_put(HostBlock &b) {
 
 struct spgo_plan {
   int32_t precision = SPGO_PREC_MIXED;
+  int32_t tc_split = SPGO_TC_SPLIT, simt_split = SPGO_KSPLIT;  // Schur work shapes (spgo_plan_options)
   int32_t B = 0, F = 0, NP = 0, L = 0;
   int64_t O = 0;
   int32_t max_P = 0, max_D = 1, max_nb = 1, total_params = 0;
@@ -463,15 +464,16 @@ static void plan_problem(const spgo_host_problem &q, int b, int64_t lm_base, int
   for (int ti = 0; ti < ntile; ++ti)
     for (int tj = 0; tj <= ti; ++tj) {
       const auto &lst = lists[(size_t)ti * ntile + tj];
-      for (size_t s0 = 0; s0 < lst.size(); s0 += SPGO_KSPLIT) {
+      const size_t ks = (size_t)p->simt_split;
+      for (size_t s0 = 0; s0 < lst.size(); s0 += ks) {
         o.wk_ti.push_back(ti);
         o.wk_tj.push_back(tj);
         o.wk_cbeg.push_back((int32_t)o.wk_chunks.size());
-        for (size_t k = s0; k < std::min(lst.size(), s0 + SPGO_KSPLIT); ++k) o.wk_chunks.push_back(lst[k]);
+        for (size_t k = s0; k < std::min(lst.size(), s0 + ks); ++k) o.wk_chunks.push_back(lst[k]);
         o.wk_cend.push_back((int32_t)o.wk_chunks.size());
       }
     }
-  // tensor-core Schur work list: 128 x 128 tiles of the lower triangle, <= SPGO_TC_SPLIT chunks each
+  // tensor-core Schur work list: 128 x 128 tiles of the lower triangle, <= tc_split chunks each
   const int P = 6 * N;
   for (int row0 = 0; row0 < P; row0 += 128) {
     for (int col0 = 0; col0 <= row0; col0 += 128) {
@@ -481,12 +483,13 @@ static void plan_problem(const spgo_host_problem &q, int b, int64_t lm_base, int
         const int s0 = 6 * o.ch_f0[c], s1 = 6 * (o.ch_f0[c] + o.ch_nb[c]);
         if (s1 > row0 && s0 < row0 + 128 && s1 > col0 && s0 < col0 + ncols) lst.push_back(c);
       }
-      for (size_t st = 0; st < lst.size(); st += SPGO_TC_SPLIT) {
+      const size_t ts = (size_t)p->tc_split;
+      for (size_t st = 0; st < lst.size(); st += ts) {
         o.tc_row0.push_back(row0);
         o.tc_col0.push_back(col0);
         o.tc_ncols.push_back(ncols);
         o.tc_cbeg.push_back((int32_t)o.tc_chunks.size());
-        for (size_t k = st; k < std::min(lst.size(), st + SPGO_TC_SPLIT); ++k) o.tc_chunks.push_back(lst[k]);
+        for (size_t k = st; k < std::min(lst.size(), st + ts); ++k) o.tc_chunks.push_back(lst[k]);
         o.tc_cend.push_back((int32_t)o.tc_chunks.size());
       }
     }
@@ -863,7 +866,8 @@ static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
     CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st));
     for (const int b : s->plan->large)
       CUDA_TRY(launch_factor_large<T>(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b],
-                                      mixed ? s->prm.refine_steps : 0, st));
+                                      (mixed && !(s->prm.outer_steps > 0 && s->wv.facs)) ? s->prm.refine_steps : 0,
+                                      st));
   }
   return SPGO_OK;
 }
@@ -983,10 +987,23 @@ void spgo_default_params(spgo_params *p) {
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
+  return spgo_plan_create_opts(problems, n_problems, precision, nullptr, out);
+}
+
+int spgo_plan_create_opts(const spgo_host_problem *problems, int32_t n_problems, int32_t precision,
+                          const spgo_plan_options *opts, spgo_plan **out) {
   if (!out) return fail(SPGO_ERR_INVALID_ARG, "out is null");
   *out = nullptr;
+  if (opts) {
+    if (opts->tc_split < 0 || opts->tc_split > SPGO_TC_SPLIT || opts->simt_split < 0 || opts->simt_split > 64)
+      return fail(SPGO_ERR_INVALID_ARG, "plan options out of range (tc_split 1..64, simt_split 1..64, 0: default)");
+    for (int k = 0; k < 6; ++k)
+      if (opts->reserved[k] != 0) return fail(SPGO_ERR_INVALID_ARG, "plan options: reserved fields must be zero");
+  }
   spgo_plan *p = new (std::nothrow) spgo_plan();
   if (!p) return fail(SPGO_ERR_INVALID_ARG, "host allocation failed");
+  if (opts && opts->tc_split > 0) p->tc_split = opts->tc_split;
+  if (opts && opts->simt_split > 0) p->simt_split = opts->simt_split;
   int rc;
   try {
     rc = plan_build(problems, n_problems, precision, p);
@@ -1021,6 +1038,8 @@ int spgo_plan_sizes_get(const spgo_plan *p, spgo_plan_sizes *o) {
   }
   o->n_tc_items = (int32_t)p->tc_prob.size();
   o->tc_chunk_tiles = (int32_t)p->tc_chunks.size();
+  o->tc_split = p->tc_split;
+  o->simt_split = p->simt_split;
   o->static_bytes = p->static_bytes;
   o->workspace_bytes = p->ws_bytes;
   o->slab_elems = p->total_slab;

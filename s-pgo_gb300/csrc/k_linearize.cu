@@ -492,15 +492,21 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
 //   * every product of the pair records (21 Hessian and 6 gradient values per
 //     observation) is formed exactly (two-product) and summed in double-float;
 //     each run of equal target frame goes to the FP64 pair record by an FP64 atomic
-//     (the pair reduction then runs in FP64, k_system.cu);
+//     (the pair reduction then runs in double-float about one origin, k_system.cu);
 //   * the slab terms s (w h)(w j_alpha) likewise, from the same rounded rows (moved
 //     from the pair origin to the anchor centre in double-float), and the
 //     per-landmark suffix / prefix sums along the window and the move to each pose
-//     frame run in double-float; the slab is rounded to FP32 once, at the end.
+//     frame run in double-float; the slab is rounded to FP32 once, at the end.  The
+//     slab only enters the preconditioner of the refined step, but a slab accumulated
+//     in FP32, and also one whose double-float moments were rounded before an FP32
+//     rotation to the pose axes, left single ill-conditioned problems of the config-3
+//     batch with an unusable preconditioner: they stalled 7 % to 70x above the plain
+//     FP64 cost (the assembled S cancels A against W D^-1 W^T, and W must match A's
+//     rounding-once accuracy).
 // C and g_a (positive sums and the preconditioner's own right-hand side) stay FP32;
 // g_a is also summed exactly (per observation an exact four-product sum, per landmark
-// FP64) for the refined step's predicted decrease, which near the optimum is a small
-// difference of large terms.
+// double-float) for the refined step's predicted decrease, which near the optimum is a
+// small difference of large terms.
 struct JacSmem {
   float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre (hi)
   float Xl[SPGO_CHUNK][3];  // its low words
@@ -508,13 +514,18 @@ struct JacSmem {
   float C[SPGO_CHUNK], ga[SPGO_CHUNK];
   int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
   int key[8][32];           // per warp: target frame of each lane's observation (-1: none)
-  double gl[8][SPGO_CHUNK]; // per warp: exactly summed g_a
+  float glh[8][SPGO_CHUNK];  // per warp: exactly summed g_a, double-float (h, l)
+  float gll[8][SPGO_CHUNK];
 };
 constexpr int kJacVals = 27;          // 21 Hessian + 6 gradient values per pair record
+constexpr int kJacRound = 9;          // pair values staged per round (three rounds of 9)
+constexpr int kJacSegs = 3;           // observation segments per staged value in the run sums
+constexpr int kJacSegLen = 11;        // ceil(32 / 3)
 constexpr int kJacPitch = 33;
 
-// dynamic shared memory: dc [W][6] float x 2 (hi, lo) | stage [warps][2 * 27][33]
-// float (double-float pair terms) | slab hi and lo [6 (W - 1)][32] float each
+// dynamic shared memory: dc [W][6] float x 2 (hi, lo) | stage [warps][2 * 9][33]
+// float (double-float pair terms, one round) | slab hi and lo [6 (W - 1)][32] float
+// each.  For 32-frame windows 74.6 KB: three 8-warp CTAs per SM.
 struct JacLayout {
   size_t dc, stage, slab_h, slab_l, total;
   __host__ __device__ JacLayout(int max_nb, int warps) {
@@ -522,11 +533,65 @@ struct JacLayout {
     auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
     dc = up(sizeof(JacSmem));
     stage = dc + up(W * 12 * sizeof(float));
-    slab_h = stage + up((size_t)warps * 2 * kJacVals * kJacPitch * sizeof(float));
+    slab_h = stage + up((size_t)warps * 2 * kJacRound * kJacPitch * sizeof(float));
     slab_l = slab_h + up((size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(float));
     total = slab_l + (size_t)6 * (W - 1) * SPGO_CHUNK * sizeof(float);
   }
 };
+
+// Stages pair values [V0, V1) (the packed upper 6 x 6 block 0..20, then the gradient
+// 21..26) of the lane's observation, each the exact four-product sum, as (h, l) rows
+template <int V0, int V1>
+__device__ __forceinline__ void jac_stage(const float (&K)[2][2][6], const float (&RW)[2][2], float *st, int lane) {
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      const int v = tri6(i, j);
+      if (v >= V0 && v < V1) {
+        const df x = sum4_prod(K[0][0][i], K[0][0][j], K[0][1][i], K[0][1][j], K[1][0][i], K[1][0][j], K[1][1][i],
+                               K[1][1][j]);
+        st[(2 * (v - V0)) * kJacPitch + lane] = x.h;
+        st[(2 * (v - V0) + 1) * kJacPitch + lane] = x.l;
+      }
+    }
+    const int v = 21 + i;
+    if (v >= V0 && v < V1) {
+      const df x = sum4_prod(K[0][0][i], RW[0][0], K[0][1][i], RW[0][1], K[1][0][i], RW[1][0], K[1][1][i], RW[1][1]);
+      st[(2 * (v - V0)) * kJacPitch + lane] = x.h;
+      st[(2 * (v - V0) + 1) * kJacPitch + lane] = x.l;
+    }
+  }
+}
+
+// Sums the staged values [V0, V1) over the runs of equal target frame: lane = (value,
+// 11-observation segment); every run goes to its FP64 pair record (a run crossing a
+// segment boundary arrives in parts)
+template <int V0, int V1>
+__device__ __forceinline__ void jac_runs(const float *st, const int *keys, int lane, int host_a, int D,
+                                         double *pair_base) {
+  constexpr int NV = V1 - V0;
+  if (lane >= kJacSegs * NV) return;
+  const int v = lane % NV, i0 = (lane / NV) * kJacSegLen, i1 = min(32, i0 + kJacSegLen);
+  const float *ch = st + (2 * v) * kJacPitch, *cl = st + (2 * v + 1) * kJacPitch;
+  auto emit = [&](int n, const df_acc &a) {
+    const int lo = min(host_a, n), hi = max(host_a, n);
+    atomicAdd(pair_base + ((size_t)lo * D + (hi - lo - 1)) * kJacVals + V0 + v, df_acc_value(a));
+  };
+  df_acc acc;
+  int cur = keys[i0];
+#pragma unroll 4
+  for (int i = i0; i < i1; ++i) {
+    const int k = keys[i];
+    if (k != cur) {
+      if (cur >= 0) emit(cur, acc);
+      acc = df_acc();
+      cur = k;
+    }
+    acc.add(ch[i], cl[i]);
+  }
+  if (cur >= 0) emit(cur, acc);
+}
 
 __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView wv, Params prm,
                                                          const double *__restrict__ alpha_state, int gate) {
@@ -586,7 +651,7 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
     }
   }
   for (int i = tid; i < rows * SPGO_CHUNK; i += blockDim.x) slab_h[i] = slab_l[i] = 0.f;
-  for (int i = tid; i < 8 * SPGO_CHUNK; i += blockDim.x) (&sm.gl[0][0])[i] = 0.0;
+  for (int i = tid; i < 8 * SPGO_CHUNK; i += blockDim.x) (&sm.glh[0][0])[i] = (&sm.gll[0][0])[i] = 0.f;
   __syncthreads();
 
   // phase B: thread per observation; runs of equal target frame inside a warp go to
@@ -697,54 +762,42 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
     {
       // exactly summed g_a: the observation's j_a^T W r (the signs of JW and RW cancel),
       // added by the lanes sharing a landmark in rounds of their rank among those peers
-      const double vg = slot >= 0 ? df_to_double(sum4_prod(JW[0][0], RW[0][0], JW[0][1], RW[0][1], JW[1][0],
-                                                           RW[1][0], JW[1][1], RW[1][1]))
-                                  : 0.0;
+      const df vg = slot >= 0 ? sum4_prod(JW[0][0], RW[0][0], JW[0][1], RW[0][1], JW[1][0], RW[1][0], JW[1][1],
+                                          RW[1][1])
+                              : df_make(0.f);
       const unsigned peers = __match_any_sync(0xffffffffu, slot);
       const int rank = __popc(peers & ((1u << lane) - 1u));
       for (int r = 0; __any_sync(0xffffffffu, slot >= 0 && rank >= r); ++r) {
-        if (slot >= 0 && rank == r) sm.gl[tid >> 5][slot] += vg;
+        if (slot >= 0 && rank == r) {
+          df_acc a;
+          a.h = sm.glh[tid >> 5][slot];
+          a.l = sm.gll[tid >> 5][slot];
+          a.add(vg.h, vg.l);
+          sm.glh[tid >> 5][slot] = a.h;
+          sm.gll[tid >> 5][slot] = a.l;
+        }
         __syncwarp();
       }
     }
-    // stage the 27 double-float pair values, then lanes 0..26 each sum one value
-    // over the runs of equal target frame and add each run to its FP64 pair record
-    float *st = stage + (size_t)(tid >> 5) * 2 * kJacVals * kJacPitch;
+    // the 27 pair values in three rounds of 9: each staged as double-float rows, then
+    // summed over the runs of equal target frame into the FP64 pair records
+    float *st = stage + (size_t)(tid >> 5) * 2 * kJacRound * kJacPitch;
     int *keys = sm.key[tid >> 5];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-#pragma unroll
-      for (int j = i; j < 6; ++j) {
-        const df v = sum4_prod(K[0][0][i], K[0][0][j], K[0][1][i], K[0][1][j], K[1][0][i], K[1][0][j], K[1][1][i],
-                               K[1][1][j]);
-        st[(2 * tri6(i, j)) * kJacPitch + lane] = v.h;
-        st[(2 * tri6(i, j) + 1) * kJacPitch + lane] = v.l;
-      }
-      const df v = sum4_prod(K[0][0][i], RW[0][0], K[0][1][i], RW[0][1], K[1][0][i], RW[1][0], K[1][1][i], RW[1][1]);
-      st[(2 * (21 + i)) * kJacPitch + lane] = v.h;
-      st[(2 * (21 + i) + 1) * kJacPitch + lane] = v.l;
-    }
     keys[lane] = key;
-    __syncwarp();
-    if (__any_sync(0xffffffffu, key >= 0) && lane < kJacVals) {
-      const float *ch = st + (2 * lane) * kJacPitch, *cl = st + (2 * lane + 1) * kJacPitch;
+    const bool any_pose = __any_sync(0xffffffffu, key >= 0);
+    if (any_pose) {
       const int host_a = sm.a[0];
-      auto emit = [&](int n, const df_acc &v) {
-        const int lo = min(host_a, n), hi = max(host_a, n);
-        atomicAdd(pair_base + ((size_t)lo * D + (hi - lo - 1)) * kJacVals + lane, df_acc_value(v));
-      };
-      df_acc acc;
-      int cur = keys[0];
-      for (int i = 0; i < 32; ++i) {
-        const int k = keys[i];
-        if (k != cur) {
-          if (cur >= 0) emit(cur, acc);
-          acc = df_acc();
-          cur = k;
-        }
-        acc.add(ch[i], cl[i]);
-      }
-      if (cur >= 0) emit(cur, acc);
+      jac_stage<0, kJacRound>(K, RW, st, lane);
+      __syncwarp();
+      jac_runs<0, kJacRound>(st, keys, lane, host_a, D, pair_base);
+      __syncwarp();
+      jac_stage<kJacRound, 2 * kJacRound>(K, RW, st, lane);
+      __syncwarp();
+      jac_runs<kJacRound, 2 * kJacRound>(st, keys, lane, host_a, D, pair_base);
+      __syncwarp();
+      jac_stage<2 * kJacRound, kJacVals>(K, RW, st, lane);
+      __syncwarp();
+      jac_runs<2 * kJacRound, kJacVals>(st, keys, lane, host_a, D, pair_base);
     }
     __syncwarp();
   }
@@ -781,13 +834,12 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
       for (int k = 0; k < 6; ++k) gslab[at + k * SPGO_CHUNK] = 0.f;
       continue;
     }
-    const int fi = fo + i, fa = fo + sm.a[slot];
-    const float *Rh = wv.fr_Rf + (size_t)fi * 18, *Rl = wv.fr_Rl + (size_t)fi * 18;
+    const float *Rh = wv.fr_Rf + (size_t)(fo + i) * 18, *Rl = wv.fr_Rl + (size_t)(fo + i) * 18;
     df d[3], bw[3], bv[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      d[k] = df_sub(wv.fr_ch[(size_t)fi * 6 + k], wv.fr_ch[(size_t)fa * 6 + k]) +
-             df_make(wv.fr_cl[(size_t)fi * 6 + k] - wv.fr_cl[(size_t)fa * 6 + k]);
+      // c_i - c_a: the negated host-to-frame offset of the window table (one host per chunk)
+      d[k] = df{-dch[(i - f0) * 6 + k], -dcl[(i - f0) * 6 + k]};
       bw[k] = df{slab_h[at + k * SPGO_CHUNK], slab_l[at + k * SPGO_CHUNK]};
       bv[k] = df{slab_h[at + (3 + k) * SPGO_CHUNK], slab_l[at + (3 + k) * SPGO_CHUNK]};
     }
@@ -808,10 +860,10 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
     reinterpret_cast<float *>(wv.C)[lm0 + tid] = sm.C[tid];
     reinterpret_cast<float *>(wv.ga)[lm0 + tid] = sm.ga[tid];
     if (wv.gaacc) {
-      double g = 0.0;
+      df_acc g;
 #pragma unroll
-      for (int w = 0; w < 8; ++w) g += sm.gl[w][tid];
-      wv.gaacc[lm0 + tid] = g;
+      for (int w = 0; w < 8; ++w) g.add(sm.glh[w][tid], sm.gll[w][tid]);
+      wv.gaacc[lm0 + tid] = df_acc_value(g);
     }
   }
 }
@@ -936,6 +988,9 @@ int launch_linearize(const PlanView &pv, const WorkView &wv, const Params &prm, 
     const int nt = prm.lin_block > 0 ? prm.lin_block : kLinThreads;
     const size_t sm = JacLayout(pv.max_nb, nt / 32).total;
     cudaFuncSetAttribute(k_jacobian_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    // all of the unified L1 / shared memory as shared: three CTAs of 74.6 KB per SM
+    cudaFuncSetAttribute(k_jacobian_acc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
     k_jacobian_acc<<<pv.n_chunks, nt, sm, st>>>(pv, wv, prm, alpha, gate);
   } else {
     const int nt = prm.lin_block > 0 ? prm.lin_block : kLinThreads;

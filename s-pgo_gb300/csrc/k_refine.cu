@@ -145,7 +145,8 @@ struct RefSmem {
   float da[SPGO_CHUNK];     // inverse-depth step (FP32 copy for the residuals)
   float t[SPGO_CHUNK];      // D^-1 r_a
   int a[SPGO_CHUNK];
-  double dl[kRpWarps][SPGO_CHUNK];  // j_a^T W e, per warp
+  float dlh[kRpWarps][SPGO_CHUNK];  // j_a^T W e, per warp, double-float (h, l)
+  float dll[kRpWarps][SPGO_CHUNK];
   int key[kRpWarps][32];
 };
 
@@ -185,6 +186,18 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
   const float fxs[2] = {intr[0], intr[4]}, fys[2] = {intr[1], intr[5]};
   const double lam = wv.lm[b].lam;
   const float eps = prm.eps;
+  {
+    // the chunk's observation records (slot, frame, residuals) towards L2 while the
+    // prologue runs: one prefetch per 128-byte line
+    const int64_t ob0 = pv.lm_obs[lm0], oe0 = pv.lm_obs[lm0 + cnt];
+    const float *res0 = wv.res + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 4;
+    const int nres = (int)(((oe0 - ob0) * 16 + 127) / 128), nfr = (int)(((oe0 - ob0) * 4 + 127) / 128);
+    for (int k = tid; k < nres + nfr; k += blockDim.x) {
+      const void *a = k < nres ? (const void *)(reinterpret_cast<const char *>(res0 + 4 * ob0) + 128 * k)
+                               : (const void *)(reinterpret_cast<const char *>(pv.obs_frame + ob0) + 128 * (k - nres));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+    }
+  }
   const RpLayout lay(pv.max_nb);
   float *dch = reinterpret_cast<float *>(smem_raw + lay.dc);
   float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
@@ -219,7 +232,7 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
       sm.a[lane] = a;
     }
 #pragma unroll
-    for (int w = 0; w < kRpWarps; ++w) sm.dl[w][lane] = 0.0;
+    for (int w = 0; w < kRpWarps; ++w) sm.dlh[w][lane] = sm.dll[w][lane] = 0.f;
   } else if (warp == 1) {
     // inverse-depth step: first pass x_a = D^-1 (g_a - W^T x_p) from the FP32 system,
     // later x_a += t - D^-1 W^T dx_p (the previous pass's t and pose correction)
@@ -371,17 +384,23 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
       }
       if (has_pose) key = n;
     }
-    const double vle =  // this observation's landmark dual
-        slot >= 0 ? df_to_double(sum4_prod(JA[0][0], EW[0][0], JA[0][1], EW[0][1], JA[1][0], EW[1][0], JA[1][1],
-                                           EW[1][1]))
-                  : 0.0;
+    const df vle =  // this observation's landmark dual
+        slot >= 0 ? sum4_prod(JA[0][0], EW[0][0], JA[0][1], EW[0][1], JA[1][0], EW[1][0], JA[1][1], EW[1][1])
+                  : df_make(0.f);
     {
       // the warp's own landmark accumulators: lanes sharing a landmark (different
       // frames) add in rounds of their rank among those peers, no atomics
       const unsigned peers = __match_any_sync(0xffffffffu, slot);
       const int rank = __popc(peers & ((1u << lane) - 1u));
       for (int r = 0; __any_sync(0xffffffffu, slot >= 0 && rank >= r); ++r) {
-        if (slot >= 0 && rank == r) sm.dl[warp][slot] += vle;
+        if (slot >= 0 && rank == r) {
+          df_acc a;
+          a.h = sm.dlh[warp][slot];
+          a.l = sm.dll[warp][slot];
+          a.add(vle.h, vle.l);
+          sm.dlh[warp][slot] = a.h;
+          sm.dll[warp][slot] = a.l;
+        }
         __syncwarp();
       }
     }
@@ -429,9 +448,10 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
     const int li = lm0 + tid;
     const float C = Cv[li];
     const float Dd = C * (float)(1.0 + lam) + eps;
-    double dsum = 0.0;
+    df_acc acc;
 #pragma unroll
-    for (int w = 0; w < kRpWarps; ++w) dsum += sm.dl[w][tid];
+    for (int w = 0; w < kRpWarps; ++w) acc.add(sm.dlh[w][tid], sm.dll[w][tid]);
+    const double dsum = df_acc_value(acc);
     const double ra = dsum - (lam * (double)C + (double)eps) * wv.dal[li];
     const float t = (float)(ra / (double)Dd);
     sm.t[tid] = t;
@@ -440,11 +460,22 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
     sm.t[tid] = 0.f;
   }
   __syncthreads();
-  // W t into the pose right-hand side: warp per slab row, lane = landmark slot
+  // W t into the pose right-hand side: warp per slab row, lane = landmark slot; eight
+  // of the warp's rows loaded before any is reduced
   const float tv = sm.t[lane];
-  for (int r = warp; r < rows; r += kRpWarps) {
-    const float v = warp_sum(slab[(size_t)r * SPGO_CHUNK + lane] * tv);
-    if (lane == 0 && v != 0.f) atomicAdd(wv.rhsB + po + 6 * f0 + r, v);
+  for (int r0 = warp; r0 < rows; r0 += 8 * kRpWarps) {
+    float x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int r = r0 + q * kRpWarps;
+      x[q] = r < rows ? slab[(size_t)r * SPGO_CHUNK + lane] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int r = r0 + q * kRpWarps;
+      const float v = warp_sum(x[q] * tv);
+      if (lane == 0 && r < rows && v != 0.f) atomicAdd(wv.rhsB + po + 6 * f0 + r, v);
+    }
   }
 }
 

@@ -345,8 +345,10 @@ template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed, void *stream) {
   if (pv.max_P_small <= 0) return 0;
   const size_t sm = factor_packed_bytes(pv.max_P_small, sizeof(T));
-  const int refine = mixed ? prm.refine_steps : 0;
   const int store = (mixed && prm.outer_steps > 0 && wv.facs) ? 1 : 0;
+  // the reduced solve's own refinement only without the refinement of the whole step,
+  // which supersedes it (its residual is exact, not that of the assembled S)
+  const int refine = (mixed && !store) ? prm.refine_steps : 0;
   cudaFuncSetAttribute(k_factor_solve<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_factor_solve<T><<<pv.B, 256, sm, (cudaStream_t)stream>>>(pv, wv, refine, store);
   ++g_launches;

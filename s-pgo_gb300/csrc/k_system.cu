@@ -285,36 +285,42 @@ __device__ __forceinline__ void df_rel_c(const WorkView &wv, int fx, int fy, df 
 
 constexpr int kPrThreads = 512;
 
-// one CTA per problem: 0. records read, cleared, split and moved from c_lo to o;
-// 1. thread per (hi, component): prefix over lo, P(i, hi) = sum_{lo <= i} M(lo, hi);
-// 2. thread per (i, component): suffix over hi, F(i, i + e) = sum_{d > e} P(i, i + d)
-__global__ void __launch_bounds__(kPrThreads) k_pair_reduce_df(PlanView pv, WorkView wv) {
+// 0. every record (lo, hi): read (FP64) and cleared, split into double-float, moved from
+// c_lo to o; one thread per record
+__global__ void __launch_bounds__(128) k_pair_shift_df(PlanView pv, WorkView wv) {
+  const int b = blockIdx.y;
+  if (!problem_active(wv.lm, b, GATE_RELIN)) return;
+  const int N = pv.p_npose[b], D = pv.p_pair_D[b];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N * D) return;
+  const int lo = r / D, hi = lo + r % D + 1;
+  if (hi > N) return;
+  const int fo = pv.p_frame_off[b];
+  double *rec = reinterpret_cast<double *>(wv.pair_acc) + ((size_t)pv.p_pair_off[b] + r) * 27;
+  df v[27];
+#pragma unroll
+  for (int k = 0; k < 27; ++k) v[k] = df_split_double(rec[k]);
+#pragma unroll
+  for (int k = 0; k < 27; ++k) rec[k] = 0.0;  // cleared for the next linearisation
+  if (lo > 0) {
+    df z[3];
+    df_rel_c(wv, fo + lo, fo, z);  // from c_lo to o = c_0
+    shift_record(v, z);
+  }
+  df *out = reinterpret_cast<df *>(wv.pairF) + ((size_t)pv.p_pair_off[b] + r) * 27;
+#pragma unroll
+  for (int k = 0; k < 27; ++k) out[k] = v[k];
+}
+
+// one CTA per problem: 1. thread per (hi, component): prefix over lo,
+// P(i, hi) = sum_{lo <= i} M(lo, hi);  2. thread per (i, component): suffix over hi,
+// F(i, i + e) = sum_{d > e} P(i, i + d)
+__global__ void __launch_bounds__(kPrThreads) k_pair_scan_df(PlanView pv, WorkView wv) {
   const int b = blockIdx.x;
   if (!problem_active(wv.lm, b, GATE_RELIN)) return;
   const int N = pv.p_npose[b], D = pv.p_pair_D[b];
-  const int fo = pv.p_frame_off[b];
   const int tid = threadIdx.x, nt = blockDim.x;
-  double *acc = reinterpret_cast<double *>(wv.pair_acc) + (size_t)pv.p_pair_off[b] * 27;
   df *F = reinterpret_cast<df *>(wv.pairF) + (size_t)pv.p_pair_off[b] * 27;
-  for (int r = tid; r < N * D; r += nt) {
-    const int lo = r / D, hi = lo + r % D + 1;
-    if (hi > N) continue;
-    double *rec = acc + (size_t)r * 27;
-    df v[27];
-#pragma unroll
-    for (int k = 0; k < 27; ++k) v[k] = df_split_double(rec[k]);
-#pragma unroll
-    for (int k = 0; k < 27; ++k) rec[k] = 0.0;  // cleared for the next linearisation
-    if (lo > 0) {
-      df z[3];
-      df_rel_c(wv, fo + lo, fo, z);  // from c_lo to o = c_0
-      shift_record(v, z);
-    }
-    df *out = F + (size_t)r * 27;
-#pragma unroll
-    for (int k = 0; k < 27; ++k) out[k] = v[k];
-  }
-  __syncthreads();
   // the running sums: eight records loaded before any is summed and stored back (the
   // stores could alias later loads, so without that each step is a round trip)
   for (int t = tid; t < N * 27; t += nt) {
@@ -455,9 +461,10 @@ int launch_system(const PlanView &pv, const WorkView &wv, int gate, void *stream
   const int nmax = pv.max_P / 6;
   const int nd = pv.max_D > 0 ? pv.max_D : 1;
   if constexpr (std::is_same<T, float>::value) {
-    k_pair_reduce_df<<<pv.B, kPrThreads, 0, st>>>(pv, wv);
+    k_pair_shift_df<<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
+    k_pair_scan_df<<<pv.B, kPrThreads, 0, st>>>(pv, wv);
     k_pairs_to_A_df<<<dim3(grid_for((long long)nmax * nd, 128), pv.B), 128, 0, st>>>(pv, wv);
-    g_launches += 2;
+    g_launches += 3;
   } else {
     k_pair_prefix_rec<<<dim3(grid_for(nmax, 64), pv.B), 64, 0, st>>>(pv, wv);
     k_pair_suffix<double><<<dim3(grid_for((long long)nmax * 27, 128), pv.B), 128, 0, st>>>(pv, wv);

@@ -21,7 +21,8 @@ MAX_WINDOW = 96
 
 # symbols include/spgo.h declares (checked by the tests)
 EXPORTED = [
-    "spgo_version", "spgo_last_error", "spgo_default_params", "spgo_plan_create", "spgo_plan_sizes_get",
+    "spgo_version", "spgo_last_error", "spgo_default_params", "spgo_plan_create", "spgo_plan_create_opts",
+    "spgo_plan_sizes_get",
     "spgo_plan_destroy", "spgo_plan_offsets", "spgo_solver_create", "spgo_solver_destroy", "spgo_set_params",
     "spgo_gn_step", "spgo_lm_reset", "spgo_lm_iterate", "spgo_lm_status", "spgo_lm_solve",
     "spgo_export_system", "spgo_launch_count", "spgo_profile_enable", "spgo_profile_read",
@@ -52,7 +53,12 @@ class PlanSizes(C.Structure):
                 ("max_params", C.c_int32), ("schur_chunk_tiles", C.c_int32), ("static_bytes", C.c_size_t),
                 ("workspace_bytes", C.c_size_t), ("slab_elems", C.c_int64), ("pair_records", C.c_int64),
                 ("schur_flops", C.c_int64), ("n_tc_items", C.c_int32), ("tc_chunk_tiles", C.c_int32),
-                ("schur_flops_landmark", C.c_int64)]
+                ("schur_flops_landmark", C.c_int64), ("tc_split", C.c_int32), ("simt_split", C.c_int32)]
+
+
+class PlanOptions(C.Structure):
+    """``spgo_plan_options``: Schur work shapes chosen when the batch is planned."""
+    _fields_ = [("tc_split", C.c_int32), ("simt_split", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class Params(C.Structure):
@@ -96,6 +102,7 @@ def lib() -> C.CDLL:
     L.spgo_default_params.argtypes = [C.POINTER(Params)]
     L.spgo_default_params.restype = None
     L.spgo_plan_create.argtypes = [C.POINTER(HostProblem), i32, i32, C.POINTER(vp)]
+    L.spgo_plan_create_opts.argtypes = [C.POINTER(HostProblem), i32, i32, C.POINTER(PlanOptions), C.POINTER(vp)]
     L.spgo_plan_sizes_get.argtypes = [vp, C.POINTER(PlanSizes)]
     L.spgo_plan_destroy.argtypes = [vp]
     L.spgo_plan_offsets.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
@@ -129,7 +136,8 @@ def lib() -> C.CDLL:
     L.spgo_cost_noalloc.restype = C.c_int
     L.spgo_launch_count.argtypes = [vp]
     L.spgo_launch_count.restype = i64
-    for name in ("spgo_plan_create", "spgo_plan_sizes_get", "spgo_plan_destroy", "spgo_plan_offsets",
+    for name in ("spgo_plan_create", "spgo_plan_create_opts", "spgo_plan_sizes_get", "spgo_plan_destroy",
+                 "spgo_plan_offsets",
                  "spgo_solver_create", "spgo_solver_destroy", "spgo_set_params", "spgo_gn_step", "spgo_lm_reset",
                  "spgo_lm_iterate", "spgo_lm_status", "spgo_lm_solve", "spgo_export_system", "spgo_profile_enable",
                  "spgo_profile_read"):

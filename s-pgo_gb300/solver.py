@@ -48,7 +48,9 @@ class HostPlan:
     page-locked staging).  It needs no device work, so it can be built on another
     thread while an earlier batch solves (the planner releases the GIL)."""
 
-    def __init__(self, problems: Sequence[Problem], precision: str = "mixed"):
+    def __init__(self, problems: Sequence[Problem], precision: str = "mixed", options: Optional[dict] = None):
+        """options: the Schur work shapes (``tc_split``, ``simt_split``;
+        ``spgo_plan_options``), None for the defaults."""
         self.L = nat.lib()
         self.problems = list(problems)
         if not self.problems:
@@ -79,7 +81,11 @@ class HostPlan:
             h.obs_frame = arrs[5].ctypes.data
             h.obs_uv_f64 = arrs[6].ctypes.data
         plan = C.c_void_p()
-        nat.check(self.L.spgo_plan_create(hp, len(self.problems), _PREC[precision], C.byref(plan)), "plan_create")
+        opts = nat.PlanOptions()
+        for k, v in (options or {}).items():
+            setattr(opts, k, int(v))
+        nat.check(self.L.spgo_plan_create_opts(hp, len(self.problems), _PREC[precision], C.byref(opts),
+                                               C.byref(plan)), "plan_create")
         self.handle = plan
 
     def close(self):
@@ -98,16 +104,18 @@ class BatchSolver:
     """Solve a batch of independent problems with one set of kernel launches."""
 
     def __init__(self, problems: Optional[Sequence[Problem]] = None, precision: str = "mixed", device="cuda",
-                 stream: Optional[torch.cuda.Stream] = None, plan: Optional[HostPlan] = None):
-        """``problems`` are planned here, or ``plan`` (a ``HostPlan``, whose
-        ownership passes to this solver) was planned beforehand."""
+                 stream: Optional[torch.cuda.Stream] = None, plan: Optional[HostPlan] = None,
+                 plan_options: Optional[dict] = None):
+        """``problems`` are planned here (with the Schur work shapes ``plan_options``,
+        see ``HostPlan``), or ``plan`` (a ``HostPlan``, whose ownership passes to this
+        solver) was planned beforehand."""
         self.L = nat.lib()
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError("BatchSolver runs on a CUDA device only")
         self._stream = stream
         if plan is None:
-            plan = HostPlan(problems if problems is not None else [], precision)
+            plan = HostPlan(problems if problems is not None else [], precision, plan_options)
         self._host_plan = plan
         self.problems = plan.problems
         self.precision = plan.precision
@@ -287,6 +295,38 @@ class BatchSolver:
         self.params = out
         return dict(cost_block=out.cost_block, lin_block=out.lin_block, use_tc=out.use_tc)
 
+    def autotune_plan_shapes(self, candidates=None, iterations: int = 2, repeats: int = 2) -> dict:
+        """Time the plan-time Schur work shapes (``spgo_plan_options``: chunks per
+        tensor-core or SIMT work item) on this solver's batch: for each candidate a
+        solver of the same problems and parameters is planned, reset and run for
+        ``iterations`` LM iterations (best of ``repeats``).  This solver's state is not
+        touched; returns ``{"best": options, "ms": {candidate: ms}}``.  A new
+        ``BatchSolver(..., plan_options=best)`` uses the choice."""
+        if candidates is None:
+            candidates = ([dict(tc_split=t) for t in (16, 32, 64)] if self.params.use_tc
+                          else [dict(simt_split=k) for k in (8, 16, 32)])
+        timings = {}
+        for cand in candidates:
+            s = BatchSolver(self.problems, precision=self.precision, device=self.device, stream=self._stream,
+                            plan_options=cand)
+            s.params = nat.Params.from_buffer_copy(self.params)
+            nat.check(self.L.spgo_set_params(s._solver, C.byref(s.params)), "set_params")
+            best = None
+            for _ in range(repeats + 1):
+                st = torch.cuda.current_stream(self.device) if self._stream is None else self._stream
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.reset()
+                e0.record(st)
+                s.iterate(iterations)
+                e1.record(st)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1)
+                best = ms if best is None else min(best, ms)
+            s.close()
+            timings[tuple(sorted(cand.items()))] = best
+        key = min(timings, key=timings.get)
+        return {"best": dict(key), "ms": {str(dict(k)): round(v, 4) for k, v in timings.items()}}
+
     def gn_step(self, iterations: int = 1, step_size: float = 1.0):
         nat.check(self.L.spgo_gn_step(self._solver, int(iterations), float(step_size), self._sp()), "gn_step")
 
@@ -374,9 +414,9 @@ class BatchSolver:
             pass
 
 
-def _plan_on(device: torch.device, problems, precision):
+def _plan_on(device: torch.device, problems, precision, plan_options=None):
     torch.cuda.set_device(device)  # page-locked staging is allocated in this device's context
-    return HostPlan(problems, precision)
+    return HostPlan(problems, precision, plan_options)
 
 
 def _drive(device: torch.device, stream: torch.cuda.Stream, plan_future, params, controller, check_every):
@@ -399,7 +439,7 @@ def _drive(device: torch.device, stream: torch.cuda.Stream, plan_future, params,
 
 def solve_stream(batches: Iterable[Sequence[Problem]], precision: str = "mixed", params: Optional[dict] = None,
                  controller: Optional[torch.Tensor] = None, device="cuda", inflight: int = 2,
-                 check_every: int = 8) -> Iterator[Tuple[List[dict], list, list]]:
+                 check_every: int = 8, plan_options: Optional[dict] = None) -> Iterator[Tuple[List[dict], list, list]]:
     """Solve batch after batch (each a sequence of ``Problem``) with Nielsen LM (or
     the learned controller), yielding ``(statuses, poses, inverse_depths)`` per batch
     in order.
@@ -408,7 +448,8 @@ def solve_stream(batches: Iterable[Sequence[Problem]], precision: str = "mixed",
     host thread, so one batch's latency-bound launches fill the SMs another leaves
     idle; one more thread plans the upcoming batches (marshalling, sorting, chunking:
     the planner releases the GIL).  Every batch still has its own upload and
-    readback.  Up to ``inflight + 1`` batches are planned ahead of the solving ones."""
+    readback.  Up to ``inflight + 1`` batches are planned ahead of the solving ones.
+    ``plan_options``: the Schur work shapes every batch is planned with (``HostPlan``)."""
     dev = torch.device(device)
     if dev.index is None:
         dev = torch.device("cuda", torch.cuda.current_device())
@@ -425,7 +466,7 @@ def solve_stream(batches: Iterable[Sequence[Problem]], precision: str = "mixed",
                 nxt = next(it, None)
                 if nxt is None:
                     return
-                plans.append(planner.submit(_plan_on, dev, nxt, precision))
+                plans.append(planner.submit(_plan_on, dev, nxt, precision, plan_options))
 
         def start_one():
             nonlocal k

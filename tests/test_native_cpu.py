@@ -132,3 +132,29 @@ def test_host_plan_on_a_worker_thread(built_lib):
     assert (a.static_bytes, a.workspace_bytes, a.n_chunks) == (b.static_bytes, b.workspace_bytes, b.n_chunks)
     hp.close()
     built_lib.spgo_plan_destroy(pl)
+
+
+def test_plan_options_shape_the_schur_work_lists(built_lib):
+    """spgo_plan_create_opts: the Schur work shapes change how the (chunk, tile)
+    products are split into work items, never which products there are; out-of-range
+    options are refused."""
+    from spgo_gb300.solver import HostPlan
+    ps = [scenes.circle_scene(40 + s, 12 + 6 * s, 900 + 400 * s) for s in range(3)]
+    sizes = {}
+    for opts in (None, dict(tc_split=16), dict(tc_split=64), dict(simt_split=4, tc_split=8)):
+        hp = HostPlan(ps, "mixed", opts)
+        sz = nat.PlanSizes()
+        assert built_lib.spgo_plan_sizes_get(hp.handle, C.byref(sz)) == 0
+        sizes[str(opts)] = sz
+        assert sz.tc_split == (opts or {}).get("tc_split", 64)
+        assert sz.simt_split == (opts or {}).get("simt_split", 16)
+        hp.close()
+    base = sizes["None"]
+    for sz in sizes.values():
+        assert (sz.tc_chunk_tiles, sz.schur_chunk_tiles, sz.n_chunks) == \
+            (base.tc_chunk_tiles, base.schur_chunk_tiles, base.n_chunks)
+    assert sizes[str(dict(tc_split=16))].n_tc_items > base.n_tc_items
+    assert sizes[str(dict(simt_split=4, tc_split=8))].n_schur_items > base.n_schur_items
+    for bad in (dict(tc_split=65), dict(simt_split=-1), dict(tc_split=128)):
+        with pytest.raises(RuntimeError):
+            HostPlan(ps, "mixed", bad)
