@@ -686,6 +686,10 @@ struct spgo_solver {
   // threads and the planner's share the host cores, and a spinning wait would take
   // one from them, while a sleeping wait would wake up late and leave the GPU idle
   cudaEvent_t status_ev = nullptr;
+  // a second stream for the LM iteration's fork: the pose-pair reduction runs beside
+  // the landmark Schur complement (both read only the linearisation's output)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 static void drop_graphs(spgo_solver *s) {
@@ -852,15 +856,18 @@ static int enqueue_reset(spgo_solver *s, cudaStream_t st, double lam) {
 }
 
 template <typename T>
-static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
-  const int mixed = s->plan->precision == SPGO_PREC_MIXED;
-  if (mixed && s->prm.use_tc) {
-    PROF(K_SCHUR);
+static int enqueue_schur(spgo_solver *s, cudaStream_t st) {
+  PROF(K_SCHUR);
+  if (s->plan->precision == SPGO_PREC_MIXED && s->prm.use_tc)
     CUDA_TRY(launch_schur_tc(s->pv, s->wv, s->prm, st));
-  } else {
-    PROF(K_SCHUR);
+  else
     CUDA_TRY(launch_schur<T>(s->pv, s->wv, s->prm, st));
-  }
+  return SPGO_OK;
+}
+
+template <typename T>
+static int enqueue_factor(spgo_solver *s, cudaStream_t st) {
+  const int mixed = s->plan->precision == SPGO_PREC_MIXED;
   {
     PROF(K_FACTOR);
     CUDA_TRY(launch_factor_solve<T>(s->pv, s->wv, s->prm, mixed, st));
@@ -872,14 +879,21 @@ static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
   return SPGO_OK;
 }
 
+template <typename T>
+static int enqueue_solve_step(spgo_solver *s, cudaStream_t st) {
+  int rc;
+  if ((rc = enqueue_schur<T>(s, st)) != SPGO_OK) return rc;
+  return enqueue_factor<T>(s, st);
+}
+
 // the candidate state of the damped step: solve, then (mixed path, outer_steps > 0)
 // iterative refinement against the accurately summed residual of the whole system,
 // then the inverse-depth back-substitution and the pose update (each adding its share
 // of the predicted decrease)
 template <typename T>
-static int enqueue_candidate(spgo_solver *s, cudaStream_t st) {
+static int enqueue_candidate(spgo_solver *s, cudaStream_t st, bool solved = false) {
   int rc;
-  if ((rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
+  if (!solved && (rc = enqueue_solve_step<T>(s, st)) != SPGO_OK) return rc;
   const int outer = std::is_same<T, float>::value && s->wv.facs ? s->prm.outer_steps : 0;
   if (outer <= 0) {
     { PROF(K_BACKSUB); CUDA_TRY(launch_backsub<T>(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, 0, st)); }
@@ -903,11 +917,33 @@ static int enqueue_candidate(spgo_solver *s, cudaStream_t st) {
   return SPGO_OK;
 }
 
+// Without the learned controller (whose statistics read A and g, and whose lambda the
+// Schur complement uses) the iteration forks after the Jacobian pass: the pose-pair
+// reduction (A, g) on the solver's second stream beside the landmark Schur complement
+// (S_L, g_L) on the caller's; both read only the linearisation's output, the
+// factorisation joins them.  Under stream capture the fork becomes two graph branches.
 template <typename T>
 static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
   int rc;
-  if ((rc = enqueue_linearize<T>(s, st, s->controller, s->controller)) != SPGO_OK) return rc;
-  if ((rc = enqueue_candidate<T>(s, st)) != SPGO_OK) return rc;
+  if (!s->controller && s->side) {
+    { PROF(K_LINEARIZE); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->alpha, 0, GATE_RELIN, st)); }
+    CUDA_TRY(cudaEventRecord(s->ev_fork, st));
+    CUDA_TRY(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+    {
+      ProfScope side_scope(s, s->side, K_SYSTEM);
+      CUDA_TRY(launch_system<T>(s->pv, s->wv, GATE_RELIN, s->side));
+    }
+    CUDA_TRY(cudaEventRecord(s->ev_join, s->side));
+    if ((rc = enqueue_schur<T>(s, st)) != SPGO_OK) return rc;
+    CUDA_TRY(cudaStreamWaitEvent(st, s->ev_join, 0));
+    // (the pair reduction gates on the relinearisation flag this clears)
+    { PROF(K_BOOKKEEP); CUDA_TRY(launch_post_linearize(s->pv, s->wv, st)); }
+    if ((rc = enqueue_factor<T>(s, st)) != SPGO_OK) return rc;
+    if ((rc = enqueue_candidate<T>(s, st, true)) != SPGO_OK) return rc;
+  } else {
+    if ((rc = enqueue_linearize<T>(s, st, s->controller, s->controller)) != SPGO_OK) return rc;
+    if ((rc = enqueue_candidate<T>(s, st)) != SPGO_OK) return rc;
+  }
   { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, kF64<T>, st)); }
   { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st)); }
   {
@@ -1116,10 +1152,16 @@ int spgo_solver_create(const spgo_plan *plan, void *d_static, size_t static_byte
   }
   {
     cudaError_t e = cudaEventCreateWithFlags(&s->status_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
+      if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+      if (s->side) cudaStreamDestroy(s->side);
+      if (s->status_ev) cudaEventDestroy(s->status_ev);
       arena_put(s->h_lm);
       delete s;
-      return fail(SPGO_ERR_CUDA, std::string("status event: ") + cudaGetErrorString(e));
+      return fail(SPGO_ERR_CUDA, std::string("solver events / stream: ") + cudaGetErrorString(e));
     }
   }
   s->launches0 = g_launches;
@@ -1133,6 +1175,12 @@ int spgo_solver_destroy(spgo_solver *s) {
     drop_graphs(s);
     arena_put(s->h_lm);
     if (s->status_ev) cudaEventDestroy(s->status_ev);
+    if (s->side) {
+      cudaStreamSynchronize(s->side);  // its work always joins the caller's stream; this is belt and braces
+      cudaStreamDestroy(s->side);
+    }
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
   }
   delete s;
   return SPGO_OK;
