@@ -238,6 +238,24 @@ def measured_traffic(kind: str, sizes):
     return k["bytes_per_unit"] * units, f"ncu capture of {k['case']}, scaled per {k['per']}"
 
 
+def measured_instructions(kind: str):
+    """Executed warp instructions per stereo observation of a kernel kind from the
+    committed ncu record (profiles/dram_traffic.json); None if absent or stale."""
+    import hashlib
+    try:
+        rec = json.load(open(os.path.join(REPO, "profiles", "dram_traffic.json")))
+    except Exception:
+        return None
+    k = rec.get("kernels", {}).get(kind)
+    if not k or k.get("per") != "obs" or "instructions_per_unit" not in k:
+        return None
+    h = hashlib.sha256()
+    for f in k["sources"]:
+        with open(os.path.join(REPO, f), "rb") as fh:
+            h.update(fh.read())
+    return k["instructions_per_unit"] if h.hexdigest() == k["source_sha256"] else None
+
+
 def _reached(costs, plain):
     import numpy as np
     return np.asarray(costs) <= np.asarray(plain) * (1.0 + REACH_TOL)
@@ -462,6 +480,19 @@ def run_ours(args):
             "algorithmic_per_launch": amount, "avg_launch_ms": avg_ms, "peak_source": peak_src,
             "note": "algorithmic work per launch / CUDA-event launch duration (profiled step after the "
                     "timed region, CUDA graphs off)"}
+    # the passes over the observations are bound by instruction issue, not DRAM: their
+    # executed warp instructions (from the committed ncu record, per observation) over
+    # the launch time, against 4 issue slots per SM per cycle at the sampled SM clock
+    issue = {}
+    for k in ("linearize", "resid_pass", "cost"):
+        ipu = measured_instructions(k)
+        if ipu is not None and prof.get(k, (0, 0))[1]:
+            ms_ = prof[k][0] / prof[k][1]
+            rate = ipu * bs.sizes.total_obs / (ms_ / 1e3)
+            peak_i = 152 * 4 * float(clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)) * 1e6
+            issue[k] = {"warp_instructions_per_launch": ipu * bs.sizes.total_obs, "per_s": rate,
+                        "peak_per_s": peak_i, "frac": rate / peak_i}
+    roof["issue"] = issue
     if "schur" in prof and prof["schur"][1] and bs.sizes.tc_chunk_tiles:
         # the tensor-core kernel executes more than the algorithmic count: 128 x 128 tiles
         # padded to the chunk windows, and three TF32 products per split value pair
