@@ -148,15 +148,18 @@ typedef struct spgo_params {
                                     residual J^T (r - J x) - Lambda x formed from the FP32
                                     Jacobian with exact products and FP64-grade sums; the FP32
                                     system (pose Hessian, tensor-core Schur complement, FP32
-                                    Cholesky) only preconditions.  Default 1; 0: the FP32 step
-                                    as solved */
+                                    Cholesky) only preconditions.  Default 2 (the second only
+                                    where outer_tol asks for it); 0: the FP32 step as solved */
     int32_t wait_us;             /* limit of every bounded device-side wait, microseconds
                                     (0: 2 s).  Shortening it only makes waits give up sooner:
                                     the problem is flagged and its step rejected */
     float   ctl_min_log10;       /* learned damping: the largest decrease of lambda one proposal
                                     may make, as log10 of the factor, in [-6, 0] (default -6:
                                     the network's own range) */
-    int32_t pad_;
+    float   outer_tol;           /* mixed path, outer_steps > 1: a problem takes the next
+                                    refinement step only while its last correction exceeds
+                                    outer_tol times its step (largest entries); default 1e-3;
+                                    0: every step */
 } spgo_params;
 
 typedef struct spgo_problem_status {

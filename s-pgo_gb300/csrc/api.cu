@@ -904,7 +904,7 @@ static int enqueue_candidate(spgo_solver *s, cudaStream_t st, bool solved = fals
   for (int k = 0; k < outer; ++k) {
     { PROF(K_RESID); CUDA_TRY(launch_resid_pass(s->pv, s->wv, s->prm, s->alpha, k == 0, st)); }
     PROF(K_REFINE);
-    CUDA_TRY(launch_resid_solve(s->pv, s->wv, k == 0, st));
+    CUDA_TRY(launch_resid_solve(s->pv, s->wv, s->prm, k == 0, st));
     for (const int b : s->plan->large)
       CUDA_TRY(launch_refine_large(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b], st));
     if (k + 1 < outer) CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
@@ -1017,9 +1017,10 @@ void spgo_default_params(spgo_params *p) {
   p->refine_steps = 1;
   p->use_graph = 1;
   p->use_tc = 1;
-  p->outer_steps = 1;
+  p->outer_steps = 2;
   p->wait_us = 0;
   p->ctl_min_log10 = -6.0f;
+  p->outer_tol = 1e-3f;
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
@@ -1219,7 +1220,7 @@ int spgo_set_params(spgo_solver *s, const spgo_params *p) {
   if (p->loss < 0 || p->loss > 2) return fail(SPGO_ERR_INVALID_ARG, "unknown loss");
   if (!(p->loss_scale > 0) || !(p->eps >= 0) || !(p->alpha_min < p->alpha_max) || p->max_iters < 0 ||
       p->refine_steps < 0 || !(p->lambda0 >= 0) || p->outer_steps < 0 || p->outer_steps > 8 || p->wait_us < 0 ||
-      !(p->ctl_min_log10 <= 0.f && p->ctl_min_log10 >= -6.f))
+      !(p->ctl_min_log10 <= 0.f && p->ctl_min_log10 >= -6.f) || !(p->outer_tol >= 0.f && p->outer_tol < 1.f))
     return fail(SPGO_ERR_INVALID_ARG, "parameter out of range");
   for (const int32_t blk : {p->cost_block, p->lin_block})
     if (blk != 0 && (blk < 32 || blk > 256 || blk % 32 != 0))

@@ -60,8 +60,10 @@ __device__ __forceinline__ void frame_Rc(const WorkView &wv, int f, double *R, d
   for (int k = 0; k < 3; ++k) c[k] = (double)wv.fr_ch[(size_t)f * 6 + k] + (double)wv.fr_cl[(size_t)f * 6 + k];
 }
 
+// a problem takes (the next step of) the refinement: running, its step not failed, and
+// its refinement not yet converged (outer_tol)
 __device__ __forceinline__ bool refine_active(const WorkView &wv, int b) {
-  return problem_active(wv.lm, b, GATE_RUNNING) && !wv.lm[b].fail;
+  return problem_active(wv.lm, b, GATE_RUNNING) && !wv.lm[b].fail && !wv.lm[b].ref_done;
 }
 
 // ---- pose-pair twists -------------------------------------------------------
@@ -533,7 +535,7 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkView wv) {
+__global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkView wv, float outer_tol) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int b = pv.fs_prob[blockIdx.x];
   if (!refine_active(wv, b)) return;
@@ -638,19 +640,31 @@ __global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkVie
   cp_async_wait_all();
   __syncthreads();
   chol_substitute<float>(Lm, cb, y, dinv, tmp, P);
+  __shared__ unsigned mx_dx, mx_x;  // largest |correction|, |step| (float bits: non-negative floats order as ints)
+  if (tid == 0) mx_dx = mx_x = 0u;
+  __syncthreads();
   for (int k = tid; k < P; k += nt) {
     const double dx = (double)y[k];
-    wv.delta[po + k] += dx;
+    const double x = wv.delta[po + k] + dx;
+    wv.delta[po + k] = x;
     wv.ddelta[po + k] = dx;
+    if (outer_tol > 0.f) {
+      atomicMax(&mx_dx, __float_as_uint(fabsf((float)dx)));
+      atomicMax(&mx_x, __float_as_uint(fabsf((float)x)));
+    }
   }
+  __syncthreads();
+  // converged: the correction is a small fraction of the step, further steps are skipped
+  if (tid == 0 && outer_tol > 0.f && __uint_as_float(mx_dx) <= outer_tol * __uint_as_float(mx_x))
+    wv.lm[b].ref_done = 1;
 }
 
-int launch_resid_solve(const PlanView &pv, const WorkView &wv, int first, void *stream) {
+int launch_resid_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int first, void *stream) {
   (void)first;  // every pass reduces the same duals of e
   const size_t sm = resid_solve_smem(pv.max_P_small, pv.max_P / 6);
   cudaStream_t st = (cudaStream_t)stream;
   cudaFuncSetAttribute(k_resid_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_resid_solve<<<pv.B, kRsThreads, sm, st>>>(pv, wv);
+  k_resid_solve<<<pv.B, kRsThreads, sm, st>>>(pv, wv, prm.outer_steps > 1 ? prm.outer_tol : 0.f);
   ++g_launches;
   return (int)cudaGetLastError();
 }

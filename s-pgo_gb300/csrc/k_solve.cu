@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(256) k_factor_solve(PlanView pv, WorkView wv, 
   __syncthreads();
   const bool failed = fail_s != 0;
   for (int i = threadIdx.x; i < P; i += blockDim.x) wv.delta[po + i] = failed ? 0.0 : x[i];
+  if (threadIdx.x == 0) wv.lm[b].ref_done = 0;  // this step's refinement starts afresh
   if (threadIdx.x == 0 && failed) atomicOr(&wv.lm[b].fail, FAIL_PIVOT);
   if constexpr (std::is_same<T, float>::value) {
     if (store && !failed) {  // packed factor, then the pivots' reciprocals
@@ -531,7 +532,7 @@ __global__ void k_reset(PlanView pv, WorkView wv, double lam) {
   s.rho1 = s.rho2 = s.rho3 = s.last_rel = s.last_predrel = 0.0;
   s.gnorm = s.dmean = s.dmax = s.dmin = s.cmean = 0.0;
   s.last_acc = s.rej_streak = 0;
-  s.wait_timeouts = s.pad2 = 0;
+  s.wait_timeouts = s.ref_done = 0;
   wv.lm[b] = s;
   wv.cost_acc[b] = 0.0;
   wv.pred_acc[b] = 0.0;

@@ -77,7 +77,8 @@ struct LMState {
   double rho1, rho2, rho3, last_rel, last_predrel;
   double gnorm, dmean, dmax, dmin, cmean;
   int32_t last_acc, rej_streak;
-  int32_t wait_timeouts, pad2;  // steps rejected because a bounded device wait ran out
+  int32_t wait_timeouts;  // steps rejected because a bounded device wait ran out
+  int32_t ref_done;       // this step's refinement has converged (outer_tol): skip its further steps
 };
 
 constexpr int32_t FAIL_PIVOT = 1, FAIL_TIMEOUT = 2;
@@ -140,7 +141,7 @@ struct Params {
   int32_t cost_block, lin_block;
   int32_t outer_steps, wait_us;
   float ctl_min_log10;
-  int32_t pad_;
+  float outer_tol;
 };
 
 // bounded device-side waits: the limit in nanoseconds (wait_us = 0: 2 s)
@@ -168,7 +169,7 @@ int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &pr
 int launch_pair_twists(const PlanView &pv, const WorkView &wv, void *stream);
 int launch_resid_pass(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha, int first,
                       void *stream);
-int launch_resid_solve(const PlanView &pv, const WorkView &wv, int first, void *stream);
+int launch_resid_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int first, void *stream);
 int launch_refine_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
                         void *stream);
 int launch_backsub_refined(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,

@@ -214,7 +214,7 @@ class BatchSolver:
     def set_params(self, loss: Optional[str] = None, loss_scale=None, near_boost=None, eps=None,
                    alpha_min=None, alpha_max=None, lambda0=None, lambda_max=None, tol=None, max_iters=None,
                    refine_steps=None, use_graph=None, use_tc=None, cost_block=None, lin_block=None,
-                   outer_steps=None, wait_us=None, ctl_min_log10=None):
+                   outer_steps=None, wait_us=None, ctl_min_log10=None, outer_tol=None):
         p = self.params
         if loss is not None:
             p.loss = _LOSS[loss]
@@ -243,6 +243,8 @@ class BatchSolver:
             p.wait_us = int(wait_us)
         if ctl_min_log10 is not None:
             p.ctl_min_log10 = float(ctl_min_log10)
+        if outer_tol is not None:
+            p.outer_tol = float(outer_tol)
         self._apply_params()
 
     def _apply_params(self):
