@@ -174,7 +174,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
   // residual store: the Jacobian pass reads the state's half; the cost pass of the
   // state after a reset writes the state's half, a candidate's the other half
   const int sel = wv.lm[b].res_sel;
-  float *res_buf = wv.res + (size_t)(COST && gate != GATE_FIRST ? 1 - sel : sel) * (size_t)pv.O * 4;
+  const size_t half = (size_t)(COST && gate != GATE_FIRST ? 1 - sel : sel);
+  float *res_buf = wv.res + half * (size_t)pv.O * 4;
+  float *tcam_buf = wv.tcam ? wv.tcam + half * (size_t)pv.O * 6 : nullptr;  // mixed path: camera-frame points
   // cost pass: each thread's observation record is loaded one loop pass ahead (the
   // first one here, so its DRAM latency overlaps phase A), so a pass does not open
   // with a round trip to DRAM; the Jacobian pass has no registers to spare for it
@@ -278,6 +280,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
       const int n = cur_n;
       const float4 z = cur_z;
       float4 rstore = make_float4(0.f, 0.f, 0.f, 0.f);  // cost pass: residuals to keep
+      float tstore[6];                                    // and the camera-frame points
       const int a = sm.a[slot];
       const Vec3<T> X = v3<T>(sm.X[slot][0], sm.X[slot][1], sm.X[slot][2]);
       const int fa = fo + a, fn = fo + n;
@@ -322,6 +325,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
           r0 = (nu.h + nu.l) * itz;
           r1 = (nv.h + nv.l) * itz;
           t = v3<T>(tt[0].h, tt[1].h, tt[2].h);
+          tstore[3 * cam] = tt[0].h;
+          tstore[3 * cam + 1] = tt[1].h;
+          tstore[3 * cam + 2] = tt[2].h;
           if (cam) {
             rstore.z = r0;
             rstore.w = r1;
@@ -372,7 +378,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
           q[5] += u0.z * sj0 + u1.z * sj1;
         }
       }
-      if constexpr (COST && std::is_same<T, float>::value) reinterpret_cast<float4 *>(res_buf)[o] = rstore;
+      if constexpr (COST && std::is_same<T, float>::value) {
+        reinterpret_cast<float4 *>(res_buf)[o] = rstore;
+        if (tcam_buf) {  // 24 bytes at 8-byte alignment
+          float2 *tp = reinterpret_cast<float2 *>(tcam_buf + (size_t)o * 6);
+          tp[0] = make_float2(tstore[0], tstore[1]);
+          tp[1] = make_float2(tstore[2], tstore[3]);
+          tp[2] = make_float2(tstore[4], tstore[5]);
+        }
+      }
       if (!COST) {
         atomicAdd(&sm.C[slot], accC);
         atomicAdd(&sm.ga[slot], accG);
@@ -508,8 +522,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
 // double-float) for the refined step's predicted decrease, which near the optimum is a
 // small difference of large terms.
 struct JacSmem {
-  float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre (hi)
-  float Xl[SPGO_CHUNK][3];  // its low words
+  float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre
   float dX[SPGO_CHUNK][3];  // dX / d alpha
   float C[SPGO_CHUNK], ga[SPGO_CHUNK];
   int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
@@ -614,6 +627,7 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
   const int rows = 6 * nb;
   const int64_t ob = pv.lm_obs[lm0], oe = pv.lm_obs[lm0 + cnt];
   const float *res_buf = wv.res + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 4;  // the state's residuals
+  const float *tcam_buf = wv.tcam + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 6;  // and camera-frame points
 
   // phase A: the chunk's anchor points (double-float, then split)
   if (tid < cnt) {
@@ -630,7 +644,6 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
       const df v = df{Rh[3 * k], Rl[3 * k]} * t3[0] + df{Rh[3 * k + 1], Rl[3 * k + 1]} * t3[1] +
                    df{Rh[3 * k + 2], Rl[3 * k + 2]} * t3[2];
       sm.X[tid][k] = v.h;
-      sm.Xl[tid][k] = v.l;
       sm.dX[tid][k] = -v.h / alf;
     }
     sm.C[tid] = 0.f;
@@ -692,20 +705,14 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
       if (has_pose && lo != a) d = FramesT<float>::rel(wv, fo + a, 0, fo + lo, 0);
       const Vec3<float> Xp = v3<float>(X.x + d.x, X.y + d.y, X.z + d.z);
       float accC = 0.f, accG = 0.f;
+      // the camera-frame points of both cameras, as the cost pass at this state formed
+      // them (double-float, rounded once)
+      const float2 *tp = reinterpret_cast<const float2 *>(tcam_buf + (size_t)o * 6);
+      const float2 t01 = tp[0], t23 = tp[1], t45 = tp[2];
 #pragma unroll
       for (int cam = 0; cam < 2; ++cam) {
         const float *Rn = FramesT<float>::R(wv, fn, cam);
-        const float *Rl = wv.fr_Rl + (size_t)fn * 18 + cam * 9;
-        const int fw = n - f0;
-        df Xc[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-          Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{dch[fw * 6 + cam * 3 + k], dcl[fw * 6 + cam * 3 + k]};
-        df tt[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-          tt[k] = df_dot3(Rn[k], Rl[k], Rn[3 + k], Rl[3 + k], Rn[6 + k], Rl[6 + k], Xc[0], Xc[1], Xc[2]);
-        const Vec3<float> t = v3<float>(tt[0].h, tt[1].h, tt[2].h);
+        const Vec3<float> t = cam ? v3<float>(t23.y, t45.x, t45.y) : v3<float>(t01.x, t01.y, t23.x);
         const float r0 = cam ? rl.z : rl.x, r1 = cam ? rl.w : rl.y;
         float rho;
         const float w2 = boost * robust<float>(prm.loss, lscale, r0 * r0 + r1 * r1, rho);

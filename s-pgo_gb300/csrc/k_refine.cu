@@ -141,8 +141,7 @@ constexpr int kRpWarps = kRpThreads / 32;
 constexpr int kRpPitch = 33;
 
 struct RefSmem {
-  float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre (hi)
-  float Xl[SPGO_CHUNK][3];  // its low words
+  float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre
   float dX[SPGO_CHUNK][3];  // dX / d alpha
   float da[SPGO_CHUNK];     // inverse-depth step (FP32 copy for the residuals)
   float t[SPGO_CHUNK];      // D^-1 r_a
@@ -152,18 +151,16 @@ struct RefSmem {
   int key[kRpWarps][32];
 };
 
-// dynamic shared memory (W = window frames): dc [W][6] float x 2 (hi, lo) | the
-// window's frame tables [W][36] (rotations of both cameras, hi then lo words) | the
-// pair origins' offsets [W][4] | the pair twists [W][6] | the per-warp staging
-// [warps][2 x 6][33] float of the pair duals
+// dynamic shared memory (W = window frames): the window's rotations [W][18] (both
+// cameras) | the pair origins' offsets [W][4] | the pair twists [W][6] | the per-warp
+// staging [warps][2 x 6][33] float of the pair duals
 struct RpLayout {
-  size_t dc, rw, xpo, tws, stage, total;
+  size_t rw, xpo, tws, stage, total;
   __host__ __device__ explicit RpLayout(int max_nb) {
     const size_t W = (size_t)max_nb + 1;
     auto up = [](size_t x) { return (x + 15) & ~(size_t)15; };
-    dc = 0;
-    rw = up(W * 12 * sizeof(float));
-    xpo = rw + up(W * 36 * sizeof(float));
+    rw = 0;
+    xpo = rw + up(W * 18 * sizeof(float));
     tws = xpo + up(W * 4 * sizeof(float));
     stage = tws + up(W * 6 * sizeof(float));
     total = stage + (size_t)kRpWarps * 2 * 6 * kRpPitch * sizeof(float);
@@ -201,8 +198,6 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
     }
   }
   const RpLayout lay(pv.max_nb);
-  float *dch = reinterpret_cast<float *>(smem_raw + lay.dc);
-  float *dcl = dch + (size_t)(pv.max_nb + 1) * 6;
   float *Rw = reinterpret_cast<float *>(smem_raw + lay.rw);
   float *xpo = reinterpret_cast<float *>(smem_raw + lay.xpo);
   float *tws = reinterpret_cast<float *>(smem_raw + lay.tws);
@@ -228,7 +223,6 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
         const df v = df{Rh[3 * k], Rl[3 * k]} * t3[0] + df{Rh[3 * k + 1], Rl[3 * k + 1]} * t3[1] +
                      df{Rh[3 * k + 2], Rl[3 * k + 2]} * t3[2];
         sm.X[lane][k] = v.h;
-        sm.Xl[lane][k] = v.l;
         sm.dX[lane][k] = -v.h / alf;
       }
       sm.a[lane] = a;
@@ -267,23 +261,11 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
       sm.da[lane] = (float)da;
     }
   } else {
-    // the host's left centre minus every window frame's camera centres (double-float),
-    // the window's frame tables, and per window frame n the offset c_a - c_n of the
-    // pair origin (n < a) and the twist of the pair (a, n)
+    // the window's rotations, and per window frame n the offset c_a - c_n of the pair
+    // origin (n < a) and the twist of the pair (a, n)
     const int ah = pv.lm_host[lm0], fh = fo + ah;
-    for (int idx = tid - 64; idx < (nb + 1) * 6; idx += blockDim.x - 64) {
-      const int f = idx / 6, cam = (idx / 3) & 1, k = idx % 3;
-      const size_t fn = (size_t)(fo + f0 + f);
-      df d = df_sub(wv.fr_ch[(size_t)fh * 6 + k], wv.fr_ch[fn * 6 + cam * 3 + k]);
-      d = d + df_make(wv.fr_cl[(size_t)fh * 6 + k] - wv.fr_cl[fn * 6 + cam * 3 + k]);
-      dch[idx] = d.h;
-      dcl[idx] = d.l;
-    }
-    for (int idx = tid - 64; idx < (nb + 1) * 36; idx += blockDim.x - 64) {
-      const int f = idx / 36, r = idx % 36;
-      const size_t fn = (size_t)(fo + f0 + f);
-      Rw[idx] = r < 18 ? wv.fr_Rf[fn * 18 + r] : wv.fr_Rl[fn * 18 + r - 18];
-    }
+    for (int idx = tid - 64; idx < (nb + 1) * 18; idx += blockDim.x - 64)
+      Rw[idx] = wv.fr_Rf[(size_t)(fo + f0) * 18 + idx];
     for (int f = tid - 64; f < nb + 1; f += blockDim.x - 64) {
       const int n = f0 + f;
       Vec3<float> d = v3<float>(0.f, 0.f, 0.f);
@@ -308,6 +290,7 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
   const float lscale = prm.loss_scale;
   // residuals at the linearisation point: the state's half of the residual store
   const float *res_buf = wv.res + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 4;
+  const float *tcam_buf = wv.tcam + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 6;
   for (int64_t base = ob + (tid & ~31); base < oe; base += blockDim.x) {
     const int64_t o = base + lane;
     // this observation's pose rows s K of both cameras (zero without a pose term), its
@@ -341,20 +324,14 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
       float W[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) W[k] = tws[6 * fw + k];
+      const float2 *tp = reinterpret_cast<const float2 *>(tcam_buf + (size_t)o * 6);
+      const float2 t01 = tp[0], t23 = tp[1], t45 = tp[2];
 #pragma unroll
       for (int cam = 0; cam < 2; ++cam) {
-        // camera-frame point as the linearisation forms it (double-float, rounded once)
-        const float *Rn = Rw + fw * 36 + cam * 9;
-        const float *Rl = Rw + fw * 36 + 18 + cam * 9;
-        df Xc[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-          Xc[k] = df{sm.X[slot][k], sm.Xl[slot][k]} + df{dch[fw * 6 + cam * 3 + k], dcl[fw * 6 + cam * 3 + k]};
-        df tt[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-          tt[k] = df_dot3(Rn[k], Rl[k], Rn[3 + k], Rl[3 + k], Rn[6 + k], Rl[6 + k], Xc[0], Xc[1], Xc[2]);
-        const Vec3<float> t = v3<float>(tt[0].h, tt[1].h, tt[2].h);
+        // the camera-frame point as the cost pass at the state formed it (double-float,
+        // rounded once): the same Jacobian the linearisation used
+        const float *Rn = Rw + fw * 18 + cam * 9;
+        const Vec3<float> t = cam ? v3<float>(t23.y, t45.x, t45.y) : v3<float>(t01.x, t01.y, t23.x);
         const float r0 = cam ? rl.z : rl.x, r1 = cam ? rl.w : rl.y;
         float rho;
         const float w2 = boost * robust<float>(prm.loss, lscale, r0 * r0 + r1 * r1, rho);

@@ -96,6 +96,8 @@ struct WorkView {
   double *alpha_cand;   // [L] (caller order)
   float *res;           // [2][O][4] residuals of the cost passes (FP32 path): u_l, v_l, u_r, v_r; half
                         // LMState::res_sel holds the state's, the other the last candidate's
+  float *tcam;          // [2][O][6] the camera-frame points of the same cost passes (left, right),
+                        // the double-float value rounded once; halves as res (mixed path)
   void *pair_acc;       // [total_pairs][27] T  (accumulated by the linearisation)
   void *pairF;          // [total_pairs][27] T  (prefix / suffix sums)
   void *A;              // [total_S] T      pose-pose blocks
