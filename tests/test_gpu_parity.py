@@ -3,6 +3,7 @@ through the C ABI.  Tolerances: FP64 path 1e-9 relative; mixed path (FP32
 Jacobians / Hessian blocks) 1e-4 relative on H and g blocks (relative to the
 largest entry), 1e-6 relative on the FP64 cost; converged LM state: cost 1e-6
 relative, poses 1e-5 rad / 1e-5 m."""
+import ctypes as C
 import os
 import types
 
@@ -441,3 +442,26 @@ def test_large_path_step_matches_fp64_step(built_lib, cuda_device, config):
     dc = abs(out["mixed"][2] - out["fp64"][2]) / out["fp64"][2]
     print(f"{config}: pose step {dp:.2e}, inverse-depth step {da:.2e}, cost after the step {dc:.2e}")
     assert dp < 1e-5 and da < 1e-5 and dc < 1e-7
+
+
+def test_adaptive_refinement_brackets(built_lib, cuda_device):
+    """The second refinement step is adaptive (outer_tol): with a tolerance no
+    correction can exceed, every problem stops after one step and the solve repeats
+    the one-step solve; with tolerance 0 every problem takes both steps; the default
+    sits between.  All of them reach the FP64 oracle's cost on problems that converge
+    to their optimum."""
+    probs = [f32_obs(scenes.circle_scene(s, n, l)) for s, n, l in [(200, 8, 500), (205, 18, 455), (214, 31, 234)]]
+    ref = [S.lm_solve(p.copy(), S.Loss(), max_iters=30, tol=1e-6).cost for p in probs]
+    d = nat.Params()
+    built_lib.spgo_default_params(C.byref(d))
+    assert d.outer_steps == 2 and abs(d.outer_tol - 1e-3) < 1e-9
+    out = {}
+    for name, kw in (("one", dict(outer_steps=1)), ("skip_all", dict(outer_steps=2, outer_tol=0.999)),
+                     ("default", {}), ("both", dict(outer_steps=2, outer_tol=0.0))):
+        bs = BatchSolver([p.copy() for p in probs], precision="mixed")
+        bs.set_params(loss="l2", max_iters=30, tol=1e-6, **kw)
+        st = bs.solve()
+        out[name] = [s["cost"] for s in st]
+        for s, c in zip(st, ref):
+            assert abs(s["cost"] - c) / c < 1e-6, (name, s["cost"], c)
+        bs.close()

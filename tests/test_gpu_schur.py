@@ -77,3 +77,26 @@ def test_autotune_picks_valid_shapes_and_restores_state(built_lib, cuda_device):
     after = [s["cost"] for s in bs.solve()]
     for c0, c1 in zip(base, after):
         assert abs(c1 - c0) / c0 < 1e-6
+
+
+def test_plan_shapes_autotune_and_equal_results(built_lib, cuda_device):
+    """The plan-time Schur work shapes (chunks per tensor-core work item) change how
+    the products are split into CTAs, not the reduced system: every shape reaches the
+    oracle's cost, and autotune_plan_shapes returns one of its candidates without
+    touching the solver it was called on."""
+    probs = [scenes.circle_scene(s, n, l) for s, n, l in [(200, 8, 500), (205, 18, 455), (214, 31, 234)]]
+    ref = [S.lm_solve(f32_obs(p), S.Loss(), max_iters=30, tol=1e-6).cost for p in probs]
+    for split in (8, 32, 64):
+        bs = BatchSolver([f32_obs(p) for p in probs], precision="mixed", plan_options=dict(tc_split=split))
+        assert bs.sizes.tc_split == split
+        bs.set_params(loss="l2", max_iters=30, tol=1e-6, use_tc=1)
+        for st, c in zip(bs.solve(), ref):
+            assert abs(st["cost"] - c) / c < 1e-6, (split, st["cost"], c)
+        bs.close()
+    bs = BatchSolver([f32_obs(p) for p in probs], precision="mixed")
+    bs.set_params(loss="l2", max_iters=30, tol=1e-6, use_tc=1)
+    p0, a0 = bs.poses.clone(), bs.alpha.clone()
+    out = bs.autotune_plan_shapes(iterations=1, repeats=1)
+    assert out["best"]["tc_split"] in (16, 32, 64) and len(out["ms"]) == 3
+    assert bool((bs.poses == p0).all()) and bool((bs.alpha == a0).all())
+    bs.close()

@@ -49,7 +49,7 @@ def Ad(R, c, x):
 
 def pair_assembly(prob, loss, one_origin=False):
     """A, g_T, B of the problem assembled the way the kernels do (FP64).  one_origin:
-    the mixed path's order (csrc/k_system.cu k_pair_reduce_df, k_pairs_to_A_df; the slab
+    the mixed path's order (csrc/k_system.cu k_pair_shift_df, k_pair_scan_df, k_pairs_to_A_df; the slab
     terms of csrc/k_linearize.cu k_jacobian_acc): every record moved once from c_lo to
     c_0, prefix and suffix sums about c_0, each block moved from c_0 to c_i; the slab
     terms formed from the rows about the pair origin and moved to the anchor centre."""
