@@ -526,6 +526,8 @@ struct JacSmem {
   float dX[SPGO_CHUNK][3];  // dX / d alpha
   float C[SPGO_CHUNK], ga[SPGO_CHUNK];
   int a[SPGO_CHUNK], lo[SPGO_CHUNK], hi[SPGO_CHUNK];
+  unsigned rmask[SPGO_MAX_WINDOW];  // per window row: the landmarks whose window holds its frame
+  int rsp[SPGO_MAX_WINDOW + 1];     // exclusive prefix of the rows' landmark counts
   int key[8][32];           // per warp: target frame of each lane's observation (-1: none)
   float glh[8][SPGO_CHUNK];  // per warp: exactly summed g_a, double-float (h, l)
   float gll[8][SPGO_CHUNK];
@@ -651,6 +653,19 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
     sm.a[tid] = a;
     sm.lo[tid] = pv.lm_lo[li];
     sm.hi[tid] = pv.lm_hi[li];
+  }
+  if (tid < 32) {  // per window row, the landmarks whose window [lo, hi) holds its frame
+    const int lo = tid < cnt ? pv.lm_lo[lm0 + tid] : 0, hi = tid < cnt ? pv.lm_hi[lm0 + tid] : 0;
+    int run = 0;
+    for (int i = 0; i < nb; ++i) {
+      const unsigned m = __ballot_sync(0xffffffffu, lo <= f0 + i && f0 + i < hi);
+      if (tid == 0) {
+        sm.rmask[i] = m;
+        sm.rsp[i] = run;
+      }
+      run += __popc(m);
+    }
+    if (tid == 0) sm.rsp[nb] = run;
   }
   {  // the host's left centre minus every window frame's camera centres (double-float)
     const int fh = fo + pv.lm_host[lm0];
@@ -831,16 +846,32 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
   }
   __syncthreads();
   // phase C.2: B_l(i) = Ad_i^T b_l(i) about the anchor centre,
-  //   [R_i^T (b_w - (c_i - c_a) x b_v) ; R_i^T b_v], in double-float, rounded once
-  float *gslab = reinterpret_cast<float *>(wv.slab) + pv.ch_slab[c];
-  for (int idx = tid; idx < cnt * nb; idx += blockDim.x) {
-    const int slot = idx % cnt, i = f0 + idx / cnt;
-    const size_t at = (size_t)(6 * (i - f0)) * SPGO_CHUNK + slot;
-    if (i < sm.lo[slot] || i >= sm.hi[slot]) {
+  //   [R_i^T (b_w - (c_i - c_a) x b_v) ; R_i^T b_v], in double-float, rounded once,
+  // for the (landmark, frame) pairs inside the landmark's window [lo, hi) only (about
+  // 60 % of the chunk window's pairs), enumerated row by row so that a warp's lanes
+  // take different landmarks (slab columns, distinct banks); each result replaces its
+  // own b_l(i) in slab_h, whose other entries (outside the windows, empty columns) are
+  // still zero
+  const int n_in = sm.rsp[nb];
+  for (int j = tid; j < n_in; j += blockDim.x) {
+    int row = 0;  // the last window row whose pairs start at or before pair j
 #pragma unroll
-      for (int k = 0; k < 6; ++k) gslab[at + k * SPGO_CHUNK] = 0.f;
-      continue;
+    for (int step = 64; step >= 1; step >>= 1)
+      if (row + step < nb && sm.rsp[row + step] <= j) row += step;
+    // the landmark: the (j - rsp[row])-th set bit of the row's mask
+    unsigned m = sm.rmask[row];
+    int r = j - sm.rsp[row], slot = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+      const int c = __popc(m & ((1u << w) - 1u));
+      if (r >= c) {
+        r -= c;
+        m >>= w;
+        slot += w;
+      }
     }
+    const int i = f0 + row;
+    const size_t at = (size_t)(6 * (i - f0)) * SPGO_CHUNK + slot;
     const float *Rh = wv.fr_Rf + (size_t)(fo + i) * 18, *Rl = wv.fr_Rl + (size_t)(fo + i) * 18;
     df d[3], bw[3], bv[3];
 #pragma unroll
@@ -857,12 +888,16 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
       // (R^T v)_r = sum_k R(k, r) v_k
       const df Bw = df_dot3(Rh[r], Rl[r], Rh[3 + r], Rl[3 + r], Rh[6 + r], Rl[6 + r], tw[0], tw[1], tw[2]);
       const df Bv = df_dot3(Rh[r], Rl[r], Rh[3 + r], Rl[3 + r], Rh[6 + r], Rl[6 + r], bv[0], bv[1], bv[2]);
-      gslab[at + r * SPGO_CHUNK] = Bw.h + Bw.l;
-      gslab[at + (3 + r) * SPGO_CHUNK] = Bv.h + Bv.l;
+      slab_h[at + r * SPGO_CHUNK] = Bw.h + Bw.l;
+      slab_h[at + (3 + r) * SPGO_CHUNK] = Bv.h + Bv.l;
     }
   }
-  for (int idx = tid; idx < rows * SPGO_CHUNK; idx += blockDim.x)  // empty columns: the Schur pass reads all 32
-    if (idx % SPGO_CHUNK >= cnt) gslab[idx] = 0.f;
+  __syncthreads();
+  {  // the chunk's slab, every row and all 32 columns (the Schur pass reads them all)
+    float4 *g4 = reinterpret_cast<float4 *>(reinterpret_cast<float *>(wv.slab) + pv.ch_slab[c]);
+    const float4 *s4 = reinterpret_cast<const float4 *>(slab_h);
+    for (int idx = tid; idx < rows * (SPGO_CHUNK / 4); idx += blockDim.x) g4[idx] = s4[idx];
+  }
   if (tid < cnt) {
     reinterpret_cast<float *>(wv.C)[lm0 + tid] = sm.C[tid];
     reinterpret_cast<float *>(wv.ga)[lm0 + tid] = sm.ga[tid];

@@ -144,7 +144,7 @@ struct RefSmem {
   float X[SPGO_CHUNK][3];   // anchor point, world axes, relative to the anchor centre
   float dX[SPGO_CHUNK][3];  // dX / d alpha
   float da[SPGO_CHUNK];     // inverse-depth step (FP32 copy for the residuals)
-  float t[SPGO_CHUNK];      // D^-1 r_a
+  __align__(16) float t[SPGO_CHUNK];  // D^-1 r_a
   int a[SPGO_CHUNK];
   float dlh[kRpWarps][SPGO_CHUNK];  // j_a^T W e, per warp, double-float (h, l)
   float dll[kRpWarps][SPGO_CHUNK];
@@ -439,22 +439,23 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
     sm.t[tid] = 0.f;
   }
   __syncthreads();
-  // W t into the pose right-hand side: warp per slab row, lane = landmark slot; eight
-  // of the warp's rows loaded before any is reduced
-  const float tv = sm.t[lane];
-  for (int r0 = warp; r0 < rows; r0 += 8 * kRpWarps) {
-    float x[8];
+  // W t into the pose right-hand side: thread per slab row, its 32 landmark entries read
+  // as eight 16-byte loads (the chunk's slab starts 16-byte aligned, rows are 128 bytes)
+  const float4 *t4 = reinterpret_cast<const float4 *>(sm.t);
+  for (int r = tid; r < rows; r += blockDim.x) {
+    const float4 *sr = reinterpret_cast<const float4 *>(slab + (size_t)r * SPGO_CHUNK);
+    float4 x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = sr[q];
+    float v0 = 0.f, v1 = 0.f;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      const int r = r0 + q * kRpWarps;
-      x[q] = r < rows ? slab[(size_t)r * SPGO_CHUNK + lane] : 0.f;
+      const float4 t = t4[q];
+      v0 += x[q].x * t.x + x[q].y * t.y;
+      v1 += x[q].z * t.z + x[q].w * t.w;
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int r = r0 + q * kRpWarps;
-      const float v = warp_sum(x[q] * tv);
-      if (lane == 0 && r < rows && v != 0.f) atomicAdd(wv.rhsB + po + 6 * f0 + r, v);
-    }
+    const float v = v0 + v1;
+    if (v != 0.f) atomicAdd(wv.rhsB + po + 6 * f0 + r, v);
   }
 }
 
