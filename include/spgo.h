@@ -160,6 +160,11 @@ typedef struct spgo_params {
                                     refinement step only while its last correction exceeds
                                     outer_tol times its step (largest entries); default 1e-3;
                                     0: every step */
+    float   stop_rho;            /* an accepted step whose relative decrease is below tol ends
+                                    the solve only if its gain ratio (actual / predicted
+                                    decrease) is at least stop_rho; a smaller ratio marks a
+                                    poor local model, not a converged problem, and the solve
+                                    goes on.  In [0, 1); default 0: every such step ends it */
 } spgo_params;
 
 typedef struct spgo_problem_status {

@@ -319,14 +319,15 @@ class LMResult:
 
 
 def lm_solve(prob, loss: Loss = Loss(), max_iters=20, tol=1e-6, lam0=1e-4, eps=1e-4,
-             alpha_min=1.0 / 30.0, alpha_max=1.0 / 0.2, lam_max=1e16):
+             alpha_min=1.0 / 30.0, alpha_max=1.0 / 0.2, lam_max=1e16, stop_rho=0.0):
     """Nielsen-damped Levenberg-Marquardt (new; the reference has no schedule).
 
     Marquardt scaling (see ``solve_damped``); gain ratio rho = (F - F') / pred.
     rho > 0: accept, lam *= max(1/3, 1 - (2 rho - 1)^3), nu = 2;
     otherwise reject, lam *= nu, nu *= 2.  Stops when an accepted step lowers
-    the cost by less than ``tol`` relative, or after ``max_iters`` solves
-    (accepted + rejected).  Mutates ``prob`` and returns an ``LMResult``.
+    the cost by less than ``tol`` relative with rho >= ``stop_rho`` (default 0:
+    any accepted step), or after ``max_iters`` solves (accepted + rejected).
+    Mutates ``prob`` and returns an ``LMResult``.
     """
     lam, nu = lam0, 2.0
     lin = linearize(prob, loss)
@@ -351,7 +352,7 @@ def lm_solve(prob, loss: Loss = Loss(), max_iters=20, tol=1e-6, lam0=1e-4, eps=1
             F = Fn
             lam *= max(1.0 / 3.0, 1.0 - (2.0 * rho - 1.0) ** 3)
             nu = 2.0
-            if rel < tol:
+            if rel < tol and rho >= stop_rho:
                 converged = True
                 break
             lin = linearize(prob, loss)

@@ -1023,6 +1023,7 @@ void spgo_default_params(spgo_params *p) {
   p->wait_us = 0;
   p->ctl_min_log10 = -6.0f;
   p->outer_tol = 1e-3f;
+  p->stop_rho = 0.f;
 }
 
 int spgo_plan_create(const spgo_host_problem *problems, int32_t n_problems, int32_t precision, spgo_plan **out) {
@@ -1222,7 +1223,8 @@ int spgo_set_params(spgo_solver *s, const spgo_params *p) {
   if (p->loss < 0 || p->loss > 2) return fail(SPGO_ERR_INVALID_ARG, "unknown loss");
   if (!(p->loss_scale > 0) || !(p->eps >= 0) || !(p->alpha_min < p->alpha_max) || p->max_iters < 0 ||
       p->refine_steps < 0 || !(p->lambda0 >= 0) || p->outer_steps < 0 || p->outer_steps > 8 || p->wait_us < 0 ||
-      !(p->ctl_min_log10 <= 0.f && p->ctl_min_log10 >= -6.f) || !(p->outer_tol >= 0.f && p->outer_tol < 1.f))
+      !(p->ctl_min_log10 <= 0.f && p->ctl_min_log10 >= -6.f) || !(p->outer_tol >= 0.f && p->outer_tol < 1.f) ||
+      !(p->stop_rho >= 0.f && p->stop_rho < 1.f))
     return fail(SPGO_ERR_INVALID_ARG, "parameter out of range");
   for (const int32_t blk : {p->cost_block, p->lin_block})
     if (blk != 0 && (blk < 32 || blk > 256 || blk % 32 != 0))

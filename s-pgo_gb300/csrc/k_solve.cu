@@ -607,7 +607,7 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
     s.nu = 2.0;
     s.relin = 1;
     s.res_sel ^= 1;  // the candidate's residuals are now the state's
-    if (rel < prm.tol) s.status = SPGO_STATUS_CONVERGED;
+    if (rel < prm.tol && rho >= (double)prm.stop_rho) s.status = SPGO_STATUS_CONVERGED;
   } else {
     if (s.fail & FAIL_TIMEOUT)
       s.wait_timeouts += 1;

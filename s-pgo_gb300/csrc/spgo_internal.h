@@ -144,6 +144,7 @@ struct Params {
   int32_t outer_steps, wait_us;
   float ctl_min_log10;
   float outer_tol;
+  float stop_rho;
 };
 
 // bounded device-side waits: the limit in nanoseconds (wait_us = 0: 2 s)

@@ -67,7 +67,8 @@ class Params(C.Structure):
                 ("lambda_max", C.c_double), ("tol", C.c_double), ("max_iters", C.c_int32),
                 ("refine_steps", C.c_int32), ("use_graph", C.c_int32), ("use_tc", C.c_int32),
                 ("cost_block", C.c_int32), ("lin_block", C.c_int32), ("outer_steps", C.c_int32),
-                ("wait_us", C.c_int32), ("ctl_min_log10", C.c_float), ("outer_tol", C.c_float)]
+                ("wait_us", C.c_int32), ("ctl_min_log10", C.c_float), ("outer_tol", C.c_float),
+                ("stop_rho", C.c_float)]
 
 
 class ProblemStatus(C.Structure):

@@ -214,7 +214,8 @@ class BatchSolver:
     def set_params(self, loss: Optional[str] = None, loss_scale=None, near_boost=None, eps=None,
                    alpha_min=None, alpha_max=None, lambda0=None, lambda_max=None, tol=None, max_iters=None,
                    refine_steps=None, use_graph=None, use_tc=None, cost_block=None, lin_block=None,
-                   outer_steps=None, wait_us=None, ctl_min_log10=None, outer_tol=None):
+                   outer_steps=None, wait_us=None, ctl_min_log10=None, outer_tol=None,
+                   stop_rho=None):
         p = self.params
         if loss is not None:
             p.loss = _LOSS[loss]
@@ -245,6 +246,8 @@ class BatchSolver:
             p.ctl_min_log10 = float(ctl_min_log10)
         if outer_tol is not None:
             p.outer_tol = float(outer_tol)
+        if stop_rho is not None:
+            p.stop_rho = float(stop_rho)
         self._apply_params()
 
     def _apply_params(self):

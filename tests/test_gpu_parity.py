@@ -444,6 +444,32 @@ def test_large_path_step_matches_fp64_step(built_lib, cuda_device, config):
     assert dp < 1e-5 and da < 1e-5 and dc < 1e-7
 
 
+@pytest.mark.parametrize("prec,cost_tols", [("fp64", (1e-6, 1e-6)), ("mixed", (1e-4, 1e-6))])
+def test_stop_rho_matches_oracle(built_lib, cuda_device, prec, cost_tols):
+    """The gain-ratio condition of the stopping test (spgo_params.stop_rho) against the
+    oracle's LM with the same rule: with tol 0.2 the plain rule stops this scene on an
+    accepted step with rho ~0.06 (iteration 4, mid-descent); with stop_rho 0.25 both go
+    on to the same later stop.  Same iteration counts; costs to cost_tols (the mixed
+    step's ~1e-7 difference from the FP64 step moves the cost of that poorly modelled
+    step by ~1e-5)."""
+    p = f32_obs(scenes.circle_scene(301, 8, 200))
+    its = []
+    for sr, cost_tol in zip((0.0, 0.25), cost_tols):
+        ref = S.lm_solve(p.copy(), S.Loss(), max_iters=30, tol=0.2, stop_rho=sr)
+        bs = BatchSolver([p.copy()], precision=prec)
+        bs.set_params(loss="l2", max_iters=30, tol=0.2, lambda0=1e-4, stop_rho=sr)
+        st = bs.solve()[0]
+        bs.close()
+        assert st["status"] == nat.STATUS_CONVERGED
+        assert st["iterations"] == ref.iterations, (sr, st["iterations"], ref.iterations)
+        assert abs(st["cost"] - ref.cost) / ref.cost < cost_tol
+        its.append(ref.iterations)
+    assert its[1] > its[0]
+    d = nat.Params()
+    nat.lib().spgo_default_params(C.byref(d))
+    assert d.stop_rho == 0.0
+
+
 def test_adaptive_refinement_brackets(built_lib, cuda_device):
     """The second refinement step is adaptive (outer_tol): with a tolerance no
     correction can exceed, every problem stops after one step and the solve repeats

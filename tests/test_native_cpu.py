@@ -63,6 +63,18 @@ def plan(problems, prec=nat.PREC_MIXED, f64=False):
     return rc, out
 
 
+def test_default_params_layout(built_lib):
+    """The ctypes mirror of spgo_params matches the C struct: spgo_default_params
+    writes nothing past it, and every field reads back its documented default."""
+    n = C.sizeof(nat.Params)
+    buf = (C.c_ubyte * (n + 64))(*([0xA5] * (n + 64)))
+    nat.lib().spgo_default_params(C.cast(buf, C.POINTER(nat.Params)))
+    assert all(b == 0xA5 for b in bytes(buf)[n:])
+    d = nat.Params.from_buffer_copy(bytes(buf)[:n])
+    assert d.max_iters > 0 and d.outer_steps == 2 and d.use_tc == 1
+    assert abs(d.outer_tol - 1e-3) < 1e-9 and d.ctl_min_log10 == -6.0 and d.stop_rho == 0.0
+
+
 @pytest.mark.parametrize("f64", [False, True])
 def test_plan_sizes(built_lib, f64):
     ps = [scenes.circle_scene(s, 8 + s, 100 + 37 * s) for s in range(5)]

@@ -96,6 +96,23 @@ def test_lm_converges_config0():
     assert np.abs(lin.g_T).max() < 1e-3 * np.abs(S.linearize(scenes.config0(), S.Loss()).g_T).max()
 
 
+def test_lm_stop_rho_defers_a_poorly_modelled_stop():
+    """With a loose tolerance (0.2) the plain rule stops this scene on an accepted step
+    whose gain ratio is 0.06; with stop_rho = 0.25 that step no longer ends the solve:
+    the solve ends on a step with rho >= 0.25, later and at a lower cost."""
+    p = scenes.circle_scene(301, 8, 200)
+    r0 = S.lm_solve(p.copy(), S.Loss(), max_iters=30, tol=0.2)
+    r1 = S.lm_solve(p.copy(), S.Loss(), max_iters=30, tol=0.2, stop_rho=0.25)
+    last0 = [t for t in r0.trace if t["rho"] > 0][-1]
+    last1 = [t for t in r1.trace if t["rho"] > 0][-1]
+    assert r0.converged and r1.converged
+    assert last0["rho"] < 0.25 and (last0["cost"] - last0["cand"]) < 0.2 * last0["cost"]
+    assert last1["rho"] >= 0.25 and (last1["cost"] - last1["cand"]) < 0.2 * last1["cost"]
+    assert r1.iterations > r0.iterations and r1.cost < r0.cost
+    # the two runs agree up to the deferred stop
+    assert [t["cand"] for t in r1.trace[:r0.iterations]] == [t["cand"] for t in r0.trace]
+
+
 def test_reference_gn_step_decreases_cost():
     p = scenes.circle_scene(5, 6, 80)
     c0 = S.cost(p, S.REFERENCE_GPU_LOSS)
