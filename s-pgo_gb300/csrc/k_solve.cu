@@ -34,8 +34,9 @@ __device__ __forceinline__ T s_entry(const T *A, const T *SL, int P, int r, int 
 // One CTA per problem: assemble S (lower) into the factor storage, then a
 // right-looking blocked Cholesky S = L L^T with 16-column blocks: warp 0
 // factorises the 16x16 diagonal block, all threads solve the rows below it
-// (independent per row) and apply the rank-16 trailing update; three barriers
-// per block.  The substitutions are blocked the same way (two barriers per
+// (independent per row) and apply the rank-16 trailing update, the next block's
+// columns first, so that warp 0 factorises the next diagonal block while the other
+// warps update the rest (one block of look-ahead); three barriers per block.  The substitutions are blocked the same way (two barriers per
 // block).  `refine` iterative-refinement steps form the residual g_S - S x
 // (double-float on the FP32 path, FP64 otherwise) from A and S_L in one
 // coalesced pass over the lower triangle.  Clears the S_L / g_L tiles it consumed.
@@ -85,38 +86,74 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
   }
   if (tid == 0) *fail_s = 0;
   __syncthreads();
+  // warp 0: the diagonal block [kb, kb + kPanel) in registers; lane i < w holds row i
+  // (a[j] = L(kb+i, kb+j), j <= i); column k is finished with one shuffle of the pivot
+  // and one per later row
+  auto factor_diag = [&](int kb) {
+    const int w = min(kb + kPanel, P) - kb;
+    T a[kPanel];
+#pragma unroll
+    for (int j = 0; j < kPanel; ++j) a[j] = (lane < w && j <= lane) ? Lm[ix(kb + lane, kb + j)] : T(0);
+    bool bad = false;
+    // (columns k >= w of a narrow last block run on a unit pivot and are discarded)
+#pragma unroll
+    for (int k = 0; k < kPanel; ++k) {
+      const T dk = __shfl_sync(0xffffffffu, a[k], k);
+      const T d = k < w ? dk : T(1);
+      bad = bad || !(d > T(0)) || !(d < T(INFINITY));  // (no FP64 conversion on the pivot chain)
+      const T lkk = sqrt(d), rinv = T(1) / lkk;  // correctly rounded: the refinement step relies on it
+      const T lik = lane > k ? a[k] * rinv : (lane == k ? lkk : a[k]);
+      a[k] = lik;
+#pragma unroll
+      for (int j = 0; j < kPanel; ++j) {
+        const T ljk = __shfl_sync(0xffffffffu, lik, j);
+        if (j > k && lane >= j) a[j] -= lik * ljk;
+      }
+      if (lane == 0 && k < w) dinv[kb + k] = rinv;
+    }
+#pragma unroll
+    for (int j = 0; j < kPanel; ++j)
+      if (lane < w && j <= lane) Lm[ix(kb + lane, kb + j)] = a[j];
+    if (bad && lane == 0) *fail_s = 1;
+  };
+  // the update of columns [c0, c1) (rows i >= j) with the finished block kb: warp wi of
+  // nwu, KC columns per warp pass (each loaded panel row serves KC columns)
+  auto update_cols = [&](auto kc_tag, const int (&cbk)[kPanel], int w, int c0, int c1, int wi, int nwu) {
+    constexpr int KC = decltype(kc_tag)::value;
+    for (int j0 = c0 + KC * wi; j0 < c1; j0 += KC * nwu) {
+      T ljk[KC][kPanel];
+#pragma unroll
+      for (int c = 0; c < KC; ++c)
+#pragma unroll
+        for (int k = 0; k < kPanel; ++k) ljk[c][k] = (k < w && j0 + c < c1) ? Lm[cbk[k] + j0 + c] : T(0);
+      for (int i = j0 + lane; i < P; i += 32) {
+        T li[kPanel];
+#pragma unroll
+        for (int k = 0; k < kPanel; ++k) li[k] = Lm[cbk[k] + i];
+#pragma unroll
+        for (int c = 0; c < KC; ++c) {
+          if (j0 + c < c1 && i >= j0 + c) {
+            T a0 = T(0), a1 = T(0);  // two half-length FMA chains per output
+#pragma unroll
+            for (int k = 0; k < kPanel; k += 2) {
+              a0 += li[k] * ljk[c][k];
+              a1 += li[k + 1] * ljk[c][k + 1];
+            }
+            Lm[cb[j0 + c] + i] -= a0 + a1;
+          }
+        }
+      }
+    }
+  };
+  // right-looking with one block of look-ahead: once block kb's rows are solved, the
+  // next block's columns take its update first; then warp 0 factors the next diagonal
+  // block while the other warps update the remaining columns.  Every element takes
+  // the same updates in the same order as without the look-ahead.
+  if (warp == 0) factor_diag(0);
+  __syncthreads();
+  if (*fail_s) return;
   for (int kb = 0; kb < P; kb += kPanel) {
     const int ke = min(kb + kPanel, P), w = ke - kb;
-    if (warp == 0) {
-      // diagonal block in registers: lane i < w holds row i (a[j] = L(kb+i, kb+j), j <= i);
-      // column k is finished with one shuffle of the pivot and one per later row
-      T a[kPanel];
-#pragma unroll
-      for (int j = 0; j < kPanel; ++j) a[j] = (lane < w && j <= lane) ? Lm[ix(kb + lane, kb + j)] : T(0);
-      bool bad = false;
-      // (columns k >= w of a narrow last block run on a unit pivot and are discarded)
-#pragma unroll
-      for (int k = 0; k < kPanel; ++k) {
-        const T dk = __shfl_sync(0xffffffffu, a[k], k);
-        const T d = k < w ? dk : T(1);
-        bad = bad || !(d > T(0)) || !(d < T(INFINITY));  // (no FP64 conversion on the pivot chain)
-        const T lkk = sqrt(d), rinv = T(1) / lkk;  // correctly rounded: the refinement step relies on it
-        const T lik = lane > k ? a[k] * rinv : (lane == k ? lkk : a[k]);
-        a[k] = lik;
-#pragma unroll
-        for (int j = 0; j < kPanel; ++j) {
-          const T ljk = __shfl_sync(0xffffffffu, lik, j);
-          if (j > k && lane >= j) a[j] -= lik * ljk;
-        }
-        if (lane == 0 && k < w) dinv[kb + k] = rinv;
-      }
-#pragma unroll
-      for (int j = 0; j < kPanel; ++j)
-        if (lane < w && j <= lane) Lm[ix(kb + lane, kb + j)] = a[j];
-      if (bad && lane == 0) *fail_s = 1;
-    }
-    __syncthreads();
-    if (*fail_s) return;
     // rows below the block: L(i, kb:ke) = S(i, kb:ke) L_D^-T
     int cbk[kPanel];
 #pragma unroll
@@ -139,34 +176,17 @@ __device__ void factor_solve_body(T *Lm, const int *cb, T *y, double *x, float *
         if (c < w) Lm[cbk[c] + i] = r[c];
     }
     __syncthreads();
-    // trailing update with the finished block, kCols columns per warp pass (each
-    // loaded panel row serves kCols columns; 2 in FP64 to bound registers)
-    constexpr int kCols = sizeof(T) == 8 ? 2 : 4;
-    for (int j0 = ke + kCols * warp; j0 < P; j0 += kCols * nw) {
-      T ljk[kCols][kPanel];
-#pragma unroll
-      for (int c = 0; c < kCols; ++c)
-#pragma unroll
-        for (int k = 0; k < kPanel; ++k) ljk[c][k] = (k < w && j0 + c < P) ? Lm[cbk[k] + j0 + c] : T(0);
-      for (int i = j0 + lane; i < P; i += 32) {
-        T li[kPanel];
-#pragma unroll
-        for (int k = 0; k < kPanel; ++k) li[k] = Lm[cbk[k] + i];
-#pragma unroll
-        for (int c = 0; c < kCols; ++c) {
-          if (j0 + c < P && i >= j0 + c) {
-            T a0 = T(0), a1 = T(0);  // two half-length FMA chains per output
-#pragma unroll
-            for (int k = 0; k < kPanel; k += 2) {
-              a0 += li[k] * ljk[c][k];
-              a1 += li[k + 1] * ljk[c][k + 1];
-            }
-            Lm[cb[j0 + c] + i] -= a0 + a1;
-          }
-        }
-      }
-    }
+    if (ke >= P) break;
+    const int ke2 = min(ke + kPanel, P);
+    update_cols(std::integral_constant<int, 2>{}, cbk, w, ke, ke2, warp, nw);  // the next block's columns
     __syncthreads();
+    // (4 columns per pass in FP32, 2 in FP64 to bound registers)
+    if (warp == 0)
+      factor_diag(ke);
+    else
+      update_cols(std::integral_constant<int, sizeof(T) == 8 ? 2 : 4>{}, cbk, w, ke2, P, warp - 1, nw - 1);
+    __syncthreads();
+    if (*fail_s) return;
   }
   for (int it = 0; it <= refine; ++it) {
     chol_substitute<T>(Lm, cb, y, dinv, tmp, P);
