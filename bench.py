@@ -347,7 +347,8 @@ def run_ours(args):
     ctl_params = net_params if args.controller else None
 
     plain_params = dict(loss="l2", max_iters=30, tol=1e-6, lambda0=1e-4)
-    base_params = dict(plain_params, max_iters=args.max_iters, use_tc=args.tc, stop_rho=args.stop_rho)
+    stop_rho = 0.25 if args.stop_rho is None else args.stop_rho
+    base_params = dict(plain_params, max_iters=args.max_iters, use_tc=args.tc, stop_rho=stop_rho)
     if args.outer >= 0:
         base_params["outer_steps"] = args.outer
     tuned = None
@@ -630,7 +631,7 @@ def run_ours(args):
             "raw_solves_per_s": raw_value, "solves_to_plain_cost_per_s": value,
             "config": {"workload": WORKLOAD, "problems_per_gpu": N_PROBLEMS, "landmarks": n_lm, "obs": n_obs,
                        "precision": "mixed", "outer_refinement_steps": int(bs.params.outer_steps),
-                       "chosen_max_iters": int(args.max_iters), "chosen_stop_rho": float(args.stop_rho),
+                       "chosen_max_iters": int(args.max_iters), "chosen_stop_rho": float(stop_rho),
                        "schur": "tcgen05 split TF32" if tuned["use_tc"] else "SIMT FP32",
                        "damping": "learned MLP + Nielsen fallback" if ctl_params is not None else "Nielsen",
                        "autotuned": tuned, "autotuned_plan": plan_tune,
@@ -697,7 +698,7 @@ def run_single(args):
         s = sv.BatchSolver([p], precision=prec, device=dev, stream=stream)
         s.set_params(**params)
         if prec == "mixed":
-            s.set_params(use_tc=args.tc, stop_rho=args.stop_rho)
+            s.set_params(use_tc=args.tc, stop_rho=0.0 if args.stop_rho is None else args.stop_rho)
             if args.outer >= 0:
                 s.set_params(outer_steps=args.outer)
         q0, a0 = s.poses.clone(), s.alpha.clone()
@@ -759,6 +760,7 @@ def run_single(args):
             "data": f"synthetic (seeded config-{args.config} generator)",
             "config": {"workload": workload, "poses": int(p.n_poses), "landmarks": int(p.n_landmarks),
                        "obs": int(p.n_obs), "reduced_system": 6 * int(p.n_poses),
+                       "chosen_stop_rho": 0.0 if args.stop_rho is None else float(args.stop_rho),
                        "l2": "256 MB flush written between timed steps"},
             "iterations": int(st["iterations"]), "ms_per_iteration": chosen_ms / max(1, st["iterations"]),
             "iterations_to_plain_cost": hit[0] if hit else None,
@@ -790,8 +792,9 @@ def main():
                     "0 Nielsen")
     ap.add_argument("--outer", type=int, default=-1, help="refinement steps of the mixed step (-1: library default)")
     ap.add_argument("--max-iters", type=int, default=35, help="LM iteration cap of the chosen form")
-    ap.add_argument("--stop-rho", type=float, default=0.25, help="chosen form: least gain ratio of a step that "
-                    "ends the solve by the relative-decrease test (0: any accepted step)")
+    ap.add_argument("--stop-rho", type=float, default=None, help="chosen form: least gain ratio of a step that "
+                    "ends the solve by the relative-decrease test (0: any accepted step; default 0.25 on the "
+                    "config-3 batch, 0 on the single problems of configs 1 and 2)")
     ap.add_argument("--autotune", type=int, default=1, help="1: time the run-time launch shapes first")
     ap.add_argument("--inflight", type=int, default=4, help="e2e: batches solving at once in solve_stream")
     ap.add_argument("--shapes", default="", help="COST,LIN: cost-pass and Jacobian-pass CTA sizes instead of "

@@ -162,9 +162,12 @@ typedef struct spgo_params {
                                     0: every step */
     float   stop_rho;            /* an accepted step whose relative decrease is below tol ends
                                     the solve only if its gain ratio (actual / predicted
-                                    decrease) is at least stop_rho; a smaller ratio marks a
-                                    poor local model, not a converged problem, and the solve
-                                    goes on.  In [0, 1); default 0: every such step ends it */
+                                    decrease) is at least stop_rho, or its predicted decrease
+                                    is itself below tol, or the accepted step before it was
+                                    also below tol; a single poorly modelled step that
+                                    predicted more marks a plateau, not a converged problem,
+                                    and the solve goes on.  In [0, 1); default 0: every such
+                                    step ends it */
 } spgo_params;
 
 typedef struct spgo_problem_status {

@@ -325,8 +325,10 @@ def lm_solve(prob, loss: Loss = Loss(), max_iters=20, tol=1e-6, lam0=1e-4, eps=1
     Marquardt scaling (see ``solve_damped``); gain ratio rho = (F - F') / pred.
     rho > 0: accept, lam *= max(1/3, 1 - (2 rho - 1)^3), nu = 2;
     otherwise reject, lam *= nu, nu *= 2.  Stops when an accepted step lowers
-    the cost by less than ``tol`` relative with rho >= ``stop_rho`` (default 0:
-    any accepted step), or after ``max_iters`` solves (accepted + rejected).
+    the cost by less than ``tol`` relative with rho >= ``stop_rho``, a predicted
+    decrease below ``tol`` relative, or an accepted step before it that was also
+    below ``tol`` (default stop_rho 0: any accepted step), or after ``max_iters``
+    solves (accepted + rejected).
     Mutates ``prob`` and returns an ``LMResult``.
     """
     lam, nu = lam0, 2.0
@@ -335,6 +337,7 @@ def lm_solve(prob, loss: Loss = Loss(), max_iters=20, tol=1e-6, lam0=1e-4, eps=1
     F0 = F
     it = acc = 0
     converged = False
+    small_prev = False
     trace = []
     while it < max_iters:
         st = solve_damped(lin, lam, eps)
@@ -349,12 +352,14 @@ def lm_solve(prob, loss: Loss = Loss(), max_iters=20, tol=1e-6, lam0=1e-4, eps=1
         if np.isfinite(Fn) and rho > 0:
             acc += 1
             rel = (F - Fn) / max(F, 1e-300)
+            pred_rel = st.pred / max(F, 1e-300)
             F = Fn
             lam *= max(1.0 / 3.0, 1.0 - (2.0 * rho - 1.0) ** 3)
             nu = 2.0
-            if rel < tol and rho >= stop_rho:
+            if rel < tol and (rho >= stop_rho or pred_rel < tol or small_prev):
                 converged = True
                 break
+            small_prev = rel < tol
             lin = linearize(prob, loss)
         else:
             prob.poses, prob.alpha = old

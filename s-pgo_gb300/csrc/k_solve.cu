@@ -553,6 +553,7 @@ __global__ void k_reset(PlanView pv, WorkView wv, double lam) {
   s.gnorm = s.dmean = s.dmax = s.dmin = s.cmean = 0.0;
   s.last_acc = s.rej_streak = 0;
   s.wait_timeouts = s.ref_done = 0;
+  s.small_prev = s.pad_ = 0;
   wv.lm[b] = s;
   wv.cost_acc[b] = 0.0;
   wv.pred_acc[b] = 0.0;
@@ -627,7 +628,13 @@ __global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
     s.nu = 2.0;
     s.relin = 1;
     s.res_sel ^= 1;  // the candidate's residuals are now the state's
-    if (rel < prm.tol && rho >= (double)prm.stop_rho) s.status = SPGO_STATUS_CONVERGED;
+    // a small decrease ends the solve when the model predicted it (rho >= stop_rho), when
+    // the model itself predicts no more than tol, or when the last accepted step was
+    // small too
+    const bool small = rel < prm.tol;
+    if (small && (rho >= (double)prm.stop_rho || pred < prm.tol * F || s.small_prev))
+      s.status = SPGO_STATUS_CONVERGED;
+    s.small_prev = small ? 1 : 0;
   } else {
     if (s.fail & FAIL_TIMEOUT)
       s.wait_timeouts += 1;

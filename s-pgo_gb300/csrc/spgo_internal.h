@@ -79,6 +79,8 @@ struct LMState {
   int32_t last_acc, rej_streak;
   int32_t wait_timeouts;  // steps rejected because a bounded device wait ran out
   int32_t ref_done;       // this step's refinement has converged (outer_tol): skip its further steps
+  int32_t small_prev;     // the last accepted step lowered the cost by less than tol (relative)
+  int32_t pad_;
 };
 
 constexpr int32_t FAIL_PIVOT = 1, FAIL_TIMEOUT = 2;
