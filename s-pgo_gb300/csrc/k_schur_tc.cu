@@ -80,12 +80,6 @@ static_assert(sizeof(OpStage) % 1024 == 0, "operand stage alignment");
 static_assert(sizeof(RawSlot) % 16 == 0, "raw slot alignment");
 static_assert(sizeof(TcSmem) + 1024 <= 232448, "fits the 227 KB opt-in shared memory");
 
-// x rounded to the nearest TF32 value (10 explicit mantissa bits, ties away from
-// zero), so that the tensor core reads it exactly whatever its own conversion
-__device__ __forceinline__ float tf32_round(float x) {
-  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-}
-
 // scale one slab row (or zeros) by s and write its hi/lo parts as row r of an
 // operand in core-matrix layout; piece order rotated by r (bank-conflict free).
 // With gs != nullptr also returns sum_k x_k gs_k.
@@ -101,8 +95,8 @@ __device__ __forceinline__ float split_row(const float *src, bool valid, const f
     float hi[4], lo[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      hi[i] = tf32_round(x[i]);
-      lo[i] = tf32_round(x[i] - hi[i]);
+      hi[i] = tc::tf32_round(x[i]);
+      lo[i] = tc::tf32_round(x[i] - hi[i]);
     }
     const uint32_t off = tc::kmajor_offset(r, 4 * kq);
     *reinterpret_cast<float4 *>(reinterpret_cast<unsigned char *>(h) + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);

@@ -16,6 +16,12 @@
 namespace spgo {
 namespace tc {
 
+// x rounded to the nearest TF32 value (10 explicit mantissa bits, ties away from
+// zero), so that the tensor core reads it exactly whatever its own conversion
+__device__ __forceinline__ float tf32_round(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
