@@ -8,7 +8,8 @@
 //                  full, row-major) for the residual, g0 = g - g_L; clears S_L, g_L
 //   per 64-column panel kb:
 //     k_lg_potrf   one CTA factors the 64x64 diagonal block in shared memory,
-//                  16 columns at a time (register-resident 16x16 blocks)
+//                  16 columns at a time (register-resident 16x16 blocks); on the
+//                  FP32 path k_lg_potrf_rows, one thread per row of the block
 //     k_lg_trsm    thread per row below it: L(i, kb:) = S(i, kb:) L_kk^-T
 //     k_lg_syrk    one CTA per 64x64 tile of the trailing lower triangle,
 //                  C -= L_i L_j^T from shared-memory tiles, 4x4 outputs per thread
@@ -160,6 +161,56 @@ __global__ void __launch_bounds__(256) k_lg_potrf(PlanView pv, WorkView wv, int 
     const int i = idx % nb, j = idx / nb;
     if (i >= j) fac[(size_t)(kb + j) * P + kb + i] = D[i][j];
   }
+}
+
+// FP32 path: one CTA of 64 threads factors the 64x64 diagonal block, thread i holding row i of
+// the block in registers.  Column k: the threads of rows i >= k put their entry of
+// column k into a shared column (double-buffered: one barrier per column), then each
+// reads the pivot, and row i > k forms L(i, k) = a(i, k) / L(k, k) and updates its own
+// entries j in (k, i]: a(i, j) -= L(i, k) L(j, k), with L(j, k) taken as a(j, k) from
+// the shared column times 1 / L(k, k).  The serial part per column is one barrier,
+// one square root and one reciprocal; the update is spread over the rows.  (The FP64
+// path keeps k_lg_potrf: FP64 issues at 1/64 of the FP32 rate, and 64 threads carrying
+// the update alone made it slower.)
+__global__ void __launch_bounds__(kLgNB) k_lg_potrf_rows(PlanView pv, WorkView wv, int b, int kb) {
+  if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
+  __shared__ float col[2][kLgNB];
+  const int P = 6 * pv.p_npose[b], nb = min(kLgNB, P - kb), i = threadIdx.x;
+  float *fac = reinterpret_cast<float *>(wv.fac) + pv.p_S_off[b];
+  float *dinv = reinterpret_cast<float *>(wv.lg_dinv) + pv.p_param_off[b];
+  float a[kLgNB];
+#pragma unroll
+  for (int j = 0; j < kLgNB; ++j) a[j] = (i < nb && j <= i) ? fac[(size_t)(kb + j) * P + kb + i] : 0.f;
+  bool bad = false;
+  float rdiag = 0.f;  // 1 / L(i, i)
+#pragma unroll
+  for (int k = 0; k < kLgNB; ++k) {
+    if (k >= nb) break;  // (uniform: a narrow last panel)
+    float *c = col[k & 1];
+    if (i >= k) c[i] = a[k];
+    __syncthreads();
+    const float d = c[k];
+    bad = bad || !(d > 0.f) || !(d < INFINITY);
+    const float lkk = sqrtf(d), rinv = 1.f / lkk;  // correctly rounded, as in the batched factorisation
+    if (i == k) {
+      a[k] = lkk;
+      rdiag = rinv;
+    } else if (i > k) {
+      const float lik = a[k] * rinv;
+      a[k] = lik;
+      const float s = lik * rinv;  // L(i, k) / L(k, k): times a(j, k) gives L(i, k) L(j, k)
+#pragma unroll
+      for (int j = k + 1; j < kLgNB; ++j)
+        if (j <= i) a[j] -= s * c[j];
+    }
+  }
+  if (i < nb) {
+#pragma unroll
+    for (int j = 0; j < kLgNB; ++j)
+      if (j <= i) fac[(size_t)(kb + j) * P + kb + i] = a[j];
+    dinv[kb + i] = rdiag;
+  }
+  if (bad && i == 0) atomicOr(&wv.lm[b].fail, FAIL_PIVOT);
 }
 
 // thread per row below the panel: L(i, kb:ke) = S(i, kb:ke) L_kk^-T, right-looking
@@ -518,7 +569,10 @@ int launch_factor_large(const PlanView &pv, const WorkView &wv, const Params &pr
   int n = 1;
   for (int kb = 0; kb < P; kb += kLgNB) {
     const int ke = min(P, kb + kLgNB);
-    k_lg_potrf<T><<<1, 256, 0, st>>>(pv, wv, b, kb);
+    if constexpr (std::is_same<T, float>::value)
+      k_lg_potrf_rows<<<1, kLgNB, 0, st>>>(pv, wv, b, kb);
+    else
+      k_lg_potrf<T><<<1, 256, 0, st>>>(pv, wv, b, kb);
     ++n;
     if (ke < P) {
       const int M = P - ke, nt = (M + kLgNB - 1) / kLgNB;
