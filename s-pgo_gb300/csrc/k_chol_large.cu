@@ -338,6 +338,8 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   __shared__ T part[4][kLgNB];
   __shared__ T zs[kLgNB];
+  __shared__ T Ld[kLgNB][kLgNB + 1];  // the diagonal block (lower, zero elsewhere) and its pivots,
+  __shared__ T ds[kLgNB];             // staged while the earlier blocks are still being solved
   __shared__ int timed_out;
   const int P = 6 * pv.p_npose[b], po = pv.p_param_off[b];
   const int k = blockIdx.x, kb = k * kLgNB, nb = min(kLgNB, P - kb);
@@ -349,19 +351,25 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
   int *flag = wv.lg_flag + po;
   const uint64_t deadline = lg_clock_ns() + wait_ns;
   if (tid == 0) timed_out = 0;
+  for (int idx = tid; idx < kLgNB * kLgNB; idx += blockDim.x) {
+    const int i = idx % kLgNB, j = idx / kLgNB;
+    Ld[i][j] = (i < nb && j <= i) ? Lat(kb + i, kb + j) : T(0);
+  }
+  if (tid < kLgNB) ds[tid] = tid < nb ? dinv[kb + tid] : T(0);
   __syncthreads();
   T acc = T(0);
   for (int j = 0; j < k; ++j) {  // earlier blocks are full 64-wide
+    // this block's part of L is loaded before the wait for block j's solution
+    const int c0 = j * kLgNB + 16 * q;
+    T lv[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) lv[c] = r < nb ? Lat(kb + r, c0 + c) : T(0);
     if (tid == 0 && !timed_out && !lg_wait_flag(flag + j, deadline)) timed_out = 1;
     __syncthreads();
     if (r < nb) {
-      const int c0 = j * kLgNB + 16 * q;
-      T lv[16], zv[16];
+      T zv[16];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        lv[c] = Lat(kb + r, c0 + c);
-        zv[c] = __ldcg(z + c0 + c);
-      }
+      for (int c = 0; c < 16; ++c) zv[c] = __ldcg(z + c0 + c);
 #pragma unroll
       for (int c = 0; c < 16; ++c) acc += lv[c] * zv[c];
     }
@@ -380,7 +388,7 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
       if (h > 0) {  // the first half is final: loads first, four chains
         T lq[32];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) lq[c] = lane < w ? Lat(u, kb + c) : T(0);
+        for (int c = 0; c < 32; ++c) lq[c] = lane < w ? Ld[h + lane][c] : T(0);
         T v1 = T(0), v2 = T(0), v3 = T(0);
 #pragma unroll
         for (int c = 0; c < 32; c += 4) {
@@ -394,8 +402,8 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
       T lr[32], di[32];
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
-        lr[c] = (lane < w && c < lane) ? Lat(u, kb + h + c) : T(0);
-        di[c] = c < w ? dinv[kb + h + c] : T(0);
+        lr[c] = (lane < w && c < lane) ? Ld[h + lane][h + c] : T(0);
+        di[c] = c < w ? ds[h + c] : T(0);
       }
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
@@ -427,6 +435,8 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   __shared__ T part[4][kLgNB];
   __shared__ T zs[kLgNB];
+  __shared__ T Ld[kLgNB][kLgNB + 1];  // the diagonal block (lower, zero elsewhere) and its pivots,
+  __shared__ T ds[kLgNB];             // staged while the later blocks are still being solved
   __shared__ int timed_out;
   const int P = 6 * pv.p_npose[b], po = pv.p_param_off[b];
   const int nblk = (P + kLgNB - 1) / kLgNB, k = nblk - 1 - (int)blockIdx.x;
@@ -439,18 +449,29 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
   int *flag = wv.lg_flag + pv.total_params + po;
   const uint64_t deadline = lg_clock_ns() + wait_ns;
   if (tid == 0) timed_out = 0;
+  for (int idx = tid; idx < kLgNB * kLgNB; idx += blockDim.x) {
+    const int i = idx % kLgNB, j = idx / kLgNB;
+    Ld[i][j] = (i < nb && j <= i) ? Lat(kb + i, kb + j) : T(0);
+  }
+  if (tid < kLgNB) ds[tid] = tid < nb ? dinv[kb + tid] : T(0);
   __syncthreads();
   T acc = T(0);
   for (int j = nblk - 1; j > k; --j) {  // later blocks, finished by lower-numbered CTAs
+    // this block's part of L is loaded before the wait for block j's solution
+    const int jb = j * kLgNB, nbj = min(kLgNB, P - jb);
+    T lv[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const int i = 16 * q + c;
+      lv[c] = (r < nb && i < nbj) ? Lat(jb + i, kb + r) : T(0);  // column kb + r: contiguous per thread
+    }
     if (tid == 0 && !timed_out && !lg_wait_flag(flag + j, deadline)) timed_out = 1;
     __syncthreads();
-    const int jb = j * kLgNB, nbj = min(kLgNB, P - jb);
     if (r < nb) {
-      T lv[16], xv[16];
+      T xv[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
         const int i = 16 * q + c;
-        lv[c] = i < nbj ? Lat(jb + i, kb + r) : T(0);  // column kb + r: contiguous per thread
         xv[c] = i < nbj ? __ldcg(x + jb + i) : T(0);
       }
 #pragma unroll
@@ -468,7 +489,7 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
       if (h + w < nb) {  // the later half is final (h = 0): loads first
         T lq[32];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) lq[c] = (lane < w && 32 + c < nb) ? Lat(kb + 32 + c, u) : T(0);
+        for (int c = 0; c < 32; ++c) lq[c] = (lane < w && 32 + c < nb) ? Ld[32 + c][h + lane] : T(0);
         T v1 = T(0), v2 = T(0), v3 = T(0);
 #pragma unroll
         for (int c = 0; c < 32; c += 4) {
@@ -482,8 +503,8 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
       T lc[32], di[32];  // column `lane` of the diagonal block, pivots
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
-        lc[c] = (c < w && lane < c) ? Lat(kb + h + c, u) : T(0);
-        di[c] = c < w ? dinv[kb + h + c] : T(0);
+        lc[c] = (c < w && lane < c) ? Ld[h + c][h + lane] : T(0);
+        di[c] = c < w ? ds[h + c] : T(0);
       }
 #pragma unroll
       for (int c = 31; c >= 0; --c) {
