@@ -173,7 +173,7 @@ struct spgo_plan {
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl, w_trace;
   // refinement of the mixed path's step (k_refine.cu)
-  size_t w_tcam = 0, w_facs = 0, w_twist = 0, w_pdual = 0, w_dal = 0, w_tl = 0, w_gaacc = 0, w_gacc = 0, w_rhsB = 0, w_ddelta = 0;
+  size_t w_tcam = 0, w_xanc = 0, w_facs = 0, w_twist = 0, w_pdual = 0, w_dal = 0, w_tl = 0, w_gaacc = 0, w_gacc = 0, w_rhsB = 0, w_ddelta = 0;
 
   ~spgo_plan() {
     for (cudaEvent_t e : uploads) {  // the blocks go back to the cache only once no copy reads them
@@ -311,6 +311,7 @@ static void build_layout(spgo_plan *p) {
   p->w_trace = take((size_t)p->B * SPGO_TRACE_MAX * 3 * 8);
   if (p->precision == SPGO_PREC_MIXED) {
     p->w_tcam = take((size_t)p->O * 24 * 2);  // camera-frame points, halves as the residuals
+    p->w_xanc = take((size_t)p->L * 32 * 2);  // anchor points, halves as the residuals
     p->w_facs = take((size_t)p->total_S * 4);
     p->w_twist = take((size_t)p->total_pairs * 6 * 4);
     p->w_pdual = take((size_t)p->total_pairs * 6 * 8);
@@ -809,6 +810,7 @@ static void make_views(spgo_solver *s) {
   x.ctrl = w + p->w_ctrl;
   if (p->precision == SPGO_PREC_MIXED) {
     x.tcam = reinterpret_cast<float *>(w + p->w_tcam);
+    x.xanc = reinterpret_cast<float *>(w + p->w_xanc);
     x.facs = reinterpret_cast<float *>(w + p->w_facs);
     x.twist = reinterpret_cast<float *>(w + p->w_twist);
     x.pdual = reinterpret_cast<double *>(w + p->w_pdual);

@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
   const size_t half = (size_t)(COST && gate != GATE_FIRST ? 1 - sel : sel);
   float *res_buf = wv.res + half * (size_t)pv.O * 4;
   float *tcam_buf = wv.tcam ? wv.tcam + half * (size_t)pv.O * 6 : nullptr;  // mixed path: camera-frame points
+  float *xanc_buf = wv.xanc ? wv.xanc + half * (size_t)pv.L * 8 : nullptr;   // and anchor points
   // cost pass: each thread's observation record is loaded one loop pass ahead (the
   // first one here, so its DRAM latency overlaps phase A), so a pass does not open
   // with a round trip to DRAM; the Jacobian pass has no registers to spare for it
@@ -218,6 +219,11 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_linearize(PlanV
     }
     sm.X[tid][0] = X.x; sm.X[tid][1] = X.y; sm.X[tid][2] = X.z;
     sm.dX[tid][0] = -X.x / alpha; sm.dX[tid][1] = -X.y / alpha; sm.dX[tid][2] = -X.z / alpha;
+    if (COST && xanc_buf) {  // kept for the Jacobian and residual passes at this state
+      float4 *xa = reinterpret_cast<float4 *>(xanc_buf + (size_t)li * 8);
+      xa[0] = make_float4((float)X.x, (float)X.y, (float)X.z, (float)sm.dX[tid][0]);
+      xa[1] = make_float4((float)sm.dX[tid][1], (float)sm.dX[tid][2], 0.f, 0.f);
+    }
     sm.C[tid] = T(0);
     sm.ga[tid] = T(0);
     sm.a[tid] = a;
@@ -631,23 +637,19 @@ __global__ void __launch_bounds__(256, 3) k_jacobian_acc(PlanView pv, WorkView w
   const float *res_buf = wv.res + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 4;  // the state's residuals
   const float *tcam_buf = wv.tcam + (size_t)wv.lm[b].res_sel * (size_t)pv.O * 6;  // and camera-frame points
 
-  // phase A: the chunk's anchor points (double-float, then split)
+  // phase A: the chunk's anchor points, as the cost pass at this state formed them
+  // (double-float, rounded to the high part)
   if (tid < cnt) {
     const int li = lm0 + tid;
     const int a = pv.lm_host[li];
-    const double al = alpha_state[pv.lm_user[li]];
-    const df ald = df_from_double(al);
-    const df t3[3] = {df_sub(pv.lm_uv[2 * li], intr[2]) / df_make(intr[0]) / ald,
-                      df_sub(pv.lm_uv[2 * li + 1], intr[3]) / df_make(intr[1]) / ald, df_make(1.f) / ald};
-    const float *Rh = wv.fr_Rf + (size_t)(fo + a) * 18, *Rl = wv.fr_Rl + (size_t)(fo + a) * 18;
-    const float alf = (float)al;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const df v = df{Rh[3 * k], Rl[3 * k]} * t3[0] + df{Rh[3 * k + 1], Rl[3 * k + 1]} * t3[1] +
-                   df{Rh[3 * k + 2], Rl[3 * k + 2]} * t3[2];
-      sm.X[tid][k] = v.h;
-      sm.dX[tid][k] = -v.h / alf;
-    }
+    const float4 *xa = reinterpret_cast<const float4 *>(wv.xanc + ((size_t)wv.lm[b].res_sel * pv.L + li) * 8);
+    const float4 x0 = xa[0], x1 = xa[1];
+    sm.X[tid][0] = x0.x;
+    sm.X[tid][1] = x0.y;
+    sm.X[tid][2] = x0.z;
+    sm.dX[tid][0] = x0.w;
+    sm.dX[tid][1] = x1.x;
+    sm.dX[tid][2] = x1.y;
     sm.C[tid] = 0.f;
     sm.ga[tid] = 0.f;
     sm.a[tid] = a;

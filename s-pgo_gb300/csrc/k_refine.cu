@@ -208,24 +208,19 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
   const int rows = 6 * nb;
 
   if (warp == 0) {
-    // the chunk's anchor points (as in the linearisation: double-float, then split)
+    // the chunk's anchor points, as the cost pass at this state formed them (the same
+    // points the linearisation used)
     if (lane < cnt) {
       const int li = lm0 + lane;
-      const int a = pv.lm_host[li];
-      const double al = alpha_state[pv.lm_user[li]];
-      const df ald = df_from_double(al);
-      const df t3[3] = {df_sub(pv.lm_uv[2 * li], intr[2]) / df_make(intr[0]) / ald,
-                        df_sub(pv.lm_uv[2 * li + 1], intr[3]) / df_make(intr[1]) / ald, df_make(1.f) / ald};
-      const float *Rh = wv.fr_Rf + (size_t)(fo + a) * 18, *Rl = wv.fr_Rl + (size_t)(fo + a) * 18;
-      const float alf = (float)al;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const df v = df{Rh[3 * k], Rl[3 * k]} * t3[0] + df{Rh[3 * k + 1], Rl[3 * k + 1]} * t3[1] +
-                     df{Rh[3 * k + 2], Rl[3 * k + 2]} * t3[2];
-        sm.X[lane][k] = v.h;
-        sm.dX[lane][k] = -v.h / alf;
-      }
-      sm.a[lane] = a;
+      const float4 *xa = reinterpret_cast<const float4 *>(wv.xanc + ((size_t)wv.lm[b].res_sel * pv.L + li) * 8);
+      const float4 x0 = xa[0], x1 = xa[1];
+      sm.X[lane][0] = x0.x;
+      sm.X[lane][1] = x0.y;
+      sm.X[lane][2] = x0.z;
+      sm.dX[lane][0] = x0.w;
+      sm.dX[lane][1] = x1.x;
+      sm.dX[lane][2] = x1.y;
+      sm.a[lane] = pv.lm_host[li];
     }
 #pragma unroll
     for (int w = 0; w < kRpWarps; ++w) sm.dlh[w][lane] = sm.dll[w][lane] = 0.f;

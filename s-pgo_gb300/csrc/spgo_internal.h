@@ -100,6 +100,10 @@ struct WorkView {
                         // LMState::res_sel holds the state's, the other the last candidate's
   float *tcam;          // [2][O][6] the camera-frame points of the same cost passes (left, right),
                         // the double-float value rounded once; halves as res (mixed path)
+  float *xanc;          // [2][L][8] per landmark (internal order), from the same cost passes: the
+                        // anchor point's double-float value rounded to its high part (x, y, z),
+                        // then d/d alpha of that rounded point (x, y, z), 2 pad; halves as res
+                        // (mixed path)
   void *pair_acc;       // [total_pairs][27] T  (accumulated by the linearisation)
   void *pairF;          // [total_pairs][27] T  (prefix / suffix sums)
   void *A;              // [total_S] T      pose-pose blocks
