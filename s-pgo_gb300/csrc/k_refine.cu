@@ -149,6 +149,7 @@ struct RefSmem {
   float dlh[kRpWarps][SPGO_CHUNK];  // j_a^T W e, per warp, double-float (h, l)
   float dll[kRpWarps][SPGO_CHUNK];
   int key[kRpWarps][32];
+  float bt[2][SPGO_CHUNK];  // warps 0 and 1: partial W^T x_p over their slab row blocks
 };
 
 // dynamic shared memory (W = window frames): the window's rotations [W][18] (both
@@ -207,6 +208,27 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
   const float *Cv = reinterpret_cast<const float *>(wv.C);
   const int rows = 6 * nb;
 
+  if (warp < 2) {
+    // inverse-depth step: first pass x_a = D^-1 (g_a - W^T x_p) from the FP32 system,
+    // later x_a += t - D^-1 W^T dx_p (the previous pass's t and pose correction); warps
+    // 0 and 1 take alternate 32-row blocks of the slab for W^T x_p
+    const double *v = (FIRST ? wv.delta : wv.ddelta) + po + 6 * f0;
+    float s0 = 0.f, s1 = 0.f;
+    for (int rb = 32 * warp; rb < rows; rb += 64) {
+      const float dv = rb + lane < rows ? (float)v[rb + lane] : 0.f;
+      const float *sr = slab + (size_t)rb * SPGO_CHUNK + lane;
+      const int nr = min(32, rows - rb);
+      float q[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) q[k] = k < nr ? sr[(size_t)k * SPGO_CHUNK] : 0.f;
+#pragma unroll
+      for (int k = 0; k < 32; k += 2) {
+        s0 += q[k] * __shfl_sync(0xffffffffu, dv, k);
+        s1 += q[k + 1] * __shfl_sync(0xffffffffu, dv, k + 1);
+      }
+    }
+    sm.bt[warp][lane] = s0 + s1;
+  }
   if (warp == 0) {
     // the chunk's anchor points, as the cost pass at this state formed them (the same
     // points the linearisation used)
@@ -224,29 +246,14 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
     }
 #pragma unroll
     for (int w = 0; w < kRpWarps; ++w) sm.dlh[w][lane] = sm.dll[w][lane] = 0.f;
-  } else if (warp == 1) {
-    // inverse-depth step: first pass x_a = D^-1 (g_a - W^T x_p) from the FP32 system,
-    // later x_a += t - D^-1 W^T dx_p (the previous pass's t and pose correction)
-    const double *v = (FIRST ? wv.delta : wv.ddelta) + po + 6 * f0;
-    float s0 = 0.f, s1 = 0.f;
-    for (int rb = 0; rb < rows; rb += 32) {
-      const float dv = rb + lane < rows ? (float)v[rb + lane] : 0.f;
-      const float *sr = slab + (size_t)rb * SPGO_CHUNK + lane;
-      const int nr = min(32, rows - rb);
-      float q[32];
-#pragma unroll
-      for (int k = 0; k < 32; ++k) q[k] = k < nr ? sr[(size_t)k * SPGO_CHUNK] : 0.f;
-#pragma unroll
-      for (int k = 0; k < 32; k += 2) {
-        s0 += q[k] * __shfl_sync(0xffffffffu, dv, k);
-        s1 += q[k + 1] * __shfl_sync(0xffffffffu, dv, k + 1);
-      }
-    }
+  }
+  if (warp < 2) named_sync(1, 64);  // both partial sums written
+  if (warp == 1) {
     if (lane < cnt) {
       const int li = lm0 + lane;
       const float C = Cv[li];
       const float Dd = C * (float)(1.0 + lam) + eps;
-      const float s = s0 + s1;
+      const float s = sm.bt[0][lane] + sm.bt[1][lane];
       double da;
       if (FIRST)
         da = (double)((reinterpret_cast<const float *>(wv.ga)[li] - s) / Dd);
@@ -255,7 +262,7 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
       wv.dal[li] = da;
       sm.da[lane] = (float)da;
     }
-  } else {
+  } else if (warp >= 2) {
     // the window's rotations, and per window frame n the offset c_a - c_n of the pair
     // origin (n < a) and the twist of the pair (a, n)
     const int ah = pv.lm_host[lm0], fh = fo + ah;
@@ -426,8 +433,8 @@ __global__ void __launch_bounds__(kRpThreads, 8) k_resid_pass(PlanView pv, WorkV
 #pragma unroll
     for (int w = 0; w < kRpWarps; ++w) acc.add(sm.dlh[w][tid], sm.dll[w][tid]);
     const double dsum = df_acc_value(acc);
-    const double ra = dsum - (lam * (double)C + (double)eps) * wv.dal[li];
-    const float t = (float)(ra / (double)Dd);
+    const double ra = dsum - (lam * (double)C + (double)eps) * wv.dal[li];  // summed in FP64
+    const float t = (float)ra / Dd;  // (t is an FP32 preconditioner term: no FP64 division)
     sm.t[tid] = t;
     wv.tl[li] = t;
   } else if (tid < SPGO_CHUNK) {

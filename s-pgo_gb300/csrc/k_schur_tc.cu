@@ -105,7 +105,6 @@ __device__ __forceinline__ float split_row(const float *src, bool valid, const f
   return gacc;
 }
 
-__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_schur_tc(PlanView pv, WorkView wv, Params prm, int gate) {
   extern __shared__ __align__(16) unsigned char smem_raw[];

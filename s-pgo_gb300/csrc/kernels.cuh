@@ -25,6 +25,8 @@ __device__ __forceinline__ T warp_sum(T v) {
 
 // fire-and-forget accumulation (compiles to RED for an unused return value)
 __device__ __forceinline__ void red_add(float *p, float v) { atomicAdd(p, v); }
+// barrier `id` (1..15) for the first n threads of the CTA (n a multiple of 32)
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 __device__ __forceinline__ void red_add(double *p, double v) { atomicAdd(p, v); }
 
 template <typename T> struct Vec3 { T x, y, z; };
