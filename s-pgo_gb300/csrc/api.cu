@@ -169,7 +169,7 @@ struct spgo_plan {
   mutable std::vector<cudaEvent_t> uploads;  // one per upload from the blocks
   mutable std::mutex upload_mu;              // solvers bound from several threads
   // workspace segment offsets
-  size_t w_Sx = 0, w_lg = 0, w_lgflag = 0;
+  size_t w_Sx = 0, w_lg = 0, w_lgflag = 0, w_lgred = 0;
   size_t w_frRf, w_frRl, w_frRd, w_frc, w_frch, w_frcl, w_pcand, w_acand, w_res, w_pacc, w_pF, w_A, w_g, w_SL, w_gL, w_fac,
       w_delta, w_C, w_ga, w_slab, w_lm, w_cost, w_pred, w_lmb, w_probe, w_ctrl, w_trace;
   // refinement of the mixed path's step (k_refine.cu)
@@ -298,6 +298,7 @@ static void build_layout(spgo_plan *p) {
   p->w_Sx = take(any_large ? (size_t)p->total_S * 8 : 0);
   p->w_lg = take(any_large ? (size_t)p->total_params * 8 * 6 : 0);
   p->w_lgflag = take(any_large ? (size_t)p->total_params * 2 * sizeof(int) : 0);
+  p->w_lgred = take(any_large && p->precision == SPGO_PREC_MIXED ? (size_t)(p->NP + p->B) * 12 * 8 : 0);
   p->w_delta = take((size_t)p->total_params * 8);
   p->w_C = take((size_t)(p->L + 64) * ts);  // + 64: the tensor-core Schur copies 16-byte aligned supersets
   p->w_ga = take((size_t)(p->L + 64) * ts);  // + 64: as C
@@ -796,6 +797,7 @@ static void make_views(spgo_solver *s) {
     x.lg_y = lg + 3 * tp;
     x.lg_dinv = lg + 4 * tp;
     x.lg_flag = reinterpret_cast<int *>(w + p->w_lgflag);
+    x.lg_red = p->w_lgred ? reinterpret_cast<double *>(w + p->w_lgred) : nullptr;
   }
   x.delta = reinterpret_cast<double *>(w + p->w_delta);
   x.C = w + p->w_C;
@@ -909,8 +911,10 @@ static int enqueue_candidate(spgo_solver *s, cudaStream_t st, bool solved = fals
     { PROF(K_RESID); CUDA_TRY(launch_resid_pass(s->pv, s->wv, s->prm, s->alpha, k == 0, st)); }
     PROF(K_REFINE);
     CUDA_TRY(launch_resid_solve(s->pv, s->wv, s->prm, k == 0, st));
-    for (const int b : s->plan->large)
+    for (const int b : s->plan->large) {
+      CUDA_TRY(launch_resid_reduce_large(s->pv, s->wv, b, s->plan->p_npose[b], st));
       CUDA_TRY(launch_refine_large(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b], st));
+    }
     if (k + 1 < outer) CUDA_TRY(launch_pair_twists(s->pv, s->wv, st));
   }
   { PROF(K_BACKSUB); CUDA_TRY(launch_backsub_refined(s->pv, s->wv, s->prm, s->alpha, s->wv.alpha_cand, st)); }

@@ -525,6 +525,7 @@ __global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkVie
   size_t o_cb, o_y, o_tmp, o_L;
   rs_layout(pv.max_P_small, pv.max_P / 6, &o_cb, &o_y, &o_tmp, &o_L);
   const bool small = P <= pv.max_P_small;
+  if (!small && wv.lg_red) return;  // wide problems: the grid-wide kernels below
   const size_t npk = (size_t)P * (P + 1) / 2;
   float *Lm = reinterpret_cast<float *>(smem_raw + o_L);
   if (small) {
@@ -637,6 +638,152 @@ __global__ void __launch_bounds__(kRsThreads) k_resid_solve(PlanView pv, WorkVie
   // converged: the correction is a small fraction of the step, further steps are skipped
   if (tid == 0 && outer_tol > 0.f && __uint_as_float(mx_dx) <= outer_tol * __uint_as_float(mx_x))
     wv.lm[b].ref_done = 1;
+}
+
+// ---- the same reduction for wide problems, spread over the GPU ----------------------
+// One CTA per problem puts a wide problem's FP64 pair sums on one SM (GB300 issues FP64
+// at 1/64 of its FP32 rate): for P = 3000 that was 267 us per refinement step.  Here
+//   k_rs_sums_large   thread per (pose, component): the row sums (over hi) and the
+//                     column sums (over lo, moved to c_lo) of the pair duals, into lg_red
+//   k_rs_scan_large   one CTA: the rows' prefix over the poses, as segment sums, an
+//                     exclusive scan of the segments and a second walk of each segment
+//   k_rs_rhs_large    thread per pose: the world-to-pose transform, the right-hand side
+//                     into lg_y for the multi-CTA substitutions; clears the pair duals
+// The per-pose values are those of k_resid_solve; only the prefix is summed in another
+// order (FP64, segments of ~N / 42 poses).
+__global__ void __launch_bounds__(256) k_rs_sums_large(PlanView pv, WorkView wv, int b) {
+  if (!refine_active(wv, b)) return;
+  const int N = pv.p_npose[b], D = pv.p_pair_D[b], fo = pv.p_frame_off[b];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 12 * N) return;
+  double *rowm = wv.lg_red + ((size_t)pv.p_pose_off[b] + b) * 12, *colm = rowm + (size_t)(N + 1) * 6;
+  const double *recs = wv.pdual + (size_t)pv.p_pair_off[b] * 6;
+  auto cen = [&](int f, int k) {
+    return (double)wv.fr_ch[(size_t)(fo + f) * 6 + k] + (double)wv.fr_cl[(size_t)(fo + f) * 6 + k];
+  };
+  const int k = t % 6;
+  if (t < 6 * N) {  // row lo = t / 6
+    const int lo = t / 6;
+    const double *r = recs + (size_t)lo * D * 6 + k;
+    const int nd = min(D, N - lo);
+    double acc = 0.0;
+#pragma unroll 4
+    for (int d = 0; d < nd; ++d) acc += r[(size_t)d * 6];
+    rowm[lo * 6 + k] = acc;
+    if (lo == 0) colm[k] = 0.0;  // no record ends at pose 0
+  } else {  // column hi = (t - 6 N) / 6 + 1
+    const int hi = (t - 6 * N) / 6 + 1;
+    double acc = 0.0;
+    if (k < 3) {
+      const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+#pragma unroll 4
+      for (int lo = max(0, hi - D); lo < hi; ++lo) {
+        const double *r = recs + ((size_t)lo * D + (hi - lo - 1)) * 6;
+        acc += r[k] + (cen(lo, k1) * r[3 + k2] - cen(lo, k2) * r[3 + k1]);
+      }
+    } else {
+#pragma unroll 4
+      for (int lo = max(0, hi - D); lo < hi; ++lo) acc += recs[((size_t)lo * D + (hi - lo - 1)) * 6 + k];
+    }
+    colm[hi * 6 + k] = acc;
+  }
+}
+
+constexpr int kScanSegs = 42;  // segments per component: 6 x 42 = 252 of the 256 threads
+
+// dynamic shared memory: the per-pose terms [N][6] (FP64)
+__global__ void __launch_bounds__(256) k_rs_scan_large(PlanView pv, WorkView wv, int b) {
+  if (!refine_active(wv, b)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *val = reinterpret_cast<double *>(smem_raw);
+  __shared__ double seg[6][kScanSegs];
+  const int N = pv.p_npose[b], fo = pv.p_frame_off[b], tid = threadIdx.x;
+  double *rowm = wv.lg_red + ((size_t)pv.p_pose_off[b] + b) * 12;
+  const double *colm = rowm + (size_t)(N + 1) * 6;
+  // pose i's term: its row sums moved from c_i (the origin of the records starting there)
+  // less the column sums of the records ending there
+  for (int t = tid; t < 6 * N; t += blockDim.x) {
+    const int i = t / 6, k = t % 6, k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+    const double *m = rowm + i * 6;
+    double nrow = m[k];
+    if (k < 3) {
+      const double c1 = (double)wv.fr_ch[(size_t)(fo + i) * 6 + k1] + (double)wv.fr_cl[(size_t)(fo + i) * 6 + k1];
+      const double c2 = (double)wv.fr_ch[(size_t)(fo + i) * 6 + k2] + (double)wv.fr_cl[(size_t)(fo + i) * 6 + k2];
+      nrow += c1 * m[3 + k2] - c2 * m[3 + k1];
+    }
+    val[t] = nrow - colm[t];
+  }
+  __syncthreads();
+  const int len = (N + kScanSegs - 1) / kScanSegs;
+  const int k = tid / kScanSegs, s = tid % kScanSegs, i0 = s * len, i1 = min(N, i0 + len);
+  if (tid < 6 * kScanSegs) {
+    double acc = 0.0;
+    for (int i = i0; i < i1; ++i) acc += val[i * 6 + k];
+    seg[k][s] = acc;
+  }
+  __syncthreads();
+  if (tid < 6) {  // exclusive scan of the segment sums
+    double acc = 0.0;
+    for (int q = 0; q < kScanSegs; ++q) {
+      const double v = seg[tid][q];
+      seg[tid][q] = acc;
+      acc += v;
+    }
+  }
+  __syncthreads();
+  if (tid < 6 * kScanSegs) {
+    double acc = seg[k][s];
+    for (int i = i0; i < i1; ++i) {
+      acc += val[i * 6 + k];
+      rowm[i * 6 + k] = acc;  // the sum of the records covering pose i
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_rs_rhs_large(PlanView pv, WorkView wv, int b) {
+  if (!refine_active(wv, b)) return;
+  const int N = pv.p_npose[b], D = pv.p_pair_D[b], P = 6 * N;
+  const int fo = pv.p_frame_off[b], po = pv.p_param_off[b];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const double *rowm = wv.lg_red + ((size_t)pv.p_pose_off[b] + b) * 12;
+  // the pair duals are summed: cleared for the next pass
+  double *recs = wv.pdual + (size_t)pv.p_pair_off[b] * 6;
+  for (size_t q = t; q < (size_t)N * D * 6; q += (size_t)gridDim.x * blockDim.x) recs[q] = 0.0;
+  if (t >= N) return;
+  const int i = t;
+  const double lam = wv.lm[b].lam;
+  const float *A = reinterpret_cast<const float *>(wv.A) + pv.p_S_off[b];
+  double R[9], ci[3];
+  frame_Rc(wv, fo + i, R, ci);
+  const double *S = rowm + i * 6;
+  const double w[3] = {S[0] - (ci[1] * S[5] - ci[2] * S[4]), S[1] - (ci[2] * S[3] - ci[0] * S[5]),
+                       S[2] - (ci[0] * S[4] - ci[1] * S[3])};
+  double out[6];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    out[r] = R[r] * w[0] + R[3 + r] * w[1] + R[6 + r] * w[2];
+    out[3 + r] = R[r] * S[3] + R[3 + r] * S[4] + R[6 + r] * S[5];
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const int p = 6 * i + k;
+    const double x = wv.delta[po + p];
+    const double rhs = out[k] - lam * (double)A[(size_t)p * P + p] * x - (double)wv.rhsB[po + p];
+    wv.rhsB[po + p] = 0.f;
+    reinterpret_cast<float *>(wv.lg_y)[po + p] = (float)rhs;
+  }
+}
+
+int launch_resid_reduce_large(const PlanView &pv, const WorkView &wv, int b, int N, void *stream) {
+  if (!wv.lg_red) return 0;  // (the FP64 path has no refinement)
+  cudaStream_t st = (cudaStream_t)stream;
+  k_rs_sums_large<<<(12 * N + 255) / 256, 256, 0, st>>>(pv, wv, b);
+  const size_t sm = (size_t)N * 6 * sizeof(double);
+  cudaFuncSetAttribute(k_rs_scan_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_rs_scan_large<<<1, 256, sm, st>>>(pv, wv, b);
+  k_rs_rhs_large<<<(N + 127) / 128, 128, 0, st>>>(pv, wv, b);
+  g_launches += 3;
+  return (int)cudaGetLastError();
 }
 
 int launch_resid_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int first, void *stream) {

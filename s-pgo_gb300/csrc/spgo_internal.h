@@ -126,6 +126,8 @@ struct WorkView {
   float *lg_xs;         // [2 total_params] its double-float split
   void *lg_y, *lg_dinv; // [total_params] T: right-hand side / residual; 1 / L_kk
   int *lg_flag;         // [2 total_params]: block-done flags of the multi-CTA substitutions
+  double *lg_red;       // [NP + B][12] mixed path, wide problems: per pose the refinement's row and
+                        // column sums of the pair duals ([N + 1][6] each), then the rows' prefix
   double *cost_acc;     // [B]
   double *pred_acc;     // [B]
   // iterative refinement of the mixed path's step (k_refine.cu); null on the FP64 path
@@ -179,6 +181,7 @@ int launch_pair_twists(const PlanView &pv, const WorkView &wv, void *stream);
 int launch_resid_pass(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha, int first,
                       void *stream);
 int launch_resid_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int first, void *stream);
+int launch_resid_reduce_large(const PlanView &pv, const WorkView &wv, int b, int N, void *stream);
 int launch_refine_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
                         void *stream);
 int launch_backsub_refined(const PlanView &pv, const WorkView &wv, const Params &prm, const double *alpha,
