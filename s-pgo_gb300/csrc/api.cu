@@ -880,7 +880,7 @@ static int enqueue_factor(spgo_solver *s, cudaStream_t st) {
     for (const int b : s->plan->large)
       CUDA_TRY(launch_factor_large<T>(s->pv, s->wv, s->prm, b, 6 * s->plan->p_npose[b], s->plan->p_param_off[b],
                                       (mixed && !(s->prm.outer_steps > 0 && s->wv.facs)) ? s->prm.refine_steps : 0,
-                                      st));
+                                      st, s->side, s->ev_fork, s->ev_join));
   }
   return SPGO_OK;
 }

@@ -256,18 +256,31 @@ __global__ void __launch_bounds__(128) k_lg_trsm(PlanView pv, WorkView wv, int b
     if (j < nb) fac[(size_t)(kb + j) * P + i] = x[j];
 }
 
+// tiles of the trailing lower triangle: mode 0 all of them, mode 1 the first tile column
+// (the next panel's columns), mode 2 the others
 template <typename T>
-__global__ void __launch_bounds__(256) k_lg_syrk(PlanView pv, WorkView wv, int b, int kb) {
+__global__ void __launch_bounds__(256) k_lg_syrk(PlanView pv, WorkView wv, int b, int kb, int mode) {
   if (!problem_active(wv.lm, b, GATE_RUNNING)) return;
   __shared__ T LR[kLgNB][kLgNB + 1];
   __shared__ T LC[kLgNB][kLgNB + 1];
   const int P = 6 * pv.p_npose[b], nb = min(kLgNB, P - kb), ke = kb + nb, tid = threadIdx.x;
-  // tile t -> (ti >= tj) of the trailing lower triangle
+  // tile t -> (ti >= tj) of the trailing lower triangle (mode 2: of the triangle without
+  // its first tile column, shifted by one)
   const int t = blockIdx.x;
-  int ti = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
-  while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-  while (ti * (ti + 1) / 2 > t) --ti;
-  const int tj = t - ti * (ti + 1) / 2;
+  int ti, tj;
+  if (mode == 1) {
+    ti = t;
+    tj = 0;
+  } else {
+    ti = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+    while (ti * (ti + 1) / 2 > t) --ti;
+    tj = t - ti * (ti + 1) / 2;
+    if (mode == 2) {
+      ++ti;
+      ++tj;
+    }
+  }
   const int R0 = ke + kLgNB * ti, C0 = ke + kLgNB * tj;
   T *fac = reinterpret_cast<T *>(wv.fac) + pv.p_S_off[b];
   for (int idx = tid; idx < nb * kLgNB; idx += blockDim.x) {
@@ -583,24 +596,50 @@ __global__ void __launch_bounds__(256) k_lg_resid(PlanView pv, WorkView wv, int 
 
 template <typename T>
 int launch_factor_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
-                        int refine, void *stream) {
+                        int refine, void *stream, void *side, void *ev_a, void *ev_b) {
   cudaStream_t st = (cudaStream_t)stream;
   const uint64_t wait_ns = wait_limit_ns(prm);
   k_lg_assemble<T><<<P, 256, 0, st>>>(pv, wv, b);
   int n = 1;
+  auto potrf = [&](int kb, cudaStream_t on) {
+    if constexpr (std::is_same<T, float>::value)
+      k_lg_potrf_rows<<<1, kLgNB, 0, on>>>(pv, wv, b, kb);
+    else
+      k_lg_potrf<T><<<1, 256, 0, on>>>(pv, wv, b, kb);
+    ++n;
+  };
+  // one panel of look-ahead: once panel kb's rows are solved, the next panel's columns take
+  // its update first and the next diagonal block is factored on the side stream while the
+  // rest of the trailing matrix is updated; every element takes the same updates in the
+  // same order as without it
+  cudaStream_t sd = (cudaStream_t)side;
+  cudaEvent_t ea = (cudaEvent_t)ev_a, eb = (cudaEvent_t)ev_b;
+  const bool ahead = sd && ea && eb;
+  potrf(0, st);
   for (int kb = 0; kb < P; kb += kLgNB) {
     const int ke = min(P, kb + kLgNB);
-    if constexpr (std::is_same<T, float>::value)
-      k_lg_potrf_rows<<<1, kLgNB, 0, st>>>(pv, wv, b, kb);
-    else
-      k_lg_potrf<T><<<1, 256, 0, st>>>(pv, wv, b, kb);
-    ++n;
-    if (ke < P) {
-      const int M = P - ke, nt = (M + kLgNB - 1) / kLgNB;
-      k_lg_trsm<T><<<(M + 127) / 128, 128, 0, st>>>(pv, wv, b, kb);
-      k_lg_syrk<T><<<nt * (nt + 1) / 2, 256, 0, st>>>(pv, wv, b, kb);
-      n += 2;
+    if (ke >= P) break;  // (the last diagonal block is factored: nothing below it)
+    const int M = P - ke, nt = (M + kLgNB - 1) / kLgNB;
+    k_lg_trsm<T><<<(M + 127) / 128, 128, 0, st>>>(pv, wv, b, kb);
+    n += 1;
+    if (!ahead) {
+      k_lg_syrk<T><<<nt * (nt + 1) / 2, 256, 0, st>>>(pv, wv, b, kb, 0);
+      ++n;
+      potrf(ke, st);
+      continue;
     }
+    k_lg_syrk<T><<<nt, 256, 0, st>>>(pv, wv, b, kb, 1);
+    ++n;
+    cudaError_t e = cudaEventRecord(ea, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(sd, ea, 0);
+    if (e != cudaSuccess) return (int)e;
+    potrf(ke, sd);
+    if ((e = cudaEventRecord(eb, sd)) != cudaSuccess) return (int)e;
+    if (nt > 1) {
+      k_lg_syrk<T><<<(nt - 1) * nt / 2, 256, 0, st>>>(pv, wv, b, kb, 2);
+      ++n;
+    }
+    if ((e = cudaStreamWaitEvent(st, eb, 0)) != cudaSuccess) return (int)e;
   }
   const int nblk = (P + kLgNB - 1) / kLgNB;
   int *ff = wv.lg_flag + param_off, *fb = wv.lg_flag + pv.total_params + param_off;
@@ -642,8 +681,8 @@ int launch_refine_large(const PlanView &pv, const WorkView &wv, const Params &pr
 }
 
 template int launch_factor_large<float>(const PlanView &, const WorkView &, const Params &, int, int, int, int,
-                                        void *);
+                                        void *, void *, void *, void *);
 template int launch_factor_large<double>(const PlanView &, const WorkView &, const Params &, int, int, int, int,
-                                         void *);
+                                         void *, void *, void *, void *);
 
 }  // namespace spgo

@@ -172,7 +172,7 @@ int launch_schur(const PlanView &pv, const WorkView &wv, const Params &prm, void
 size_t factor_packed_bytes(int P, size_t ts);  // shared memory of the batched factorisation
 template <typename T>
 int launch_factor_large(const PlanView &pv, const WorkView &wv, const Params &prm, int b, int P, int param_off,
-                        int refine, void *stream);
+                        int refine, void *stream, void *side = nullptr, void *ev_a = nullptr, void *ev_b = nullptr);
 template <typename T>
 int launch_factor_solve(const PlanView &pv, const WorkView &wv, const Params &prm, int mixed,
                         void *stream);
