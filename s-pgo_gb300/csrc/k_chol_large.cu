@@ -12,10 +12,13 @@
 //                  FP32 path k_lg_potrf_rows, one thread per row of the block
 //     k_lg_trsm    thread per row below it: L(i, kb:) = S(i, kb:) L_kk^-T
 //     k_lg_syrk    one CTA per 64x64 tile of the trailing lower triangle,
-//                  C -= L_i L_j^T from shared-memory tiles, 4x4 outputs per thread
+//                  C -= L_i L_j^T from shared-memory tiles, 4x4 outputs per thread;
+//                  the next panel's tile column first, then (with the solver's second
+//                  stream) the next k_lg_potrf beside the rest of the update
 //   k_lg_fwd/bwd   forward / backward substitution with one CTA per 64-row block,
 //                  chained by per-block flags (32-unknown shuffle chains inside each
-//                  diagonal block), x += solution
+//                  diagonal block, staged in shared memory while the CTA waits its
+//                  turn), x += solution
 //   k_lg_resid     warp per row: g0 - S x from the exact S (between two solves)
 // Replaces, for such problems, the reference's libtorch Cholesky of the dense
 // reduced system (src/Optimization/linear_solvers.cu:195-218).

@@ -28,8 +28,9 @@
 //                     t = D^-1 r_a and W t into the pose right-hand side
 //   k_resid_solve     per problem: the pair records reduced to per-pose vectors
 //                     (FP64), the right-hand side, and the solve with the stored FP32
-//                     factor (or, for systems too wide for one CTA, the multi-CTA
-//                     substitutions of k_chol_large.cu)
+//                     factor; systems too wide for one CTA take the same reduction
+//                     from k_rs_sums_large, k_rs_scan_large and k_rs_rhs_large (spread
+//                     over the GPU) and the multi-CTA substitutions of k_chol_large.cu
 //   k_backsub_refined per chunk: the last inverse-depth correction, the candidate
 //                     inverse depths and their share of the predicted decrease
 //
