@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(256) k_lg_fwd(PlanView pv, WorkView wv, int b,
   __syncthreads();
   if (warp == 0) {  // L_kk z_k = zs: two 32-unknown halves, lane = unknown
     for (int h = 0; h < nb; h += 32) {
-      const int w = min(32, nb - h), u = kb + h + lane;
+      const int w = min(32, nb - h);
       T v = lane < w ? zs[h + lane] : T(0);
       if (h > 0) {  // the first half is final: loads first, four chains
         T lq[32];
@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(256) k_lg_bwd(PlanView pv, WorkView wv, int b,
   __syncthreads();
   if (warp == 0) {  // L_kk^T x_k = zs, halves from the bottom
     for (int h = ((nb - 1) / 32) * 32; h >= 0; h -= 32) {
-      const int w = min(32, nb - h), u = kb + h + lane;
+      const int w = min(32, nb - h);
       T v = lane < w ? zs[h + lane] : T(0);
       if (h + w < nb) {  // the later half is final (h = 0): loads first
         T lq[32];
