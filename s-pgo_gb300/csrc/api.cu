@@ -954,7 +954,11 @@ static int enqueue_lm_iteration(spgo_solver *s, cudaStream_t st) {
   }
   { PROF(K_CHAIN); CUDA_TRY(launch_chain(s->pv, s->wv, s->wv.poses_cand, GATE_RUNNING, kF64<T>, st)); }
   { PROF(K_COST); CUDA_TRY(launch_linearize<T>(s->pv, s->wv, s->prm, s->wv.alpha_cand, 1, GATE_RUNNING, st)); }
-  { PROF(K_BOOKKEEP); CUDA_TRY(launch_decide_commit(s->pv, s->wv, s->prm, s->poses, s->alpha, st)); }
+  {
+    PROF(K_BOOKKEEP);
+    CUDA_TRY(launch_decide(s->pv, s->wv, s->prm, st));
+  }
+  { PROF(K_BOOKKEEP); CUDA_TRY(launch_commit(s->pv, s->wv, s->poses, s->alpha, st)); }
   if (std::is_same<T, float>::value && s->wv.facs && s->prm.outer_steps > 0) {
     // the refinement recomputes the Jacobian at the state from the frame tables, which
     // a rejected candidate's chain has overwritten: back to the state's

@@ -591,8 +591,9 @@ int launch_post_linearize(const PlanView &pv, const WorkView &wv, void *stream) 
 
 // Nielsen schedule: rho = (F - F') / pred, pred = 0.5 d^T (g + Lambda d).
 // accept (rho > 0): lam *= max(1/3, 1 - (2 rho - 1)^3), nu = 2; else lam *= nu, nu *= 2.
-// the LM decision of problem b on the candidate's cost and predicted decrease
-__device__ __forceinline__ void decide_problem(const PlanView &pv, const WorkView &wv, const Params &prm, int b) {
+__global__ void k_decide(PlanView pv, WorkView wv, Params prm) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= pv.B) return;
   if (wv.lm[b].status != 0) {
     wv.lm[b].flag = 0;
     return;
@@ -656,31 +657,37 @@ __device__ __forceinline__ void decide_problem(const PlanView &pv, const WorkVie
   }
 }
 
-// One CTA per problem: thread 0 takes the LM decision, then the CTA commits an accepted
-// candidate (the problem's poses and inverse depths; poses and landmarks are stored
-// problem by problem)
-__global__ void __launch_bounds__(128) k_decide_commit(PlanView pv, WorkView wv, Params prm, double *poses,
-                                                       double *alpha) {
-  const int b = blockIdx.x;
-  __shared__ int accepted;
-  if (threadIdx.x == 0) {
-    decide_problem(pv, wv, prm, b);
-    accepted = wv.lm[b].flag;
+int launch_decide(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream) {
+  k_decide<<<grid_for(pv.B, 128), 128, 0, (cudaStream_t)stream>>>(pv, wv, prm);
+  ++g_launches;
+  return (int)cudaGetLastError();
+}
+
+// accepted candidates become the state
+__global__ void k_commit(PlanView pv, WorkView wv, double *poses, double *alpha) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < pv.NP) {
+    const int b = pv.pose_prob[t];
+    if (wv.lm[b].flag) {
+      double v[12];  // all loads before the stores (the two buffers may alias as far as the compiler knows)
+#pragma unroll
+      for (int q = 0; q < 12; ++q) v[q] = wv.poses_cand[12 * t + q];
+#pragma unroll
+      for (int q = 0; q < 12; ++q) poses[12 * t + q] = v[q];
+    }
   }
-  __syncthreads();
-  if (!accepted) return;
-  const size_t p0 = 12 * (size_t)pv.p_pose_off[b];
-  for (int t = threadIdx.x; t < 12 * pv.p_npose[b]; t += blockDim.x) poses[p0 + t] = wv.poses_cand[p0 + t];
-  const int l0 = pv.p_lm_off[b];
-  for (int t = threadIdx.x; t < pv.p_lm_cnt[b]; t += blockDim.x) {
-    const int u = pv.lm_user[l0 + t];
-    alpha[u] = wv.alpha_cand[u];
+  if (t < pv.L) {
+    const int b = pv.lm_prob[t];
+    if (wv.lm[b].flag) {
+      const int u = pv.lm_user[t];
+      alpha[u] = wv.alpha_cand[u];
+    }
   }
 }
 
-int launch_decide_commit(const PlanView &pv, const WorkView &wv, const Params &prm, double *poses, double *alpha,
-                         void *stream) {
-  k_decide_commit<<<pv.B, 128, 0, (cudaStream_t)stream>>>(pv, wv, prm, poses, alpha);
+int launch_commit(const PlanView &pv, const WorkView &wv, double *poses, double *alpha, void *stream) {
+  const long long n = pv.NP > pv.L ? pv.NP : pv.L;
+  k_commit<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(pv, wv, poses, alpha);
   ++g_launches;
   return (int)cudaGetLastError();
 }

@@ -193,8 +193,8 @@ int launch_backsub(const PlanView &pv, const WorkView &wv, const Params &prm, co
 template <typename T>
 int launch_update_poses(const PlanView &pv, const WorkView &wv, const double *poses, double *poses_out,
                         double scale, int direct, void *stream, const double *gacc = nullptr);
-int launch_decide_commit(const PlanView &pv, const WorkView &wv, const Params &prm, double *poses, double *alpha,
-                         void *stream);
+int launch_decide(const PlanView &pv, const WorkView &wv, const Params &prm, void *stream);
+int launch_commit(const PlanView &pv, const WorkView &wv, double *poses, double *alpha, void *stream);
 int launch_post_linearize(const PlanView &pv, const WorkView &wv, void *stream);
 int launch_reset(const PlanView &pv, const WorkView &wv, const Params &prm, double lam, void *stream);
 template <typename T>

@@ -1,7 +1,7 @@
 """The stopping rule of the oracle's LM (``oracle.solver.lm_solve``) clause by clause, on
 scripted steps: the linearisation, damped solve, update and cost are replaced by fakes
 that return a given sequence of candidate costs and predicted decreases, so each case
-exercises one clause of the rule (the GPU's k_decide_commit applies the same rule;
+exercises one clause of the rule (the GPU's k_decide applies the same rule;
 ``test_stop_rho_matches_oracle`` compares the two on a real scene).
 
 An accepted step whose relative decrease is below tol ends the solve when
